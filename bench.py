@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Benchmark of the proving hot path on GB300: committed + sumchecked field elements per second.
+
+Workload (one step): the 256-polynomial commitment, 256 rows of k = 2^20 uniform Goldilocks
+values encoded at rate 1/2 (n = 2^21), absorbed into 2^21 column chains in blocks of B = 32 rows
+and merkled into a root; then a degree-3 sumcheck of Σ f·g·h over three tables of 2^22 values
+with challenges from the BLAKE3 transcript. Units per step: 2^28 committed elements plus
+3·2^22 sumchecked table entries. Inputs are SplitMix64 streams (seeded synthetic data).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+`value` times K steps with every input already in HBM (CUDA events on the library's stream);
+`e2e` times the same steps through the host-memory API, the host-to-device copy of the inputs
+from pinned memory and the read-back of the root and proof inside. The reference arm times the
+CPU port of the reference's algorithms (the plain-C oracle) on this host's cores.
+Multi-GPU: one independent replica per GPU (the path needs no exchange), weak scaling.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+NPOLYS, LOG_K, LOG_R, ROW_BLOCK = 256, 20, 1, 32
+SC_VARS, SC_DEGREE = 22, 3
+SEED = 0x00650002
+COMMITTED = NPOLYS << LOG_K
+SUMCHECKED = SC_DEGREE << SC_VARS
+UNITS = COMMITTED + SUMCHECKED
+CONFIG = {
+    "workload": "commit 256 x 2^20 Goldilocks at rate 1/2 (n = 2^21, B = 32, BLAKE3 column chains + Merkle root) "
+                "+ degree-3 sumcheck of f*g*h over 3 x 2^22",
+    "polys": NPOLYS, "log_k": LOG_K, "log_inv_rate": LOG_R, "row_block": ROW_BLOCK,
+    "sumcheck_vars": SC_VARS, "sumcheck_degree": SC_DEGREE,
+    "l2": "inputs larger than L2 (2 GiB rows, 4 GiB codewords per step)",
+    "data": "SplitMix64 uniform Goldilocks",
+}
+MASK64 = (1 << 64) - 1
+P = 0xFFFFFFFF00000001
+
+
+def splitmix_np(seed: int, n: int) -> np.ndarray:
+    """SplitMix64 outputs reduced once below p (the reference bench's from_u64_reduced)."""
+    out = np.empty(n, dtype=np.uint64)
+    chunk = 1 << 24
+    golden = np.uint64(0x9E3779B97F4A7C15)
+    with np.errstate(over="ignore"):
+        for s in range(0, n, chunk):
+            m = min(chunk, n - s)
+            z = (np.arange(s + 1, s + m + 1, dtype=np.uint64) * golden) + np.uint64(seed)
+            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+            z = z ^ (z >> np.uint64(31))
+            z = np.where(z >= np.uint64(P), z - np.uint64(P), z)
+            out[s:s + m] = z
+    return out
+
+
+class Clocks:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index, self.rows, self.proc = index, [], None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            threading.Thread(target=self._read, daemon=True).start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ---- CPU port (the reference arm and the cpu_baseline leg) ---------------------------------------
+
+def cpu_sample(threads: int, polys: int, sc_vars: int) -> tuple[float, int, str]:
+    """Times the oracle (the plain-C port of the reference's algorithms) on a bounded sample of
+    the workload: `polys` rows of 2^20 committed at rate 1/2 with B = 32 (all 2^21 columns
+    chained and merkled), then the degree-3 sumcheck over three tables of 2^sc_vars."""
+    from oracle import oracle as O
+
+    rows = O.splitmix(SEED, polys << LOG_K)
+    f, g, h = (O.splitmix(SEED + 1 + i, 1 << sc_vars) for i in range(3))
+    ctx = bench_context().tce()
+    t0 = time.perf_counter()
+    O.commit_unmasked(rows, LOG_K, LOG_R, ROW_BLOCK, bytes([0x65]) * 32, threads=threads, keep_codewords=False)
+    t1 = time.perf_counter()
+    O.prove_batch(O.OracleTranscript(ctx), "stage/0", SC_DEGREE, [[(f, False, False), (g, False, False), (h, False, False)]])
+    t2 = time.perf_counter()
+    units = (polys << LOG_K) + (SC_DEGREE << sc_vars)
+    sample = (f"{polys} of 256 polynomials of 2^20 committed (all 2^21 columns chained and merkled) in {t1 - t0:.2f} s, "
+              f"sumcheck over 3 x 2^{sc_vars} in {t2 - t1:.2f} s, {threads} threads for the commitment")
+    return t2 - t0, units, sample
+
+
+def bench_context():
+    from tessera_gb300.hash import Mode, SessionContext
+
+    return SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([0x65]) * 32, bytes([0x65]) * 16)
+
+
+def run_reference(args) -> None:
+    world, rank, _ = dist_env()
+    if rank != 0:
+        return
+    from oracle import oracle as O
+
+    O.build()
+    threads = O.threads_available()
+    times, units, sample = [], 0, ""
+    for i in range(args.warmup + args.steps):
+        dt, units, sample = cpu_sample(threads, args.ref_polys, SC_VARS)
+        if i >= args.warmup:
+            times.append(dt)
+    ms = 1e3 * statistics.mean(times)
+    value = units / (ms / 1e3)
+    line = {
+        "metric": "committed+sumchecked field elems/s", "value": value, "unit": "elems/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic", "impl": "reference",
+        "config": CONFIG,
+        "cpu_baseline": {"value": value, "unit": "elems/s", "cores": threads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": "elems/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * max(times)},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---- GPU arm ------------------------------------------------------------------------------------
+
+def measured_peaks() -> dict:
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return {"hbm_gbs": float(d["hbm_gbs"]), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def traffic_table() -> dict:
+    p = ROOT / "profiles" / "traffic.json"
+    return json.loads(p.read_text()) if p.exists() else {}
+
+
+def run_gpu(args) -> None:
+    import ctypes
+
+    import torch
+
+    from tessera_gb300 import _native as N
+    from tessera_gb300.device import Device
+    from tessera_gb300.hash import Transcript
+    from tessera_gb300.sumcheck import Instance, Protocol, Table, prove_batch
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    dev = Device(local)
+    cuda = f"cuda:{local}"
+    stream = torch.cuda.ExternalStream(dev.stream_ptr(), device=cuda)
+
+    # inputs: host (pinned, for e2e) and resident device copies
+    rows_h = torch.from_numpy(splitmix_np(SEED, COMMITTED).view(np.int64)).pin_memory()
+    tabs_h = [torch.from_numpy(splitmix_np(SEED + 1 + i, 1 << SC_VARS).view(np.int64)).pin_memory() for i in range(3)]
+    rows_d = rows_h.to(cuda)
+    tabs_d = [t.to(cuda) for t in tabs_h]
+    n = 1 << (LOG_K + LOG_R)
+    cw_d = torch.empty(NPOLYS * n, dtype=torch.int64, device=cuda)
+    nodes_d = torch.empty((2 * n - 1) * 32, dtype=torch.uint8, device=cuda)
+    rows_e = torch.empty_like(rows_d)  # e2e staging
+    tabs_e = [torch.empty_like(t) for t in tabs_d]
+    torch.cuda.synchronize()
+    cid = (ctypes.c_uint8 * 32)(*([0x65] * 32))
+    root = ctypes.create_string_buffer(32)
+
+    def commit(src):
+        N.call("tg_commit_unmasked_dev", dev.handle, LOG_K, LOG_R, ROW_BLOCK, cid, ctypes.c_void_p(src.data_ptr()), NPOLYS,
+               ctypes.c_void_p(cw_d.data_ptr()), ctypes.c_void_p(nodes_d.data_ptr()), root, None)
+
+    def sumcheck(tabs):
+        t = Transcript(bench_context())
+        return prove_batch(t, Protocol.ONE, "stage/0", SC_DEGREE, [Instance([Table.base(x) for x in tabs])], device=dev)
+
+    def step():
+        commit(rows_d)
+        return sumcheck(tabs_d)
+
+    def step_e2e():
+        # pinned host -> device on the library's stream, the proof and root back to the host
+        with torch.cuda.stream(stream):
+            rows_e.copy_(rows_h, non_blocking=True)
+            for a, b in zip(tabs_e, tabs_h):
+                a.copy_(b, non_blocking=True)
+        commit(rows_e)
+        return sumcheck(tabs_e)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+
+    # the timed region: K steps, inputs resident
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    launches0 = dev.launches()
+    dev.profile(True)
+    with Clocks(local) as clocks:
+        ev[0].record(stream)
+        for i in range(args.steps):
+            step()
+            ev[i + 1].record(stream)
+        stream.synchronize()
+    dev.profile(False)
+    prof = dev.profile_read()
+    launches = dev.launches() - launches0
+    barrier()
+    step_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([total_ms], device=cuda)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        total_ms = float(tt.item())
+    ms_per_step = total_ms / args.steps
+    value = UNITS * world / (total_ms / 1e3 / args.steps)
+
+    # end to end through the host-memory path
+    for _ in range(max(1, args.warmup // 2)):
+        step_e2e()
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step_e2e()
+    e1.record(stream)
+    stream.synchronize()
+    e2e_ms = e0.elapsed_time(e1) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+
+        tt = torch.tensor([e2e_ms], device=cuda)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e_ms = float(tt.item())
+    h2d = COMMITTED * 8 + 3 * (1 << SC_VARS) * 8
+    d2h = 32 + SC_VARS * SC_DEGREE * 16 + 3 * 16
+
+    if rank != 0:
+        return
+    # roofline of the dominant kernel: the encoder's three passes together, against HBM
+    kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
+                   "share": v[0] / max(1e-9, sum(x[0] for x in prof.values()))} for k, v in prof.items()}
+    lde_ms = sum(prof.get(k, (0, 0, 0))[0] for k in ("lde_pass_a", "lde_pass_m", "lde_pass_c"))
+    lde_launch_groups = prof.get("lde_pass_a", (0, 1, 0))[1]
+    rows_done = prof.get("lde_pass_a", (0, 0, 0))[2]
+    bytes_per_row = 8 * (1 << LOG_K) + 8 * (1 << (LOG_K + LOG_R))
+    peaks = measured_peaks()
+    achieved = (bytes_per_row * rows_done) / (lde_ms / 1e3) / 1e9 if lde_ms else None
+    traffic = traffic_table().get("lde_dram_bytes_per_row")
+    roofline = {
+        "kernel": "lde (passes A+M+C, one launch group = rows encoded together)",
+        "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+        "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "peak_source": peaks["source"],
+        "algorithmic_bytes_per_row": bytes_per_row,
+        "traffic": (traffic * rows_done / max(1, lde_launch_groups)) if traffic else None,
+        "traffic_unit": "bytes per launch group",
+        "note": "the encoder is bound by integer multiply throughput, not by HBM; see int_rate",
+    }
+    butterflies_per_row = ((1 << LOG_K) // 2) * LOG_K + ((1 << (LOG_K + LOG_R)) // 2) * (LOG_K + LOG_R)
+    int_rate = {"butterflies_per_s": butterflies_per_row * rows_done / (lde_ms / 1e3) if lde_ms else None,
+                "radix2_butterflies_per_row": butterflies_per_row}
+
+    line = {
+        "metric": "committed+sumchecked field elems/s", "value": value, "unit": "elems/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic", "config": CONFIG,
+        "e2e": {"value": UNITS * world / (e2e_ms / 1e3), "unit": "elems/s", "ms_per_step": e2e_ms,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "latency_ms": {"p50": statistics.median(step_ms), "p99": max(step_ms) if len(step_ms) < 100 else
+                       sorted(step_ms)[int(0.99 * len(step_ms))]},
+        "gpu_launches": launches,
+        "roofline": roofline,
+        "int_rate": int_rate,
+        "kernels": kernels,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline and world == 1:
+        from oracle import oracle as O
+
+        O.build()
+        threads = O.threads_available()
+        dt, units, sample = cpu_sample(threads, args.cpu_polys, SC_VARS)
+        line["cpu_baseline"] = {"value": units / dt, "unit": "elems/s", "cores": threads, "kind": "port", "sample": sample}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--cpu-polys", type=int, default=32, help="rows in the CPU baseline's bounded sample")
+    ap.add_argument("--ref-polys", type=int, default=32, help="rows per step in the reference arm's sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,196 @@
+/* SPDX-License-Identifier: Apache-2.0 OR MIT
+ *
+ * libtessera_gb300: the GB300 (sm_103a) proving hot path of Tessera behind a C ABI.
+ *
+ * The entry points replace the device seams of the reference prover (AbdelStark/tessera);
+ * each declaration cites the reference interface it stands in for. Field elements are
+ * canonical Goldilocks words (uint64_t in [0, p), p = 2^64 - 2^32 + 1, little-endian in memory
+ * as the reference's repr(transparent) Goldilocks); an Fp2 element is two words (c0, c1) for
+ * c0 + c1 X, X^2 = 7, laid out as the reference's repr(C) QuadraticExt; digests are 32 bytes.
+ * Matrices are row-major by polynomial: row r (one polynomial of k values) at rows + r*k, its
+ * codeword at codewords + r*n.
+ *
+ * Every function returns TG_OK (0) or a negative status, with the reason in tg_last_error()
+ * (per thread). "_dev" entry points take device pointers and an optional cudaStream_t (NULL:
+ * the device handle's own stream) and return once the work is queued; the others take host
+ * memory and return when the results are in it. A handle may be used from one thread at a
+ * time unless its comment says otherwise.
+ */
+#ifndef TESSERA_GB300_H
+#define TESSERA_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+    TG_OK = 0,
+    TG_DECLINED = 1,        /* an offload declined the work (the host does it) */
+    TG_ERR_INVALID = -1,    /* a shape or argument the reference would refuse */
+    TG_ERR_CUDA = -2,       /* a CUDA call failed */
+    TG_ERR_NOMEM = -3,      /* device memory exhausted */
+    TG_ERR_STATE = -4,      /* a call out of order (absorb after finish, after a short block) */
+};
+
+typedef struct tg_device tg_device;
+typedef struct tg_sink tg_sink;
+typedef struct tg_matrix tg_matrix;
+typedef struct tg_level tg_level;
+
+/* Device configuration; zero fields take their defaults. The level fields are the reference's
+ * TESSERA_GPU_LEVEL_GIB / TESSERA_GPU_LEVEL_MIN (crates/tessera-prover/src/gpu.rs:121-134). */
+typedef struct {
+    uint64_t level_budget_bytes; /* default 16 GiB */
+    uint64_t level_min_entries;  /* default 2^14 (gpu.rs:89 LEVEL_MIN_ENTRIES) */
+    uint64_t lde_group_bytes;    /* LDE scratch per group of rows; default 96 MiB (L2-resident) */
+} tg_config;
+
+/* Library version, and the message of the calling thread's last failure. */
+int tg_version(void);
+const char *tg_last_error(void);
+
+/* Opens one GPU (replaces Gpu::open / Device::new, crates/tessera-prover/src/gpu.rs:111-146,
+ * crates/tessera-gpu/src/device.rs:125-146). */
+int tg_device_open(int ordinal, const tg_config *cfg, tg_device **out);
+int tg_device_close(tg_device *dev);
+int tg_device_sync(tg_device *dev);
+/* The handle's own CUDA stream (a cudaStream_t), where calls given a NULL stream run. */
+int tg_device_stream(tg_device *dev, void **stream);
+/* Kernels launched through this handle so far (the library's own, counted at launch). */
+int tg_device_launches(tg_device *dev, uint64_t *launches);
+/* Per-kernel timing (no counterpart in the reference; its GPU timing lives in benchmark
+ * harnesses, crates/tessera-bench/examples/gpu_unit_costs.rs): while enabled, every launch is
+ * bracketed by CUDA events on its own stream. tg_profile_read sums the elapsed times by kernel
+ * name since the last read: names come newline-separated in `names`; ms, launches and units
+ * (work items) fill the first `cap` entries; *count is the number of kernels seen. */
+int tg_profile_enable(tg_device *dev, int on);
+int tg_profile_read(tg_device *dev, char *names, size_t names_len, double *ms, uint64_t *launches, uint64_t *units,
+                    size_t cap, size_t *count);
+
+/* ---- Reed–Solomon encoding: RowEncoder::encode_rows (crates/tessera-pcs/src/encoding.rs:257)
+ * nrows rows of k = 2^log_k values -> codewords of n = 2^(log_k + log_inv_rate) symbols,
+ * symbol j = g(7 ω_n^j), g = f + (X^k - 1) m, masks: nrows x mask_coeffs (m_0 first) or NULL
+ * for mask_coeffs = 0. 1 <= log_inv_rate <= 4, log_k <= 24, mask_coeffs <= k. */
+int tg_encode_rows_dev(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t mask_coeffs,
+                       const uint64_t *rows, size_t nrows, const uint64_t *masks, uint64_t *codewords,
+                       void *stream);
+int tg_encode_rows(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t mask_coeffs,
+                   const uint64_t *rows, size_t nrows, const uint64_t *masks, uint64_t *codewords);
+
+/* ---- Column chains and Merkle trees (crates/tessera-hash/src/columns.rs:72-104,
+ * crates/tessera-hash/src/merkle.rs:93-113). chains: ncols x 32 bytes. */
+int tg_column_init_dev(tg_device *dev, const uint8_t commitment_id[32], uint64_t ncols, uint8_t *chains,
+                       void *stream);
+/* Absorbs `count` rows (count x ncols symbols, row-major) in blocks of `row_block` rows
+ * (1 <= row_block <= 124, each step one BLAKE3 chunk). */
+int tg_column_absorb_dev(tg_device *dev, uint8_t *chains, uint64_t ncols, const uint64_t *rows, size_t count,
+                         uint32_t row_block, void *stream);
+/* Every node of the tree over n (a power of two) leaves: nodes holds 2n - 1 digests, leaves
+ * first, the root last (the reference's level order). */
+int tg_merkle_tree_dev(tg_device *dev, const uint8_t *leaves, size_t n, uint8_t *nodes, void *stream);
+/* leaf_j = H("column-merge", d_j^(1) || ... || d_j^(S)) over S x n segment chains
+ * (crates/tessera-pcs/src/streaming.rs:432-438). */
+int tg_column_merge_dev(tg_device *dev, const uint8_t *segment_chains, size_t nsegments, uint64_t n,
+                        uint8_t *leaves, void *stream);
+
+/* ---- Resident unmasked commitment: ReferenceCommitment::commit_unmasked
+ * (crates/tessera-pcs/src/commitment.rs:343-458): encode, one chain per column over blocks of
+ * row_block rows (leaf = last chain), Merkle tree. Device form: codewords (npolys x n) and
+ * nodes (2n - 1 digests) are caller device buffers; the root is copied to host `root`. */
+int tg_commit_unmasked_dev(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t row_block,
+                           const uint8_t commitment_id[32], const uint64_t *rows, size_t npolys,
+                           uint64_t *codewords, uint8_t *nodes, uint8_t root[32], void *stream);
+/* Host form: rows in host memory; leaves (n x 32, may be NULL) and root returned to the host. */
+int tg_commit_unmasked(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t row_block,
+                       const uint8_t commitment_id[32], const uint64_t *rows, size_t npolys, uint8_t *leaves,
+                       uint8_t root[32]);
+/* merge_segments on host buffers (crates/tessera-pcs/src/streaming.rs:382-404). */
+int tg_merge_segments(tg_device *dev, const uint8_t *segment_chains, size_t nsegments, uint64_t n,
+                      uint8_t *leaves, uint8_t root[32]);
+
+/* ---- BlockSink: the advice sink (crates/tessera-pcs/src/streaming.rs:24-37; the reference's
+ * AdviceSink, crates/tessera-prover/src/gpu.rs:570-667). Opened with the commitment's k, rate,
+ * P and B; starts from the chains of commitment_id over n columns. absorb takes one block of
+ * 1..B whole rows (k values each) and their masks (P per row, m_0 first); a block shorter than
+ * B must be the last. finish writes the n chains (n x 32). Device copies of rows, masks and
+ * codewords are zeroed before their memory is released. */
+int tg_advice_sink_open(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t mask_coeffs,
+                        uint32_t row_block, const uint8_t commitment_id[32], tg_sink **out);
+int tg_sink_absorb(tg_sink *sink, const uint64_t *rows, size_t nrows, const uint64_t *masks);
+int tg_sink_finish(tg_sink *sink, uint8_t *chains);
+int tg_sink_close(tg_sink *sink);
+
+/* ---- MatrixSink / WeightEncoding (crates/tessera-pcs/src/weights/regenerated.rs:24-58):
+ * unmasked rows at any rate 1/2^r, chained leaves, answering `queries` (codeword columns,
+ * distinct and increasing). absorb writes nrows x nqueries answers, row by row. */
+int tg_matrix_open(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t row_block,
+                   const uint8_t commitment_id[32], const uint64_t *queries, size_t nqueries, tg_matrix **out);
+int tg_matrix_absorb(tg_matrix *m, const uint64_t *rows, size_t nrows, uint64_t *answers);
+int tg_matrix_finish(tg_matrix *m, uint8_t *chains);
+int tg_matrix_close(tg_matrix *m);
+
+/* ---- Fiat–Shamir transcript (crates/tessera-hash/src/transcript.rs:127-250), host side.
+ * context_tce is TCE(SessionContext). */
+typedef struct {
+    uint8_t state[32];
+    uint64_t counter;
+} tg_transcript;
+int tg_hash(const char *domain, const uint8_t *in, size_t len, uint8_t out[32]);
+int tg_transcript_init(tg_transcript *t, const uint8_t *context_tce, size_t len);
+int tg_transcript_absorb(tg_transcript *t, const char *label, const uint8_t *value, size_t len);
+int tg_transcript_absorb_fp2s(tg_transcript *t, const char *label, const uint64_t *values, size_t count);
+int tg_transcript_squeeze(tg_transcript *t, const char *label, uint8_t out[32]);
+int tg_transcript_challenge_fp(tg_transcript *t, const char *label, uint64_t *out);
+int tg_transcript_challenge_fp2(tg_transcript *t, const char *label, uint64_t out[2]);
+int tg_transcript_challenge_indices(tg_transcript *t, const char *label, uint32_t log_n, uint32_t count,
+                                    uint64_t *out);
+int tg_transcript_check_grind(tg_transcript *t, const char *label, uint32_t bits, uint64_t nonce, int *valid);
+/* grind (transcript.rs:241-250): the smallest nonce meeting `bits`, searched on the GPU,
+ * then absorbed. */
+int tg_transcript_grind(tg_device *dev, tg_transcript *t, const char *label, uint32_t bits, uint64_t *nonce);
+
+/* ---- Batched sumcheck: prove_batch (crates/tessera-sumcheck/src/prover.rs:1122) for
+ * product instances, Protocol One (degree 1..7). A table is 2^vars entries: words (is_ext = 0,
+ * Table::base) or Fp2 pairs (is_ext = 1, Table::ext); is_public leaves it out of the final
+ * evaluations (Table::public). Tables are device pointers when tables_on_device, else host.
+ * Outputs: gamma; rounds: n_max x degree Fp2 (p(0), p(2), ..., p(d)); challenges: n_max Fp2;
+ * final_evals: the evaluations (count in *n_evals). The transcript advances exactly as the
+ * reference's does. */
+typedef struct {
+    const uint64_t *values;
+    int is_ext;
+    int is_public;
+} tg_table;
+typedef struct {
+    const tg_table *tables;
+    int ntables;
+    int vars;
+} tg_instance;
+int tg_prove_batch(tg_device *dev, tg_transcript *t, const char *prefix, int degree, const tg_instance *instances,
+                   int ninstances, int tables_on_device, uint64_t gamma[2], uint64_t *rounds, uint64_t *challenges,
+                   uint64_t *final_evals, size_t *n_evals);
+
+/* ---- LevelOffload / DeviceLevel (crates/tessera-sumcheck/src/offload.rs:17-79; the
+ * reference's GpuLevels, crates/tessera-gpu/src/level.rs:52-146). shape 0: fraction
+ * N0 D1 + N1 D0 + λ D0 D1 over [N0, N1, D0, D1]; shape 1: product V0 V1 over [V0, V1].
+ * tables: ntables host pointers to len Fp2 entries each. Returns TG_DECLINED with *out = NULL
+ * when the level is below the minimum size, over the budget or malformed, as load() declines.
+ * Handles are safe to use from several threads. */
+int tg_level_load(tg_device *dev, int shape, const uint64_t lambda[2], const uint64_t *const *tables, int ntables,
+                  size_t len, tg_level **out);
+/* Σ_p w(p) P(line_x(p)) for x = 0, 2, 3 over the current pairs, w(p) = low[p mod 2^low_bits]
+ * high[p >> low_bits]; low has 2^low_bits Fp2, high nhigh Fp2. out: 3 Fp2. */
+int tg_level_sums(tg_level *l, const uint64_t *low, const uint64_t *high, size_t nhigh, uint32_t low_bits,
+                  uint64_t out[6]);
+int tg_level_bind(tg_level *l, const uint64_t r[2]);
+/* Each table's first entry, in table order (ntables Fp2). */
+int tg_level_firsts(tg_level *l, uint64_t *out);
+int tg_level_free(tg_level *l);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

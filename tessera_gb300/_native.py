@@ -1,0 +1,126 @@
+"""ctypes bindings of libtessera_gb300.so (include/tessera_gb300.h).
+
+The library is the only implementation of the hot path: there is no CPU fallback. If it is not
+built, or a call fails, an exception says why.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_build" / "libtessera_gb300.so"
+
+TG_OK, TG_DECLINED = 0, 1
+TG_ERR_INVALID, TG_ERR_CUDA, TG_ERR_NOMEM, TG_ERR_STATE = -1, -2, -3, -4
+
+
+class TesseraError(RuntimeError):
+    """A failed library call: `code` is the TG_ERR_* status."""
+
+    def __init__(self, code: int, message: str):
+        super().__init__(f"{message} (status {code})")
+        self.code = code
+
+
+class InvalidInput(TesseraError, ValueError):
+    pass
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("level_budget_bytes", ctypes.c_uint64), ("level_min_entries", ctypes.c_uint64),
+                ("lde_group_bytes", ctypes.c_uint64)]
+
+
+class TranscriptState(ctypes.Structure):
+    _fields_ = [("state", ctypes.c_uint8 * 32), ("counter", ctypes.c_uint64)]
+
+
+class TableC(ctypes.Structure):
+    _fields_ = [("values", ctypes.c_void_p), ("is_ext", ctypes.c_int), ("is_public", ctypes.c_int)]
+
+
+class InstanceC(ctypes.Structure):
+    _fields_ = [("tables", ctypes.POINTER(TableC)), ("ntables", ctypes.c_int), ("vars", ctypes.c_int)]
+
+
+_lib = None
+
+V, U32, U64, SZ, INT = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t, ctypes.c_int
+CSTR = ctypes.c_char_p
+
+# name -> argument types (every function returns int unless listed in _RESTYPE)
+SIGNATURES = {
+    "tg_version": [],
+    "tg_last_error": [],
+    "tg_device_open": [INT, V, V],
+    "tg_device_close": [V],
+    "tg_device_sync": [V],
+    "tg_device_launches": [V, V],
+    "tg_device_stream": [V, V],
+    "tg_profile_enable": [V, INT],
+    "tg_profile_read": [V, V, SZ, V, V, V, SZ, V],
+    "tg_encode_rows_dev": [V, U32, U32, U32, V, SZ, V, V, V],
+    "tg_encode_rows": [V, U32, U32, U32, V, SZ, V, V],
+    "tg_column_init_dev": [V, V, U64, V, V],
+    "tg_column_absorb_dev": [V, V, U64, V, SZ, U32, V],
+    "tg_merkle_tree_dev": [V, V, SZ, V, V],
+    "tg_column_merge_dev": [V, V, SZ, U64, V, V],
+    "tg_commit_unmasked_dev": [V, U32, U32, U32, V, V, SZ, V, V, V, V],
+    "tg_commit_unmasked": [V, U32, U32, U32, V, V, SZ, V, V],
+    "tg_merge_segments": [V, V, SZ, U64, V, V],
+    "tg_advice_sink_open": [V, U32, U32, U32, U32, V, V],
+    "tg_sink_absorb": [V, V, SZ, V],
+    "tg_sink_finish": [V, V],
+    "tg_sink_close": [V],
+    "tg_matrix_open": [V, U32, U32, U32, V, V, SZ, V],
+    "tg_matrix_absorb": [V, V, SZ, V],
+    "tg_matrix_finish": [V, V],
+    "tg_matrix_close": [V],
+    "tg_hash": [CSTR, V, SZ, V],
+    "tg_transcript_init": [V, V, SZ],
+    "tg_transcript_absorb": [V, CSTR, V, SZ],
+    "tg_transcript_absorb_fp2s": [V, CSTR, V, SZ],
+    "tg_transcript_squeeze": [V, CSTR, V],
+    "tg_transcript_challenge_fp": [V, CSTR, V],
+    "tg_transcript_challenge_fp2": [V, CSTR, V],
+    "tg_transcript_challenge_indices": [V, CSTR, U32, U32, V],
+    "tg_transcript_check_grind": [V, CSTR, U32, U64, V],
+    "tg_transcript_grind": [V, V, CSTR, U32, V],
+    "tg_prove_batch": [V, V, CSTR, INT, V, INT, INT, V, V, V, V, V],
+    "tg_level_load": [V, INT, V, V, INT, SZ, V],
+    "tg_level_sums": [V, V, V, SZ, U32, V],
+    "tg_level_bind": [V, V],
+    "tg_level_firsts": [V, V],
+    "tg_level_free": [V],
+}
+_RESTYPE = {"tg_last_error": ctypes.c_char_p}
+
+
+def lib():
+    """The loaded library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(
+                f"libtessera_gb300 is not built ({LIB_PATH} missing): run "
+                "`python -c 'import tessera_gb300.build as b; b.build()'` with the CUDA toolkit")
+        L = ctypes.CDLL(str(LIB_PATH))
+        for name, args in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = _RESTYPE.get(name, ctypes.c_int)
+        _lib = L
+    return _lib
+
+
+def check(rc: int) -> int:
+    """Raises for a negative status; returns TG_OK or TG_DECLINED."""
+    if rc < 0:
+        msg = lib().tg_last_error().decode(errors="replace")
+        cls = InvalidInput if rc == TG_ERR_INVALID else TesseraError
+        raise cls(rc, msg)
+    return rc
+
+
+def call(name: str, *args) -> int:
+    return check(getattr(lib(), name)(*args))

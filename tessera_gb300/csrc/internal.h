@@ -1,0 +1,104 @@
+// SPDX-License-Identifier: Apache-2.0 OR MIT
+//
+// Internal host-side declarations shared by the translation units of libtessera_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <atomic>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/tessera_gb300.h"
+
+namespace tg {
+
+// Records the failure message for tg_last_error() (thread-local) and returns `code`.
+int fail(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define TG_CUDA(call)                                      \
+    do {                                                   \
+        cudaError_t e_ = (call);                           \
+        if (e_ != cudaSuccess) return tg::cuda_fail(e_, #call); \
+    } while (0)
+
+// A device buffer that grows on demand and is freed with its owner.
+struct DevBuf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+    int ensure(size_t want);
+    void release();
+    ~DevBuf() { release(); }
+};
+
+// Twiddle tables for one codeword length n = 2^lgn and message length k = 2^lgk:
+// pw[m] = ω_n^m for m < n, and pow7k[i] = 7^i / k for i < k. Built once and kept on the device.
+struct Tables {
+    uint32_t lgn = 0, lgk = 0;
+    uint64_t* pw = nullptr;
+    uint64_t* pow7k = nullptr;
+};
+
+// Per-kernel timing on the launching stream: when enabled, each launch is bracketed by a pair of
+// CUDA events; tg_profile_read sums their elapsed times by kernel name.
+struct ProfRec {
+    const char* name;
+    cudaEvent_t begin, end;
+    uint64_t units;  // work units of the launch (rows, columns, pairs), for per-unit rates
+};
+
+struct Device {
+    int ordinal = 0;
+    cudaStream_t stream = nullptr;
+    int sm_count = 0;
+    size_t smem_optin = 0;
+    std::mutex mu;  // guards the caches and the shared scratch below
+    std::map<uint64_t, Tables> tables;
+    DevBuf scratch_y, scratch_z, scratch_misc;
+    DevBuf err;  // device error words for bounded waits
+    tg_config cfg;
+    std::atomic<uint64_t> launches{0};  // kernels this handle has launched
+    bool prof_on = false;
+    std::mutex prof_mu;
+    std::vector<ProfRec> prof;
+    std::vector<cudaEvent_t> event_pool;
+    // Returns the tables for (lgn, lgk), building them on first use.
+    int get_tables(uint32_t lgn, uint32_t lgk, const Tables** out);
+};
+
+cudaStream_t pick_stream(Device* d, void* stream);
+
+// Brackets the kernel launches of one logical kernel on stream s: counts them, and records
+// events around them while profiling is on.
+struct Launch {
+    Device* d;
+    cudaStream_t s;
+    int idx = -1;
+    Launch(Device* d, cudaStream_t s, const char* name, uint64_t nkernels, uint64_t units);
+    ~Launch();
+};
+
+// ---- LDE (lde.cu) ---------------------------------------------------------------------------
+// Encodes npolys rows of k = 2^lgk values (device, row-major) into codewords of n = 2^(lgk+lgr)
+// symbols (device, row-major), with P mask coefficients per row (device, may be null for P = 0).
+int lde_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P, const uint64_t* rows, size_t npolys,
+               const uint64_t* masks, uint64_t* codewords, cudaStream_t s);
+
+// ---- hashing (hash.cu) ----------------------------------------------------------------------
+// Context keys of the domains the hot path uses, derived on the host.
+void context_key(const char* name, uint32_t key[8]);
+int column_init(Device* d, const uint8_t id[32], uint64_t ncols, uint8_t* chains, cudaStream_t s);
+// Absorbs `count` rows (row-major, count x ncols, row stride `ld` symbols) in blocks of
+// `block` rows into the chains.
+int column_absorb(Device* d, uint8_t* chains, uint64_t ncols, const uint64_t* rows, size_t ld, size_t count,
+                  uint32_t block, cudaStream_t s);
+int merkle_tree(Device* d, const uint8_t* leaves, size_t n, uint8_t* nodes, cudaStream_t s);
+int column_merge(Device* d, const uint8_t* segs, size_t nseg, uint64_t n, uint8_t* leaves, cudaStream_t s);
+
+// ---- host BLAKE3 and transcript (host.cpp) --------------------------------------------------
+void host_hash(const uint32_t key[8], const uint8_t* in, size_t len, uint8_t out[32]);
+
+}  // namespace tg
