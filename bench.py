@@ -213,7 +213,8 @@ def run_gpu(args) -> None:
     rows_d = rows_h.to(cuda)
     tabs_d = [t.to(cuda) for t in tabs_h]
     n = 1 << (LOG_K + LOG_R)
-    cw_d = torch.empty(NPOLYS * n, dtype=torch.int64, device=cuda)
+    npolys = COMMITTED >> LOG_K
+    cw_d = torch.empty(npolys * n, dtype=torch.int64, device=cuda)
     nodes_d = torch.empty((2 * n - 1) * 32, dtype=torch.uint8, device=cuda)
     rows_e = torch.empty_like(rows_d)  # e2e staging
     tabs_e = [torch.empty_like(t) for t in tabs_d]
@@ -222,7 +223,7 @@ def run_gpu(args) -> None:
     root = ctypes.create_string_buffer(32)
 
     def commit(src):
-        N.call("tg_commit_unmasked_dev", dev.handle, LOG_K, LOG_R, ROW_BLOCK, cid, ctypes.c_void_p(src.data_ptr()), NPOLYS,
+        N.call("tg_commit_unmasked_dev", dev.handle, LOG_K, LOG_R, ROW_BLOCK, cid, ctypes.c_void_p(src.data_ptr()), npolys,
                ctypes.c_void_p(cw_d.data_ptr()), ctypes.c_void_p(nodes_d.data_ptr()), root, None)
 
     def sumcheck(tabs):
@@ -297,6 +298,11 @@ def run_gpu(args) -> None:
         e2e_ms = float(tt.item())
     h2d = COMMITTED * 8 + 3 * (1 << SC_VARS) * 8
     d2h = 32 + SC_VARS * SC_DEGREE * 16 + 3 * 16
+    # Release torch's buffers while the library's stream (which their copies used) still exists.
+    stream.synchronize()
+    del rows_h, tabs_h, rows_d, tabs_d, cw_d, nodes_d, rows_e, tabs_e
+    torch.cuda.synchronize()
+    dev.close()
 
     if rank != 0:
         return
@@ -356,7 +362,15 @@ def main():
     ap.add_argument("--cpu-polys", type=int, default=32, help="rows in the CPU baseline's bounded sample")
     ap.add_argument("--ref-polys", type=int, default=32, help="rows per step in the reference arm's sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--polys", type=int, default=NPOLYS,
+                    help="rows committed per step (a smaller case for profiler captures; the headline uses 256)")
     args = ap.parse_args()
+    if args.polys != NPOLYS:
+        global COMMITTED, UNITS
+        COMMITTED = args.polys << LOG_K
+        UNITS = COMMITTED + SUMCHECKED
+        CONFIG["polys"] = args.polys
+        CONFIG["workload"] = CONFIG["workload"].replace("commit 256", f"commit {args.polys}")
     if args.impl == "reference":
         run_reference(args)
     else:
