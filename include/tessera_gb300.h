@@ -79,6 +79,16 @@ int tg_encode_rows_dev(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, ui
                        void *stream);
 int tg_encode_rows(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t mask_coeffs,
                    const uint64_t *rows, size_t nrows, const uint64_t *masks, uint64_t *codewords);
+/* tg_encode_rows_dev without any device allocation, for callers that cannot call cudaMalloc
+ * (device memory owned by another allocator, or a loop that must not synchronize the device as
+ * cudaMalloc/cudaFree do). No counterpart in the reference. Tables and scratch live in one fixed
+ * 32 MiB device array that every GPU loading the library holds until exit; shapes need
+ * 2 (k + n) <= 2^22 words (k <= 2^19 at rate 1/2) and larger ones are refused. The first call on a
+ * device looks up the array's address, so make it before any stream capture. Calls share the
+ * array: calls that overlap on the GPU race, so order them on one stream. */
+int tg_encode_rows_noalloc_dev(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t mask_coeffs,
+                               const uint64_t *rows, size_t nrows, const uint64_t *masks, uint64_t *codewords,
+                               void *stream);
 
 /* ---- Column chains and Merkle trees (crates/tessera-hash/src/columns.rs:72-104,
  * crates/tessera-hash/src/merkle.rs:93-113). chains: ncols x 32 bytes. */

@@ -61,6 +61,7 @@ SIGNATURES = {
     "tg_profile_read": [V, V, SZ, V, V, V, SZ, V],
     "tg_encode_rows_dev": [V, U32, U32, U32, V, SZ, V, V, V],
     "tg_encode_rows": [V, U32, U32, U32, V, SZ, V, V],
+    "tg_encode_rows_noalloc_dev": [V, U32, U32, U32, V, SZ, V, V, V],
     "tg_column_init_dev": [V, V, U64, V, V],
     "tg_column_absorb_dev": [V, V, U64, V, SZ, U32, V],
     "tg_merkle_tree_dev": [V, V, SZ, V, V],

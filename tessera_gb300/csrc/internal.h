@@ -87,6 +87,12 @@ struct Launch {
 int lde_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P, const uint64_t* rows, size_t npolys,
                const uint64_t* masks, uint64_t* codewords, cudaStream_t s);
 
+// The same encoder over caller-owned tables (pw: n words, pow7k: k words; rebuilt when
+// build_tables) and scratch (y: group x k words, z: group x n words); allocates nothing.
+int lde_encode_into(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P, const uint64_t* rows, size_t npolys,
+                    const uint64_t* masks, uint64_t* codewords, cudaStream_t s, uint64_t* pw, uint64_t* pow7k,
+                    bool build_tables, uint64_t* y, uint64_t* z, size_t group);
+
 // ---- hashing (hash.cu) ----------------------------------------------------------------------
 // Context keys of the domains the hot path uses, derived on the host.
 void context_key(const char* name, uint32_t key[8]);

@@ -415,3 +415,100 @@ int lde_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_
 }
 
 }  // namespace tg
+
+namespace tg {
+
+// The encoder over caller-owned tables and scratch, for the allocation-free entry point: it
+// launches the same kernels as lde_encode but allocates nothing. When `build_tables` is set it
+// first writes pw (n words, ω_n^m) and pow7k (k words, 7^i/k) on stream s; y and z hold
+// `group` rows of scratch (k and n words per row).
+int lde_encode_into(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_t* rows, size_t npolys,
+                    const uint64_t* masks, uint64_t* codewords, cudaStream_t s, uint64_t* pw, uint64_t* pow7k,
+                    bool build_tables, uint64_t* y, uint64_t* z, size_t group) {
+    const uint32_t lgn = lgk + lgr;
+    const uint64_t k = 1ull << lgk, n = 1ull << lgn;
+    if (build_tables) {
+        const uint32_t cl = 6;
+        const size_t threads_n = (n + (1u << cl) - 1) >> cl, threads_k = (k + (1u << cl) - 1) >> cl;
+        Launch L(d, s, "tables", 2, n + k);
+        fill_powers<<<(unsigned)((threads_n + 255) / 256), 256, 0, s>>>(pw, n, root_of_unity(lgn), 1, cl);
+        fill_powers<<<(unsigned)((threads_k + 255) / 256), 256, 0, s>>>(pow7k, k, 7, inv(k % P), cl);
+        TG_CUDA(cudaGetLastError());
+    }
+    if (npolys == 0) return TG_OK;
+    LdeArgs a = {};
+    a.pw = pw;
+    a.pow7k = pow7k;
+    a.lgk = (int)lgk;
+    a.lgr = (int)lgr;
+    a.P = (int)P_;
+    const uint64_t pow7_k = pow(7, k);
+    const uint64_t w_r = root_of_unity(lgr);
+    uint64_t we = 1;
+    for (int e = 0; e < (1 << lgr); e++) {
+        a.mk[e] = mul(k % P, sub(mul(pow7_k, we), 1));
+        we = mul(we, w_r);
+    }
+    const int limit = smem_limit(d);
+    if (lgk <= 11) {
+        const size_t K = (size_t)1 << lgk;
+        const size_t smem = (2 * K + 2 * std::max<size_t>(K / 2, 1)) * 8;
+        TG_CUDA(cudaFuncSetAttribute(lde_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const int threads = (int)std::min<size_t>(512, std::max<size_t>(32, K / 2));
+        for (size_t r0 = 0; r0 < npolys; r0 += 65535) {
+            const size_t g = std::min<size_t>(65535, npolys - r0);
+            a.rows = rows + (r0 << lgk);
+            a.masks = masks ? masks + r0 * P_ : nullptr;
+            a.out = codewords + (r0 << lgn);
+            Launch L(d, s, "lde_small", 1, g);
+            lde_small<<<(unsigned)g, threads, smem, s>>>(a);
+        }
+        TG_CUDA(cudaGetLastError());
+        return TG_OK;
+    }
+    a.lgk1 = (int)(lgk + 1) / 2;
+    a.lgk2 = (int)lgk / 2;
+    const size_t K1 = (size_t)1 << a.lgk1, K2 = (size_t)1 << a.lgk2;
+    const size_t R = (size_t)1 << lgr;
+    int lgw_a = 4, lgw_m = 3, lgw_c = 3;
+    while (lgw_a > 0 && ((K2 << lgw_a) * 8 > 128 * 1024)) lgw_a--;
+    while (lgw_m > 0 && (2 * ((K1 + 1) << lgw_m) * 8 + K1 * 8 > (size_t)limit)) lgw_m--;
+    while (lgw_c > 0 && (R * ((K2 + 1) << lgw_c) * 8 + K2 * 4 > (size_t)limit)) lgw_c--;
+    const size_t smem_a = ((K2 << lgw_a) + K2 / 2) * 8;
+    const size_t smem_m = (2 * ((K1 + 1) << lgw_m) + K1) * 8;
+    const size_t smem_c = (R * ((K2 + 1) << lgw_c) + K2 / 2) * 8;
+    if (smem_m > (size_t)limit || smem_c > (size_t)limit)
+        return fail(TG_ERR_INVALID, "row length 2^%u at rate 1/2^%u exceeds shared memory", lgk, lgr);
+    TG_CUDA(cudaFuncSetAttribute(lde_pass_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a));
+    TG_CUDA(cudaFuncSetAttribute(lde_pass_m, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_m));
+    TG_CUDA(cudaFuncSetAttribute(lde_pass_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
+    if (group < 1) return fail(TG_ERR_INVALID, "no scratch for one row");
+    group = std::min<size_t>(group, 65535);
+    a.y = y;
+    a.z = z;
+    for (size_t r0 = 0; r0 < npolys; r0 += group) {
+        const unsigned g = (unsigned)std::min(group, npolys - r0);
+        a.rows = rows + (r0 << lgk);
+        a.masks = masks ? masks + r0 * P_ : nullptr;
+        a.out = codewords + (r0 << lgn);
+        a.lgw = lgw_a;
+        {
+            Launch L(d, s, "lde_pass_a", 1, g);
+            lde_pass_a<<<dim3((unsigned)(K1 >> lgw_a), g), 512, smem_a, s>>>(a);
+        }
+        a.lgw = lgw_m;
+        {
+            Launch L(d, s, "lde_pass_m", 1, g);
+            lde_pass_m<<<dim3((unsigned)(K2 >> lgw_m), g), 512, smem_m, s>>>(a);
+        }
+        a.lgw = lgw_c;
+        {
+            Launch L(d, s, "lde_pass_c", 1, g);
+            lde_pass_c<<<dim3((unsigned)(K1 >> lgw_c), g), 512, smem_c, s>>>(a);
+        }
+    }
+    TG_CUDA(cudaGetLastError());
+    return TG_OK;
+}
+
+}  // namespace tg
