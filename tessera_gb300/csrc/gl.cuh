@@ -113,3 +113,111 @@ __host__ __device__ __forceinline__ uint64_t mul_small(uint64_t x, uint32_t k) {
 }
 
 }  // namespace tg
+
+// ---- lazy arithmetic for the transforms --------------------------------------------------------
+//
+// Values are any 64-bit word x, standing for x mod p (so both x and x − p may appear); sums and
+// products fold every carry out of bit 64 back in as 2^64 = 2^32 − 1 with the carry flag, and a
+// value is made canonical once, when it leaves a transform. Every function here is exact for all
+// 64-bit inputs.
+namespace tg {
+namespace lz {
+
+__device__ __forceinline__ uint32_t lo32(uint64_t x) { return (uint32_t)x; }
+__device__ __forceinline__ uint32_t hi32(uint64_t x) { return (uint32_t)(x >> 32); }
+__device__ __forceinline__ uint64_t mk64(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
+// c·(2^64 mod p) for a carry c ∈ {0, 1}, as a 64-bit word.
+__device__ __forceinline__ uint64_t eps_if(uint32_t c) { return (uint64_t)(uint32_t)(-(int32_t)c); }
+
+__device__ __forceinline__ uint64_t add(uint64_t a, uint64_t b) {
+    uint64_t s;
+    uint32_t c, c2;
+    asm("add.cc.u64 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=l"(s), "=r"(c) : "l"(a), "l"(b));
+    // a second carry needs a + b ≥ 2^64 + p, possible only for inputs at or above p
+    asm("add.cc.u64 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=l"(s), "=r"(c2) : "l"(s), "l"(eps_if(c)));
+    return s + eps_if(c2);
+}
+
+__device__ __forceinline__ uint64_t sub(uint64_t a, uint64_t b) {
+    uint64_t d;
+    uint32_t br, br2;  // 0xFFFFFFFF on a borrow, which is 2^64 mod p as a word
+    asm("sub.cc.u64 %0, %2, %3;\n\tsubc.u32 %1, 0, 0;" : "=l"(d), "=r"(br) : "l"(a), "l"(b));
+    asm("sub.cc.u64 %0, %2, %3;\n\tsubc.u32 %1, 0, 0;" : "=l"(d), "=r"(br2) : "l"(d), "l"((uint64_t)br));
+    return d - (uint64_t)br2;
+}
+
+// (lo + hl·2^64 + hh·2^96) mod p for hl, hh < 2^32: lo + hl·(2^32 − 1) − hh, the product on the
+// multiply pipe with its carry.
+__device__ __forceinline__ uint64_t fold(uint64_t lo, uint32_t hl, uint32_t hh) {
+    uint32_t r0, r1, c;
+    asm("mad.lo.cc.u32 %0, %3, 0xFFFFFFFF, %4;\n\t"
+        "madc.hi.cc.u32 %1, %3, 0xFFFFFFFF, %5;\n\t"
+        "addc.u32 %2, 0, 0;"
+        : "=r"(r0), "=r"(r1), "=r"(c)
+        : "r"(hl), "r"(lo32(lo)), "r"(hi32(lo)));
+    uint64_t d;
+    uint32_t br;
+    asm("sub.cc.u64 %0, %2, %3;\n\tsubc.u32 %1, 0, 0;" : "=l"(d), "=r"(br) : "l"(mk64(r0, r1)), "l"((uint64_t)hh));
+    // carry and borrow: +2^64 and −2^64 cancel; one alone adds or removes 2^32 − 1 without wrapping
+    return d + eps_if(c) - (uint64_t)br;
+}
+
+// (lo + h·2^64) mod p for h < 2^32: lo + h·(2^32 − 1).
+__device__ __forceinline__ uint64_t fold_lo(uint64_t lo, uint32_t h) {
+    uint32_t r0, r1, c;
+    asm("mad.lo.cc.u32 %0, %3, 0xFFFFFFFF, %4;\n\t"
+        "madc.hi.cc.u32 %1, %3, 0xFFFFFFFF, %5;\n\t"
+        "addc.u32 %2, 0, 0;"
+        : "=r"(r0), "=r"(r1), "=r"(c)
+        : "r"(h), "r"(lo32(lo)), "r"(hi32(lo)));
+    // with a carry, the word is below h·(2^32 − 1) < 2^64 − 2^33: adding 2^32 − 1 cannot wrap
+    return mk64(r0, r1) + eps_if(c);
+}
+
+// x·2^E for 0 ≤ E < 96.
+template <int E>
+__device__ __forceinline__ uint64_t mulp2(uint64_t x) {
+    static_assert(E >= 0 && E < 96, "shift exponent");
+    if constexpr (E == 0) {
+        return x;
+    } else if constexpr (E <= 32) {
+        return fold_lo(x << E, (uint32_t)(x >> (64 - E)));
+    } else if constexpr (E < 64) {
+        const uint64_t hi = x >> (64 - E);
+        return fold(x << E, lo32(hi), hi32(hi));
+    } else {
+        // x·2^64 ≡ x0·2^32 − (x0 + x1), x = x0 + 2^32·x1; then ·2^(E−64)
+        const uint32_t x0 = lo32(x), x1 = hi32(x);
+        uint64_t y;
+        uint32_t br;
+        asm("sub.cc.u64 %0, %2, %3;\n\tsubc.u32 %1, 0, 0;"
+            : "=l"(y), "=r"(br)
+            : "l"((uint64_t)x0 << 32), "l"((uint64_t)x0 + x1));
+        return mulp2<E - 64>(y - (uint64_t)br);
+    }
+}
+
+// a·b: the 128-bit product in 32-bit multiply-add carry chains, then fold.
+__device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) {
+    uint32_t r0, r1, r2, r3;
+    asm("{\n\t"
+        "mul.lo.u32 %0, %4, %6;\n\t"
+        "mul.hi.u32 %1, %4, %6;\n\t"
+        "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
+        "madc.hi.u32 %2, %4, %7, 0;\n\t"
+        "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
+        "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
+        "madc.hi.u32 %3, %5, %7, 0;\n\t"
+        "mad.lo.cc.u32 %2, %5, %7, %2;\n\t"
+        "addc.u32 %3, %3, 0;\n\t"
+        "}"
+        : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
+        : "r"(lo32(a)), "r"(hi32(a)), "r"(lo32(b)), "r"(hi32(b)));
+    return fold(mk64(r0, r1), r2, r3);
+}
+
+// The canonical representative.
+__device__ __forceinline__ uint64_t canon(uint64_t x) { return x >= P ? x - P : x; }
+
+}  // namespace lz
+}  // namespace tg

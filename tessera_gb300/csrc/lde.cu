@@ -26,6 +26,7 @@
 
 #include "gl.cuh"
 #include "internal.h"
+#include "lde_fast.cuh"
 
 namespace tg {
 
@@ -312,6 +313,104 @@ int Device::get_tables(uint32_t lgn, uint32_t lgk, const Tables** out) {
     return TG_OK;
 }
 
+// ---- register-resident passes (lde_fast.cuh) for 2^14 <= k <= 2^20 ---------------------------
+
+static int set_smem(const void* fn, int words) {
+    TG_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, words * 8));
+    return TG_OK;
+}
+
+// Launches pass `which` (0 = A, 1 = M1, 2 = M2, 3 = C) for a column length 2^lg.
+static int fast_pass(int which, int lg, dim3 grid, const fast::Args& a, cudaStream_t s) {
+    using namespace fast;
+#define TG_FAST_CASE(LG, RA, RB)                                                                   \
+    case LG: {                                                                                     \
+        const void* fns[4] = {(const void*)pass_a<RA, RB>, (const void*)pass_m1<RA, RB>,          \
+                              (const void*)pass_m2<RA, RB>, (const void*)pass_c<RA, RB>};          \
+        const int words = Shape<RA, RB>::WORDS + RA * RB;                                          \
+        int rc = set_smem(fns[which], words);                                                      \
+        if (rc) return rc;                                                                         \
+        if (which == 0) pass_a<RA, RB><<<grid, THREADS, words * 8, s>>>(a);                        \
+        else if (which == 1) pass_m1<RA, RB><<<grid, THREADS, words * 8, s>>>(a);                  \
+        else if (which == 2) pass_m2<RA, RB><<<grid, THREADS, words * 8, s>>>(a);                  \
+        else pass_c<RA, RB><<<grid, THREADS, words * 8, s>>>(a);                                   \
+        return TG_OK;                                                                              \
+    }
+    switch (lg) {
+        TG_FAST_CASE(6, 8, 8)
+        TG_FAST_CASE(7, 16, 8)
+        TG_FAST_CASE(8, 16, 16)
+        TG_FAST_CASE(9, 32, 16)
+        TG_FAST_CASE(10, 32, 32)
+        default:
+            return fail(TG_ERR_INVALID, "no register-resident transform of length 2^%d", lg);
+    }
+#undef TG_FAST_CASE
+}
+
+static bool fast_shape(uint32_t lgk) { return lgk >= 13 && lgk <= 20; }
+
+// Encodes rows in groups through the three register-resident passes; y/z hold `group` rows.
+static int fast_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_t* rows, size_t npolys,
+                       const uint64_t* masks, uint64_t* codewords, cudaStream_t s, const uint64_t* pw,
+                       const uint64_t* pow7k, uint64_t* y, uint64_t* z, size_t group) {
+    fast::Args a = {};
+    a.pw = pw;
+    a.pow7k = pow7k;
+    a.lgk = (int)lgk;
+    a.lgr = (int)lgr;
+    a.P = (int)P_;
+    a.lgk1 = (int)(lgk + 1) / 2;
+    a.lgk2 = (int)lgk / 2;
+    a.y = y;
+    a.z = z;
+    const uint32_t lgn = lgk + lgr;
+    const uint64_t k = 1ull << lgk;
+    const uint64_t pow7_k = pow(7, k);
+    const uint64_t w_r = root_of_unity(lgr), w_n = root_of_unity(lgn);
+    // pass M's chain step s_e^{K2·RB}, RB the second radix of the length-K1 transform
+    const int lg1 = a.lgk1;
+    const int rb = lg1 == 6 ? 8 : lg1 == 7 ? 8 : lg1 == 8 ? 16 : lg1 == 9 ? 16 : 32;
+    const uint64_t m = (uint64_t)rb << a.lgk2;
+    uint64_t we = 1;
+    for (int e = 0; e < (1 << lgr); e++) {
+        a.mk[e] = mul(k % P, sub(mul(pow7_k, we), 1));
+        a.sstep[e] = mul(pow(7, m), pow(w_n, ((uint64_t)e * m) & ((1ull << lgn) - 1)));
+        we = mul(we, w_r);
+    }
+    const size_t tiles = k / fast::TILE;
+    group = std::min<size_t>(std::max<size_t>(group, 1), 65535);
+    for (size_t r0 = 0; r0 < npolys; r0 += group) {
+        const unsigned g = (unsigned)std::min(group, npolys - r0);
+        a.rows = rows + (r0 << lgk);
+        a.masks = masks ? masks + r0 * P_ : nullptr;
+        a.out = codewords + (r0 << lgn);
+        int rc;
+        {
+            Launch L(d, s, "lde_pass_a", 1, g);
+            rc = fast_pass(0, a.lgk2, dim3((unsigned)tiles, g), a, s);
+        }
+        if (rc) return rc;
+        {
+            Launch L(d, s, "lde_pass_m1", 1, g);
+            rc = fast_pass(1, a.lgk1, dim3((unsigned)tiles, g), a, s);
+        }
+        if (rc) return rc;
+        {
+            Launch L(d, s, "lde_pass_m2", 1, g);
+            rc = fast_pass(2, a.lgk1, dim3((unsigned)(tiles << lgr), g), a, s);
+        }
+        if (rc) return rc;
+        {
+            Launch L(d, s, "lde_pass_c", 1, g);
+            rc = fast_pass(3, a.lgk2, dim3((unsigned)(tiles << lgr), g), a, s);
+        }
+        if (rc) return rc;
+    }
+    TG_CUDA(cudaGetLastError());
+    return TG_OK;
+}
+
 // ---- launcher --------------------------------------------------------------------------------
 
 static int smem_limit(Device* d) { return (int)std::min<size_t>(d->smem_optin, 227 * 1024); }
@@ -361,6 +460,17 @@ int lde_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_
         return TG_OK;
     }
 
+    if (fast_shape(lgk)) {
+        const size_t per_row_fast = (k + (k << lgr)) * 8;
+        size_t gfast = std::max<size_t>(1, d->cfg.lde_group_bytes / per_row_fast);
+        gfast = std::min<size_t>(gfast, std::min<size_t>(npolys, 65535));
+        rc = d->scratch_y.ensure(gfast * k * 8);
+        if (rc) return rc;
+        rc = d->scratch_z.ensure(gfast * (k << lgr) * 8);
+        if (rc) return rc;
+        return fast_encode(d, lgk, lgr, P_, rows, npolys, masks, codewords, s, t->pw, t->pow7k,
+                           (uint64_t*)d->scratch_y.ptr, (uint64_t*)d->scratch_z.ptr, gfast);
+    }
     a.lgk1 = (int)(lgk + 1) / 2;
     a.lgk2 = (int)lgk / 2;
     const size_t K1 = (size_t)1 << a.lgk1, K2 = (size_t)1 << a.lgk2;
@@ -465,6 +575,10 @@ int lde_encode_into(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const ui
         }
         TG_CUDA(cudaGetLastError());
         return TG_OK;
+    }
+    if (fast_shape(lgk)) {
+        if (group < 1) return fail(TG_ERR_INVALID, "no scratch for one row");
+        return fast_encode(d, lgk, lgr, P_, rows, npolys, masks, codewords, s, pw, pow7k, y, z, group);
     }
     a.lgk1 = (int)(lgk + 1) / 2;
     a.lgk2 = (int)lgk / 2;

@@ -1,0 +1,384 @@
+// SPDX-License-Identifier: Apache-2.0 OR MIT
+//
+// The encoder's four passes with register-resident sub-transforms (2^13 ≤ k ≤ 2^20).
+//
+// With k = K1·K2 and the codeword interleaving the 2^r cosets s_e·H (symbol q·2^r + e is
+// NTT_k(c_e)[q], c_e[i] = s_e^i·(a_i + m_i (s_e^k − 1)), a = iNTT_k(row)):
+//
+//   pass A   inverse length-K2 transforms down the strided columns t1, × ω_k^{−j2·t1}  → Y[j2][t1]
+//   pass M1  per column j2: inverse length-K1 transform; per coset the scale s_e^i/k (+ mask)
+//                                                                               → C_e[j1][j2]
+//   pass M2  per coset and column j2: forward length-K1 transform, × ω_k^{v2·j2} → Z_e[v2][j2]
+//            (written over C_e: a tile reads all of its columns before it writes)
+//   pass C   per coset and column v2: forward length-K2 transform, written interleaved into the
+//            codeword at (v2 + K1·v1)·2^r + e
+//
+// A column transform of length L = RA·RB runs in two rounds. Round 1: each thread takes RA/T
+// sub-transforms of length RB (T = L/32 threads per column, 32 elements per thread) over the
+// strided elements ta + RA·tb, multiplies output kb by w^{ta·kb}, and parks the results in shared
+// memory. Round 2: each thread takes RB/T sub-transforms of length RA over ta for its kb. The
+// sub-transforms are radix-2 butterflies fully unrolled in registers whose twiddles are powers of
+// ω_R for R ≤ 32, which in Goldilocks are powers of two (ω_32 = 2^78, ω_16 = 2^156, ω_8 = 2^120,
+// ω_4 = 2^48, ω_2 = 2^96 = −1, exponents mod 192): a twiddle is a shift and a fold, never a 64 x 64
+// product. All arithmetic is lazy (tg::lz): values stay any 64-bit word until the codeword is
+// written, and every carry is folded with the carry flag.
+//
+// A CTA holds an 8,192-element tile (W = 8192/L columns, 64 KiB of shared memory) with 256
+// threads, so that two CTAs share an SM and one's loads overlap the other's arithmetic. Each
+// round maps threads to columns so that its global accesses are coalesced: when the column's
+// elements are contiguous in memory the warp runs along the column ("q-fast"), when the
+// columns are contiguous the warp runs across columns ("c-fast"); Shape::slot keeps both
+// mappings free of shared-memory bank conflicts.
+#pragma once
+#include <stdint.h>
+
+#include <utility>
+
+#include "gl.cuh"
+
+namespace tg {
+namespace fast {
+
+constexpr int TILE = 8192;
+constexpr int THREADS = 256;
+
+template <typename F, int... Is>
+__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, Is...>) {
+    (f(std::integral_constant<int, Is>{}), ...);
+}
+template <int N, typename F>
+__device__ __forceinline__ void static_for(F&& f) {
+    static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+constexpr int ilog2(int x) { return x <= 1 ? 0 : 1 + ilog2(x >> 1); }
+constexpr int brev_c(int x, int bits) {
+    int r = 0;
+    for (int b = 0; b < bits; b++) r |= ((x >> b) & 1) << (bits - 1 - b);
+    return r;
+}
+
+// ω_R = 2^root_exp(R) (mod p), ω_R = 7^((p−1)/R).
+constexpr int root_exp(int R) {
+    return R == 1 ? 0 : R == 2 ? 96 : R == 4 ? 48 : R == 8 ? 120 : R == 16 ? 156 : R == 32 ? 78 : 39;
+}
+// The exponent of ω_R^{±m}, in [0, 192).
+constexpr int tw_exp(int R, int m, bool inverse) {
+    const int e = (m * root_exp(R)) % 192;
+    return inverse ? (192 - e) % 192 : e;
+}
+
+// Gentleman–Sande butterfly with twiddle 2^E, E in [0, 192): (a, b) → (a + b, (a − b)·2^E).
+template <int E>
+__device__ __forceinline__ void bf_gs(uint64_t& a, uint64_t& b) {
+    const uint64_t s = lz::add(a, b);
+    if constexpr (E >= 96)
+        b = lz::mulp2<E - 96>(lz::sub(b, a));
+    else
+        b = lz::mulp2<E>(lz::sub(a, b));
+    a = s;
+}
+
+// Cooley–Tukey butterfly with twiddle 2^E: (a, b) → (a + b·2^E, a − b·2^E).
+template <int E>
+__device__ __forceinline__ void bf_ct(uint64_t& a, uint64_t& b) {
+    if constexpr (E >= 96) {
+        const uint64_t t = lz::mulp2<E - 96>(b);  // b·2^E = −t
+        b = lz::add(a, t);
+        a = lz::sub(a, t);
+    } else {
+        const uint64_t t = lz::mulp2<E>(b);
+        b = lz::sub(a, t);
+        a = lz::add(a, t);
+    }
+}
+
+// Length-R transform of x[BASE + i], i < R, with root ω_R^{±1}: natural order in, bit-reversed
+// order out (position p holds X[rev(p)]).
+template <int R, bool INV, int BASE, int N>
+__device__ __forceinline__ void dft_dif(uint64_t (&x)[N]) {
+    static_for<ilog2(R)>([&](auto s_) {
+        constexpr int s = decltype(s_)::value;
+        constexpr int h = R >> (s + 1);
+        static_for<R / 2>([&](auto b_) {
+            constexpr int b = decltype(b_)::value;
+            constexpr int o = b % h, g = b / h;
+            constexpr int i0 = g * 2 * h + o;
+            bf_gs<tw_exp(R, o << s, INV)>(x[BASE + i0], x[BASE + i0 + h]);
+        });
+    });
+}
+
+struct Args {
+    const uint64_t* rows;
+    const uint64_t* masks;
+    uint64_t* y;            // k words per row
+    uint64_t* z;            // n words per row: C_e, then Z_e in place
+    uint64_t* out;
+    const uint64_t* pw;     // ω_n^m, m < n
+    const uint64_t* pow7k;  // 7^i / k
+    uint64_t mk[16];        // k (s_e^k − 1)
+    uint64_t sstep[16];     // s_e^{K2·RB1}: the scale's step along a thread's elements in pass M1
+    int lgk, lgr, lgk1, lgk2, P;
+};
+
+// ω_L^{±m} from pw (n = 2^lgn ≥ L = 2^lg).
+__device__ __forceinline__ uint64_t rootp(const uint64_t* pw, int lgn, int lg, uint64_t m, bool inverse) {
+    const uint64_t n = 1ull << lgn;
+    uint64_t e = (m & ((1ull << lg) - 1)) << (lgn - lg);
+    if (inverse) e = (n - e) & (n - 1);
+    return pw[e];
+}
+
+template <int RA, int RB>
+struct Shape {
+    static constexpr int L = RA * RB;
+    static constexpr int T = L / 32;    // threads per column
+    static constexpr int W = TILE / L;  // columns per CTA
+    static constexpr int NA = RA / T;   // round-1 sub-transforms per thread (length RB)
+    static constexpr int NB = RB / T;   // round-2 sub-transforms per thread (length RA)
+    static_assert(L >= 32 && L <= 1024 && NA >= 1 && NB >= 1, "column length");
+    static_assert(W >= 8, "at least 8 columns per tile");
+    // Exchange slots. With W ≥ 16 columns a row of the tile spans every bank and the column is
+    // XORed with ta: a warp along a column (fixed c, 32 ta) and a warp across columns both hit
+    // 16 distinct 8-byte bank pairs. With W = 8 a row is half the banks: kb-planes are padded by
+    // 8 words so that rows of odd ta + kb take the other half, and the column is XORed with ta/2.
+    static constexpr int PAD = W >= 16 ? 0 : 8;
+    static constexpr int WORDS = RB * (RA * W + PAD);
+    __device__ static __forceinline__ int slot(int c, int ta, int kb) {
+        if constexpr (W >= 16)
+            return (kb * RA + ta) * W + (c ^ (ta & 15));
+        else
+            return kb * (RA * W + PAD) + ta * W + (c ^ ((ta >> 1) & 7));
+    }
+};
+
+// tw[kb·RA + ta] = ω_L^{±ta·kb}.
+template <int RA, int RB>
+__device__ __forceinline__ void fill_inner(uint64_t* tw, const uint64_t* pw, int lgn, bool inverse) {
+    constexpr int L = RA * RB;
+    for (int i = threadIdx.x; i < L; i += blockDim.x) {
+        const int kb = i / RA, ta = i % RA;
+        tw[i] = rootp(pw, lgn, ilog2(L), (uint64_t)ta * kb, inverse);
+    }
+}
+
+// Round-1 loads. c-fast: the tile's columns are adjacent words (column c at src + c) and element
+// t of a column at stride `es`. q-fast: column c starts at src + c·cs and its elements are adjacent.
+template <int RA, int RB>
+__device__ __forceinline__ void load_cfast(uint64_t (&v)[32], const uint64_t* src, size_t es, int c, int q) {
+    using S = Shape<RA, RB>;
+    static_for<S::NA>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        const int ta = q + S::T * i;
+        static_for<RB>([&](auto tb_) {
+            constexpr int tb = decltype(tb_)::value;
+            v[i * RB + tb] = src[c + (size_t)(ta + RA * tb) * es];
+        });
+    });
+}
+template <int RA, int RB>
+__device__ __forceinline__ void load_qfast(uint64_t (&v)[32], const uint64_t* src, size_t cs, int c, int q) {
+    using S = Shape<RA, RB>;
+    const uint64_t* col = src + (size_t)c * cs;
+    static_for<S::NA>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        const int ta = q + S::T * i;
+        static_for<RB>([&](auto tb_) {
+            constexpr int tb = decltype(tb_)::value;
+            v[i * RB + tb] = col[ta + RA * tb];
+        });
+    });
+}
+
+// Round 1: DIF of length RB on each loaded sub-transform, inner twiddle, park in shared memory.
+template <int RA, int RB, bool INV>
+__device__ __forceinline__ void round1_store(uint64_t (&v)[32], uint64_t* sm, const uint64_t* tw, int c, int q) {
+    using S = Shape<RA, RB>;
+    static_for<S::NA>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        dft_dif<RB, INV, i * RB>(v);
+        const int ta = q + S::T * i;
+        static_for<RB>([&](auto p_) {
+            constexpr int p = decltype(p_)::value;
+            constexpr int kb = brev_c(p, ilog2(RB));
+            const uint64_t val = kb == 0 ? v[i * RB + p] : lz::mul(v[i * RB + p], tw[kb * RA + ta]);
+            sm[S::slot(c, ta, kb)] = val;
+        });
+    });
+}
+
+// Round 2 (c-fast): v[i·RA + ta] = Y[ta][kb_i], kb_i = q + T·i, then DIF of length RA:
+// v[i·RA + p] holds output kb_i + RB·rev(p).
+template <int RA, int RB, bool INV>
+__device__ __forceinline__ void round2(uint64_t (&v)[32], const uint64_t* sm, int c, int q) {
+    using S = Shape<RA, RB>;
+    static_for<S::NB>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        const int kb = q + S::T * i;
+        static_for<RA>([&](auto ta_) {
+            constexpr int ta = decltype(ta_)::value;
+            v[i * RA + ta] = sm[S::slot(c, ta, kb)];
+        });
+        dft_dif<RA, INV, i * RA>(v);
+    });
+}
+
+// ---- pass A ------------------------------------------------------------------------------------
+template <int RA, int RB>
+__global__ void __launch_bounds__(THREADS, 2) pass_a(Args a) {
+    using S = Shape<RA, RB>;
+    extern __shared__ uint64_t sm[];
+    uint64_t* tw = sm + S::WORDS;
+    const int lgn = a.lgk + a.lgr;
+    fill_inner<RA, RB>(tw, a.pw, lgn, true);
+    const size_t row = blockIdx.y;
+    const int t1_0 = blockIdx.x * S::W;
+    const int K1 = 1 << a.lgk1;
+    const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast throughout
+    uint64_t v[32];
+    load_cfast<RA, RB>(v, a.rows + (row << a.lgk) + t1_0, K1, c, q);
+    __syncthreads();  // the twiddle table
+    round1_store<RA, RB, true>(v, sm, tw, c, q);
+    __syncthreads();
+    round2<RA, RB, true>(v, sm, c, q);
+    const uint32_t t1 = t1_0 + c;
+    uint64_t* y = a.y + (row << a.lgk) + t1;
+    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * t1, true);
+    static_for<S::NB>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        const int kb = q + S::T * i;
+        // output j2 = kb + RB·ka at v[i·RA + rev(ka)]; × ω_k^{−j2·t1}; Y[j2][t1]
+        uint64_t t = rootp(a.pw, lgn, a.lgk, (uint64_t)kb * t1, true);
+        static_for<RA>([&](auto ka_) {
+            constexpr int ka = decltype(ka_)::value;
+            y[(size_t)(kb + RB * ka) * K1] = lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t);
+            if constexpr (ka + 1 < RA) t = lz::mul(t, step);
+        });
+    });
+}
+
+// ---- pass M1 -----------------------------------------------------------------------------------
+template <int RA, int RB>
+__global__ void __launch_bounds__(THREADS, 2) pass_m1(Args a) {
+    using S = Shape<RA, RB>;
+    extern __shared__ uint64_t sm[];
+    uint64_t* tw = sm + S::WORDS;
+    const int lgn = a.lgk + a.lgr;
+    fill_inner<RA, RB>(tw, a.pw, lgn, true);
+    const size_t row = blockIdx.y;
+    const int j2_0 = blockIdx.x * S::W;
+    const int K2 = 1 << a.lgk2;
+    uint64_t v[32];
+    {
+        const int q = threadIdx.x % S::T, c = threadIdx.x / S::T;  // q-fast: a column's t1 are adjacent
+        load_qfast<RA, RB>(v, a.y + (row << a.lgk) + ((size_t)j2_0 << a.lgk1), S::L, c, q);
+        __syncthreads();
+        round1_store<RA, RB, true>(v, sm, tw, c, q);
+    }
+    __syncthreads();
+    const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast
+    round2<RA, RB, true>(v, sm, c, q);
+    // v[i·RA + rev(ka)] = k·a_idx, idx = j2 + K2·(kb + RB·ka)
+    const uint32_t j2 = j2_0 + c;
+    const uint64_t* masks = a.masks ? a.masks + row * (size_t)a.P : nullptr;
+    uint64_t* z = a.z + (row << lgn) + j2;
+    for (int e = 0; e < (1 << a.lgr); e++) {
+        uint64_t* ce = z + ((size_t)e << a.lgk);
+        static_for<S::NB>([&](auto i_) {
+            constexpr int i = decltype(i_)::value;
+            const int kb = q + S::T * i;
+            const uint32_t idx0 = j2 + (uint32_t)K2 * kb;
+            uint64_t t = a.pow7k[idx0];  // s_e^idx0 / k
+            if (e) t = lz::mul(t, a.pw[((uint64_t)e * idx0) & ((1ull << lgn) - 1)]);
+            const uint64_t step = a.sstep[e];
+            const bool masked = masks && idx0 < (uint32_t)a.P;
+            static_for<RA>([&](auto ka_) {
+                constexpr int ka = decltype(ka_)::value;
+                uint64_t x = v[i * RA + brev_c(ka, ilog2(RA))];
+                if (masked) {
+                    const uint32_t idx = idx0 + (uint32_t)K2 * RB * ka;
+                    if (idx < (uint32_t)a.P) x = lz::add(x, lz::mul(masks[idx], a.mk[e]));
+                }
+                ce[(size_t)(kb + RB * ka) * K2] = lz::mul(x, t);  // C_e[j1][j2]
+                if constexpr (ka + 1 < RA) t = lz::mul(t, step);
+            });
+        });
+    }
+}
+
+// ---- pass M2 -----------------------------------------------------------------------------------
+template <int RA, int RB>
+__global__ void __launch_bounds__(THREADS, 2) pass_m2(Args a) {
+    using S = Shape<RA, RB>;
+    extern __shared__ uint64_t sm[];
+    uint64_t* tw = sm + S::WORDS;
+    const int lgn = a.lgk + a.lgr;
+    fill_inner<RA, RB>(tw, a.pw, lgn, false);
+    const size_t row = blockIdx.y;
+    const int tiles = (1 << a.lgk2) / S::W;
+    const int e = blockIdx.x / tiles;
+    const int j2_0 = (blockIdx.x % tiles) * S::W;
+    const int K2 = 1 << a.lgk2;
+    const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast throughout
+    uint64_t* z = a.z + (row << lgn) + ((size_t)e << a.lgk) + j2_0;
+    uint64_t v[32];
+    load_cfast<RA, RB>(v, z, K2, c, q);
+    __syncthreads();  // the twiddle table; every load of this tile is done before any store below
+    round1_store<RA, RB, false>(v, sm, tw, c, q);
+    __syncthreads();
+    round2<RA, RB, false>(v, sm, c, q);
+    const uint32_t j2 = j2_0 + c;
+    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * j2, false);
+    static_for<S::NB>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        const int kb = q + S::T * i;
+        // output v2 = kb + RB·ka; × ω_k^{v2·j2}; Z_e[v2][j2]
+        uint64_t t = rootp(a.pw, lgn, a.lgk, (uint64_t)kb * j2, false);
+        static_for<RA>([&](auto ka_) {
+            constexpr int ka = decltype(ka_)::value;
+            z[c + (size_t)(kb + RB * ka) * K2] = lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t);
+            if constexpr (ka + 1 < RA) t = lz::mul(t, step);
+        });
+    });
+}
+
+// ---- pass C ------------------------------------------------------------------------------------
+template <int RA, int RB>
+__global__ void __launch_bounds__(THREADS, 2) pass_c(Args a) {
+    using S = Shape<RA, RB>;
+    extern __shared__ uint64_t sm[];
+    uint64_t* tw = sm + S::WORDS;
+    const int lgn = a.lgk + a.lgr;
+    fill_inner<RA, RB>(tw, a.pw, lgn, false);
+    const size_t row = blockIdx.y;
+    const int R = 1 << a.lgr;
+    const int col0 = blockIdx.x * S::W;  // columns are (v2, e) pairs, e fastest
+    const int K1 = 1 << a.lgk1;
+    const uint64_t* z = a.z + (row << lgn);
+    uint64_t v[32];
+    {
+        const int q = threadIdx.x % S::T, c = threadIdx.x / S::T;  // q-fast
+        const int colid = col0 + c;
+        const int e = colid & (R - 1), v2 = colid >> a.lgr;
+        load_qfast<RA, RB>(v, z + ((size_t)e << a.lgk) + (size_t)v2 * S::L, 0, 0, q);
+        __syncthreads();  // the twiddle table
+        round1_store<RA, RB, false>(v, sm, tw, c, q);
+    }
+    __syncthreads();
+    const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast
+    round2<RA, RB, false>(v, sm, c, q);
+    uint64_t* out = a.out + (row << lgn) + col0 + c;
+    static_for<S::NB>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        const int kb = q + S::T * i;
+        static_for<RA>([&](auto ka_) {
+            constexpr int ka = decltype(ka_)::value;
+            // symbol (v2 + K1·v1)·2^r + e with v1 = kb + RB·ka
+            out[((size_t)(kb + RB * ka) * K1) << a.lgr] = lz::canon(v[i * RA + brev_c(ka, ilog2(RA))]);
+        });
+    });
+}
+
+}  // namespace fast
+}  // namespace tg
