@@ -203,7 +203,7 @@ def run_gpu(args) -> None:
         import torch.distributed as dist
 
         dist.init_process_group("nccl")
-    dev = Device(local)
+    dev = Device(local, lde_group_bytes=args.lde_group_mib << 20)
     cuda = f"cuda:{local}"
     stream = torch.cuda.ExternalStream(dev.stream_ptr(), device=cuda)
 
@@ -362,6 +362,7 @@ def main():
     ap.add_argument("--cpu-polys", type=int, default=32, help="rows in the CPU baseline's bounded sample")
     ap.add_argument("--ref-polys", type=int, default=32, help="rows per step in the reference arm's sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--lde-group-mib", type=int, default=0, help="encoder scratch per group of rows (0: the library default)")
     ap.add_argument("--polys", type=int, default=NPOLYS,
                     help="rows committed per step (a smaller case for profiler captures; the headline uses 256)")
     args = ap.parse_args()

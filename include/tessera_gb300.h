@@ -45,7 +45,7 @@ typedef struct tg_level tg_level;
 typedef struct {
     uint64_t level_budget_bytes; /* default 16 GiB */
     uint64_t level_min_entries;  /* default 2^14 (gpu.rs:89 LEVEL_MIN_ENTRIES) */
-    uint64_t lde_group_bytes;    /* LDE scratch per group of rows; default 96 MiB (L2-resident) */
+    uint64_t lde_group_bytes;    /* encoder scratch per group of rows; default 768 MiB */
 } tg_config;
 
 /* Library version, and the message of the calling thread's last failure. */

@@ -185,7 +185,7 @@ int tg_device_open(int ordinal, const tg_config* cfg, tg_device** out) {
     if (cfg) d->cfg = *cfg;
     if (!d->cfg.level_budget_bytes) d->cfg.level_budget_bytes = 16ull << 30;
     if (!d->cfg.level_min_entries) d->cfg.level_min_entries = 1ull << 14;
-    if (!d->cfg.lde_group_bytes) d->cfg.lde_group_bytes = 96ull << 20;
+    if (!d->cfg.lde_group_bytes) d->cfg.lde_group_bytes = 768ull << 20;
     cudaError_t e = cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking);
     if (e != cudaSuccess) {
         delete d;

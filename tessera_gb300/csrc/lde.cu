@@ -396,6 +396,11 @@ static int fast_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const
             rc = fast_pass(1, a.lgk1, dim3((unsigned)tiles, g), a, s);
         }
         if (rc) return rc;
+        if (P_ > 0 && masks) {
+            Launch L(d, s, "lde_mask_fixup", 1, g);
+            const unsigned threads = (unsigned)P_ << lgr;
+            fast::mask_fixup<<<dim3((threads + 255) / 256, g), 256, 0, s>>>(a);
+        }
         {
             Launch L(d, s, "lde_pass_m2", 1, g);
             rc = fast_pass(2, a.lgk1, dim3((unsigned)(tiles << lgr), g), a, s);

@@ -6,8 +6,9 @@
 // NTT_k(c_e)[q], c_e[i] = s_e^i·(a_i + m_i (s_e^k − 1)), a = iNTT_k(row)):
 //
 //   pass A   inverse length-K2 transforms down the strided columns t1, × ω_k^{−j2·t1}  → Y[j2][t1]
-//   pass M1  per column j2: inverse length-K1 transform; per coset the scale s_e^i/k (+ mask)
+//   pass M1  per column j2: inverse length-K1 transform; per coset the scale s_e^i/k
 //                                                                               → C_e[j1][j2]
+//            (mask_fixup then adds the P mask terms of each row into C_e)
 //   pass M2  per coset and column j2: forward length-K1 transform, × ω_k^{v2·j2} → Z_e[v2][j2]
 //            (written over C_e: a tile reads all of its columns before it writes)
 //   pass C   per coset and column v2: forward length-K2 transform, written interleaved into the
@@ -109,6 +110,31 @@ __device__ __forceinline__ void dft_dif(uint64_t (&x)[N]) {
     });
 }
 
+// Cache hints: the input rows are read once and the codewords written once, so both stream past
+// L2 (evict-first); the group's scratch (Y, C_e/Z_e) is written with evict-last so that it is still
+// in L2 when the next pass reads it.
+__device__ __forceinline__ uint64_t policy_first() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ uint64_t policy_last() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+__device__ __forceinline__ ulonglong2 ld_hint(const uint64_t* p, uint64_t pol) {
+    ulonglong2 v;
+    asm("ld.global.L2::cache_hint.v2.u64 {%0, %1}, [%2], %3;" : "=l"(v.x), "=l"(v.y) : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ void st_hint(uint64_t* p, uint64_t v, uint64_t pol) {
+    asm volatile("st.global.L2::cache_hint.u64 [%0], %1, %2;" ::"l"(p), "l"(v), "l"(pol) : "memory");
+}
+__device__ __forceinline__ ulonglong2 ld_stream(const uint64_t* p) { return ld_hint(p, policy_first()); }
+__device__ __forceinline__ void st_stream(uint64_t* p, uint64_t v) { st_hint(p, v, policy_first()); }
+__device__ __forceinline__ void st_keep(uint64_t* p, uint64_t v) { st_hint(p, v, policy_last()); }
+
 struct Args {
     const uint64_t* rows;
     const uint64_t* masks;
@@ -163,20 +189,57 @@ __device__ __forceinline__ void fill_inner(uint64_t* tw, const uint64_t* pw, int
     }
 }
 
-// Round-1 loads. c-fast: the tile's columns are adjacent words (column c at src + c) and element
-// t of a column at stride `es`. q-fast: column c starts at src + c·cs and its elements are adjacent.
-template <int RA, int RB>
-__device__ __forceinline__ void load_cfast(uint64_t (&v)[32], const uint64_t* src, size_t es, int c, int q) {
+// A tile whose columns are adjacent words, copied cooperatively into shared memory as rows of W
+// words (element t of column c at sm[t·W + c]) with 16-byte loads, then read by each thread in its
+// round-1 pattern: fewer live addresses than loading every strided element into registers.
+template <int RA, int RB, bool STREAM>
+__device__ __forceinline__ void load_staged(uint64_t (&v)[32], uint64_t* sm, const uint64_t* src, size_t es, int c,
+                                            int q) {
     using S = Shape<RA, RB>;
+    constexpr int VPR = S::W / 2;  // 16-byte vectors per row
+    for (int i = threadIdx.x; i < S::L * VPR; i += THREADS) {
+        const int t = i / VPR, w = i % VPR;
+        const uint64_t* g = src + (size_t)t * es + 2 * w;
+        const ulonglong2 x = STREAM ? ld_stream(g) : *reinterpret_cast<const ulonglong2*>(g);
+        *reinterpret_cast<ulonglong2*>(sm + t * S::W + 2 * w) = x;
+    }
+    __syncthreads();
     static_for<S::NA>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
         const int ta = q + S::T * i;
         static_for<RB>([&](auto tb_) {
             constexpr int tb = decltype(tb_)::value;
-            v[i * RB + tb] = src[c + (size_t)(ta + RA * tb) * es];
+            v[i * RB + tb] = sm[(ta + RA * tb) * S::W + c];
         });
     });
+    __syncthreads();  // the buffer becomes the exchange
 }
+
+// A tile of W columns whose elements are adjacent (column c at src + c·cs), copied into shared
+// memory as sm[c·L + t] with 16-byte loads, then read by each thread in its round-1 pattern.
+template <int RA, int RB>
+__device__ __forceinline__ void load_staged_q(uint64_t (&v)[32], uint64_t* sm, const uint64_t* src, size_t cs, int c,
+                                              int q) {
+    using S = Shape<RA, RB>;
+    constexpr int VPC = S::L / 2;  // 16-byte vectors per column
+    for (int i = threadIdx.x; i < S::W * VPC; i += THREADS) {
+        const int cc = i / VPC, w = i % VPC;
+        const ulonglong2 x = *reinterpret_cast<const ulonglong2*>(src + (size_t)cc * cs + 2 * w);
+        *reinterpret_cast<ulonglong2*>(sm + cc * S::L + 2 * w) = x;
+    }
+    __syncthreads();
+    static_for<S::NA>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        const int ta = q + S::T * i;
+        static_for<RB>([&](auto tb_) {
+            constexpr int tb = decltype(tb_)::value;
+            v[i * RB + tb] = sm[c * S::L + ta + RA * tb];
+        });
+    });
+    __syncthreads();  // the buffer becomes the exchange
+}
+
+// Round-1 loads. q-fast: column c starts at src + c·cs and its elements are adjacent.
 template <int RA, int RB>
 __device__ __forceinline__ void load_qfast(uint64_t (&v)[32], const uint64_t* src, size_t cs, int c, int q) {
     using S = Shape<RA, RB>;
@@ -237,8 +300,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_a(Args a) {
     const int K1 = 1 << a.lgk1;
     const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast throughout
     uint64_t v[32];
-    load_cfast<RA, RB>(v, a.rows + (row << a.lgk) + t1_0, K1, c, q);
-    __syncthreads();  // the twiddle table
+    load_staged<RA, RB, true>(v, sm, a.rows + (row << a.lgk) + t1_0, K1, c, q);  // its syncs cover the twiddles
     round1_store<RA, RB, true>(v, sm, tw, c, q);
     __syncthreads();
     round2<RA, RB, true>(v, sm, c, q);
@@ -252,7 +314,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_a(Args a) {
         uint64_t t = rootp(a.pw, lgn, a.lgk, (uint64_t)kb * t1, true);
         static_for<RA>([&](auto ka_) {
             constexpr int ka = decltype(ka_)::value;
-            y[(size_t)(kb + RB * ka) * K1] = lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t);
+            st_keep(y + (size_t)(kb + RB * ka) * K1, lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t));
             if constexpr (ka + 1 < RA) t = lz::mul(t, step);
         });
     });
@@ -272,16 +334,15 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m1(Args a) {
     uint64_t v[32];
     {
         const int q = threadIdx.x % S::T, c = threadIdx.x / S::T;  // q-fast: a column's t1 are adjacent
-        load_qfast<RA, RB>(v, a.y + (row << a.lgk) + ((size_t)j2_0 << a.lgk1), S::L, c, q);
-        __syncthreads();
+        load_staged_q<RA, RB>(v, sm, a.y + (row << a.lgk) + ((size_t)j2_0 << a.lgk1), S::L, c, q);
         round1_store<RA, RB, true>(v, sm, tw, c, q);
     }
     __syncthreads();
     const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast
     round2<RA, RB, true>(v, sm, c, q);
-    // v[i·RA + rev(ka)] = k·a_idx, idx = j2 + K2·(kb + RB·ka)
+    // v[i·RA + rev(ka)] = k·a_idx, idx = j2 + K2·(kb + RB·ka); C_e[j1][j2] = that × s_e^idx / k
+    // (mask terms are added afterwards by mask_fixup)
     const uint32_t j2 = j2_0 + c;
-    const uint64_t* masks = a.masks ? a.masks + row * (size_t)a.P : nullptr;
     uint64_t* z = a.z + (row << lgn) + j2;
     for (int e = 0; e < (1 << a.lgr); e++) {
         uint64_t* ce = z + ((size_t)e << a.lgk);
@@ -292,19 +353,31 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m1(Args a) {
             uint64_t t = a.pow7k[idx0];  // s_e^idx0 / k
             if (e) t = lz::mul(t, a.pw[((uint64_t)e * idx0) & ((1ull << lgn) - 1)]);
             const uint64_t step = a.sstep[e];
-            const bool masked = masks && idx0 < (uint32_t)a.P;
             static_for<RA>([&](auto ka_) {
                 constexpr int ka = decltype(ka_)::value;
-                uint64_t x = v[i * RA + brev_c(ka, ilog2(RA))];
-                if (masked) {
-                    const uint32_t idx = idx0 + (uint32_t)K2 * RB * ka;
-                    if (idx < (uint32_t)a.P) x = lz::add(x, lz::mul(masks[idx], a.mk[e]));
-                }
-                ce[(size_t)(kb + RB * ka) * K2] = lz::mul(x, t);  // C_e[j1][j2]
+                st_keep(ce + (size_t)(kb + RB * ka) * K2, lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t));
                 if constexpr (ka + 1 < RA) t = lz::mul(t, step);
             });
         });
     }
+}
+
+// Adds the mask terms into C_e after pass M1: C_e[idx] += m_idx·k(s_e^k − 1)·s_e^idx/k for idx < P,
+// where C_e[idx] sits at C_e[j1][j2], idx = j2 + K2·j1. One thread per (coset, idx).
+__global__ void mask_fixup(Args a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int R = 1 << a.lgr;
+    if (i >= a.P * R) return;
+    const int e = i % R;
+    const uint32_t idx = (uint32_t)(i / R);
+    const size_t row = blockIdx.y;
+    const int lgn = a.lgk + a.lgr;
+    uint64_t scale = a.pow7k[idx];
+    if (e) scale = lz::mul(scale, a.pw[((uint64_t)e * idx) & ((1ull << lgn) - 1)]);
+    const uint64_t term = lz::mul(lz::mul(a.masks[row * (size_t)a.P + idx], a.mk[e]), scale);
+    const uint32_t j2 = idx & ((1u << a.lgk2) - 1), j1 = idx >> a.lgk2;
+    uint64_t* ce = a.z + (row << lgn) + ((size_t)e << a.lgk) + ((size_t)j1 << a.lgk2) + j2;
+    *ce = lz::add(*ce, term);
 }
 
 // ---- pass M2 -----------------------------------------------------------------------------------
@@ -323,8 +396,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m2(Args a) {
     const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast throughout
     uint64_t* z = a.z + (row << lgn) + ((size_t)e << a.lgk) + j2_0;
     uint64_t v[32];
-    load_cfast<RA, RB>(v, z, K2, c, q);
-    __syncthreads();  // the twiddle table; every load of this tile is done before any store below
+    load_staged<RA, RB, false>(v, sm, z, K2, c, q);  // every load of this tile is done before any store below
     round1_store<RA, RB, false>(v, sm, tw, c, q);
     __syncthreads();
     round2<RA, RB, false>(v, sm, c, q);
@@ -337,7 +409,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m2(Args a) {
         uint64_t t = rootp(a.pw, lgn, a.lgk, (uint64_t)kb * j2, false);
         static_for<RA>([&](auto ka_) {
             constexpr int ka = decltype(ka_)::value;
-            z[c + (size_t)(kb + RB * ka) * K2] = lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t);
+            st_keep(z + c + (size_t)(kb + RB * ka) * K2, lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t));
             if constexpr (ka + 1 < RA) t = lz::mul(t, step);
         });
     });
@@ -375,7 +447,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_c(Args a) {
         static_for<RA>([&](auto ka_) {
             constexpr int ka = decltype(ka_)::value;
             // symbol (v2 + K1·v1)·2^r + e with v1 = kb + RB·ka
-            out[((size_t)(kb + RB * ka) * K1) << a.lgr] = lz::canon(v[i * RA + brev_c(ka, ilog2(RA))]);
+            st_stream(out + (((size_t)(kb + RB * ka) * K1) << a.lgr), lz::canon(v[i * RA + brev_c(ka, ilog2(RA))]));
         });
     });
 }
