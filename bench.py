@@ -306,24 +306,27 @@ def run_gpu(args) -> None:
 
     if rank != 0:
         return
-    # roofline of the dominant kernel: the encoder's three passes together, against HBM
+    # roofline of the dominant kernel: the encoder (its passes run back to back over one launch
+    # group of rows) against HBM; algorithmic bytes = each row read once + its codeword written once
     kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps,
                    "share": v[0] / max(1e-9, sum(x[0] for x in prof.values()))} for k, v in prof.items()}
-    lde_ms = sum(prof.get(k, (0, 0, 0))[0] for k in ("lde_pass_a", "lde_pass_m", "lde_pass_c"))
+    lde_names = sorted(k for k in prof if k.startswith("lde_"))
+    lde_ms = sum(prof[k][0] for k in lde_names)
     lde_launch_groups = prof.get("lde_pass_a", (0, 1, 0))[1]
     rows_done = prof.get("lde_pass_a", (0, 0, 0))[2]
     bytes_per_row = 8 * (1 << LOG_K) + 8 * (1 << (LOG_K + LOG_R))
     peaks = measured_peaks()
     achieved = (bytes_per_row * rows_done) / (lde_ms / 1e3) / 1e9 if lde_ms else None
     traffic = traffic_table().get("lde_dram_bytes_per_row")
+    rows_per_group = rows_done / max(1, lde_launch_groups)
     roofline = {
-        "kernel": "lde (passes A+M+C, one launch group = rows encoded together)",
+        "kernel": "lde encoder (" + "+".join(lde_names) + "; one launch = one group of rows through all passes)",
         "bound": "hbm", "achieved": achieved, "peak": peaks["hbm_gbs"], "unit": "GB/s",
         "frac": (achieved / peaks["hbm_gbs"]) if achieved else None, "peak_source": peaks["source"],
-        "algorithmic_bytes_per_row": bytes_per_row,
-        "traffic": (traffic * rows_done / max(1, lde_launch_groups)) if traffic else None,
-        "traffic_unit": "bytes per launch group",
-        "note": "the encoder is bound by integer multiply throughput, not by HBM; see int_rate",
+        "algorithmic_bytes_per_row": bytes_per_row, "rows_per_launch": rows_per_group,
+        "traffic": (traffic * rows_per_group) if traffic else None,
+        "traffic_unit": "DRAM bytes per launch (all passes, ncu, scaled by rows)",
+        "note": "the encoder is bound by 64-bit integer multiply-add throughput, not by HBM; see int_rate",
     }
     butterflies_per_row = ((1 << LOG_K) // 2) * LOG_K + ((1 << (LOG_K + LOG_R)) // 2) * (LOG_K + LOG_R)
     int_rate = {"butterflies_per_s": butterflies_per_row * rows_done / (lde_ms / 1e3) if lde_ms else None,

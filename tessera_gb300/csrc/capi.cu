@@ -230,6 +230,7 @@ int tg_device_close(tg_device* dev) {
     d->scratch_y.release();
     d->scratch_z.release();
     d->scratch_misc.release();
+    d->scratch_sc.release();
     d->err.release();
     cudaStreamDestroy(d->stream);
     delete d;

@@ -58,6 +58,7 @@ struct Device {
     std::mutex mu;  // guards the caches and the shared scratch below
     std::map<uint64_t, Tables> tables;
     DevBuf scratch_y, scratch_z, scratch_misc;
+    DevBuf scratch_sc;  // the sumcheck's tables, transcript state and outputs
     DevBuf err;  // device error words for bounded waits
     tg_config cfg;
     std::atomic<uint64_t> launches{0};  // kernels this handle has launched
