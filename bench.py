@@ -216,8 +216,9 @@ def run_gpu(args) -> None:
     npolys = COMMITTED >> LOG_K
     cw_d = torch.empty(npolys * n, dtype=torch.int64, device=cuda)
     nodes_d = torch.empty((2 * n - 1) * 32, dtype=torch.uint8, device=cuda)
-    rows_e = torch.empty_like(rows_d)  # e2e staging
-    tabs_e = [torch.empty_like(t) for t in tabs_d]
+    # the host-buffer path reads the pinned words in place (uint64 views, no host copies)
+    rows_hw = rows_h.numpy().view(np.uint64)
+    tabs_hw = [t.numpy().view(np.uint64) for t in tabs_h]
     torch.cuda.synchronize()
     cid = (ctypes.c_uint8 * 32)(*([0x65] * 32))
     root = ctypes.create_string_buffer(32)
@@ -235,13 +236,11 @@ def run_gpu(args) -> None:
         return sumcheck(tabs_d)
 
     def step_e2e():
-        # pinned host -> device on the library's stream, the proof and root back to the host
-        with torch.cuda.stream(stream):
-            rows_e.copy_(rows_h, non_blocking=True)
-            for a, b in zip(tabs_e, tabs_h):
-                a.copy_(b, non_blocking=True)
-        commit(rows_e)
-        return sumcheck(tabs_e)
+        # the C ABI's host-buffer calls: rows and tables from pinned host memory, the root and the
+        # proof back to the host (the library overlaps the row copies with the encoder)
+        N.call("tg_commit_unmasked", dev.handle, LOG_K, LOG_R, ROW_BLOCK, cid, ctypes.c_void_p(rows_hw.ctypes.data),
+               npolys, None, root)
+        return sumcheck(tabs_hw)
 
     def barrier():
         torch.cuda.synchronize()
@@ -300,7 +299,7 @@ def run_gpu(args) -> None:
     d2h = 32 + SC_VARS * SC_DEGREE * 16 + 3 * 16
     # Release torch's buffers while the library's stream (which their copies used) still exists.
     stream.synchronize()
-    del rows_h, tabs_h, rows_d, tabs_d, cw_d, nodes_d, rows_e, tabs_e
+    del rows_hw, tabs_hw, rows_h, tabs_h, rows_d, tabs_d, cw_d, nodes_d
     torch.cuda.synchronize()
     dev.close()
 

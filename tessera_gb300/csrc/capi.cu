@@ -227,6 +227,17 @@ int tg_device_close(tg_device* dev) {
     clear(d->scratch_y, d->stream);
     clear(d->scratch_z, d->stream);
     cudaStreamSynchronize(d->stream);
+    if (d->copy_stream) {
+        cudaStreamSynchronize(d->copy_stream);
+        cudaStreamDestroy(d->copy_stream);
+    }
+    for (int b = 0; b < 2; b++) {
+        if (d->staged[b]) cudaEventDestroy(d->staged[b]);
+        if (d->consumed[b]) cudaEventDestroy(d->consumed[b]);
+    }
+    d->stage_rows.release();
+    d->stage_cw.release();
+    d->stage_nodes.release();
     d->scratch_y.release();
     d->scratch_z.release();
     d->scratch_misc.release();
@@ -402,26 +413,63 @@ int tg_commit_unmasked_dev(tg_device* dev, uint32_t log_k, uint32_t log_inv_rate
     return TG_OK;
 }
 
+// Host rows in, root (and optionally the leaves) out. The rows travel in chunks of whole row
+// blocks: chunk c is copied on the copy stream while chunk c − 1 is encoded and absorbed into the
+// column chains on the device stream, so the transfer hides behind the encoder. The staging
+// buffers stay with the device handle for the next call and are zeroed once the call ends.
 int tg_commit_unmasked(tg_device* dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t row_block,
                        const uint8_t commitment_id[32], const uint64_t* rows, size_t npolys, uint8_t* leaves,
                        uint8_t root[32]) {
     Device* d = reinterpret_cast<Device*>(dev);
     if (!d || !commitment_id || !root || (npolys && !rows)) return fail(TG_ERR_INVALID, "tg_commit_unmasked: null argument");
     if (log_inv_rate == 0 || log_inv_rate > 4 || log_k > 24) return fail(TG_ERR_INVALID, "unsupported shape 2^%u rate 1/2^%u", log_k, log_inv_rate);
+    if (row_block == 0 || row_block > 124) return fail(TG_ERR_INVALID, "row block %u outside 1..124", row_block);
     const size_t k = (size_t)1 << log_k, n = k << log_inv_rate;
-    DevBuf r, c, nd;
-    int rc = r.ensure(std::max<size_t>(npolys, 1) * k * 8);
-    if (!rc) rc = c.ensure(std::max<size_t>(npolys, 1) * n * 8);
-    if (!rc) rc = nd.ensure((2 * n - 1) * 32);
+    // rows per chunk: the encoder's group, rounded down to whole row blocks (at least one block)
+    size_t chunk = std::max<size_t>(1, d->cfg.lde_group_bytes / ((k + n) * 8));
+    chunk = std::max<size_t>(row_block, chunk / row_block * row_block);
+    chunk = std::min<size_t>(chunk, std::max<size_t>(npolys, 1));
+    std::lock_guard<std::mutex> lock(d->mu);
+    int rc = d->stage_rows.ensure(2 * chunk * k * 8);
+    if (!rc) rc = d->stage_cw.ensure(chunk * n * 8);
+    if (!rc) rc = d->stage_nodes.ensure((2 * n - 1) * 32);
     if (rc) return rc;
-    cudaStream_t s = d->stream;
-    if (npolys) TG_CUDA(cudaMemcpyAsync(r.ptr, rows, npolys * k * 8, cudaMemcpyHostToDevice, s));
-    rc = tg_commit_unmasked_dev(dev, log_k, log_inv_rate, row_block, commitment_id, (const uint64_t*)r.ptr, npolys,
-                                (uint64_t*)c.ptr, (uint8_t*)nd.ptr, root, s);
+    if (!d->copy_stream) {
+        TG_CUDA(cudaStreamCreateWithFlags(&d->copy_stream, cudaStreamNonBlocking));
+        for (int b = 0; b < 2; b++) {
+            TG_CUDA(cudaEventCreateWithFlags(&d->staged[b], cudaEventDisableTiming));
+            TG_CUDA(cudaEventCreateWithFlags(&d->consumed[b], cudaEventDisableTiming));
+        }
+    }
+    cudaStream_t s = d->stream, cs = d->copy_stream;
+    uint64_t* stage = (uint64_t*)d->stage_rows.ptr;
+    uint64_t* cw = (uint64_t*)d->stage_cw.ptr;
+    uint8_t* nodes = (uint8_t*)d->stage_nodes.ptr;
+    // the copy stream starts after everything already queued on the device stream
+    TG_CUDA(cudaEventRecord(d->consumed[0], s));
+    TG_CUDA(cudaEventRecord(d->consumed[1], s));
+    rc = column_init(d, commitment_id, n, nodes, s);
     if (rc) return rc;
-    if (leaves) TG_CUDA(cudaMemcpyAsync(leaves, nd.ptr, n * 32, cudaMemcpyDeviceToHost, s));
-    clear(r, s);
-    clear(c, s);
+    for (size_t r0 = 0, c = 0; r0 < npolys; r0 += chunk, c++) {
+        const size_t g = std::min(chunk, npolys - r0);
+        const int b = (int)(c & 1);
+        uint64_t* half = stage + b * chunk * k;
+        TG_CUDA(cudaStreamWaitEvent(cs, d->consumed[b], 0));
+        TG_CUDA(cudaMemcpyAsync(half, rows + r0 * k, g * k * 8, cudaMemcpyHostToDevice, cs));
+        TG_CUDA(cudaEventRecord(d->staged[b], cs));
+        TG_CUDA(cudaStreamWaitEvent(s, d->staged[b], 0));
+        rc = lde_encode(d, log_k, log_inv_rate, 0, half, g, nullptr, cw, s);
+        if (rc) return rc;
+        TG_CUDA(cudaEventRecord(d->consumed[b], s));
+        rc = column_absorb(d, nodes, n, cw, n, g, row_block, s);
+        if (rc) return rc;
+    }
+    rc = merkle_tree(d, nodes, n, nodes, s);
+    if (rc) return rc;
+    if (leaves) TG_CUDA(cudaMemcpyAsync(leaves, nodes, n * 32, cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaMemcpyAsync(root, nodes + 32 * (2 * n - 2), 32, cudaMemcpyDeviceToHost, s));
+    clear(d->stage_rows, s);
+    clear(d->stage_cw, s);
     TG_CUDA(cudaStreamSynchronize(s));
     return TG_OK;
 }

@@ -59,6 +59,11 @@ struct Device {
     std::map<uint64_t, Tables> tables;
     DevBuf scratch_y, scratch_z, scratch_misc;
     DevBuf scratch_sc;  // the sumcheck's tables, transcript state and outputs
+    // The host-buffer commitment's pipeline: row chunks are copied into one half of stage_rows on
+    // copy_stream while the chunk in the other half is encoded on `stream`.
+    DevBuf stage_rows, stage_cw, stage_nodes;
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t staged[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
     DevBuf err;  // device error words for bounded waits
     tg_config cfg;
     std::atomic<uint64_t> launches{0};  // kernels this handle has launched

@@ -189,6 +189,28 @@ def test_commit_unmasked_shapes(dev, npolys, log_k, log_r, B):
     assert c.root() == root and b"".join(c.leaves()) == leaves.tobytes()
 
 
+@pytest.mark.parametrize("npolys,B,group_rows", [(37, 2, 5), (37, 3, 5), (20, 7, 5), (16, 4, 8), (9, 32, 2)])
+def test_commit_unmasked_pipelined_chunks(npolys, B, group_rows):
+    """The host-buffer commitment copies rows in chunks of whole row blocks while the previous
+    chunk encodes: a small encoder group forces many chunks (and a short last one); the root and
+    leaves match the oracle."""
+    from tessera_gb300.device import Device
+    from tessera_gb300.pcs import CommitmentParams, ReferenceCommitment
+
+    log_k, log_r = 12, 2
+    per_row = ((1 << log_k) + (1 << (log_k + log_r))) * 8
+    d = Device(0, lde_group_bytes=group_rows * per_row)
+    try:
+        cid = bytes(range(7, 39))
+        rows = rand_fp(0x5EED + npolys * B, npolys << log_k)
+        _, leaves, root = O.commit_unmasked(rows, log_k, log_r, B, cid, threads=THREADS)
+        for _ in range(2):  # the staging buffers are reused by the second call
+            c = ReferenceCommitment.commit_unmasked(CommitmentParams(log_k, log_r, 0, B, cid), rows, device=d)
+            assert c.root() == root and b"".join(c.leaves()) == leaves.tobytes()
+    finally:
+        d.close()
+
+
 def test_commit_unmasked_256x2p20(dev):
     """The 256-polynomial, k = 2^20, rate 1/2 workload in full: 2^21 columns chained over 8
     blocks of 32 rows, and the root over 2^21 leaves."""
