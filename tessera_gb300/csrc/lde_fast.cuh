@@ -196,13 +196,21 @@ template <int RA, int RB, bool STREAM>
 __device__ __forceinline__ void load_staged(uint64_t (&v)[32], uint64_t* sm, const uint64_t* src, size_t es, int c,
                                             int q) {
     using S = Shape<RA, RB>;
-    constexpr int VPR = S::W / 2;  // 16-byte vectors per row
-    for (int i = threadIdx.x; i < S::L * VPR; i += THREADS) {
-        const int t = i / VPR, w = i % VPR;
-        const uint64_t* g = src + (size_t)t * es + 2 * w;
-        const ulonglong2 x = STREAM ? ld_stream(g) : *reinterpret_cast<const ulonglong2*>(g);
-        *reinterpret_cast<ulonglong2*>(sm + t * S::W + 2 * w) = x;
-    }
+    constexpr int VPR = S::W / 2;                    // 16-byte vectors per row
+    constexpr int ITERS = S::L * VPR / THREADS;      // vectors per thread, all in flight at once
+    static_assert(S::L * VPR % THREADS == 0, "whole vectors per thread");
+    ulonglong2 x[ITERS];
+    static_for<ITERS>([&](auto it_) {
+        constexpr int it = decltype(it_)::value;
+        const int i = threadIdx.x + it * THREADS;
+        const uint64_t* g = src + (size_t)(i / VPR) * es + 2 * (i % VPR);
+        x[it] = STREAM ? ld_stream(g) : *reinterpret_cast<const ulonglong2*>(g);
+    });
+    static_for<ITERS>([&](auto it_) {
+        constexpr int it = decltype(it_)::value;
+        const int i = threadIdx.x + it * THREADS;
+        *reinterpret_cast<ulonglong2*>(sm + (i / VPR) * S::W + 2 * (i % VPR)) = x[it];
+    });
     __syncthreads();
     static_for<S::NA>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
@@ -221,12 +229,20 @@ template <int RA, int RB>
 __device__ __forceinline__ void load_staged_q(uint64_t (&v)[32], uint64_t* sm, const uint64_t* src, size_t cs, int c,
                                               int q) {
     using S = Shape<RA, RB>;
-    constexpr int VPC = S::L / 2;  // 16-byte vectors per column
-    for (int i = threadIdx.x; i < S::W * VPC; i += THREADS) {
-        const int cc = i / VPC, w = i % VPC;
-        const ulonglong2 x = *reinterpret_cast<const ulonglong2*>(src + (size_t)cc * cs + 2 * w);
-        *reinterpret_cast<ulonglong2*>(sm + cc * S::L + 2 * w) = x;
-    }
+    constexpr int VPC = S::L / 2;                    // 16-byte vectors per column
+    constexpr int ITERS = S::W * VPC / THREADS;      // vectors per thread, all in flight at once
+    static_assert(S::W * VPC % THREADS == 0, "whole vectors per thread");
+    ulonglong2 x[ITERS];
+    static_for<ITERS>([&](auto it_) {
+        constexpr int it = decltype(it_)::value;
+        const int i = threadIdx.x + it * THREADS;
+        x[it] = *reinterpret_cast<const ulonglong2*>(src + (size_t)(i / VPC) * cs + 2 * (i % VPC));
+    });
+    static_for<ITERS>([&](auto it_) {
+        constexpr int it = decltype(it_)::value;
+        const int i = threadIdx.x + it * THREADS;
+        *reinterpret_cast<ulonglong2*>(sm + (i / VPC) * S::L + 2 * (i % VPC)) = x[it];
+    });
     __syncthreads();
     static_for<S::NA>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
@@ -299,19 +315,25 @@ __global__ void __launch_bounds__(THREADS, 2) pass_a(Args a) {
     const int t1_0 = blockIdx.x * S::W;
     const int K1 = 1 << a.lgk1;
     const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast throughout
+    const uint32_t t1 = t1_0 + c;
+    // the outer twiddles, fetched before the tile so that their latency hides behind it
+    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * t1, true);
+    uint64_t t0[S::NB];
+    static_for<S::NB>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        t0[i] = rootp(a.pw, lgn, a.lgk, (uint64_t)(q + S::T * i) * t1, true);
+    });
     uint64_t v[32];
     load_staged<RA, RB, true>(v, sm, a.rows + (row << a.lgk) + t1_0, K1, c, q);  // its syncs cover the twiddles
     round1_store<RA, RB, true>(v, sm, tw, c, q);
     __syncthreads();
     round2<RA, RB, true>(v, sm, c, q);
-    const uint32_t t1 = t1_0 + c;
     uint64_t* y = a.y + (row << a.lgk) + t1;
-    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * t1, true);
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
         const int kb = q + S::T * i;
         // output j2 = kb + RB·ka at v[i·RA + rev(ka)]; × ω_k^{−j2·t1}; Y[j2][t1]
-        uint64_t t = rootp(a.pw, lgn, a.lgk, (uint64_t)kb * t1, true);
+        uint64_t t = t0[i];
         static_for<RA>([&](auto ka_) {
             constexpr int ka = decltype(ka_)::value;
             st_keep(y + (size_t)(kb + RB * ka) * K1, lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t));
@@ -331,18 +353,27 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m1(Args a) {
     const size_t row = blockIdx.y;
     const int j2_0 = blockIdx.x * S::W;
     const int K2 = 1 << a.lgk2;
+    const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast (round 2 and the stores)
+    const uint32_t j2 = j2_0 + c;
+    // the scales' starting points, fetched before the tile so that their latency hides behind it:
+    // 7^idx0 / k and ω_n^idx0 (coset 1), idx0 = j2 + K2·kb
+    uint64_t p7[S::NB], w1[S::NB];
+    static_for<S::NB>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        const uint32_t idx0 = j2 + (uint32_t)K2 * (q + S::T * i);
+        p7[i] = a.pow7k[idx0];
+        w1[i] = a.pw[idx0];
+    });
     uint64_t v[32];
     {
-        const int q = threadIdx.x % S::T, c = threadIdx.x / S::T;  // q-fast: a column's t1 are adjacent
-        load_staged_q<RA, RB>(v, sm, a.y + (row << a.lgk) + ((size_t)j2_0 << a.lgk1), S::L, c, q);
-        round1_store<RA, RB, true>(v, sm, tw, c, q);
+        const int qq = threadIdx.x % S::T, cc = threadIdx.x / S::T;  // q-fast: a column's t1 are adjacent
+        load_staged_q<RA, RB>(v, sm, a.y + (row << a.lgk) + ((size_t)j2_0 << a.lgk1), S::L, cc, qq);
+        round1_store<RA, RB, true>(v, sm, tw, cc, qq);
     }
     __syncthreads();
-    const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast
     round2<RA, RB, true>(v, sm, c, q);
     // v[i·RA + rev(ka)] = k·a_idx, idx = j2 + K2·(kb + RB·ka); C_e[j1][j2] = that × s_e^idx / k
     // (mask terms are added afterwards by mask_fixup)
-    const uint32_t j2 = j2_0 + c;
     uint64_t* z = a.z + (row << lgn) + j2;
     for (int e = 0; e < (1 << a.lgr); e++) {
         uint64_t* ce = z + ((size_t)e << a.lgk);
@@ -350,8 +381,11 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m1(Args a) {
             constexpr int i = decltype(i_)::value;
             const int kb = q + S::T * i;
             const uint32_t idx0 = j2 + (uint32_t)K2 * kb;
-            uint64_t t = a.pow7k[idx0];  // s_e^idx0 / k
-            if (e) t = lz::mul(t, a.pw[((uint64_t)e * idx0) & ((1ull << lgn) - 1)]);
+            uint64_t t = p7[i];  // s_e^idx0 / k
+            if (e == 1)
+                t = lz::mul(t, w1[i]);
+            else if (e > 1)
+                t = lz::mul(t, a.pw[((uint64_t)e * idx0) & ((1ull << lgn) - 1)]);
             const uint64_t step = a.sstep[e];
             static_for<RA>([&](auto ka_) {
                 constexpr int ka = decltype(ka_)::value;
@@ -395,18 +429,24 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m2(Args a) {
     const int K2 = 1 << a.lgk2;
     const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast throughout
     uint64_t* z = a.z + (row << lgn) + ((size_t)e << a.lgk) + j2_0;
+    const uint32_t j2 = j2_0 + c;
+    // the outer twiddles, fetched before the tile so that their latency hides behind it
+    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * j2, false);
+    uint64_t t0[S::NB];
+    static_for<S::NB>([&](auto i_) {
+        constexpr int i = decltype(i_)::value;
+        t0[i] = rootp(a.pw, lgn, a.lgk, (uint64_t)(q + S::T * i) * j2, false);
+    });
     uint64_t v[32];
     load_staged<RA, RB, false>(v, sm, z, K2, c, q);  // every load of this tile is done before any store below
     round1_store<RA, RB, false>(v, sm, tw, c, q);
     __syncthreads();
     round2<RA, RB, false>(v, sm, c, q);
-    const uint32_t j2 = j2_0 + c;
-    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * j2, false);
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
         const int kb = q + S::T * i;
         // output v2 = kb + RB·ka; × ω_k^{v2·j2}; Z_e[v2][j2]
-        uint64_t t = rootp(a.pw, lgn, a.lgk, (uint64_t)kb * j2, false);
+        uint64_t t = t0[i];
         static_for<RA>([&](auto ka_) {
             constexpr int ka = decltype(ka_)::value;
             st_keep(z + c + (size_t)(kb + RB * ka) * K2, lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t));
