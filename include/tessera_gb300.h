@@ -61,6 +61,18 @@ int tg_device_sync(tg_device *dev);
 int tg_device_stream(tg_device *dev, void **stream);
 /* Kernels launched through this handle so far (the library's own, counted at launch). */
 int tg_device_launches(tg_device *dev, uint64_t *launches);
+
+/* Integer-pipe peaks of the device, measured with register-only microbenchmarks (no reference
+ * counterpart: these are the denominators of the integer-bound kernels' rooflines). Rates per
+ * second over the whole GPU: mad.wide.u32 operations, Goldilocks products, radix-2 butterflies
+ * inside radix-32 shift-twiddle transforms, and BLAKE3 compressions. Takes about 0.1 s. */
+typedef struct tg_int_peaks {
+    double imad_wide_per_s;
+    double mulmod_per_s;
+    double butterflies_per_s;
+    double blake3_compressions_per_s;
+} tg_int_peaks;
+int tg_measure_int_peaks(tg_device *dev, tg_int_peaks *out);
 /* Per-kernel timing (no counterpart in the reference; its GPU timing lives in benchmark
  * harnesses, crates/tessera-bench/examples/gpu_unit_costs.rs): while enabled, every launch is
  * bracketed by CUDA events on its own stream. tg_profile_read sums the elapsed times by kernel

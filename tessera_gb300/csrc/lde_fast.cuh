@@ -398,7 +398,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m1(Args a) {
 
 // Adds the mask terms into C_e after pass M1: C_e[idx] += m_idx·k(s_e^k − 1)·s_e^idx/k for idx < P,
 // where C_e[idx] sits at C_e[j1][j2], idx = j2 + K2·j1. One thread per (coset, idx).
-__global__ void mask_fixup(Args a) {
+static __global__ void mask_fixup(Args a) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const int R = 1 << a.lgr;
     if (i >= a.P * R) return;

@@ -52,6 +52,18 @@ class Device:
         N.call("tg_device_launches", self.handle, ctypes.byref(n))
         return n.value
 
+    def int_peaks(self) -> dict:
+        """Measured integer-pipe rates of this GPU (per second): mad.wide.u32, Goldilocks
+        products, radix-2 butterflies in radix-32 shift-twiddle transforms, BLAKE3 compressions."""
+
+        class _Peaks(ctypes.Structure):
+            _fields_ = [("imad_wide_per_s", ctypes.c_double), ("mulmod_per_s", ctypes.c_double),
+                        ("butterflies_per_s", ctypes.c_double), ("blake3_compressions_per_s", ctypes.c_double)]
+
+        p = _Peaks()
+        N.call("tg_measure_int_peaks", self.handle, ctypes.byref(p))
+        return {name: getattr(p, name) for name, _ in _Peaks._fields_}
+
     def profile(self, on: bool = True):
         N.call("tg_profile_enable", self.handle, int(on))
 
