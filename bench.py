@@ -32,6 +32,8 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
+from tessera_gb300.workloads import splitmix_words  # noqa: E402  (numpy only; loads no native code)
+
 NPOLYS, LOG_K, LOG_R, ROW_BLOCK = 256, 20, 1, 32
 SC_VARS, SC_DEGREE = 22, 3
 SEED = 0x00650002
@@ -48,23 +50,6 @@ CONFIG = {
 }
 MASK64 = (1 << 64) - 1
 P = 0xFFFFFFFF00000001
-
-
-def splitmix_np(seed: int, n: int) -> np.ndarray:
-    """SplitMix64 outputs reduced once below p (the reference bench's from_u64_reduced)."""
-    out = np.empty(n, dtype=np.uint64)
-    chunk = 1 << 24
-    golden = np.uint64(0x9E3779B97F4A7C15)
-    with np.errstate(over="ignore"):
-        for s in range(0, n, chunk):
-            m = min(chunk, n - s)
-            z = (np.arange(s + 1, s + m + 1, dtype=np.uint64) * golden) + np.uint64(seed)
-            z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
-            z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
-            z = z ^ (z >> np.uint64(31))
-            z = np.where(z >= np.uint64(P), z - np.uint64(P), z)
-            out[s:s + m] = z
-    return out
 
 
 class Clocks:
@@ -208,8 +193,8 @@ def run_gpu(args) -> None:
     stream = torch.cuda.ExternalStream(dev.stream_ptr(), device=cuda)
 
     # inputs: host (pinned, for e2e) and resident device copies
-    rows_h = torch.from_numpy(splitmix_np(SEED, COMMITTED).view(np.int64)).pin_memory()
-    tabs_h = [torch.from_numpy(splitmix_np(SEED + 1 + i, 1 << SC_VARS).view(np.int64)).pin_memory() for i in range(3)]
+    rows_h = torch.from_numpy(splitmix_words(SEED, COMMITTED).view(np.int64)).pin_memory()
+    tabs_h = [torch.from_numpy(splitmix_words(SEED + 1 + i, 1 << SC_VARS).view(np.int64)).pin_memory() for i in range(3)]
     rows_d = rows_h.to(cuda)
     tabs_d = [t.to(cuda) for t in tabs_h]
     n = 1 << (LOG_K + LOG_R)

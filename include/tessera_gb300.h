@@ -195,6 +195,26 @@ int tg_prove_batch(tg_device *dev, tg_transcript *t, const char *prefix, int deg
                    int ninstances, int tables_on_device, uint64_t gamma[2], uint64_t *rounds, uint64_t *challenges,
                    uint64_t *final_evals, size_t *n_evals);
 
+/* Many independent prove_batch calls at once (the batched pattern of uneven sumcheck instances;
+ * each job is what one tg_prove_batch call takes, with its own transcript). The jobs' rounds run
+ * in lockstep: round j of every job is one fused launch of round sums plus one launch that
+ * advances every job's transcript on the device, so a batch of J jobs of up to n variables costs
+ * about 2n launches instead of 2·Σ n_i. Results, transcripts included, are byte-identical to calling
+ * tg_prove_batch on the jobs one after another. On any error every transcript is left as it was. */
+typedef struct {
+    tg_transcript *transcript; /* this job's transcript, advanced in place */
+    const char *prefix;
+    int degree;
+    const tg_instance *instances;
+    int ninstances;
+    uint64_t gamma[2];      /* out */
+    uint64_t *rounds;       /* out (may be NULL): n_max x degree Fp2 */
+    uint64_t *challenges;   /* out (may be NULL): n_max Fp2 */
+    uint64_t *final_evals;  /* out (may be NULL): one Fp2 per non-public table */
+    size_t n_evals;         /* out */
+} tg_sumcheck_job;
+int tg_prove_many(tg_device *dev, tg_sumcheck_job *jobs, int njobs, int tables_on_device);
+
 /* ---- LevelOffload / DeviceLevel (crates/tessera-sumcheck/src/offload.rs:17-79; the
  * reference's GpuLevels, crates/tessera-gpu/src/level.rs:52-146). shape 0: fraction
  * N0 D1 + N1 D0 + λ D0 D1 over [N0, N1, D0, D1]; shape 1: product V0 V1 over [V0, V1].

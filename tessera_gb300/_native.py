@@ -43,6 +43,13 @@ class InstanceC(ctypes.Structure):
     _fields_ = [("tables", ctypes.POINTER(TableC)), ("ntables", ctypes.c_int), ("vars", ctypes.c_int)]
 
 
+class SumcheckJobC(ctypes.Structure):
+    _fields_ = [("transcript", ctypes.c_void_p), ("prefix", ctypes.c_char_p), ("degree", ctypes.c_int),
+                ("instances", ctypes.POINTER(InstanceC)), ("ninstances", ctypes.c_int),
+                ("gamma", ctypes.c_uint64 * 2), ("rounds", ctypes.c_void_p), ("challenges", ctypes.c_void_p),
+                ("final_evals", ctypes.c_void_p), ("n_evals", ctypes.c_size_t)]
+
+
 _lib = None
 
 V, U32, U64, SZ, INT = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_size_t, ctypes.c_int
@@ -89,6 +96,7 @@ SIGNATURES = {
     "tg_transcript_check_grind": [V, CSTR, U32, U64, V],
     "tg_transcript_grind": [V, V, CSTR, U32, V],
     "tg_prove_batch": [V, V, CSTR, INT, V, INT, INT, V, V, V, V, V],
+    "tg_prove_many": [V, V, INT, INT],
     "tg_level_load": [V, INT, V, V, INT, SZ, V],
     "tg_level_sums": [V, V, V, SZ, U32, V],
     "tg_level_bind": [V, V],

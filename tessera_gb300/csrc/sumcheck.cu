@@ -7,20 +7,22 @@
 // message is p(0), p(2), …, p(d); instance i weighs γ^i; an instance on fewer variables than the
 // batch is front-padded and contributes 2^{n_max − n_i − j − 1}·S_i to each of its padding rounds.
 //
-// The rounds run without returning to the host. Each own round of an instance is one kernel: it
-// binds the previous challenge into the tables (t'[i] = t[2i] + r·(t[2i+1] − t[2i])) and, in the
-// same pass over the pairs of the new table, accumulates the d node sums; the last block to
-// finish reduces the blocks' partial sums. A one-thread kernel then forms the round message
-// (weights, padding terms), absorbs it into the Fiat–Shamir transcript and squeezes the next
-// challenge with BLAKE3 on the device (crates/tessera-hash/src/transcript.rs:168-219), so the
-// next round's kernel reads its challenge from device memory. γ is drawn on the host before the
-// rounds and the final evaluations are absorbed on the host after them; the transcript state
-// travels to the device and back once per batch.
+// Many independent proofs ("jobs", each a prove_batch with its own transcript) advance in
+// lockstep: round j of every job is ONE launch of sc_rounds, whose blocks are split among the
+// (job, instance) segments of that round in proportion to their pairs, and ONE launch of
+// sc_fs_many, one thread per job, which forms the job's message, absorbs it into the job's
+// Fiat–Shamir transcript and squeezes its challenge with BLAKE3 on the device
+// (crates/tessera-hash/src/transcript.rs:168-219). A segment binds the previous challenge into its
+// tables (t'[i] = t[2i] + r·(t[2i+1] − t[2i])) in the same pass that accumulates the d node sums
+// of the new table, and the last of its blocks to finish reduces the blocks' partial sums. The
+// rounds never return to the host: γ is drawn on the host before them, and the final evaluations
+// are absorbed on the host after them; each transcript travels to the device and back once.
+// tg_prove_batch is the one-job case.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include <string.h>
 
-#include <memory>
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -31,11 +33,13 @@
 namespace tg {
 
 constexpr int SC_MAX_TABLES = 7;
+constexpr int SC_MAX_DEGREE = 7;
 constexpr int SC_THREADS = 256;
-constexpr int SC_MAX_BLOCKS = 1024;
+constexpr int SC_MAX_SEG_BLOCKS = 1024;
+constexpr int SC_MSG_WORDS = 2 * SC_MAX_DEGREE;  // one instance's round sums, as Fp2 words
 constexpr int FS_MAX_TRIES = 64;  // squeezes per challenge before giving up (each retries with p < 2^-31)
 
-// The transcript while it lives on the device.
+// A job's transcript while it lives on the device.
 struct FsState {
     uint8_t state[32];
     uint64_t counter;
@@ -48,23 +52,37 @@ struct FsKeys {
     uint32_t absorb[8], squeeze[8], ratchet[8];
 };
 
-struct FsLabel {
-    char text[192];
-    int len;
+struct FsJob {
+    char label[168];  // the job's prefix
+    int label_len;
+    int degree, ninst, n_max, inst0;  // inst0: the job's first instance in the per-instance arrays
+    uint64_t rounds_off, chal_off;    // word offsets of the job's rounds and challenges
 };
 
-struct ScArgs {
+// One instance's share of one launch.
+struct Seg {
     const uint64_t* src[SC_MAX_TABLES];  // current tables (or the tables to bind first)
     uint64_t* dst[SC_MAX_TABLES];        // bound tables (when bind)
+    const uint64_t* r;                   // the challenge to bind, in device memory
+    uint64_t* out;                       // reduced sums, Fp2 words
+    uint64_t n;                          // pairs of the (bound) table; entries for a product sum
     uint32_t base_mask;                  // bit k: table k's source holds prime-field words
-    int nt;
-    int degree;
-    int bind;             // bind src by *r into dst first
-    const uint64_t* r;    // the challenge, in device memory
-    uint64_t npairs;      // pairs of the (bound) table
-    uint64_t* partials;   // gridDim.x rows of words
-    unsigned* counter;    // blocks finished; the last resets it
-    uint64_t* out;        // the reduced sums as 2·degree Fp2 words
+    int nt, degree, bind, kind;          // kind 0: round sums, 1: Σ_x Π_k T_k[x]
+    int block0, nblocks, part0;          // the segment's blocks in the launch, its first partials row
+    int pad_;
+};
+static_assert(sizeof(Seg) % 8 == 0, "Seg copies as words");
+
+struct BindLast {
+    const uint64_t* src;
+    uint64_t* dst;
+    const uint64_t* r;
+    int base, pad_;
+};
+
+struct EvalRef {
+    const uint64_t* ptr;
+    int base, pad_;
 };
 
 __device__ __forceinline__ fp2 load_entry(const uint64_t* t, bool base, uint64_t i) {
@@ -102,139 +120,163 @@ __device__ __forceinline__ void block_sum(uint64_t (&v)[NW]) {
     __syncthreads();
 }
 
-// Writes this block's NW words, and lets the last block to finish reduce all rows into a.out
-// (as Fp2 words; prime-field sums are lifted when LIFT).
-template <int NW, bool LIFT>
-__device__ __forceinline__ void finish_partials(const ScArgs& a, uint64_t (&v)[NW]) {
+// One launch of round sums (and product sums) over all segments: a block finds its segment, runs
+// a grid-stride loop over the segment's pairs, and the segment's last block to finish reduces the
+// segment's partial rows into seg.out.
+template <int D>
+__global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nseg, uint64_t* partials,
+                                                        unsigned* counters) {
+    __shared__ Seg g;
+    __shared__ int si;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (segs[mid].block0 <= (int)blockIdx.x)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        si = lo;
+    }
+    __syncthreads();
+    {
+        const uint64_t* from = reinterpret_cast<const uint64_t*>(segs + si);
+        uint64_t* to = reinterpret_cast<uint64_t*>(&g);
+        for (int w = threadIdx.x; w < (int)(sizeof(Seg) / 8); w += blockDim.x) to[w] = from[w];
+    }
+    __syncthreads();
+    const int lb = blockIdx.x - g.block0;
+    const uint64_t stride = (uint64_t)g.nblocks * blockDim.x;
+    const int deg = g.degree, nt = g.nt;
+    uint64_t words[2 * D];
+#pragma unroll
+    for (int w = 0; w < 2 * D; w++) words[w] = 0;
+
+    if (g.kind == 1) {
+        fp2 acc = {0, 0};
+        for (uint64_t x = (uint64_t)lb * blockDim.x + threadIdx.x; x < g.n; x += stride) {
+            fp2 prod = {1, 0};
+            for (int k = 0; k < nt; k++) prod = e_mul(prod, load_entry(g.src[k], (g.base_mask >> k) & 1, x));
+            acc = e_add(acc, prod);
+        }
+        words[0] = acc.c0;
+        words[1] = acc.c1;
+    } else if (!g.bind && g.base_mask == (1u << nt) - 1) {
+        // all tables in the prime field and nothing to bind: products and sums in the prime field
+        uint64_t acc[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) acc[d] = 0;
+        for (uint64_t p = (uint64_t)lb * blockDim.x + threadIdx.x; p < g.n; p += stride) {
+            uint64_t prod[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) prod[d] = 1;
+            for (int k = 0; k < nt; k++) {
+                const ulonglong2 v = reinterpret_cast<const ulonglong2*>(g.src[k])[p];
+                const uint64_t diff = sub(v.y, v.x);
+                uint64_t x = v.y;  // value at node 1
+                prod[0] = mul(prod[0], v.x);
+#pragma unroll
+                for (int d = 1; d < D; d++) {  // nodes 2..D
+                    if (d < deg) {
+                        x = add(x, diff);
+                        prod[d] = mul(prod[d], x);
+                    }
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < D; d++) acc[d] = add(acc[d], prod[d]);
+        }
+#pragma unroll
+        for (int d = 0; d < D; d++) words[2 * d] = acc[d];
+    } else {
+        fp2 acc[D];
+#pragma unroll
+        for (int d = 0; d < D; d++) acc[d] = {0, 0};
+        const fp2 r = g.bind ? fp2{g.r[0], g.r[1]} : fp2{0, 0};
+        for (uint64_t p = (uint64_t)lb * blockDim.x + threadIdx.x; p < g.n; p += stride) {
+            fp2 prod[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) prod[d] = {1, 0};
+            for (int k = 0; k < nt; k++) {
+                const bool base = (g.base_mask >> k) & 1;
+                fp2 u, v;
+                if (g.bind) {
+                    u = bind_pair(load_entry(g.src[k], base, 4 * p), load_entry(g.src[k], base, 4 * p + 1), r, base);
+                    v = bind_pair(load_entry(g.src[k], base, 4 * p + 2), load_entry(g.src[k], base, 4 * p + 3), r, base);
+                    ulonglong2* out = reinterpret_cast<ulonglong2*>(g.dst[k]);
+                    out[2 * p] = make_ulonglong2(u.c0, u.c1);
+                    out[2 * p + 1] = make_ulonglong2(v.c0, v.c1);
+                } else {
+                    u = load_entry(g.src[k], base, 2 * p);
+                    v = load_entry(g.src[k], base, 2 * p + 1);
+                }
+                const fp2 diff = e_sub(v, u);
+                fp2 x = v;
+                prod[0] = e_mul(prod[0], u);
+#pragma unroll
+                for (int d = 1; d < D; d++) {
+                    if (d < deg) {
+                        x = e_add(x, diff);
+                        prod[d] = e_mul(prod[d], x);
+                    }
+                }
+            }
+#pragma unroll
+            for (int d = 0; d < D; d++) acc[d] = e_add(acc[d], prod[d]);
+        }
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            words[2 * d] = acc[d].c0;
+            words[2 * d + 1] = acc[d].c1;
+        }
+    }
+    block_sum<2 * D>(words);
+
+    // the segment's last block reduces its partial rows
     __shared__ bool last;
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int w = 0; w < NW; w++) a.partials[(size_t)blockIdx.x * NW + w] = v[w];
+        for (int w = 0; w < 2 * D; w++) partials[(size_t)(g.part0 + lb) * 2 * D + w] = words[w];
         __threadfence();
-        last = atomicAdd(a.counter, 1u) == gridDim.x - 1;
+        last = atomicAdd(&counters[si], 1u) == (unsigned)g.nblocks - 1;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    uint64_t t[NW];
 #pragma unroll
-    for (int w = 0; w < NW; w++) t[w] = 0;
-    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+    for (int w = 0; w < 2 * D; w++) words[w] = 0;
+    for (int b = threadIdx.x; b < g.nblocks; b += blockDim.x)
 #pragma unroll
-        for (int w = 0; w < NW; w++) t[w] = add(t[w], __ldcg(&a.partials[(size_t)b * NW + w]));
-    block_sum<NW>(t);
-    if (threadIdx.x == 0) {
-        if (LIFT) {
-            for (int w = 0; w < NW; w++) {
-                a.out[2 * w] = t[w];
-                a.out[2 * w + 1] = 0;
-            }
-        } else {
-            for (int w = 0; w < NW; w++) a.out[w] = t[w];
-        }
-        *a.counter = 0;
-    }
-}
-
-// All tables in the prime field and nothing to bind: products and sums in the prime field.
-template <int D>
-__global__ void __launch_bounds__(SC_THREADS) sc_round_base(ScArgs a) {
-    uint64_t acc[D];
-#pragma unroll
-    for (int d = 0; d < D; d++) acc[d] = 0;
-    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.npairs; p += (uint64_t)gridDim.x * blockDim.x) {
-        uint64_t prod[D];
-#pragma unroll
-        for (int d = 0; d < D; d++) prod[d] = 1;
-        for (int k = 0; k < a.nt; k++) {
-            const ulonglong2 v = reinterpret_cast<const ulonglong2*>(a.src[k])[p];
-            const uint64_t diff = sub(v.y, v.x);
-            uint64_t x = v.y;  // value at node 1
-            prod[0] = mul(prod[0], v.x);
-#pragma unroll
-            for (int d = 1; d < D; d++) {  // nodes 2..D
-                x = add(x, diff);
-                prod[d] = mul(prod[d], x);
-            }
-        }
-#pragma unroll
-        for (int d = 0; d < D; d++) acc[d] = add(acc[d], prod[d]);
-    }
-    block_sum<D>(acc);
-    finish_partials<D, true>(a, acc);
-}
-
-// General round: Fp2 values (tables may mix prime-field and extension sources), binding first
-// when a.bind.
-template <int D>
-__global__ void __launch_bounds__(SC_THREADS) sc_round_ext(ScArgs a) {
-    fp2 acc[D];
-#pragma unroll
-    for (int d = 0; d < D; d++) acc[d] = {0, 0};
-    const fp2 r = a.bind ? fp2{a.r[0], a.r[1]} : fp2{0, 0};
-    for (uint64_t p = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; p < a.npairs; p += (uint64_t)gridDim.x * blockDim.x) {
-        fp2 prod[D];
-#pragma unroll
-        for (int d = 0; d < D; d++) prod[d] = {1, 0};
-        for (int k = 0; k < a.nt; k++) {
-            const bool base = (a.base_mask >> k) & 1;
-            fp2 u, v;
-            if (a.bind) {
-                u = bind_pair(load_entry(a.src[k], base, 4 * p), load_entry(a.src[k], base, 4 * p + 1), r, base);
-                v = bind_pair(load_entry(a.src[k], base, 4 * p + 2), load_entry(a.src[k], base, 4 * p + 3), r, base);
-                ulonglong2* out = reinterpret_cast<ulonglong2*>(a.dst[k]);
-                out[2 * p] = make_ulonglong2(u.c0, u.c1);
-                out[2 * p + 1] = make_ulonglong2(v.c0, v.c1);
-            } else {
-                u = load_entry(a.src[k], base, 2 * p);
-                v = load_entry(a.src[k], base, 2 * p + 1);
-            }
-            const fp2 diff = e_sub(v, u);
-            fp2 x = v;
-            prod[0] = e_mul(prod[0], u);
-#pragma unroll
-            for (int d = 1; d < D; d++) {
-                x = e_add(x, diff);
-                prod[d] = e_mul(prod[d], x);
-            }
-        }
-#pragma unroll
-        for (int d = 0; d < D; d++) acc[d] = e_add(acc[d], prod[d]);
-    }
-    uint64_t words[2 * D];
-#pragma unroll
-    for (int d = 0; d < D; d++) {
-        words[2 * d] = acc[d].c0;
-        words[2 * d + 1] = acc[d].c1;
-    }
+        for (int w = 0; w < 2 * D; w++) words[w] = add(words[w], __ldcg(&partials[(size_t)(g.part0 + b) * 2 * D + w]));
     block_sum<2 * D>(words);
-    finish_partials<2 * D, false>(a, words);
-}
-
-// Binds the last round (tables of two entries into one): dst[0] = bind(src[0], src[1]).
-__global__ void sc_bind_last(ScArgs a) {
-    const int k = threadIdx.x;
-    if (k >= a.nt) return;
-    const bool base = (a.base_mask >> k) & 1;
-    const fp2 r = {a.r[0], a.r[1]};
-    const fp2 u = bind_pair(load_entry(a.src[k], base, 0), load_entry(a.src[k], base, 1), r, base);
-    reinterpret_cast<ulonglong2*>(a.dst[k])[0] = make_ulonglong2(u.c0, u.c1);
-}
-
-// Σ_x Π_k T_k[x] over a whole table set (a padded instance's S_i), into a.out as one Fp2.
-__global__ void __launch_bounds__(SC_THREADS) sc_product_sum(ScArgs a, uint64_t len) {
-    fp2 acc = {0, 0};
-    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < len; x += (uint64_t)gridDim.x * blockDim.x) {
-        fp2 prod = {1, 0};
-        for (int k = 0; k < a.nt; k++) prod = e_mul(prod, load_entry(a.src[k], (a.base_mask >> k) & 1, x));
-        acc = e_add(acc, prod);
+    if (threadIdx.x == 0) {
+        const int nout = g.kind == 1 ? 2 : 2 * deg;
+        for (int w = 0; w < nout; w++) g.out[w] = words[w];
+        counters[si] = 0;
     }
-    uint64_t w[2] = {acc.c0, acc.c1};
-    block_sum<2>(w);
-    finish_partials<2, false>(a, w);
 }
 
-// ---- the transcript on the device (one thread) --------------------------------------------------
+// Binds the last round (tables of two entries into one), one thread per table.
+__global__ void sc_bind_last(const BindLast* b, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const BindLast t = b[i];
+    const fp2 r = {t.r[0], t.r[1]};
+    const fp2 u = bind_pair(load_entry(t.src, t.base, 0), load_entry(t.src, t.base, 1), r, t.base);
+    reinterpret_cast<ulonglong2*>(t.dst)[0] = make_ulonglong2(u.c0, u.c1);
+}
+
+// Each table's single entry after the last bind (public factors left out), as Fp2 words.
+__global__ void sc_gather_evals(const EvalRef* refs, int n, uint64_t* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const EvalRef e = refs[i];
+    out[2 * i] = e.ptr[0];
+    out[2 * i + 1] = e.base ? 0 : e.ptr[1];
+}
+
+// ---- the transcripts on the device (one thread per job) -----------------------------------------
 
 __device__ void fs_hash(const uint32_t key[8], const uint8_t* msg, uint32_t len, uint8_t out[32]) {
     uint32_t h[8];
@@ -262,10 +304,10 @@ __device__ __forceinline__ void put64(uint8_t* p, uint64_t v) {
 }
 
 // state ‖ u64 len(label) ‖ label, label = prefix ‖ tail ‖ decimal j; returns the length.
-__device__ uint32_t fs_begin(const FsState* t, const FsLabel& pre, const char* tail, int j, uint8_t* buf) {
-    char lab[256];
+__device__ uint32_t fs_begin(const FsState* t, const FsJob& jb, const char* tail, int j, uint8_t* buf) {
+    char lab[200];
     int n = 0;
-    for (int i = 0; i < pre.len; i++) lab[n++] = pre.text[i];
+    for (int i = 0; i < jb.label_len; i++) lab[n++] = jb.label[i];
     for (const char* c = tail; *c; c++) lab[n++] = *c;
     char digits[12];
     int nd = 0;
@@ -280,103 +322,72 @@ __device__ uint32_t fs_begin(const FsState* t, const FsLabel& pre, const char* t
     return 40 + n;
 }
 
-// Round j's message: Σ over instances of w_i·(own sums, or 2^{pad_i − j − 1}·S_i while padded),
-// absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2(<prefix>/r/j).
-__global__ void sc_fs_round(FsState* t, FsKeys keys, FsLabel pre, int j, int degree, int ninst, const uint64_t* w,
-                            const int* pad, const uint64_t* S, const uint64_t* msgbuf, uint64_t* rounds_out,
-                            uint64_t* chal_out) {
-    if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    fp2 msg[8];
+// Round j's message of each job: Σ over its instances of w_i·(own sums, or 2^{pad_i − j − 1}·S_i
+// while padded), absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
+// <prefix>/r/j.
+__global__ void sc_fs_many(FsState* states, const FsJob* jobs, int njobs, int j, FsKeys keys, const uint64_t* w,
+                           const int* pad, const uint64_t* S, const uint64_t* msgbuf, uint64_t* rounds_out,
+                           uint64_t* chal_out) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= njobs) return;
+    const FsJob& jb = jobs[t];
+    if (j >= jb.n_max) return;
+    FsState* st = states + t;
+    const int degree = jb.degree;
+    fp2 msg[SC_MAX_DEGREE];
     for (int x = 0; x < degree; x++) msg[x] = {0, 0};
-    for (int i = 0; i < ninst; i++) {
+    for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {
         const fp2 wi = {w[2 * i], w[2 * i + 1]};
         if (j < pad[i]) {
             const fp2 v = e_mul(wi, e_scale(fp2{S[2 * i], S[2 * i + 1]}, (1ull << (pad[i] - j - 1)) % P));
             for (int x = 0; x < degree; x++) msg[x] = e_add(msg[x], v);
         } else {
-            const uint64_t* m = msgbuf + (size_t)i * 2 * degree;
+            const uint64_t* m = msgbuf + (size_t)i * SC_MSG_WORDS;
             for (int x = 0; x < degree; x++) msg[x] = e_add(msg[x], e_mul(wi, fp2{m[2 * x], m[2 * x + 1]}));
         }
     }
-    uint8_t buf[512];
-    uint32_t len = fs_begin(t, pre, "/round/", j, buf);
+    uint8_t buf[40 + 200 + 8 + 16 * SC_MAX_DEGREE];
+    uint32_t len = fs_begin(st, jb, "/round/", j, buf);
     put64(buf + len, (uint64_t)degree);
     len += 8;
+    uint64_t* rj = rounds_out + jb.rounds_off + (size_t)j * 2 * degree;
     for (int x = 0; x < degree; x++) {
         put64(buf + len, msg[x].c0);
         put64(buf + len + 8, msg[x].c1);
         len += 16;
-        rounds_out[(size_t)j * 2 * degree + 2 * x] = msg[x].c0;
-        rounds_out[(size_t)j * 2 * degree + 2 * x + 1] = msg[x].c1;
+        rj[2 * x] = msg[x].c0;
+        rj[2 * x + 1] = msg[x].c1;
     }
-    fs_hash(keys.absorb, buf, len, t->state);
+    fs_hash(keys.absorb, buf, len, st->state);
     for (int tries = 0; tries < FS_MAX_TRIES; tries++) {
-        len = fs_begin(t, pre, "/r/", j, buf);
-        put64(buf + len, t->counter);
+        len = fs_begin(st, jb, "/r/", j, buf);
+        put64(buf + len, st->counter);
         uint8_t out[32];
         fs_hash(keys.squeeze, buf, len + 8, out);
-        t->counter += 1;
+        st->counter += 1;
         uint8_t rb[64];
         for (int i = 0; i < 32; i++) {
-            rb[i] = t->state[i];
+            rb[i] = st->state[i];
             rb[32 + i] = out[i];
         }
-        fs_hash(keys.ratchet, rb, 64, t->state);
+        fs_hash(keys.ratchet, rb, 64, st->state);
         uint64_t c0 = 0, c1 = 0;
         for (int i = 7; i >= 0; i--) {
             c0 = (c0 << 8) | out[i];
             c1 = (c1 << 8) | out[8 + i];
         }
         if (c0 < P && c1 < P) {
-            t->r[0] = c0;
-            t->r[1] = c1;
-            chal_out[2 * j] = c0;
-            chal_out[2 * j + 1] = c1;
+            st->r[0] = c0;
+            st->r[1] = c1;
+            chal_out[jb.chal_off + 2 * j] = c0;
+            chal_out[jb.chal_off + 2 * j + 1] = c1;
             return;
         }
     }
-    t->err = 1;
-}
-
-// Each table's single entry after the last bind (public factors left out), as Fp2 words.
-__global__ void sc_gather_evals(const uint64_t* const* ptrs, const int* is_base, int n, uint64_t* out) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    out[2 * i] = ptrs[i][0];
-    out[2 * i + 1] = is_base[i] ? 0 : ptrs[i][1];
+    st->err = 1;
 }
 
 // ---- host driver -----------------------------------------------------------------------------
-
-static int grid_for(uint64_t items, const Device* d) {
-    uint64_t g = (items + SC_THREADS - 1) / SC_THREADS;
-    const uint64_t cap = std::min<uint64_t>(SC_MAX_BLOCKS, (uint64_t)d->sm_count * 4);
-    if (g > cap) g = cap;
-    return (int)(g ? g : 1);
-}
-
-struct ScTable {
-    const uint64_t* src = nullptr;  // original entries (device)
-    bool base = false, is_public = false;
-    uint64_t* buf[2] = {nullptr, nullptr};  // ping-pong bound tables
-    const uint64_t* cur = nullptr;          // current entries
-    bool cur_base = false;
-};
-
-struct ScInstance {
-    int vars = 0;
-    std::vector<ScTable> tables;
-};
-
-static void fill_args(ScArgs& a, const ScInstance& in, int degree) {
-    memset(&a, 0, sizeof a);
-    a.nt = (int)in.tables.size();
-    a.degree = degree;
-    for (int k = 0; k < a.nt; k++) {
-        a.src[k] = in.tables[k].cur;
-        if (in.tables[k].cur_base) a.base_mask |= 1u << k;
-    }
-}
 
 // A bump allocator over one device buffer, 256-byte aligned pieces.
 struct Arena {
@@ -394,256 +405,393 @@ struct Arena {
 };
 
 template <typename F>
-static int with_degree(int degree, F&& f) {
+static void with_degree(int degree, F&& f) {
     switch (degree) {
-        case 1: return f(std::integral_constant<int, 1>{});
-        case 2: return f(std::integral_constant<int, 2>{});
-        case 3: return f(std::integral_constant<int, 3>{});
-        case 4: return f(std::integral_constant<int, 4>{});
-        case 5: return f(std::integral_constant<int, 5>{});
-        case 6: return f(std::integral_constant<int, 6>{});
-        default: return f(std::integral_constant<int, 7>{});
+        case 1: f(std::integral_constant<int, 1>{}); break;
+        case 2: f(std::integral_constant<int, 2>{}); break;
+        case 3: f(std::integral_constant<int, 3>{}); break;
+        case 4: f(std::integral_constant<int, 4>{}); break;
+        case 5: f(std::integral_constant<int, 5>{}); break;
+        case 6: f(std::integral_constant<int, 6>{}); break;
+        default: f(std::integral_constant<int, 7>{}); break;
     }
+}
+
+struct TableState {
+    const uint64_t* src = nullptr;  // original entries (device)
+    bool base = false, is_public = false;
+    size_t up_off = 0, buf_off[2] = {0, 0};
+};
+
+struct InstState {
+    int job = 0, vars = 0, pad = 0;
+    std::vector<TableState> tables;
+};
+
+// check_batch (prover.rs:1196-1218), in its order: degree, instances, then each instance.
+static int check_job(const tg_sumcheck_job& jb, int index) {
+    if (!jb.transcript || !jb.prefix) return fail(TG_ERR_INVALID, "job %d: null transcript or prefix", index);
+    if (jb.degree < 1 || jb.degree > SC_MAX_DEGREE) return fail(TG_ERR_INVALID, "degree %d outside 1..=7", jb.degree);
+    if (jb.ninstances < 1 || !jb.instances) return fail(TG_ERR_INVALID, "a batch needs at least one instance");
+    for (int i = 0; i < jb.ninstances; i++) {
+        const tg_instance& in = jb.instances[i];
+        if (in.ntables < 1 || !in.tables) return fail(TG_ERR_INVALID, "instance %d has no table", i);
+        if (in.ntables > jb.degree)
+            return fail(TG_ERR_INVALID, "instance %d: a product of %d tables exceeds degree %d", i, in.ntables, jb.degree);
+        if (in.vars < 0 || in.vars > 40) return fail(TG_ERR_INVALID, "instance %d: %d variables", i, in.vars);
+        for (int k = 0; k < in.ntables; k++)
+            if (!in.tables[k].values) return fail(TG_ERR_INVALID, "instance %d table %d: null values", i, k);
+    }
+    if (strlen(jb.prefix) > 160) return fail(TG_ERR_INVALID, "prefix longer than 160 characters");
+    return TG_OK;
+}
+
+static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device) {
+    if (njobs < 1 || !jobs) return fail(TG_ERR_INVALID, "no sumcheck jobs");
+    for (int b = 0; b < njobs; b++) {
+        int rc = check_job(jobs[b], b);
+        if (rc) return rc;
+    }
+    std::lock_guard<std::mutex> lock(d->mu);
+    cudaStream_t s = d->stream;
+    std::vector<tg_transcript> saved(njobs);
+    for (int b = 0; b < njobs; b++) saved[b] = *jobs[b].transcript;
+    auto restore = [&](int rc) {
+        for (int b = 0; b < njobs; b++) *jobs[b].transcript = saved[b];
+        return rc;
+    };
+
+    // ---- per job: γ (host transcript), weights; per instance: padding
+    std::vector<InstState> inst;
+    std::vector<int> n_max(njobs, 0), inst0(njobs, 0);
+    std::vector<fp2> weights;
+    int D = 1, J = 0, nevals = 0;
+    size_t rounds_words = 0, chal_words = 0;
+    std::vector<uint64_t> rounds_off(njobs), chal_off(njobs), evals_off(njobs);
+    for (int b = 0; b < njobs; b++) {
+        tg_sumcheck_job& jb = jobs[b];
+        uint64_t g[2];
+        int rc = tg_transcript_challenge_fp2(jb.transcript, (std::string(jb.prefix) + "/gamma").c_str(), g);
+        if (rc) return restore(rc);
+        jb.gamma[0] = g[0];
+        jb.gamma[1] = g[1];
+        const fp2 gam = {g[0], g[1]};
+        D = std::max(D, jb.degree);
+        inst0[b] = (int)inst.size();
+        for (int i = 0; i < jb.ninstances; i++) n_max[b] = std::max(n_max[b], jb.instances[i].vars);
+        J = std::max(J, n_max[b]);
+        fp2 acc = {1, 0};
+        evals_off[b] = (uint64_t)nevals * 2;
+        for (int i = 0; i < jb.ninstances; i++) {
+            const tg_instance& src = jb.instances[i];
+            InstState is;
+            is.job = b;
+            is.vars = src.vars;
+            is.pad = n_max[b] - src.vars;
+            for (int k = 0; k < src.ntables; k++) {
+                TableState ts;
+                ts.src = src.tables[k].values;
+                ts.base = !src.tables[k].is_ext;
+                ts.is_public = src.tables[k].is_public != 0;
+                if (!ts.is_public) nevals++;
+                is.tables.push_back(ts);
+            }
+            inst.push_back(std::move(is));
+            weights.push_back(acc);
+            acc = e_mul(acc, gam);
+        }
+        rounds_off[b] = rounds_words;
+        chal_off[b] = chal_words;
+        rounds_words += (size_t)n_max[b] * 2 * jb.degree;
+        chal_words += (size_t)n_max[b] * 2;
+    }
+    const int ninst = (int)inst.size();
+
+    // ---- the launches' segments, all planned before anything runs
+    const int seg_cap = std::min(SC_MAX_SEG_BLOCKS, 4 * d->sm_count);
+    auto blocks_for = [&](uint64_t n) {
+        return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + SC_THREADS - 1) / SC_THREADS, seg_cap));
+    };
+    struct Plan {
+        std::vector<std::pair<int, int>> who;  // (instance, own round, or −1 for a product sum)
+        int blocks = 0;
+    };
+    std::vector<Plan> plans(1 + J);  // [0]: product sums, [1 + j]: round j
+    for (int i = 0; i < ninst; i++)
+        if (inst[i].pad > 0) plans[0].who.push_back({i, -1});
+    for (int j = 0; j < J; j++)
+        for (int i = 0; i < ninst; i++) {
+            const int own = j - inst[i].pad;
+            if (own >= 0 && own < inst[i].vars) plans[1 + j].who.push_back({i, own});
+        }
+    size_t max_segs = 1, max_blocks = 1, total_segs = 0;
+    for (auto& p : plans) {
+        for (auto& w : p.who) {
+            const InstState& is = inst[w.first];
+            const uint64_t n = w.second < 0 ? (1ull << is.vars) : (1ull << (is.vars - w.second - 1));
+            p.blocks += blocks_for(n);
+        }
+        max_segs = std::max(max_segs, p.who.size());
+        max_blocks = std::max(max_blocks, (size_t)p.blocks);
+        total_segs += p.who.size();
+    }
+
+    // ---- device memory: one arena for tables, transcripts, plans and outputs
+    Arena ar;
+    for (auto& is : inst) {
+        const size_t len = (size_t)1 << is.vars;
+        for (auto& ts : is.tables) {
+            ts.up_off = tables_on_device ? 0 : ar.take(len * (ts.base ? 8 : 16));
+            ts.buf_off[0] = is.vars >= 1 ? ar.take(std::max<size_t>(len / 2, 1) * 16) : 0;
+            ts.buf_off[1] = is.vars >= 2 ? ar.take(std::max<size_t>(len / 4, 1) * 16) : 0;
+        }
+    }
+    const size_t off_fs = ar.take(sizeof(FsState) * njobs), off_jobs = ar.take(sizeof(FsJob) * njobs);
+    const size_t off_w = ar.take(16 * ninst), off_pad = ar.take(4 * ninst), off_S = ar.take(16 * ninst);
+    const size_t off_msg = ar.take((size_t)8 * SC_MSG_WORDS * ninst);
+    const size_t off_rounds = ar.take(8 * std::max<size_t>(rounds_words, 1));
+    const size_t off_chal = ar.take(8 * std::max<size_t>(chal_words, 1));
+    const size_t off_partials = ar.take(max_blocks * 2 * SC_MAX_DEGREE * 8);
+    const size_t off_counters = ar.take(4 * max_segs);
+    const size_t off_segs = ar.take(sizeof(Seg) * std::max<size_t>(total_segs, 1));
+    size_t nbind = 0;
+    for (auto& is : inst)
+        if (is.vars >= 1) nbind += is.tables.size();
+    const size_t off_bind = ar.take(sizeof(BindLast) * std::max<size_t>(nbind, 1));
+    const size_t off_erefs = ar.take(sizeof(EvalRef) * std::max(nevals, 1));
+    const size_t off_evals = ar.take(16 * std::max(nevals, 1));
+    int rc = d->scratch_sc.ensure(ar.used);
+    if (rc) return restore(rc);
+    ar.base = (uint8_t*)d->scratch_sc.ptr;
+
+    // tables: the current entries after `bound` binds are src (bound 0), else buf[(bound − 1) & 1]
+    for (auto& is : inst)
+        for (auto& ts : is.tables) {
+            if (!tables_on_device) {
+                uint64_t* dst = ar.at<uint64_t>(ts.up_off);
+                const size_t bytes = ((size_t)1 << is.vars) * (ts.base ? 8 : 16);
+                TG_CUDA(cudaMemcpyAsync(dst, ts.src, bytes, cudaMemcpyHostToDevice, s));
+                ts.src = dst;
+            }
+        }
+    auto cur = [&](const InstState& is, int k, int bound) -> const uint64_t* {
+        return bound == 0 ? is.tables[k].src : ar.at<uint64_t>(is.tables[k].buf_off[(bound - 1) & 1]);
+    };
+    FsState* dfs = ar.at<FsState>(off_fs);
+    uint64_t* dS = ar.at<uint64_t>(off_S);
+    uint64_t* dmsg = ar.at<uint64_t>(off_msg);
+    std::vector<Seg> all_segs;
+    std::vector<size_t> plan_seg0;
+    for (auto& p : plans) {
+        plan_seg0.push_back(all_segs.size());
+        int block0 = 0;
+        for (auto& w : p.who) {
+            const InstState& is = inst[w.first];
+            Seg g;
+            memset(&g, 0, sizeof g);
+            g.nt = (int)is.tables.size();
+            g.degree = jobs[is.job].degree;
+            g.r = dfs[is.job].r;
+            const int own = w.second;
+            const int bound = own <= 0 ? 0 : own - 1;  // binds applied before this launch
+            for (int k = 0; k < g.nt; k++) {
+                g.src[k] = cur(is, k, bound);
+                if (bound == 0 && is.tables[k].base) g.base_mask |= 1u << k;
+            }
+            if (own < 0) {
+                g.kind = 1;
+                g.n = 1ull << is.vars;
+                g.out = dS + 2 * w.first;
+            } else {
+                g.kind = 0;
+                g.n = 1ull << (is.vars - own - 1);
+                g.out = dmsg + (size_t)w.first * SC_MSG_WORDS;
+                if (own >= 1) {
+                    g.bind = 1;
+                    for (int k = 0; k < g.nt; k++) g.dst[k] = ar.at<uint64_t>(is.tables[k].buf_off[(own - 1) & 1]);
+                }
+            }
+            g.block0 = block0;
+            g.nblocks = blocks_for(g.n);
+            g.part0 = block0;
+            block0 += g.nblocks;
+            all_segs.push_back(g);
+        }
+    }
+    // the last own round's challenge, bound into one entry per table; then the final evaluations
+    std::vector<BindLast> binds;
+    std::vector<EvalRef> erefs;
+    for (auto& is : inst) {
+        for (int k = 0; k < (int)is.tables.size(); k++) {
+            const uint64_t* fin = is.tables[k].src;
+            bool fin_base = is.tables[k].base;
+            if (is.vars >= 1) {
+                BindLast bl;
+                memset(&bl, 0, sizeof bl);
+                bl.src = cur(is, k, is.vars - 1);
+                bl.base = is.vars == 1 && is.tables[k].base;
+                bl.dst = ar.at<uint64_t>(is.tables[k].buf_off[(is.vars - 1) & 1]);
+                bl.r = dfs[is.job].r;
+                binds.push_back(bl);
+                fin = bl.dst;
+                fin_base = false;
+            }
+            if (!is.tables[k].is_public) {
+                EvalRef e;
+                memset(&e, 0, sizeof e);
+                e.ptr = fin;
+                e.base = fin_base;
+                erefs.push_back(e);
+            }
+        }
+    }
+
+    // ---- uploads: transcripts, jobs, weights, pads, plans
+    std::vector<FsState> fs0(njobs);
+    std::vector<FsJob> hj(njobs);
+    FsKeys keys;
+    context_key("transcript-absorb", keys.absorb);
+    context_key("transcript-squeeze", keys.squeeze);
+    context_key("transcript-ratchet", keys.ratchet);
+    for (int b = 0; b < njobs; b++) {
+        memset(&fs0[b], 0, sizeof(FsState));
+        memcpy(fs0[b].state, jobs[b].transcript->state, 32);
+        fs0[b].counter = jobs[b].transcript->counter;
+        memset(&hj[b], 0, sizeof(FsJob));
+        hj[b].label_len = (int)strlen(jobs[b].prefix);
+        memcpy(hj[b].label, jobs[b].prefix, hj[b].label_len);
+        hj[b].degree = jobs[b].degree;
+        hj[b].ninst = jobs[b].ninstances;
+        hj[b].n_max = n_max[b];
+        hj[b].inst0 = inst0[b];
+        hj[b].rounds_off = rounds_off[b];
+        hj[b].chal_off = chal_off[b];
+    }
+    std::vector<uint64_t> wv(2 * ninst);
+    std::vector<int> pads(ninst);
+    for (int i = 0; i < ninst; i++) {
+        wv[2 * i] = weights[i].c0;
+        wv[2 * i + 1] = weights[i].c1;
+        pads[i] = inst[i].pad;
+    }
+    // Each copy below reads a host vector that lives until the stream synchronizes at the end.
+    TG_CUDA(cudaMemcpyAsync(dfs, fs0.data(), sizeof(FsState) * njobs, cudaMemcpyHostToDevice, s));
+    TG_CUDA(cudaMemcpyAsync(ar.at<FsJob>(off_jobs), hj.data(), sizeof(FsJob) * njobs, cudaMemcpyHostToDevice, s));
+    TG_CUDA(cudaMemcpyAsync(ar.at<uint64_t>(off_w), wv.data(), 16 * ninst, cudaMemcpyHostToDevice, s));
+    TG_CUDA(cudaMemcpyAsync(ar.at<int>(off_pad), pads.data(), 4 * ninst, cudaMemcpyHostToDevice, s));
+    if (!all_segs.empty())
+        TG_CUDA(cudaMemcpyAsync(ar.at<Seg>(off_segs), all_segs.data(), sizeof(Seg) * all_segs.size(),
+                                cudaMemcpyHostToDevice, s));
+    if (!binds.empty())
+        TG_CUDA(cudaMemcpyAsync(ar.at<BindLast>(off_bind), binds.data(), sizeof(BindLast) * binds.size(),
+                                cudaMemcpyHostToDevice, s));
+    if (!erefs.empty())
+        TG_CUDA(cudaMemcpyAsync(ar.at<EvalRef>(off_erefs), erefs.data(), sizeof(EvalRef) * erefs.size(),
+                                cudaMemcpyHostToDevice, s));
+    TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(off_counters), 0, 4 * max_segs, s));
+
+    // ---- the launches
+    uint64_t* partials = ar.at<uint64_t>(off_partials);
+    unsigned* counters = ar.at<unsigned>(off_counters);
+    uint64_t* drounds = ar.at<uint64_t>(off_rounds);
+    uint64_t* dchal = ar.at<uint64_t>(off_chal);
+    auto run_plan = [&](int pi, const char* name) -> int {
+        const Plan& p = plans[pi];
+        if (p.who.empty()) return TG_OK;
+        const Seg* segs = ar.at<Seg>(off_segs) + plan_seg0[pi];
+        uint64_t units = 0;
+        for (size_t q = 0; q < p.who.size(); q++) units += all_segs[plan_seg0[pi] + q].n;
+        Launch L(d, s, name, 1, units);
+        with_degree(D, [&](auto D_) {
+            constexpr int DD = decltype(D_)::value;
+            sc_rounds<DD><<<p.blocks, SC_THREADS, 0, s>>>(segs, (int)p.who.size(), partials, counters);
+        });
+        TG_CUDA(cudaGetLastError());
+        return TG_OK;
+    };
+    rc = run_plan(0, "sumcheck_product_sum");
+    if (rc) return restore(rc);
+    for (int j = 0; j < J; j++) {
+        rc = run_plan(1 + j, "sumcheck_round");
+        if (rc) return restore(rc);
+        {
+            Launch L(d, s, "sumcheck_transcript", 1, njobs);
+            sc_fs_many<<<(njobs + 63) / 64, 64, 0, s>>>(dfs, ar.at<FsJob>(off_jobs), njobs, j, keys,
+                                                        ar.at<uint64_t>(off_w), ar.at<int>(off_pad), dS, dmsg,
+                                                        drounds, dchal);
+        }
+        TG_CUDA(cudaGetLastError());
+    }
+    if (!binds.empty()) {
+        Launch L(d, s, "sumcheck_bind_last", 1, binds.size());
+        sc_bind_last<<<(unsigned)((binds.size() + 127) / 128), 128, 0, s>>>(ar.at<BindLast>(off_bind), (int)binds.size());
+        TG_CUDA(cudaGetLastError());
+    }
+    uint64_t* devals = ar.at<uint64_t>(off_evals);
+    if (nevals) {
+        Launch L(d, s, "sumcheck_evals", 1, nevals);
+        sc_gather_evals<<<(nevals + 127) / 128, 128, 0, s>>>(ar.at<EvalRef>(off_erefs), nevals, devals);
+        TG_CUDA(cudaGetLastError());
+    }
+
+    // ---- one trip back: transcripts, rounds, challenges, evaluations
+    std::vector<FsState> fs1(njobs);
+    std::vector<uint64_t> hr(rounds_words), hc(chal_words), he((size_t)2 * nevals);
+    TG_CUDA(cudaMemcpyAsync(fs1.data(), dfs, sizeof(FsState) * njobs, cudaMemcpyDeviceToHost, s));
+    if (rounds_words) TG_CUDA(cudaMemcpyAsync(hr.data(), drounds, rounds_words * 8, cudaMemcpyDeviceToHost, s));
+    if (chal_words) TG_CUDA(cudaMemcpyAsync(hc.data(), dchal, chal_words * 8, cudaMemcpyDeviceToHost, s));
+    if (nevals) TG_CUDA(cudaMemcpyAsync(he.data(), devals, he.size() * 8, cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    for (int b = 0; b < njobs; b++)
+        if (fs1[b].err)
+            return restore(fail(TG_ERR_STATE, "job %d: a transcript challenge found no canonical Fp2 in %d squeezes", b,
+                                FS_MAX_TRIES));
+    for (int b = 0; b < njobs; b++) {
+        tg_sumcheck_job& jb = jobs[b];
+        memcpy(jb.transcript->state, fs1[b].state, 32);
+        jb.transcript->counter = fs1[b].counter;
+        const size_t nr = (size_t)n_max[b] * 2 * jb.degree;
+        if (jb.rounds && nr) memcpy(jb.rounds, hr.data() + rounds_off[b], nr * 8);
+        if (jb.challenges && n_max[b]) memcpy(jb.challenges, hc.data() + chal_off[b], (size_t)n_max[b] * 16);
+        const size_t ne = (b + 1 < njobs ? evals_off[b + 1] : (uint64_t)2 * nevals) - evals_off[b];
+        jb.n_evals = ne / 2;
+        if (jb.final_evals && ne) memcpy(jb.final_evals, he.data() + evals_off[b], ne * 8);
+        rc = tg_transcript_absorb_fp2s(jb.transcript, (std::string(jb.prefix) + "/evals").c_str(),
+                                       he.data() + evals_off[b], ne / 2);
+        if (rc) return rc;
+    }
+    return TG_OK;
 }
 
 }  // namespace tg
 
 using namespace tg;
 
+extern "C" int tg_prove_many(tg_device* dev, tg_sumcheck_job* jobs, int njobs, int tables_on_device) {
+    Device* d = reinterpret_cast<Device*>(dev);
+    if (!d) return fail(TG_ERR_INVALID, "tg_prove_many: null device");
+    return prove_many(d, jobs, njobs, tables_on_device);
+}
+
 extern "C" int tg_prove_batch(tg_device* dev, tg_transcript* t, const char* prefix, int degree, const tg_instance* inst,
                               int ninst, int tables_on_device, uint64_t gamma[2], uint64_t* rounds, uint64_t* challenges,
                               uint64_t* final_evals, size_t* n_evals) {
     Device* d = reinterpret_cast<Device*>(dev);
     if (!d || !t || !prefix || !gamma || !n_evals) return fail(TG_ERR_INVALID, "tg_prove_batch: null argument");
-    // check_batch (prover.rs:1196-1218), in its order: degree, instances, then each instance.
-    if (degree < 1 || degree > 7) return fail(TG_ERR_INVALID, "degree %d outside 1..=7", degree);
-    if (ninst < 1 || !inst) return fail(TG_ERR_INVALID, "a batch needs at least one instance");
-    int n_max = 0;
-    for (int i = 0; i < ninst; i++) {
-        if (inst[i].ntables < 1 || !inst[i].tables) return fail(TG_ERR_INVALID, "instance %d has no table", i);
-        if (inst[i].ntables > degree)
-            return fail(TG_ERR_INVALID, "instance %d: a product of %d tables exceeds degree %d", i, inst[i].ntables, degree);
-        if (inst[i].vars < 0 || inst[i].vars > 40) return fail(TG_ERR_INVALID, "instance %d: %d variables", i, inst[i].vars);
-        for (int k = 0; k < inst[i].ntables; k++)
-            if (!inst[i].tables[k].values) return fail(TG_ERR_INVALID, "instance %d table %d: null values", i, k);
-        n_max = std::max(n_max, inst[i].vars);
-    }
-    const size_t plen = strlen(prefix);
-    if (plen > 160) return fail(TG_ERR_INVALID, "prefix longer than 160 characters");
-    std::lock_guard<std::mutex> lock(d->mu);
-    cudaStream_t s = d->stream;
-    const std::string pre(prefix);
-    uint64_t g[2];
-    int rc = tg_transcript_challenge_fp2(t, (pre + "/gamma").c_str(), g);
+    tg_sumcheck_job jb;
+    memset(&jb, 0, sizeof jb);
+    jb.transcript = t;
+    jb.prefix = prefix;
+    jb.degree = degree;
+    jb.instances = inst;
+    jb.ninstances = ninst;
+    jb.rounds = rounds;
+    jb.challenges = challenges;
+    jb.final_evals = final_evals;
+    const int rc = prove_many(d, &jb, 1, tables_on_device);
     if (rc) return rc;
-    gamma[0] = g[0];
-    gamma[1] = g[1];
-    const fp2 gam = {g[0], g[1]};
-
-    // ---- device memory: one arena for tables, state and outputs
-    Arena ar;
-    std::vector<ScInstance> st(ninst);
-    std::vector<size_t> up_off, buf_off;  // per table, in order
-    int nevals = 0;
-    for (int i = 0; i < ninst; i++) {
-        const size_t len = (size_t)1 << inst[i].vars;
-        for (int k = 0; k < inst[i].ntables; k++) {
-            const tg_table& src = inst[i].tables[k];
-            up_off.push_back(tables_on_device ? 0 : ar.take(len * (src.is_ext ? 16 : 8)));
-            buf_off.push_back(inst[i].vars >= 1 ? ar.take(std::max<size_t>(len / 2, 1) * 16) : 0);
-            buf_off.push_back(inst[i].vars >= 2 ? ar.take(std::max<size_t>(len / 4, 1) * 16) : 0);
-            if (!src.is_public) nevals++;
-        }
-    }
-    const size_t off_fs = ar.take(sizeof(FsState));
-    const size_t off_w = ar.take(16 * ninst), off_pad = ar.take(4 * ninst), off_S = ar.take(16 * ninst);
-    const size_t off_msg = ar.take((size_t)16 * degree * ninst);
-    const size_t off_rounds = ar.take((size_t)16 * degree * std::max(n_max, 1));
-    const size_t off_chal = ar.take((size_t)16 * std::max(n_max, 1));
-    const size_t off_partials = ar.take((size_t)SC_MAX_BLOCKS * 16 * 8);
-    const size_t off_counter = ar.take(16);
-    const size_t off_evals = ar.take((size_t)16 * std::max(nevals, 1));
-    const size_t off_eptr = ar.take(sizeof(uint64_t*) * std::max(nevals, 1));
-    const size_t off_ebase = ar.take(4 * std::max(nevals, 1));
-    rc = d->scratch_sc.ensure(ar.used);
-    if (rc) return rc;
-    ar.base = (uint8_t*)d->scratch_sc.ptr;
-
-    // tables
-    std::vector<fp2> w(ninst);
-    std::vector<int> pad(ninst);
-    fp2 acc = {1, 0};
-    size_t ti = 0;
-    for (int i = 0; i < ninst; i++) {
-        w[i] = acc;
-        acc = e_mul(acc, gam);
-        st[i].vars = inst[i].vars;
-        pad[i] = n_max - inst[i].vars;
-        const size_t len = (size_t)1 << inst[i].vars;
-        for (int k = 0; k < inst[i].ntables; k++, ti++) {
-            const tg_table& src = inst[i].tables[k];
-            ScTable tb;
-            tb.base = !src.is_ext;
-            tb.is_public = src.is_public != 0;
-            if (tables_on_device) {
-                tb.src = src.values;
-            } else {
-                uint64_t* dst = ar.at<uint64_t>(up_off[ti]);
-                TG_CUDA(cudaMemcpyAsync(dst, src.values, len * (tb.base ? 8 : 16), cudaMemcpyHostToDevice, s));
-                tb.src = dst;
-            }
-            tb.buf[0] = inst[i].vars >= 1 ? ar.at<uint64_t>(buf_off[2 * ti]) : nullptr;
-            tb.buf[1] = inst[i].vars >= 2 ? ar.at<uint64_t>(buf_off[2 * ti + 1]) : nullptr;
-            tb.cur = tb.src;
-            tb.cur_base = tb.base;
-            st[i].tables.push_back(tb);
-        }
-    }
-    // transcript state, weights, padding
-    FsState fs0;
-    memset(&fs0, 0, sizeof fs0);
-    memcpy(fs0.state, t->state, 32);
-    fs0.counter = t->counter;
-    FsState* fs = ar.at<FsState>(off_fs);
-    TG_CUDA(cudaMemcpyAsync(fs, &fs0, sizeof fs0, cudaMemcpyHostToDevice, s));
-    std::vector<uint64_t> wv(2 * ninst);
-    for (int i = 0; i < ninst; i++) {
-        wv[2 * i] = w[i].c0;
-        wv[2 * i + 1] = w[i].c1;
-    }
-    uint64_t* dw = ar.at<uint64_t>(off_w);
-    int* dpad = ar.at<int>(off_pad);
-    uint64_t* dS = ar.at<uint64_t>(off_S);
-    uint64_t* dmsg = ar.at<uint64_t>(off_msg);
-    uint64_t* drounds = ar.at<uint64_t>(off_rounds);
-    uint64_t* dchal = ar.at<uint64_t>(off_chal);
-    TG_CUDA(cudaMemcpyAsync(dw, wv.data(), 16 * ninst, cudaMemcpyHostToDevice, s));
-    TG_CUDA(cudaMemcpyAsync(dpad, pad.data(), 4 * ninst, cudaMemcpyHostToDevice, s));
-    TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(off_counter), 0, 16, s));
-    FsKeys keys;
-    context_key("transcript-absorb", keys.absorb);
-    context_key("transcript-squeeze", keys.squeeze);
-    context_key("transcript-ratchet", keys.ratchet);
-    FsLabel label;
-    memset(&label, 0, sizeof label);
-    memcpy(label.text, prefix, plen);
-    label.len = (int)plen;
-
-    auto base_args = [&](ScArgs& a, uint64_t* out) {
-        a.r = fs->r;
-        a.partials = ar.at<uint64_t>(off_partials);
-        a.counter = ar.at<unsigned>(off_counter);
-        a.out = out;
-    };
-
-    // padded instances' full sums S_i
-    for (int i = 0; i < ninst; i++) {
-        if (st[i].vars >= n_max) continue;
-        ScArgs a;
-        fill_args(a, st[i], degree);
-        base_args(a, dS + 2 * i);
-        const uint64_t len = 1ull << st[i].vars;
-        const int grid = grid_for(len, d);
-        Launch L(d, s, "sumcheck_product_sum", 1, len);
-        sc_product_sum<<<grid, SC_THREADS, 0, s>>>(a, len);
-        TG_CUDA(cudaGetLastError());
-    }
-
-    std::vector<int> pending(ninst, 0);  // own rounds whose challenge is not bound yet
-    for (int j = 0; j < n_max; j++) {
-        for (int i = 0; i < ninst; i++) {
-            if (j < pad[i]) continue;
-            const int own = j - pad[i];
-            ScInstance& in = st[i];
-            ScArgs a;
-            fill_args(a, in, degree);
-            base_args(a, dmsg + (size_t)i * 2 * degree);
-            a.npairs = 1ull << (in.vars - own - 1);
-            bool all_base = true;
-            for (auto& tb : in.tables) all_base &= tb.cur_base;
-            if (pending[i]) {
-                a.bind = 1;
-                for (int k = 0; k < a.nt; k++) a.dst[k] = in.tables[k].buf[(own - 1) & 1];
-            }
-            const int grid = grid_for(a.npairs, d);
-            {
-                Launch L(d, s, "sumcheck_round", 1, a.npairs);
-                with_degree(degree, [&](auto D_) {
-                    constexpr int D = decltype(D_)::value;
-                    if (all_base && !a.bind)
-                        sc_round_base<D><<<grid, SC_THREADS, 0, s>>>(a);
-                    else
-                        sc_round_ext<D><<<grid, SC_THREADS, 0, s>>>(a);
-                    return 0;
-                });
-            }
-            TG_CUDA(cudaGetLastError());
-            if (a.bind) {
-                for (int k = 0; k < a.nt; k++) {
-                    in.tables[k].cur = a.dst[k];
-                    in.tables[k].cur_base = false;
-                }
-            }
-            pending[i] = 1;
-        }
-        {
-            Launch L(d, s, "sumcheck_transcript", 1, 1);
-            sc_fs_round<<<1, 32, 0, s>>>(fs, keys, label, j, degree, ninst, dw, dpad, dS, dmsg, drounds, dchal);
-        }
-        TG_CUDA(cudaGetLastError());
-    }
-    // the last own round's challenge, bound into one entry per table
-    for (int i = 0; i < ninst; i++) {
-        ScInstance& in = st[i];
-        if (!pending[i]) continue;
-        ScArgs a;
-        fill_args(a, in, degree);
-        base_args(a, nullptr);
-        for (int k = 0; k < a.nt; k++) a.dst[k] = in.tables[k].buf[(in.vars - 1) & 1];
-        {
-            Launch L(d, s, "sumcheck_bind_last", 1, 1);
-            sc_bind_last<<<1, 32, 0, s>>>(a);
-        }
-        TG_CUDA(cudaGetLastError());
-        for (int k = 0; k < a.nt; k++) {
-            in.tables[k].cur = a.dst[k];
-            in.tables[k].cur_base = false;
-        }
-    }
-    // final evaluations: each table's single entry, public factors left out
-    std::vector<const uint64_t*> eptr;
-    std::vector<int> ebase;
-    for (int i = 0; i < ninst; i++)
-        for (auto& tb : st[i].tables)
-            if (!tb.is_public) {
-                eptr.push_back(tb.cur);
-                ebase.push_back(tb.cur_base ? 1 : 0);
-            }
-    uint64_t* devals = ar.at<uint64_t>(off_evals);
-    if (nevals) {
-        TG_CUDA(cudaMemcpyAsync(ar.at<uint64_t*>(off_eptr), eptr.data(), sizeof(uint64_t*) * nevals, cudaMemcpyHostToDevice, s));
-        TG_CUDA(cudaMemcpyAsync(ar.at<int>(off_ebase), ebase.data(), 4 * nevals, cudaMemcpyHostToDevice, s));
-        Launch L(d, s, "sumcheck_evals", 1, nevals);
-        sc_gather_evals<<<(nevals + 127) / 128, 128, 0, s>>>(ar.at<const uint64_t* const>(off_eptr), ar.at<int>(off_ebase),
-                                                              nevals, devals);
-        TG_CUDA(cudaGetLastError());
-    }
-    // one trip back: transcript, rounds, challenges, evaluations
-    FsState fs1;
-    std::vector<uint64_t> hr((size_t)2 * degree * n_max), hc((size_t)2 * n_max), he((size_t)2 * nevals);
-    TG_CUDA(cudaMemcpyAsync(&fs1, fs, sizeof fs1, cudaMemcpyDeviceToHost, s));
-    if (n_max) {
-        TG_CUDA(cudaMemcpyAsync(hr.data(), drounds, hr.size() * 8, cudaMemcpyDeviceToHost, s));
-        TG_CUDA(cudaMemcpyAsync(hc.data(), dchal, hc.size() * 8, cudaMemcpyDeviceToHost, s));
-    }
-    if (nevals) TG_CUDA(cudaMemcpyAsync(he.data(), devals, he.size() * 8, cudaMemcpyDeviceToHost, s));
-    TG_CUDA(cudaStreamSynchronize(s));
-    if (fs1.err) return fail(TG_ERR_STATE, "a transcript challenge found no canonical Fp2 in %d squeezes", FS_MAX_TRIES);
-    memcpy(t->state, fs1.state, 32);
-    t->counter = fs1.counter;
-    if (rounds && n_max) memcpy(rounds, hr.data(), hr.size() * 8);
-    if (challenges && n_max) memcpy(challenges, hc.data(), hc.size() * 8);
-    *n_evals = (size_t)nevals;
-    if (final_evals && nevals) memcpy(final_evals, he.data(), he.size() * 8);
-    return tg_transcript_absorb_fp2s(t, (pre + "/evals").c_str(), he.data(), (size_t)nevals);
+    gamma[0] = jb.gamma[0];
+    gamma[1] = jb.gamma[1];
+    *n_evals = jb.n_evals;
+    return TG_OK;
 }
