@@ -129,6 +129,34 @@ int tg_commit_unmasked_dev(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate
 int tg_commit_unmasked(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t row_block,
                        const uint8_t commitment_id[32], const uint64_t *rows, size_t npolys, uint8_t *leaves,
                        uint8_t root[32]);
+
+/* Many unmasked commitments of uneven shapes at once (the batched pattern; each job is what one
+ * tg_commit_unmasked_dev call takes, all buffers on the device). The jobs run on `workers`
+ * streams (0: the library's default), longest first onto the least loaded stream; roots and
+ * nodes are byte-identical to committing the jobs one at a time. */
+typedef struct {
+    uint32_t log_k, log_inv_rate, row_block;
+    uint8_t commitment_id[32];
+    const uint64_t *rows;  /* device: npolys x 2^log_k */
+    size_t npolys;
+    uint64_t *codewords;   /* device out: npolys x n */
+    uint8_t *nodes;        /* device out: 2n - 1 digests, leaves first, root last */
+    uint8_t root[32];      /* out (tg_commit_many) */
+} tg_commit_job;
+int tg_commit_many(tg_device *dev, tg_commit_job *jobs, int njobs, int workers);
+
+/* A batch of commitments captured once into a CUDA graph and replayed. Creating the plan
+ * builds the twiddle tables, allocates the encoder scratch the graph keeps, and (workers = 0)
+ * autotunes the worker count over {1, 2, 4, 8} by timing a replay of each candidate on the batch;
+ * every launch then re-reads the jobs' row buffers (same addresses, new contents) and writes
+ * the codewords, nodes, and the njobs x 32 roots to host `roots`. */
+typedef struct tg_commit_plan tg_commit_plan;
+int tg_commit_plan_create(tg_device *dev, const tg_commit_job *jobs, int njobs, int workers, tg_commit_plan **out);
+int tg_commit_plan_launch(tg_commit_plan *plan, uint8_t *roots);
+/* The chosen worker count, kernels per replay, and the autotuner's replay times (ms) at
+ * 1, 2, 4 and 8 workers (0 where not tried). */
+int tg_commit_plan_info(const tg_commit_plan *plan, int *workers, uint64_t *kernels, double tuned_ms[4]);
+int tg_commit_plan_destroy(tg_commit_plan *plan);
 /* merge_segments on host buffers (crates/tessera-pcs/src/streaming.rs:382-404). */
 int tg_merge_segments(tg_device *dev, const uint8_t *segment_chains, size_t nsegments, uint64_t n,
                       uint8_t *leaves, uint8_t root[32]);

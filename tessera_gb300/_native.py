@@ -43,6 +43,12 @@ class InstanceC(ctypes.Structure):
     _fields_ = [("tables", ctypes.POINTER(TableC)), ("ntables", ctypes.c_int), ("vars", ctypes.c_int)]
 
 
+class CommitJobC(ctypes.Structure):
+    _fields_ = [("log_k", ctypes.c_uint32), ("log_inv_rate", ctypes.c_uint32), ("row_block", ctypes.c_uint32),
+                ("commitment_id", ctypes.c_uint8 * 32), ("rows", ctypes.c_void_p), ("npolys", ctypes.c_size_t),
+                ("codewords", ctypes.c_void_p), ("nodes", ctypes.c_void_p), ("root", ctypes.c_uint8 * 32)]
+
+
 class SumcheckJobC(ctypes.Structure):
     _fields_ = [("transcript", ctypes.c_void_p), ("prefix", ctypes.c_char_p), ("degree", ctypes.c_int),
                 ("instances", ctypes.POINTER(InstanceC)), ("ninstances", ctypes.c_int),
@@ -97,6 +103,11 @@ SIGNATURES = {
     "tg_transcript_grind": [V, V, CSTR, U32, V],
     "tg_prove_batch": [V, V, CSTR, INT, V, INT, INT, V, V, V, V, V],
     "tg_prove_many": [V, V, INT, INT],
+    "tg_commit_many": [V, V, INT, INT],
+    "tg_commit_plan_create": [V, V, INT, INT, V],
+    "tg_commit_plan_launch": [V, V],
+    "tg_commit_plan_info": [V, V, V, V],
+    "tg_commit_plan_destroy": [V],
     "tg_level_load": [V, INT, V, V, INT, SZ, V],
     "tg_level_sums": [V, V, V, SZ, U32, V],
     "tg_level_bind": [V, V],

@@ -70,6 +70,10 @@ static cudaEvent_t take_event(Device* d) {
 }
 
 Launch::Launch(Device* d_, cudaStream_t s_, const char* name, uint64_t nkernels, uint64_t units) : d(d_), s(s_) {
+    if (d->capturing) {
+        d->captured += nkernels;
+        return;
+    }
     d->launches += nkernels;
     if (!d->prof_on) return;
     std::lock_guard<std::mutex> g(d->prof_mu);
@@ -238,6 +242,14 @@ int tg_device_close(tg_device* dev) {
     d->stage_rows.release();
     d->stage_cw.release();
     d->stage_nodes.release();
+    for (Worker* w : d->workers) {
+        cudaStreamSynchronize(w->s);
+        cudaStreamDestroy(w->s);
+        cudaEventDestroy(w->done);
+        delete w;
+    }
+    if (d->fork) cudaEventDestroy(d->fork);
+    d->batch_roots.release();
     d->scratch_y.release();
     d->scratch_z.release();
     d->scratch_misc.release();

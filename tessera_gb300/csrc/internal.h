@@ -50,6 +50,13 @@ struct ProfRec {
     uint64_t units;  // work units of the launch (rows, columns, pairs), for per-unit rates
 };
 
+// A stream of the batched commitment path with its own encoder scratch.
+struct Worker {
+    cudaStream_t s = nullptr;
+    cudaEvent_t done = nullptr;
+    DevBuf y, z;
+};
+
 struct Device {
     int ordinal = 0;
     cudaStream_t stream = nullptr;
@@ -67,6 +74,13 @@ struct Device {
     DevBuf err;  // device error words for bounded waits
     tg_config cfg;
     std::atomic<uint64_t> launches{0};  // kernels this handle has launched
+    // While a CUDA graph is captured, Launch counts kernels into `captured` instead (a replay
+    // adds them to `launches`) and records no profiling events.
+    bool capturing = false;
+    uint64_t captured = 0;
+    std::vector<Worker*> workers;  // the batched commitment path's streams, created on demand
+    cudaEvent_t fork = nullptr;
+    DevBuf batch_roots;
     bool prof_on = false;
     std::mutex prof_mu;
     std::vector<ProfRec> prof;

@@ -219,3 +219,111 @@ class GpuWeights:
         if columns != 1 << (log_k + log2_inv_rate) or not 1 <= log2_inv_rate <= 4 or log_k > 24 or not 1 <= block <= 124:
             return None  # declined: the host encodes
         return MatrixSink(self.device, log_k, log2_inv_rate, block, commitment_id, queries)
+
+
+# ---- the batched pattern: many commitments at once ---------------------------------------------
+
+class ResidentCommitment:
+    """One commitment of a batch, kept on the device: codewords (npolys x n words), nodes
+    ((2n − 1) x 32 bytes, leaves first, root last) and the root."""
+
+    def __init__(self, params: CommitmentParams, rows, codewords, nodes):
+        self.params, self.rows, self.codewords, self.nodes = params, rows, codewords, nodes
+        self.root: Digest = b""
+
+    @property
+    def npolys(self) -> int:
+        return self.rows.numel() >> self.params.log2_k
+
+    def leaves(self) -> list[Digest]:
+        n = 1 << (self.params.log2_k + self.params.log2_inv_rate)
+        return digests(self.nodes[: 32 * n].cpu().numpy().reshape(n, 32))
+
+
+def _resident(params_list, rows_list, device: Device):
+    import torch
+
+    if len(params_list) != len(rows_list):
+        raise ValueError("one row tensor per commitment")
+    out = []
+    arr = (N.CommitJobC * len(params_list))()
+    for i, (p, rows) in enumerate(zip(params_list, rows_list)):
+        if p.mask_coeffs != 0:
+            raise ValueError("the batched commitments are unmasked")
+        if not (hasattr(rows, "is_cuda") and rows.is_cuda):
+            raise ValueError("the batched path takes rows already on the device (torch CUDA tensors)")
+        k, n = 1 << p.log2_k, 1 << (p.log2_k + p.log2_inv_rate)
+        if rows.numel() % k:
+            raise ValueError(f"{rows.numel()} values are not whole rows of {k}")
+        npolys = rows.numel() // k
+        cw = torch.empty(max(npolys * n, 1), dtype=torch.int64, device=rows.device)
+        nodes = torch.empty((2 * n - 1) * 32, dtype=torch.uint8, device=rows.device)
+        rc = ResidentCommitment(p, rows, cw, nodes)
+        out.append(rc)
+        arr[i].log_k, arr[i].log_inv_rate, arr[i].row_block = p.log2_k, p.log2_inv_rate, p.row_block
+        arr[i].commitment_id[:] = list(bytes(p.commitment_id))
+        arr[i].rows = rows.data_ptr()
+        arr[i].npolys = npolys
+        arr[i].codewords = cw.data_ptr()
+        arr[i].nodes = nodes.data_ptr()
+    return out, arr
+
+
+def commit_many(params_list: list[CommitmentParams], rows_list, device: Device | None = None,
+                workers: int = 0) -> list[ResidentCommitment]:
+    """Commits many unmasked batches of rows (device tensors, npolys x k words each) together on
+    `workers` streams; each result equals `commit_unmasked` of the same rows."""
+    import torch
+
+    d = resolve(device)
+    out, arr = _resident(params_list, rows_list, d)
+    torch.cuda.current_stream().synchronize()
+    N.call("tg_commit_many", d.handle, arr, len(out), workers)
+    for i, rc in enumerate(out):
+        rc.root = bytes(arr[i].root)
+    return out
+
+
+class CommitPlan:
+    """A batch of commitments captured into one CUDA graph: the shapes and device buffers are
+    fixed when the plan is made (the worker count autotuned on the batch unless given), and
+    every `launch()` re-commits whatever the row tensors hold then."""
+
+    def __init__(self, params_list: list[CommitmentParams], rows_list, device: Device | None = None, workers: int = 0):
+        import torch
+
+        self.device = resolve(device)
+        self.commitments, self._arr = _resident(params_list, rows_list, self.device)
+        torch.cuda.current_stream().synchronize()
+        self._plan = ctypes.c_void_p()
+        N.call("tg_commit_plan_create", self.device.handle, self._arr, len(self.commitments), workers,
+               ctypes.byref(self._plan))
+
+    def launch(self) -> list[Digest]:
+        import torch
+
+        torch.cuda.current_stream().synchronize()
+        roots = ctypes.create_string_buffer(32 * len(self.commitments))
+        N.call("tg_commit_plan_launch", self._plan, roots)
+        out = [roots.raw[32 * i: 32 * (i + 1)] for i in range(len(self.commitments))]
+        for rc, r in zip(self.commitments, out):
+            rc.root = r
+        return out
+
+    def info(self) -> dict:
+        w, kern = ctypes.c_int(), ctypes.c_uint64()
+        ms = (ctypes.c_double * 4)()
+        N.call("tg_commit_plan_info", self._plan, ctypes.byref(w), ctypes.byref(kern), ms)
+        return {"workers": w.value, "kernels_per_launch": kern.value,
+                "tuned_ms": {c: ms[i] for i, c in enumerate((1, 2, 4, 8)) if ms[i] > 0}}
+
+    def close(self):
+        if self._plan:
+            N.call("tg_commit_plan_destroy", self._plan)
+            self._plan = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

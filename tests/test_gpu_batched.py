@@ -1,7 +1,8 @@
 """The batched pattern on the GPU: many independent sumchecks proved together (one fused launch
-per round for all of them) give, byte for byte, what one-at-a-time proofs give — checked against
-the reference's golden sessions, the CPU oracle and the plain per-job path, on the batched
-workload's uneven shapes."""
+per round for all of them) and many commitments committed together (on several streams, or
+replayed from a captured CUDA graph) give, byte for byte, what one-at-a-time calls give — checked
+against the reference's golden sessions, the CPU oracle and the plain per-job path, on the
+batched workload's uneven shapes."""
 import numpy as np
 import pytest
 
@@ -164,3 +165,117 @@ def test_prove_many_refusal_leaves_transcripts(dev):
     with pytest.raises(N.TesseraError):
         prove_many(call, device=dev)
     assert [(t.state, t.counter) for t in ts] == before
+
+
+# ---- commitments --------------------------------------------------------------------------------
+
+def _commit_inputs(dev, max_log_k, max_polys, count=64):
+    import torch
+
+    from tessera_gb300.pcs import CommitmentParams
+    from tessera_gb300.workloads import batched, splitmix_words
+
+    shapes, _ = batched(0x00650003, commitments=count, sumchecks=0, max_log_k=max_log_k, max_polys=max_polys)
+    params = [CommitmentParams(s.log_k, s.log_inv_rate, 0, 32, s.commitment_id) for s in shapes]
+    rows = [torch.from_numpy(splitmix_words(s.seed, s.polys << s.log_k).view(np.int64)).to(f"cuda:{dev.ordinal}")
+            for s in shapes]
+    return params, rows
+
+
+def _plain(dev, p, rows):
+    """The plain path: one tg_commit_unmasked_dev call."""
+    import ctypes
+
+    import torch
+
+    from tessera_gb300 import _native as N
+
+    k, n = 1 << p.log2_k, 1 << (p.log2_k + p.log2_inv_rate)
+    npolys = rows.numel() // k
+    cw = torch.empty(max(npolys * n, 1), dtype=torch.int64, device=rows.device)
+    nodes = torch.empty((2 * n - 1) * 32, dtype=torch.uint8, device=rows.device)
+    root = ctypes.create_string_buffer(32)
+    cid = (ctypes.c_uint8 * 32)(*p.commitment_id)
+    torch.cuda.current_stream().synchronize()
+    N.call("tg_commit_unmasked_dev", dev.handle, p.log2_k, p.log2_inv_rate, p.row_block, cid,
+           ctypes.c_void_p(rows.data_ptr()), npolys, ctypes.c_void_p(cw.data_ptr()), ctypes.c_void_p(nodes.data_ptr()),
+           root, None)
+    return root.raw, nodes, cw
+
+
+@pytest.mark.parametrize("workers", [0, 1, 3, 8])
+def test_commit_many_vs_plain(dev, workers):
+    """64 commitments of the batched workload's uneven shapes (k up to 2^14, up to 32 rows) on
+    several streams equal the plain path, node for node and codeword for codeword."""
+    import torch
+
+    from tessera_gb300.pcs import commit_many
+
+    params, rows = _commit_inputs(dev, 14, 32)
+    res = commit_many(params, rows, device=dev, workers=workers)
+    for p, r, c in zip(params, rows, res):
+        root, nodes, cw = _plain(dev, p, r)
+        assert c.root == root
+        assert torch.equal(c.nodes, nodes) and torch.equal(c.codewords, cw)
+
+
+def test_commit_many_vs_oracle(dev):
+    from tessera_gb300.pcs import commit_many
+
+    params, rows = _commit_inputs(dev, 13, 8, count=12)
+    res = commit_many(params, rows, device=dev)
+    for p, r, c in zip(params, rows, res):
+        host = r.cpu().numpy().view(np.uint64)
+        _, leaves, root = O.commit_unmasked(host, p.log2_k, p.log2_inv_rate, 32, p.commitment_id,
+                                            threads=O.threads_available(), keep_codewords=False)
+        assert c.root == root and b"".join(c.leaves()) == leaves.tobytes()
+
+
+def test_commit_plan_replays(dev):
+    """A captured plan (worker count autotuned) equals the plain path, and a second launch after
+    the rows were overwritten in place commits the new contents."""
+    import torch
+
+    from tessera_gb300.pcs import CommitPlan
+    from tessera_gb300.workloads import splitmix_words
+
+    params, rows = _commit_inputs(dev, 15, 128, count=24)
+    plan = CommitPlan(params, rows, device=dev)
+    try:
+        info = plan.info()
+        assert info["workers"] in (1, 2, 4, 8) and info["kernels_per_launch"] > 0
+        assert set(info["tuned_ms"]) == {1, 2, 4, 8}
+        for rnd in range(2):
+            if rnd:
+                for i, r in enumerate(rows):
+                    r.copy_(torch.from_numpy(splitmix_words(0xABC + i, r.numel()).view(np.int64)).to(r.device))
+            roots = plan.launch()
+            for p, r, c, root in zip(params, rows, plan.commitments, roots):
+                proot, nodes, cw = _plain(dev, p, r)
+                assert root == proot and torch.equal(c.nodes, nodes) and torch.equal(c.codewords, cw)
+    finally:
+        plan.close()
+
+
+def test_commit_many_large_shapes(dev):
+    """The batched workload with k up to 2^18 and up to 128 rows per commitment: batched equals
+    plain on every root."""
+    from tessera_gb300.pcs import commit_many
+
+    params, rows = _commit_inputs(dev, 18, 128, count=32)
+    res = commit_many(params, rows, device=dev)
+    for p, r, c in zip(params, rows, res):
+        assert c.root == _plain(dev, p, r)[0]
+
+
+def test_commit_many_refusals(dev):
+    import torch
+
+    from tessera_gb300 import _native as N
+    from tessera_gb300.pcs import CommitmentParams, commit_many
+
+    rows = torch.zeros(4 << 10, dtype=torch.int64, device=f"cuda:{dev.ordinal}")
+    for bad in (CommitmentParams(10, 0, 0, 32, bytes(32)), CommitmentParams(10, 5, 0, 32, bytes(32)),
+                CommitmentParams(10, 1, 0, 0, bytes(32)), CommitmentParams(10, 1, 0, 125, bytes(32))):
+        with pytest.raises(N.TesseraError):
+            commit_many([CommitmentParams(10, 1, 0, 32, bytes(32)), bad], [rows, rows], device=dev)
