@@ -73,6 +73,12 @@ typedef struct tg_int_peaks {
     double blake3_compressions_per_s;
 } tg_int_peaks;
 int tg_measure_int_peaks(tg_device *dev, tg_int_peaks *out);
+
+/* Synthetic inputs on the device (no reference counterpart; the reference benchmark draws the
+ * same words on the host, crates/tessera-bench/benches/primitives.rs:52-69): out[i] is the
+ * (i + 1)-th SplitMix64 output from `seed`, reduced once below p. Enqueued on `stream` (NULL:
+ * the device's stream). */
+int tg_fill_splitmix(tg_device *dev, uint64_t *out, size_t n, uint64_t seed, void *stream);
 /* Per-kernel timing (no counterpart in the reference; its GPU timing lives in benchmark
  * harnesses, crates/tessera-bench/examples/gpu_unit_costs.rs): while enabled, every launch is
  * bracketed by CUDA events on its own stream. tg_profile_read sums the elapsed times by kernel

@@ -70,6 +70,7 @@ SIGNATURES = {
     "tg_device_sync": [V],
     "tg_device_launches": [V, V],
     "tg_measure_int_peaks": [V, V],
+    "tg_fill_splitmix": [V, V, SZ, U64, V],
     "tg_device_stream": [V, V],
     "tg_profile_enable": [V, INT],
     "tg_profile_read": [V, V, SZ, V, V, V, SZ, V],

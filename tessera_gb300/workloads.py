@@ -32,6 +32,17 @@ def splitmix_words(seed: int, n: int) -> np.ndarray:
     return out
 
 
+def fill_device(tensor, seed: int, device=None):
+    """Fills an int64 CUDA tensor in place with splitmix_words(seed, numel), generated on the GPU."""
+    from . import _native as N
+    from .device import resolve
+
+    d = resolve(device)
+    N.call("tg_fill_splitmix", d.handle, tensor.data_ptr(), tensor.numel(), seed & (2**64 - 1), None)
+    d.sync()
+    return tensor
+
+
 class _Stream:
     def __init__(self, seed: int):
         self.state = seed & (2**64 - 1)

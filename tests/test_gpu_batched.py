@@ -279,3 +279,14 @@ def test_commit_many_refusals(dev):
                 CommitmentParams(10, 1, 0, 0, bytes(32)), CommitmentParams(10, 1, 0, 125, bytes(32))):
         with pytest.raises(N.TesseraError):
             commit_many([CommitmentParams(10, 1, 0, 32, bytes(32)), bad], [rows, rows], device=dev)
+
+
+def test_fill_splitmix_matches_host(dev):
+    """The device generator of synthetic inputs equals the host SplitMix64 words."""
+    import torch
+
+    from tessera_gb300.workloads import fill_device, splitmix_words
+
+    for seed, n in ((0, 1), (0x00650003, 12345), (2**64 - 1, 1 << 20)):
+        t = fill_device(torch.empty(n, dtype=torch.int64, device=f"cuda:{dev.ordinal}"), seed, dev)
+        assert (t.cpu().numpy().view(np.uint64) == splitmix_words(seed, n)).all()
