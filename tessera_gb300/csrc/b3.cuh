@@ -40,14 +40,33 @@ __host__ __device__ __forceinline__ uint32_t rotr(uint32_t x, int n) {
 #endif
 }
 
+#ifdef __CUDACC__
+// The compression is bound by the integer ALU pipe (the XORs and the funnel-shift rotations), so
+// on the device its additions go to the otherwise idle multiply-add pipe as x·1 + y with the 1
+// read from constant memory, where the compiler cannot fold it away.
+static __constant__ uint32_t k_b3_one = 1;
+#endif
+#ifdef __CUDA_ARCH__
+__device__ __forceinline__ uint32_t madd(uint32_t x, uint32_t y) {
+    uint32_t r;
+    asm("mad.lo.u32 %0, %1, %2, %3;" : "=r"(r) : "r"(x), "r"(k_b3_one), "r"(y));
+    return r;
+}
+#define TG_B3_ADD3(a, b, x) madd(madd(b, x), a)
+#define TG_B3_ADD2(a, b) madd(b, a)
+#else
+#define TG_B3_ADD3(a, b, x) ((a) + (b) + (x))
+#define TG_B3_ADD2(a, b) ((a) + (b))
+#endif
+
 #define TG_B3_G(a, b, c, d, x, y)  \
-    a = a + b + (x);               \
+    a = TG_B3_ADD3(a, b, (x));     \
     d = rotr(d ^ a, 16);           \
-    c = c + d;                     \
+    c = TG_B3_ADD2(c, d);          \
     b = rotr(b ^ c, 12);           \
-    a = a + b + (y);               \
+    a = TG_B3_ADD3(a, b, (y));     \
     d = rotr(d ^ a, 8);            \
-    c = c + d;                     \
+    c = TG_B3_ADD2(c, d);          \
     b = rotr(b ^ c, 7);
 
 // One round on the state words s0..s15 with the message words in their permuted order for the
