@@ -163,6 +163,7 @@ int tg_commit_plan_launch(tg_commit_plan *plan, uint8_t *roots);
  * 1, 2, 4 and 8 workers (0 where not tried). */
 int tg_commit_plan_info(const tg_commit_plan *plan, int *workers, uint64_t *kernels, double tuned_ms[4]);
 int tg_commit_plan_destroy(tg_commit_plan *plan);
+
 /* merge_segments on host buffers (crates/tessera-pcs/src/streaming.rs:382-404). */
 int tg_merge_segments(tg_device *dev, const uint8_t *segment_chains, size_t nsegments, uint64_t n,
                       uint8_t *leaves, uint8_t root[32]);
@@ -265,6 +266,51 @@ int tg_level_bind(tg_level *l, const uint64_t r[2]);
 /* Each table's first entry, in table order (ntables Fp2). */
 int tg_level_firsts(tg_level *l, uint64_t *out);
 int tg_level_free(tg_level *l);
+
+/* ---- Serving: a proof server with continuous batching (no reference counterpart: the serving
+ * pattern around the hot path). A request's proof is the resident unmasked commitment of its rows
+ * (commit_unmasked, crates/tessera-pcs/src/commitment.rs:343-458), the root absorbed into the
+ * request's transcript under "<prefix>/root", then prove_batch of one instance, the product of its
+ * prime-field tables, under <prefix> (crates/tessera-sumcheck/src/prover.rs:1122). Requests are
+ * admitted first come first served while a stream slot is free and their device footprint fits
+ * the HBM budget (a request larger than the budget runs alone); admitted requests run on their own
+ * streams with stream-ordered device memory, so their work overlaps on the GPU, and a scheduler
+ * thread advances each one. Results are byte-identical to proving the request alone. Host rows and
+ * tables must stay valid until the request completes (pinned memory lets their copies overlap). */
+typedef struct {
+    uint32_t log_k, log_inv_rate, row_block;
+    uint8_t commitment_id[32];
+    const uint64_t *rows;          /* host: npolys x 2^log_k */
+    size_t npolys;
+    int degree, ntables, vars;     /* the sumcheck: ntables prime-field tables of 2^vars entries */
+    const uint64_t *const *tables; /* host */
+    tg_transcript transcript;      /* the proof's transcript at its start */
+    const char *prefix;
+} tg_proof_request;
+typedef struct {
+    int status;                    /* TG_OK once done */
+    uint8_t root[32];
+    uint64_t gamma[2];
+    uint64_t *rounds;              /* caller buffers: vars x degree Fp2 */
+    uint64_t *challenges;          /* vars Fp2 */
+    uint64_t *final_evals;         /* ntables Fp2 */
+    tg_transcript transcript;      /* at the end of the proof */
+    double queued_ms, latency_ms;  /* submission to admission, submission to completion */
+} tg_proof_result;
+typedef struct {
+    uint64_t submitted, completed, peak_inflight;
+    size_t peak_bytes;
+} tg_server_stats;
+typedef struct tg_server tg_server;
+int tg_server_open(tg_device *dev, size_t hbm_budget_bytes, int max_inflight, tg_server **out);
+/* Queues a request; *out is filled when it completes (collect it with tg_server_wait). */
+int tg_server_submit(tg_server *server, const tg_proof_request *request, tg_proof_result *out, uint64_t *ticket);
+/* Waits for a ticket (timeout_ms < 0: no limit): TG_OK, the request's error, or TG_DECLINED on
+ * timeout. Each ticket is collected once. */
+int tg_server_wait(tg_server *server, uint64_t ticket, int timeout_ms);
+int tg_server_stats_read(tg_server *server, tg_server_stats *out);
+/* Finishes every queued and running request, then releases the server. */
+int tg_server_close(tg_server *server);
 
 #ifdef __cplusplus
 }

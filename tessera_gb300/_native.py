@@ -49,6 +49,24 @@ class CommitJobC(ctypes.Structure):
                 ("codewords", ctypes.c_void_p), ("nodes", ctypes.c_void_p), ("root", ctypes.c_uint8 * 32)]
 
 
+class ProofRequestC(ctypes.Structure):
+    _fields_ = [("log_k", ctypes.c_uint32), ("log_inv_rate", ctypes.c_uint32), ("row_block", ctypes.c_uint32),
+                ("commitment_id", ctypes.c_uint8 * 32), ("rows", ctypes.c_void_p), ("npolys", ctypes.c_size_t),
+                ("degree", ctypes.c_int), ("ntables", ctypes.c_int), ("vars", ctypes.c_int),
+                ("tables", ctypes.POINTER(ctypes.c_void_p)), ("transcript", TranscriptState), ("prefix", ctypes.c_char_p)]
+
+
+class ProofResultC(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int), ("root", ctypes.c_uint8 * 32), ("gamma", ctypes.c_uint64 * 2),
+                ("rounds", ctypes.c_void_p), ("challenges", ctypes.c_void_p), ("final_evals", ctypes.c_void_p),
+                ("transcript", TranscriptState), ("queued_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+
+
+class ServerStatsC(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("peak_inflight", ctypes.c_uint64),
+                ("peak_bytes", ctypes.c_size_t)]
+
+
 class SumcheckJobC(ctypes.Structure):
     _fields_ = [("transcript", ctypes.c_void_p), ("prefix", ctypes.c_char_p), ("degree", ctypes.c_int),
                 ("instances", ctypes.POINTER(InstanceC)), ("ninstances", ctypes.c_int),
@@ -109,6 +127,11 @@ SIGNATURES = {
     "tg_commit_plan_launch": [V, V],
     "tg_commit_plan_info": [V, V, V, V],
     "tg_commit_plan_destroy": [V],
+    "tg_server_open": [V, SZ, INT, V],
+    "tg_server_submit": [V, V, V, V],
+    "tg_server_wait": [V, U64, INT],
+    "tg_server_stats_read": [V, V],
+    "tg_server_close": [V],
     "tg_level_load": [V, INT, V, V, INT, SZ, V],
     "tg_level_sums": [V, V, V, SZ, U32, V],
     "tg_level_bind": [V, V],

@@ -124,6 +124,21 @@ int column_absorb(Device* d, uint8_t* chains, uint64_t ncols, const uint64_t* ro
 int merkle_tree(Device* d, const uint8_t* leaves, size_t n, uint8_t* nodes, cudaStream_t s);
 int column_merge(Device* d, const uint8_t* segs, size_t nseg, uint64_t n, uint8_t* leaves, cudaStream_t s);
 
+// ---- sumcheck in phases (sumcheck.cu), for callers with their own streams and memory --------
+// sc_prepare validates the jobs and draws each job's γ on its host transcript (NULL and *status
+// on refusal, transcripts untouched); sc_enqueue launches everything on stream s over `arena`
+// (sc_arena_bytes of device memory) and copies the results into `host_out` (sc_host_bytes; pinned
+// memory for the copy to stay asynchronous); once the stream has run, sc_finish updates the
+// transcripts and outputs. sc_restore puts the transcripts back as they were before sc_prepare.
+struct ScRun;
+ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device, int* status);
+size_t sc_arena_bytes(const ScRun* r);
+size_t sc_host_bytes(const ScRun* r);
+int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out);
+int sc_finish(ScRun* r);
+int sc_restore(ScRun* r, int rc);
+void sc_free(ScRun* r);
+
 // ---- host BLAKE3 and transcript (host.cpp) --------------------------------------------------
 void host_hash(const uint32_t key[8], const uint8_t* in, size_t len, uint8_t out[32]);
 

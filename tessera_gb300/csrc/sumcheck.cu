@@ -418,7 +418,8 @@ static void with_degree(int degree, F&& f) {
 }
 
 struct TableState {
-    const uint64_t* src = nullptr;  // original entries (device)
+    const uint64_t* src = nullptr;  // original entries (device, once uploaded)
+    const uint64_t* host = nullptr; // original entries in host memory (when not on the device)
     bool base = false, is_public = false;
     size_t up_off = 0, buf_off[2] = {0, 0};
 };
@@ -446,99 +447,146 @@ static int check_job(const tg_sumcheck_job& jb, int index) {
     return TG_OK;
 }
 
-static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device) {
-    if (njobs < 1 || !jobs) return fail(TG_ERR_INVALID, "no sumcheck jobs");
-    for (int b = 0; b < njobs; b++) {
-        int rc = check_job(jobs[b], b);
-        if (rc) return rc;
-    }
-    std::lock_guard<std::mutex> lock(d->mu);
-    cudaStream_t s = d->stream;
-    std::vector<tg_transcript> saved(njobs);
-    for (int b = 0; b < njobs; b++) saved[b] = *jobs[b].transcript;
-    auto restore = [&](int rc) {
-        for (int b = 0; b < njobs; b++) *jobs[b].transcript = saved[b];
-        return rc;
-    };
+struct Plan {
+    std::vector<std::pair<int, int>> who;  // (instance, own round, or −1 for a product sum)
+    int blocks = 0;
+};
 
-    // ---- per job: γ (host transcript), weights; per instance: padding
+// One prove_many call in flight: planned on the host (γ drawn), then enqueued on a stream over
+// a device arena, then finished on the host once the stream has run.
+struct ScRun {
+    tg_sumcheck_job* jobs = nullptr;
+    int njobs = 0, tables_on_device = 0;
+    std::vector<tg_transcript> saved;
     std::vector<InstState> inst;
-    std::vector<int> n_max(njobs, 0), inst0(njobs, 0);
+    std::vector<int> n_max, inst0;
     std::vector<fp2> weights;
     int D = 1, J = 0, nevals = 0;
     size_t rounds_words = 0, chal_words = 0;
-    std::vector<uint64_t> rounds_off(njobs), chal_off(njobs), evals_off(njobs);
+    std::vector<uint64_t> rounds_off, chal_off, evals_off;
+    std::vector<Plan> plans;
+    size_t max_segs = 1, max_blocks = 1, total_segs = 0, nbind = 0;
+    int seg_cap = 1;
+    // arena layout (offsets from the arena's base)
+    size_t off_fs = 0, off_jobs = 0, off_w = 0, off_pad = 0, off_S = 0, off_msg = 0, off_rounds = 0, off_chal = 0,
+           off_partials = 0, off_counters = 0, off_segs = 0, off_bind = 0, off_erefs = 0, off_evals = 0;
+    size_t arena_bytes = 0;
+    // host-side staging that the enqueued copies read (kept until finish)
+    std::vector<FsState> fs0;
+    std::vector<FsJob> hj;
+    std::vector<uint64_t> wv;
+    std::vector<int> pads;
+    std::vector<Seg> all_segs;
+    std::vector<size_t> plan_seg0;
+    std::vector<BindLast> binds;
+    std::vector<EvalRef> erefs;
+    // the host block the results come back into: FsState[njobs], rounds, challenges, evaluations
+    size_t host_bytes = 0;
+    const uint8_t* host_out = nullptr;
+};
+
+int sc_restore(ScRun* r, int rc) {
+    for (int b = 0; b < r->njobs; b++) *r->jobs[b].transcript = r->saved[b];
+    return rc;
+}
+
+ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device, int* status) {
+    *status = TG_OK;
+    if (njobs < 1 || !jobs) {
+        *status = fail(TG_ERR_INVALID, "no sumcheck jobs");
+        return nullptr;
+    }
+    for (int b = 0; b < njobs; b++) {
+        *status = check_job(jobs[b], b);
+        if (*status) return nullptr;
+    }
+    ScRun* r = new ScRun();
+    r->jobs = jobs;
+    r->njobs = njobs;
+    r->tables_on_device = tables_on_device;
+    r->saved.resize(njobs);
+    for (int b = 0; b < njobs; b++) r->saved[b] = *jobs[b].transcript;
+    r->n_max.assign(njobs, 0);
+    r->inst0.assign(njobs, 0);
+    r->rounds_off.resize(njobs);
+    r->chal_off.resize(njobs);
+    r->evals_off.resize(njobs);
+
+    // per job: γ (host transcript), weights; per instance: padding
     for (int b = 0; b < njobs; b++) {
         tg_sumcheck_job& jb = jobs[b];
         uint64_t g[2];
         int rc = tg_transcript_challenge_fp2(jb.transcript, (std::string(jb.prefix) + "/gamma").c_str(), g);
-        if (rc) return restore(rc);
+        if (rc) {
+            *status = sc_restore(r, rc);
+            delete r;
+            return nullptr;
+        }
         jb.gamma[0] = g[0];
         jb.gamma[1] = g[1];
         const fp2 gam = {g[0], g[1]};
-        D = std::max(D, jb.degree);
-        inst0[b] = (int)inst.size();
-        for (int i = 0; i < jb.ninstances; i++) n_max[b] = std::max(n_max[b], jb.instances[i].vars);
-        J = std::max(J, n_max[b]);
+        r->D = std::max(r->D, jb.degree);
+        r->inst0[b] = (int)r->inst.size();
+        for (int i = 0; i < jb.ninstances; i++) r->n_max[b] = std::max(r->n_max[b], jb.instances[i].vars);
+        r->J = std::max(r->J, r->n_max[b]);
         fp2 acc = {1, 0};
-        evals_off[b] = (uint64_t)nevals * 2;
+        r->evals_off[b] = (uint64_t)r->nevals * 2;
         for (int i = 0; i < jb.ninstances; i++) {
             const tg_instance& src = jb.instances[i];
             InstState is;
             is.job = b;
             is.vars = src.vars;
-            is.pad = n_max[b] - src.vars;
+            is.pad = r->n_max[b] - src.vars;
             for (int k = 0; k < src.ntables; k++) {
                 TableState ts;
-                ts.src = src.tables[k].values;
+                if (tables_on_device)
+                    ts.src = src.tables[k].values;
+                else
+                    ts.host = src.tables[k].values;
                 ts.base = !src.tables[k].is_ext;
                 ts.is_public = src.tables[k].is_public != 0;
-                if (!ts.is_public) nevals++;
+                if (!ts.is_public) r->nevals++;
                 is.tables.push_back(ts);
             }
-            inst.push_back(std::move(is));
-            weights.push_back(acc);
+            r->inst.push_back(std::move(is));
+            r->weights.push_back(acc);
             acc = e_mul(acc, gam);
         }
-        rounds_off[b] = rounds_words;
-        chal_off[b] = chal_words;
-        rounds_words += (size_t)n_max[b] * 2 * jb.degree;
-        chal_words += (size_t)n_max[b] * 2;
+        r->rounds_off[b] = r->rounds_words;
+        r->chal_off[b] = r->chal_words;
+        r->rounds_words += (size_t)r->n_max[b] * 2 * jb.degree;
+        r->chal_words += (size_t)r->n_max[b] * 2;
     }
-    const int ninst = (int)inst.size();
+    const int ninst = (int)r->inst.size();
 
-    // ---- the launches' segments, all planned before anything runs
-    const int seg_cap = std::min(SC_MAX_SEG_BLOCKS, 4 * d->sm_count);
+    // the launches' segments, all planned before anything runs
+    r->seg_cap = std::min(SC_MAX_SEG_BLOCKS, 4 * d->sm_count);
+    const int seg_cap = r->seg_cap;
     auto blocks_for = [&](uint64_t n) {
         return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + SC_THREADS - 1) / SC_THREADS, seg_cap));
     };
-    struct Plan {
-        std::vector<std::pair<int, int>> who;  // (instance, own round, or −1 for a product sum)
-        int blocks = 0;
-    };
-    std::vector<Plan> plans(1 + J);  // [0]: product sums, [1 + j]: round j
+    r->plans.resize(1 + r->J);  // [0]: product sums, [1 + j]: round j
     for (int i = 0; i < ninst; i++)
-        if (inst[i].pad > 0) plans[0].who.push_back({i, -1});
-    for (int j = 0; j < J; j++)
+        if (r->inst[i].pad > 0) r->plans[0].who.push_back({i, -1});
+    for (int j = 0; j < r->J; j++)
         for (int i = 0; i < ninst; i++) {
-            const int own = j - inst[i].pad;
-            if (own >= 0 && own < inst[i].vars) plans[1 + j].who.push_back({i, own});
+            const int own = j - r->inst[i].pad;
+            if (own >= 0 && own < r->inst[i].vars) r->plans[1 + j].who.push_back({i, own});
         }
-    size_t max_segs = 1, max_blocks = 1, total_segs = 0;
-    for (auto& p : plans) {
+    for (auto& p : r->plans) {
         for (auto& w : p.who) {
-            const InstState& is = inst[w.first];
+            const InstState& is = r->inst[w.first];
             const uint64_t n = w.second < 0 ? (1ull << is.vars) : (1ull << (is.vars - w.second - 1));
             p.blocks += blocks_for(n);
         }
-        max_segs = std::max(max_segs, p.who.size());
-        max_blocks = std::max(max_blocks, (size_t)p.blocks);
-        total_segs += p.who.size();
+        r->max_segs = std::max(r->max_segs, p.who.size());
+        r->max_blocks = std::max(r->max_blocks, (size_t)p.blocks);
+        r->total_segs += p.who.size();
     }
 
-    // ---- device memory: one arena for tables, transcripts, plans and outputs
+    // the arena: tables, transcripts, plans and outputs
     Arena ar;
-    for (auto& is : inst) {
+    for (auto& is : r->inst) {
         const size_t len = (size_t)1 << is.vars;
         for (auto& ts : is.tables) {
             ts.up_off = tables_on_device ? 0 : ar.take(len * (ts.base ? 8 : 16));
@@ -546,47 +594,66 @@ static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on
             ts.buf_off[1] = is.vars >= 2 ? ar.take(std::max<size_t>(len / 4, 1) * 16) : 0;
         }
     }
-    const size_t off_fs = ar.take(sizeof(FsState) * njobs), off_jobs = ar.take(sizeof(FsJob) * njobs);
-    const size_t off_w = ar.take(16 * ninst), off_pad = ar.take(4 * ninst), off_S = ar.take(16 * ninst);
-    const size_t off_msg = ar.take((size_t)8 * SC_MSG_WORDS * ninst);
-    const size_t off_rounds = ar.take(8 * std::max<size_t>(rounds_words, 1));
-    const size_t off_chal = ar.take(8 * std::max<size_t>(chal_words, 1));
-    const size_t off_partials = ar.take(max_blocks * 2 * SC_MAX_DEGREE * 8);
-    const size_t off_counters = ar.take(4 * max_segs);
-    const size_t off_segs = ar.take(sizeof(Seg) * std::max<size_t>(total_segs, 1));
-    size_t nbind = 0;
-    for (auto& is : inst)
-        if (is.vars >= 1) nbind += is.tables.size();
-    const size_t off_bind = ar.take(sizeof(BindLast) * std::max<size_t>(nbind, 1));
-    const size_t off_erefs = ar.take(sizeof(EvalRef) * std::max(nevals, 1));
-    const size_t off_evals = ar.take(16 * std::max(nevals, 1));
-    int rc = d->scratch_sc.ensure(ar.used);
-    if (rc) return restore(rc);
-    ar.base = (uint8_t*)d->scratch_sc.ptr;
+    r->off_fs = ar.take(sizeof(FsState) * njobs);
+    r->off_jobs = ar.take(sizeof(FsJob) * njobs);
+    r->off_w = ar.take(16 * ninst);
+    r->off_pad = ar.take(4 * ninst);
+    r->off_S = ar.take(16 * ninst);
+    r->off_msg = ar.take((size_t)8 * SC_MSG_WORDS * ninst);
+    r->off_rounds = ar.take(8 * std::max<size_t>(r->rounds_words, 1));
+    r->off_chal = ar.take(8 * std::max<size_t>(r->chal_words, 1));
+    r->off_partials = ar.take(r->max_blocks * 2 * SC_MAX_DEGREE * 8);
+    r->off_counters = ar.take(4 * r->max_segs);
+    r->off_segs = ar.take(sizeof(Seg) * std::max<size_t>(r->total_segs, 1));
+    for (auto& is : r->inst)
+        if (is.vars >= 1) r->nbind += is.tables.size();
+    r->off_bind = ar.take(sizeof(BindLast) * std::max<size_t>(r->nbind, 1));
+    r->off_erefs = ar.take(sizeof(EvalRef) * std::max(r->nevals, 1));
+    r->off_evals = ar.take(16 * std::max(r->nevals, 1));
+    r->arena_bytes = ar.used;
+    r->host_bytes = sizeof(FsState) * njobs + 8 * (r->rounds_words + r->chal_words) + 16 * (size_t)r->nevals;
+    return r;
+}
+
+size_t sc_arena_bytes(const ScRun* r) { return r->arena_bytes; }
+size_t sc_host_bytes(const ScRun* r) { return r->host_bytes; }
+void sc_free(ScRun* r) { delete r; }
+
+int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out) {
+    Arena ar;
+    ar.base = (uint8_t*)arena;
+    ar.used = r->arena_bytes;
+    r->host_out = (const uint8_t*)host_out;
+    const int njobs = r->njobs, ninst = (int)r->inst.size();
+    tg_sumcheck_job* jobs = r->jobs;
 
     // tables: the current entries after `bound` binds are src (bound 0), else buf[(bound − 1) & 1]
-    for (auto& is : inst)
+    for (auto& is : r->inst)
         for (auto& ts : is.tables) {
-            if (!tables_on_device) {
+            if (ts.host) {
                 uint64_t* dst = ar.at<uint64_t>(ts.up_off);
                 const size_t bytes = ((size_t)1 << is.vars) * (ts.base ? 8 : 16);
-                TG_CUDA(cudaMemcpyAsync(dst, ts.src, bytes, cudaMemcpyHostToDevice, s));
+                TG_CUDA(cudaMemcpyAsync(dst, ts.host, bytes, cudaMemcpyHostToDevice, s));
                 ts.src = dst;
             }
         }
     auto cur = [&](const InstState& is, int k, int bound) -> const uint64_t* {
         return bound == 0 ? is.tables[k].src : ar.at<uint64_t>(is.tables[k].buf_off[(bound - 1) & 1]);
     };
-    FsState* dfs = ar.at<FsState>(off_fs);
-    uint64_t* dS = ar.at<uint64_t>(off_S);
-    uint64_t* dmsg = ar.at<uint64_t>(off_msg);
-    std::vector<Seg> all_segs;
-    std::vector<size_t> plan_seg0;
-    for (auto& p : plans) {
-        plan_seg0.push_back(all_segs.size());
+    const int seg_cap = r->seg_cap;
+    auto blocks_for = [&](uint64_t n) {
+        return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + SC_THREADS - 1) / SC_THREADS, seg_cap));
+    };
+    FsState* dfs = ar.at<FsState>(r->off_fs);
+    uint64_t* dS = ar.at<uint64_t>(r->off_S);
+    uint64_t* dmsg = ar.at<uint64_t>(r->off_msg);
+    r->all_segs.clear();
+    r->plan_seg0.clear();
+    for (auto& p : r->plans) {
+        r->plan_seg0.push_back(r->all_segs.size());
         int block0 = 0;
         for (auto& w : p.who) {
-            const InstState& is = inst[w.first];
+            const InstState& is = r->inst[w.first];
             Seg g;
             memset(&g, 0, sizeof g);
             g.nt = (int)is.tables.size();
@@ -615,13 +682,13 @@ static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on
             g.nblocks = blocks_for(g.n);
             g.part0 = block0;
             block0 += g.nblocks;
-            all_segs.push_back(g);
+            r->all_segs.push_back(g);
         }
     }
     // the last own round's challenge, bound into one entry per table; then the final evaluations
-    std::vector<BindLast> binds;
-    std::vector<EvalRef> erefs;
-    for (auto& is : inst) {
+    r->binds.clear();
+    r->erefs.clear();
+    for (auto& is : r->inst) {
         for (int k = 0; k < (int)is.tables.size(); k++) {
             const uint64_t* fin = is.tables[k].src;
             bool fin_base = is.tables[k].base;
@@ -632,7 +699,7 @@ static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on
                 bl.base = is.vars == 1 && is.tables[k].base;
                 bl.dst = ar.at<uint64_t>(is.tables[k].buf_off[(is.vars - 1) & 1]);
                 bl.r = dfs[is.job].r;
-                binds.push_back(bl);
+                r->binds.push_back(bl);
                 fin = bl.dst;
                 fin_base = false;
             }
@@ -641,126 +708,159 @@ static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on
                 memset(&e, 0, sizeof e);
                 e.ptr = fin;
                 e.base = fin_base;
-                erefs.push_back(e);
+                r->erefs.push_back(e);
             }
         }
     }
 
-    // ---- uploads: transcripts, jobs, weights, pads, plans
-    std::vector<FsState> fs0(njobs);
-    std::vector<FsJob> hj(njobs);
+    // uploads: transcripts, jobs, weights, pads, plans
+    r->fs0.assign(njobs, FsState());
+    r->hj.assign(njobs, FsJob());
     FsKeys keys;
     context_key("transcript-absorb", keys.absorb);
     context_key("transcript-squeeze", keys.squeeze);
     context_key("transcript-ratchet", keys.ratchet);
     for (int b = 0; b < njobs; b++) {
-        memset(&fs0[b], 0, sizeof(FsState));
-        memcpy(fs0[b].state, jobs[b].transcript->state, 32);
-        fs0[b].counter = jobs[b].transcript->counter;
-        memset(&hj[b], 0, sizeof(FsJob));
-        hj[b].label_len = (int)strlen(jobs[b].prefix);
-        memcpy(hj[b].label, jobs[b].prefix, hj[b].label_len);
-        hj[b].degree = jobs[b].degree;
-        hj[b].ninst = jobs[b].ninstances;
-        hj[b].n_max = n_max[b];
-        hj[b].inst0 = inst0[b];
-        hj[b].rounds_off = rounds_off[b];
-        hj[b].chal_off = chal_off[b];
+        memset(&r->fs0[b], 0, sizeof(FsState));
+        memcpy(r->fs0[b].state, jobs[b].transcript->state, 32);
+        r->fs0[b].counter = jobs[b].transcript->counter;
+        memset(&r->hj[b], 0, sizeof(FsJob));
+        r->hj[b].label_len = (int)strlen(jobs[b].prefix);
+        memcpy(r->hj[b].label, jobs[b].prefix, r->hj[b].label_len);
+        r->hj[b].degree = jobs[b].degree;
+        r->hj[b].ninst = jobs[b].ninstances;
+        r->hj[b].n_max = r->n_max[b];
+        r->hj[b].inst0 = r->inst0[b];
+        r->hj[b].rounds_off = r->rounds_off[b];
+        r->hj[b].chal_off = r->chal_off[b];
     }
-    std::vector<uint64_t> wv(2 * ninst);
-    std::vector<int> pads(ninst);
+    r->wv.assign(2 * ninst, 0);
+    r->pads.assign(ninst, 0);
     for (int i = 0; i < ninst; i++) {
-        wv[2 * i] = weights[i].c0;
-        wv[2 * i + 1] = weights[i].c1;
-        pads[i] = inst[i].pad;
+        r->wv[2 * i] = r->weights[i].c0;
+        r->wv[2 * i + 1] = r->weights[i].c1;
+        r->pads[i] = r->inst[i].pad;
     }
-    // Each copy below reads a host vector that lives until the stream synchronizes at the end.
-    TG_CUDA(cudaMemcpyAsync(dfs, fs0.data(), sizeof(FsState) * njobs, cudaMemcpyHostToDevice, s));
-    TG_CUDA(cudaMemcpyAsync(ar.at<FsJob>(off_jobs), hj.data(), sizeof(FsJob) * njobs, cudaMemcpyHostToDevice, s));
-    TG_CUDA(cudaMemcpyAsync(ar.at<uint64_t>(off_w), wv.data(), 16 * ninst, cudaMemcpyHostToDevice, s));
-    TG_CUDA(cudaMemcpyAsync(ar.at<int>(off_pad), pads.data(), 4 * ninst, cudaMemcpyHostToDevice, s));
-    if (!all_segs.empty())
-        TG_CUDA(cudaMemcpyAsync(ar.at<Seg>(off_segs), all_segs.data(), sizeof(Seg) * all_segs.size(),
+    // The copies read host vectors of the run, which live until sc_free.
+    TG_CUDA(cudaMemcpyAsync(dfs, r->fs0.data(), sizeof(FsState) * njobs, cudaMemcpyHostToDevice, s));
+    TG_CUDA(cudaMemcpyAsync(ar.at<FsJob>(r->off_jobs), r->hj.data(), sizeof(FsJob) * njobs, cudaMemcpyHostToDevice, s));
+    TG_CUDA(cudaMemcpyAsync(ar.at<uint64_t>(r->off_w), r->wv.data(), 16 * ninst, cudaMemcpyHostToDevice, s));
+    TG_CUDA(cudaMemcpyAsync(ar.at<int>(r->off_pad), r->pads.data(), 4 * ninst, cudaMemcpyHostToDevice, s));
+    if (!r->all_segs.empty())
+        TG_CUDA(cudaMemcpyAsync(ar.at<Seg>(r->off_segs), r->all_segs.data(), sizeof(Seg) * r->all_segs.size(),
                                 cudaMemcpyHostToDevice, s));
-    if (!binds.empty())
-        TG_CUDA(cudaMemcpyAsync(ar.at<BindLast>(off_bind), binds.data(), sizeof(BindLast) * binds.size(),
+    if (!r->binds.empty())
+        TG_CUDA(cudaMemcpyAsync(ar.at<BindLast>(r->off_bind), r->binds.data(), sizeof(BindLast) * r->binds.size(),
                                 cudaMemcpyHostToDevice, s));
-    if (!erefs.empty())
-        TG_CUDA(cudaMemcpyAsync(ar.at<EvalRef>(off_erefs), erefs.data(), sizeof(EvalRef) * erefs.size(),
+    if (!r->erefs.empty())
+        TG_CUDA(cudaMemcpyAsync(ar.at<EvalRef>(r->off_erefs), r->erefs.data(), sizeof(EvalRef) * r->erefs.size(),
                                 cudaMemcpyHostToDevice, s));
-    TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(off_counters), 0, 4 * max_segs, s));
+    TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(r->off_counters), 0, 4 * r->max_segs, s));
 
-    // ---- the launches
-    uint64_t* partials = ar.at<uint64_t>(off_partials);
-    unsigned* counters = ar.at<unsigned>(off_counters);
-    uint64_t* drounds = ar.at<uint64_t>(off_rounds);
-    uint64_t* dchal = ar.at<uint64_t>(off_chal);
+    // the launches
+    uint64_t* partials = ar.at<uint64_t>(r->off_partials);
+    unsigned* counters = ar.at<unsigned>(r->off_counters);
+    uint64_t* drounds = ar.at<uint64_t>(r->off_rounds);
+    uint64_t* dchal = ar.at<uint64_t>(r->off_chal);
     auto run_plan = [&](int pi, const char* name) -> int {
-        const Plan& p = plans[pi];
+        const Plan& p = r->plans[pi];
         if (p.who.empty()) return TG_OK;
-        const Seg* segs = ar.at<Seg>(off_segs) + plan_seg0[pi];
+        const Seg* segs = ar.at<Seg>(r->off_segs) + r->plan_seg0[pi];
         uint64_t units = 0;
-        for (size_t q = 0; q < p.who.size(); q++) units += all_segs[plan_seg0[pi] + q].n;
+        for (size_t q = 0; q < p.who.size(); q++) units += r->all_segs[r->plan_seg0[pi] + q].n;
         Launch L(d, s, name, 1, units);
-        with_degree(D, [&](auto D_) {
+        with_degree(r->D, [&](auto D_) {
             constexpr int DD = decltype(D_)::value;
             sc_rounds<DD><<<p.blocks, SC_THREADS, 0, s>>>(segs, (int)p.who.size(), partials, counters);
         });
         TG_CUDA(cudaGetLastError());
         return TG_OK;
     };
-    rc = run_plan(0, "sumcheck_product_sum");
-    if (rc) return restore(rc);
-    for (int j = 0; j < J; j++) {
+    int rc = run_plan(0, "sumcheck_product_sum");
+    if (rc) return rc;
+    for (int j = 0; j < r->J; j++) {
         rc = run_plan(1 + j, "sumcheck_round");
-        if (rc) return restore(rc);
+        if (rc) return rc;
         {
             Launch L(d, s, "sumcheck_transcript", 1, njobs);
-            sc_fs_many<<<(njobs + 63) / 64, 64, 0, s>>>(dfs, ar.at<FsJob>(off_jobs), njobs, j, keys,
-                                                        ar.at<uint64_t>(off_w), ar.at<int>(off_pad), dS, dmsg,
+            sc_fs_many<<<(njobs + 63) / 64, 64, 0, s>>>(dfs, ar.at<FsJob>(r->off_jobs), njobs, j, keys,
+                                                        ar.at<uint64_t>(r->off_w), ar.at<int>(r->off_pad), dS, dmsg,
                                                         drounds, dchal);
         }
         TG_CUDA(cudaGetLastError());
     }
-    if (!binds.empty()) {
-        Launch L(d, s, "sumcheck_bind_last", 1, binds.size());
-        sc_bind_last<<<(unsigned)((binds.size() + 127) / 128), 128, 0, s>>>(ar.at<BindLast>(off_bind), (int)binds.size());
+    if (!r->binds.empty()) {
+        Launch L(d, s, "sumcheck_bind_last", 1, r->binds.size());
+        sc_bind_last<<<(unsigned)((r->binds.size() + 127) / 128), 128, 0, s>>>(ar.at<BindLast>(r->off_bind),
+                                                                               (int)r->binds.size());
         TG_CUDA(cudaGetLastError());
     }
-    uint64_t* devals = ar.at<uint64_t>(off_evals);
-    if (nevals) {
-        Launch L(d, s, "sumcheck_evals", 1, nevals);
-        sc_gather_evals<<<(nevals + 127) / 128, 128, 0, s>>>(ar.at<EvalRef>(off_erefs), nevals, devals);
+    uint64_t* devals = ar.at<uint64_t>(r->off_evals);
+    if (r->nevals) {
+        Launch L(d, s, "sumcheck_evals", 1, r->nevals);
+        sc_gather_evals<<<(r->nevals + 127) / 128, 128, 0, s>>>(ar.at<EvalRef>(r->off_erefs), r->nevals, devals);
         TG_CUDA(cudaGetLastError());
     }
 
-    // ---- one trip back: transcripts, rounds, challenges, evaluations
-    std::vector<FsState> fs1(njobs);
-    std::vector<uint64_t> hr(rounds_words), hc(chal_words), he((size_t)2 * nevals);
-    TG_CUDA(cudaMemcpyAsync(fs1.data(), dfs, sizeof(FsState) * njobs, cudaMemcpyDeviceToHost, s));
-    if (rounds_words) TG_CUDA(cudaMemcpyAsync(hr.data(), drounds, rounds_words * 8, cudaMemcpyDeviceToHost, s));
-    if (chal_words) TG_CUDA(cudaMemcpyAsync(hc.data(), dchal, chal_words * 8, cudaMemcpyDeviceToHost, s));
-    if (nevals) TG_CUDA(cudaMemcpyAsync(he.data(), devals, he.size() * 8, cudaMemcpyDeviceToHost, s));
-    TG_CUDA(cudaStreamSynchronize(s));
+    // one trip back: transcripts, rounds, challenges, evaluations
+    uint8_t* h = (uint8_t*)host_out;
+    TG_CUDA(cudaMemcpyAsync(h, dfs, sizeof(FsState) * njobs, cudaMemcpyDeviceToHost, s));
+    h += sizeof(FsState) * njobs;
+    if (r->rounds_words) TG_CUDA(cudaMemcpyAsync(h, drounds, r->rounds_words * 8, cudaMemcpyDeviceToHost, s));
+    h += r->rounds_words * 8;
+    if (r->chal_words) TG_CUDA(cudaMemcpyAsync(h, dchal, r->chal_words * 8, cudaMemcpyDeviceToHost, s));
+    h += r->chal_words * 8;
+    if (r->nevals) TG_CUDA(cudaMemcpyAsync(h, devals, (size_t)r->nevals * 16, cudaMemcpyDeviceToHost, s));
+    return TG_OK;
+}
+
+// After the stream has run: errors, transcripts, outputs, and the evaluations absorbed.
+int sc_finish(ScRun* r) {
+    const int njobs = r->njobs;
+    const FsState* fs1 = reinterpret_cast<const FsState*>(r->host_out);
+    const uint8_t* h = r->host_out + sizeof(FsState) * njobs;
+    const uint64_t* hr = reinterpret_cast<const uint64_t*>(h);
+    const uint64_t* hc = hr + r->rounds_words;
+    const uint64_t* he = hc + r->chal_words;
     for (int b = 0; b < njobs; b++)
         if (fs1[b].err)
-            return restore(fail(TG_ERR_STATE, "job %d: a transcript challenge found no canonical Fp2 in %d squeezes", b,
-                                FS_MAX_TRIES));
+            return sc_restore(r, fail(TG_ERR_STATE, "job %d: a transcript challenge found no canonical Fp2 in %d squeezes",
+                                      b, FS_MAX_TRIES));
     for (int b = 0; b < njobs; b++) {
-        tg_sumcheck_job& jb = jobs[b];
+        tg_sumcheck_job& jb = r->jobs[b];
         memcpy(jb.transcript->state, fs1[b].state, 32);
         jb.transcript->counter = fs1[b].counter;
-        const size_t nr = (size_t)n_max[b] * 2 * jb.degree;
-        if (jb.rounds && nr) memcpy(jb.rounds, hr.data() + rounds_off[b], nr * 8);
-        if (jb.challenges && n_max[b]) memcpy(jb.challenges, hc.data() + chal_off[b], (size_t)n_max[b] * 16);
-        const size_t ne = (b + 1 < njobs ? evals_off[b + 1] : (uint64_t)2 * nevals) - evals_off[b];
+        const size_t nr = (size_t)r->n_max[b] * 2 * jb.degree;
+        if (jb.rounds && nr) memcpy(jb.rounds, hr + r->rounds_off[b], nr * 8);
+        if (jb.challenges && r->n_max[b]) memcpy(jb.challenges, hc + r->chal_off[b], (size_t)r->n_max[b] * 16);
+        const size_t ne = (b + 1 < njobs ? r->evals_off[b + 1] : (uint64_t)2 * r->nevals) - r->evals_off[b];
         jb.n_evals = ne / 2;
-        if (jb.final_evals && ne) memcpy(jb.final_evals, he.data() + evals_off[b], ne * 8);
-        rc = tg_transcript_absorb_fp2s(jb.transcript, (std::string(jb.prefix) + "/evals").c_str(),
-                                       he.data() + evals_off[b], ne / 2);
+        if (jb.final_evals && ne) memcpy(jb.final_evals, he + r->evals_off[b], ne * 8);
+        const int rc = tg_transcript_absorb_fp2s(jb.transcript, (std::string(jb.prefix) + "/evals").c_str(),
+                                                 he + r->evals_off[b], ne / 2);
         if (rc) return rc;
     }
     return TG_OK;
+}
+
+static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device) {
+    int rc;
+    ScRun* r = sc_prepare(d, jobs, njobs, tables_on_device, &rc);
+    if (!r) return rc;
+    std::vector<uint8_t> host(r->host_bytes);
+    {
+        std::lock_guard<std::mutex> lock(d->mu);
+        rc = d->scratch_sc.ensure(r->arena_bytes);
+        if (!rc) rc = sc_enqueue(d, r, d->stream, d->scratch_sc.ptr, host.data());
+        if (!rc) {
+            const cudaError_t e = cudaStreamSynchronize(d->stream);
+            if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
+        }
+    }
+    if (!rc) rc = sc_finish(r);
+    else sc_restore(r, rc);
+    sc_free(r);
+    return rc;
 }
 
 }  // namespace tg

@@ -65,6 +65,18 @@ class Transcript:
         buf = ctypes.create_string_buffer(tce, max(1, len(tce)))
         N.call("tg_transcript_init", ctypes.byref(self._t), buf, len(tce))
 
+    @classmethod
+    def from_state(cls, state: bytes, counter: int) -> "Transcript":
+        """A transcript resumed at a known state (as a fork of a proof's transcript)."""
+        t = cls.__new__(cls)
+        t._t = N.TranscriptState()
+        t._t.state[:] = list(bytes(state))
+        t._t.counter = counter
+        return t
+
+    def copy(self) -> "Transcript":
+        return Transcript.from_state(self.state, self.counter)
+
     @property
     def state(self) -> Digest:
         return bytes(self._t.state)

@@ -1,0 +1,143 @@
+"""Serving with continuous batching: a proof server on the GPU (the C ABI's tg_server_*).
+
+A request is one proof of the prover's shape: the resident unmasked commitment of its rows
+(crates/tessera-pcs/src/commitment.rs:343-458), the root absorbed into the request's transcript
+under "<prefix>/root", then a one-instance prove_batch of the product of its prime-field tables
+under <prefix> (crates/tessera-sumcheck/src/prover.rs:1122). Requests are admitted as stream
+slots and HBM budget free up and overlap on the device; `prove_plain` is the same proof through
+the one-call-at-a-time entry points, the plain path a served result must equal.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _native as N
+from .device import Device, host_u64, resolve
+from .hash import Transcript
+from .pcs import CommitmentParams
+
+
+@dataclass
+class ProofRequest:
+    params: CommitmentParams   # unmasked (mask_coeffs 0)
+    rows: object               # host words, npolys x 2^log2_k (numpy uint64, or a pinned int64 tensor)
+    degree: int
+    tables: list               # host words, each 2^vars (prime-field tables)
+    transcript: Transcript     # the proof's transcript at its start (not modified)
+    prefix: str = "stage/0"
+
+
+@dataclass
+class ProofResult:
+    root: bytes
+    gamma: tuple[int, int]
+    rounds: list[list[tuple[int, int]]]
+    challenges: list[tuple[int, int]]
+    final_evals: list[tuple[int, int]]
+    state: bytes               # the transcript at the end of the proof
+    counter: int
+    queued_ms: float = 0.0
+    latency_ms: float = 0.0
+
+    def same_proof(self, other: "ProofResult") -> bool:
+        return (self.root, self.gamma, self.rounds, self.challenges, self.final_evals, self.state, self.counter) == (
+            other.root, other.gamma, other.rounds, other.challenges, other.final_evals, other.state, other.counter)
+
+
+def _words(x) -> np.ndarray:
+    if hasattr(x, "numpy") and not getattr(x, "is_cuda", False):
+        x = x.numpy()
+    a = np.asarray(x)
+    if a.dtype == np.int64:
+        a = a.view(np.uint64)
+    return host_u64(a).reshape(-1)
+
+
+def _pairs(a, n):
+    return [(int(a[2 * i]), int(a[2 * i + 1])) for i in range(n)]
+
+
+class ProofServer:
+    """Continuous batching on one GPU: `slots` requests in flight at most, admitted first come
+    first served while their device memory fits `hbm_budget_bytes`."""
+
+    def __init__(self, device: Device | None = None, hbm_budget_bytes: int = 64 << 30, slots: int = 8):
+        self.device = resolve(device)
+        self._srv = ctypes.c_void_p()
+        N.call("tg_server_open", self.device.handle, hbm_budget_bytes, slots, ctypes.byref(self._srv))
+        self._live = {}
+
+    def submit(self, req: ProofRequest) -> int:
+        p = req.params
+        if p.mask_coeffs != 0:
+            raise ValueError("served commitments are unmasked")
+        rows = _words(req.rows)
+        tabs = [_words(t) for t in req.tables]
+        vars_ = max(len(tabs[0]), 1).bit_length() - 1 if tabs else 0
+        c = N.ProofRequestC()
+        c.log_k, c.log_inv_rate, c.row_block = p.log2_k, p.log2_inv_rate, p.row_block
+        c.commitment_id[:] = list(bytes(p.commitment_id))
+        c.rows = rows.ctypes.data if rows.size else None
+        c.npolys = rows.size >> p.log2_k
+        c.degree, c.ntables, c.vars = req.degree, len(tabs), vars_
+        tptr = (ctypes.c_void_p * max(1, len(tabs)))(*[t.ctypes.data for t in tabs])
+        c.tables = ctypes.cast(tptr, ctypes.POINTER(ctypes.c_void_p))
+        c.transcript = req.transcript.raw
+        pre = req.prefix.encode()
+        c.prefix = pre
+        rounds = np.zeros(max(1, vars_ * req.degree * 2), dtype=np.uint64)
+        chal = np.zeros(max(1, vars_ * 2), dtype=np.uint64)
+        evals = np.zeros(max(1, len(tabs) * 2), dtype=np.uint64)
+        out = N.ProofResultC()
+        out.rounds, out.challenges, out.final_evals = rounds.ctypes.data, chal.ctypes.data, evals.ctypes.data
+        ticket = ctypes.c_uint64()
+        N.call("tg_server_submit", self._srv, ctypes.byref(c), ctypes.byref(out), ctypes.byref(ticket))
+        # everything the request points at stays alive until it is collected
+        self._live[ticket.value] = (c, out, rows, tabs, tptr, pre, rounds, chal, evals, req.degree, vars_)
+        return ticket.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> ProofResult:
+        N.call("tg_server_wait", self._srv, ticket, timeout_ms)
+        c, out, rows, tabs, tptr, pre, rounds, chal, evals, degree, vars_ = self._live.pop(ticket)
+        return ProofResult(bytes(out.root), (int(out.gamma[0]), int(out.gamma[1])),
+                           [_pairs(rounds[j * degree * 2:(j + 1) * degree * 2], degree) for j in range(vars_)],
+                           _pairs(chal, vars_), _pairs(evals, len(tabs)), bytes(out.transcript.state),
+                           int(out.transcript.counter), out.queued_ms, out.latency_ms)
+
+    def stats(self) -> dict:
+        st = N.ServerStatsC()
+        N.call("tg_server_stats_read", self._srv, ctypes.byref(st))
+        return {"submitted": st.submitted, "completed": st.completed, "peak_inflight": st.peak_inflight,
+                "peak_bytes": st.peak_bytes}
+
+    def close(self):
+        if self._srv:
+            N.call("tg_server_close", self._srv)
+            self._srv = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def prove_plain(req: ProofRequest, device: Device | None = None) -> ProofResult:
+    """The same proof through the plain entry points, one call after another."""
+    from .sumcheck import Instance, Protocol, Table, prove_batch
+
+    d = resolve(device)
+    p = req.params
+    rows = _words(req.rows)
+    root = ctypes.create_string_buffer(32)
+    cid = (ctypes.c_uint8 * 32)(*bytes(p.commitment_id))
+    N.call("tg_commit_unmasked", d.handle, p.log2_k, p.log2_inv_rate, p.row_block, cid,
+           ctypes.c_void_p(rows.ctypes.data) if rows.size else None, rows.size >> p.log2_k, None, root)
+    t = req.transcript.copy()
+    t.absorb(req.prefix + "/root", root.raw)
+    pb = prove_batch(t, Protocol.ONE, req.prefix, req.degree, [Instance([Table.base(_words(x)) for x in req.tables])],
+                     device=d)
+    return ProofResult(root.raw, pb.gamma, pb.proof.rounds, pb.point, pb.proof.final_evals, t.state, t.counter)
