@@ -458,14 +458,123 @@ def run_batched(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_serve(args) -> None:
+    """Serving: a Poisson stream of proof requests (commitment + sumcheck units of uneven sizes,
+    each on its own transcript) through the proof server (continuous batching, HBM-budget
+    admission) against the plain path (one request at a time, in arrival order). Latency is
+    arrival to result; a second pass offers every request at once to measure saturated proofs/s."""
+    import random
+
+    import torch
+
+    from tessera_gb300.device import Device
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.pcs import CommitmentParams
+    from tessera_gb300.serve import ProofRequest, ProofServer, prove_plain
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = Device(local)
+    rs = random.Random(SEED_SERVE)
+    reqs, arrivals, units = [], [], 0
+    t = 0.0
+    keep = []
+    for i in range(args.requests):
+        log_k, polys, log_r = rs.randint(10, 16), rs.choice([8, 32, 128]), rs.choice([1, 2])
+        vars_, degree = rs.randint(10, 18), rs.choice([2, 3])
+        rows = torch.from_numpy(splitmix_words(SEED_SERVE + 2 * i, polys << log_k).view(np.int64)).pin_memory()
+        tabs = [torch.from_numpy(splitmix_words(SEED_SERVE + 7919 * i + k, 1 << vars_).view(np.int64)).pin_memory()
+                for k in range(degree)]
+        keep.append((rows, tabs))
+        ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([0x65]) * 32,
+                             i.to_bytes(16, "little"))
+        cid = bytes(rs.randrange(256) for _ in range(32))
+        reqs.append(ProofRequest(CommitmentParams(log_k, log_r, 0, ROW_BLOCK, cid), rows.numpy().view(np.uint64),
+                                 degree, [x.numpy().view(np.uint64) for x in tabs], Transcript(ctx), "stage/0"))
+        units += (polys << log_k) + (degree << vars_)
+        t += rs.expovariate(args.rate)
+        arrivals.append(t)
+
+    def plain(offered):
+        lat = []
+        start = time.perf_counter()
+        for r, a in zip(reqs, offered):
+            now = time.perf_counter() - start
+            if a > now:
+                time.sleep(a - now)
+            prove_plain(r, dev)
+            lat.append(time.perf_counter() - start - a)
+        return time.perf_counter() - start, lat
+
+    def served(offered):
+        with ProofServer(dev, hbm_budget_bytes=args.serve_budget_gib << 30, slots=args.slots) as srv:
+            tickets = [None] * len(reqs)
+            start = time.perf_counter()
+
+            def producer():
+                for i, (r, a) in enumerate(zip(reqs, offered)):
+                    now = time.perf_counter() - start
+                    if a > now:
+                        time.sleep(a - now)
+                    tickets[i] = srv.submit(r)
+
+            th = threading.Thread(target=producer)
+            th.start()
+            th.join()
+            res = [srv.wait(tk) for tk in tickets]
+            wall = time.perf_counter() - start
+            st = srv.stats()
+        return wall, [x.latency_ms / 1e3 for x in res], st
+
+    # warm-up: shapes' tables, pools, pinned paths
+    for r in reqs[: min(8, len(reqs))]:
+        prove_plain(r, dev)
+    served([0.0] * len(reqs))
+    out = {}
+    for mode, offered in (("poisson", arrivals), ("saturated", [0.0] * len(reqs))):
+        pw, pl = plain(offered)
+        sw, sl, st = served(offered)
+        q = lambda xs, f: sorted(xs)[min(len(xs) - 1, int(f * len(xs)))] * 1e3
+        out[mode] = {
+            "plain": {"proofs_per_s": len(reqs) / pw, "elems_per_s": units / pw, "latency_ms": {"p50": q(pl, 0.5), "p99": q(pl, 0.99)}},
+            "served": {"proofs_per_s": len(reqs) / sw, "elems_per_s": units / sw, "latency_ms": {"p50": q(sl, 0.5), "p99": q(sl, 0.99)},
+                       "peak_inflight": st["peak_inflight"], "peak_gib": st["peak_bytes"] / 2**30},
+        }
+    del keep
+    dev.close()
+    if rank != 0:
+        return
+    sat = out["saturated"]
+    line = {
+        "metric": "proofs/s and committed+sumchecked elems/s; p50/p99 proof latency, served vs plain",
+        "value": sat["served"]["proofs_per_s"], "unit": "proofs/s", "n_gpus": world, "steps": 1, "warmup": 1,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic",
+        "config": {"workload": f"serve: {len(reqs)} proof requests (commit 8/32/128 x 2^10..2^16 at rate 1/2 or 1/4, "
+                               f"B = 32, then a degree-2/3 sumcheck over 2^10..2^18 bound to the root), Poisson "
+                               f"{args.rate} req/s, then all at once", "seed": SEED_SERVE, "slots": args.slots,
+                   "hbm_budget_gib": args.serve_budget_gib, "elems": units,
+                   "timing": "host wall clock; latency = arrival to result on the host"},
+        **out,
+    }
+    print(json.dumps(line), flush=True)
+
+
+SEED_SERVE = 0x00650005
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["large", "batched"], default="large",
-                    help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain")
+    ap.add_argument("--workload", choices=["large", "batched", "serve"], default="large",
+                    help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain; "
+                         "serve: the proof server against one-at-a-time proofs")
+    ap.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
+    ap.add_argument("--rate", type=float, default=20.0, help="serve: mean Poisson arrivals per second")
+    ap.add_argument("--slots", type=int, default=8, help="serve: requests in flight at most")
+    ap.add_argument("--serve-budget-gib", type=int, default=64, help="serve: HBM budget for admitted requests")
     ap.add_argument("--cpu-polys", type=int, default=32, help="rows in the CPU baseline's bounded sample")
     ap.add_argument("--ref-polys", type=int, default=32, help="rows per step in the reference arm's sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -483,6 +592,8 @@ def main():
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_gpu(args)
 
