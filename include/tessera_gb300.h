@@ -189,6 +189,24 @@ int tg_matrix_absorb(tg_matrix *m, const uint64_t *rows, size_t nrows, uint64_t 
 int tg_matrix_finish(tg_matrix *m, uint8_t *chains);
 int tg_matrix_close(tg_matrix *m);
 
+/* ---- ColumnSink (crates/tessera-pcs/src/streaming/opening.rs:845-884; the reference's GPU
+ * ColumnsSink, crates/tessera-prover/src/gpu.rs:196-398): P5 re-encodes blocks of whole rows
+ * (mask_coeffs masks per row, m_0 first) and returns each row's symbols at `columns`
+ * (out: nrows x ncolumns, row by row; a column at or past n reads 0). select_combining also adds
+ * P4's combined rows Σ_r coefficients[g][r]·rows[r] (coefficients: groups x nrows Fp2) to sums
+ * kept on the device, with one group count per opening; combined adds those sums into `out`
+ * (groups x k Fp2) and clears them (a no-op before any combining block). Device copies of rows,
+ * masks, codewords and sums are zeroed when the sink closes. */
+typedef struct tg_column_sink tg_column_sink;
+int tg_column_sink_open(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t mask_coeffs, uint32_t block,
+                        const uint64_t *columns, size_t ncolumns, tg_column_sink **out);
+int tg_column_sink_select(tg_column_sink *sink, const uint64_t *rows, size_t nrows, const uint64_t *masks,
+                          uint64_t *out);
+int tg_column_sink_select_combining(tg_column_sink *sink, const uint64_t *rows, size_t nrows, const uint64_t *masks,
+                                    const uint64_t *coefficients, size_t groups, uint64_t *out);
+int tg_column_sink_combined(tg_column_sink *sink, uint64_t *out, size_t groups);
+int tg_column_sink_close(tg_column_sink *sink);
+
 /* ---- Fiat–Shamir transcript (crates/tessera-hash/src/transcript.rs:127-250), host side.
  * context_tce is TCE(SessionContext). */
 typedef struct {

@@ -127,6 +127,11 @@ SIGNATURES = {
     "tg_commit_plan_launch": [V, V],
     "tg_commit_plan_info": [V, V, V, V],
     "tg_commit_plan_destroy": [V],
+    "tg_column_sink_open": [V, U32, U32, U32, U32, V, SZ, V],
+    "tg_column_sink_select": [V, V, SZ, V, V],
+    "tg_column_sink_select_combining": [V, V, SZ, V, V, SZ, V],
+    "tg_column_sink_combined": [V, V, SZ],
+    "tg_column_sink_close": [V],
     "tg_server_open": [V, SZ, INT, V],
     "tg_server_submit": [V, V, V, V],
     "tg_server_wait": [V, U64, INT],

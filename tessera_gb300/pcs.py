@@ -327,3 +327,67 @@ class CommitPlan:
             self.close()
         except Exception:
             pass
+
+
+class ColumnSink:
+    """The opening's column sink on the GPU (the reference's ColumnSink and its GPU ColumnsSink):
+    `select` re-encodes a block of whole rows with their masks and returns each row's symbols at
+    the sink's columns; `select_combining` also adds the block's combined rows Σ_r c[g][r]·row_r
+    to sums kept on the device; `combined` adds those sums into the caller's rows and clears them."""
+
+    def __init__(self, encoder: RowEncoder, block: int, columns, device: Device | None = None):
+        self.device = resolve(device or encoder.device)
+        self.k, self.P = encoder.message_len(), encoder.mask_coeffs()
+        cols = host_u64(columns).reshape(-1)
+        self.m = cols.size
+        self._sink = ctypes.c_void_p()
+        N.call("tg_column_sink_open", self.device.handle, encoder.log_k, encoder.log_inv_rate, self.P, block, ptr(cols),
+               cols.size, ctypes.byref(self._sink))
+
+    def _rows(self, rows, masks):
+        r = host_u64(rows).reshape(-1)
+        if r.size % self.k:
+            raise ValueError(f"{r.size} values are not whole rows of {self.k}")
+        nrows = r.size // self.k
+        m = host_u64(masks).reshape(-1) if self.P else None
+        if self.P and (m is None or m.size != nrows * self.P):
+            raise ValueError(f"expected {nrows * self.P} mask coefficients")
+        return r, nrows, m
+
+    def select(self, rows, masks=None) -> np.ndarray:
+        r, nrows, m = self._rows(rows, masks)
+        out = np.empty((nrows, self.m), dtype=np.uint64)
+        N.call("tg_column_sink_select", self._sink, ptr(r), nrows, ptr(m), ptr(out))
+        return out
+
+    def combines(self) -> bool:
+        return True
+
+    def select_combining(self, rows, masks, coefficients) -> np.ndarray:
+        """coefficients: one list per group of this block's row coefficients, each an Fp2 (c0, c1)."""
+        r, nrows, m = self._rows(rows, masks)
+        c = host_u64([w for grp in coefficients for pair in grp for w in pair])
+        if c.size != 2 * nrows * len(coefficients):
+            raise ValueError("one coefficient per row in every group")
+        out = np.empty((nrows, self.m), dtype=np.uint64)
+        N.call("tg_column_sink_select_combining", self._sink, ptr(r), nrows, ptr(m), ptr(c), len(coefficients), ptr(out))
+        return out
+
+    def combined(self, out: np.ndarray) -> np.ndarray:
+        """Adds the sums into `out` (groups x k x 2 words, Fp2 pairs) in place and returns it."""
+        o = np.ascontiguousarray(out, dtype=np.uint64)
+        N.call("tg_column_sink_combined", self._sink, ptr(o), o.shape[0] if o.ndim == 3 else 0)
+        if o is not out:
+            out[...] = o
+        return out
+
+    def close(self):
+        if self._sink:
+            N.call("tg_column_sink_close", self._sink)
+            self._sink = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,7 +1,8 @@
 """GPU parity of the commitment path against the CPU oracle and the reference's golden vectors:
 Reed–Solomon encoding (every shape class, masks, rates 1/2 to 1/16), column chains, Merkle
 trees, the resident unmasked commitment (the 32 x 2^14 and 256 x 2^20 workloads), the advice
-BlockSink with segment merging, and the MatrixSink. Bit-exact throughout."""
+BlockSink with segment merging, the MatrixSink, and the opening's ColumnSink (queried columns and
+combined rows). Bit-exact throughout."""
 import os
 
 import numpy as np
@@ -309,3 +310,73 @@ def test_weight_encoding_declines(dev):
 
     assert GpuWeights(dev).matrix(4, 1, 200, bytes(32), 32, [0]) is None  # B above one chunk
     assert GpuWeights(dev).matrix(4, 1, 4, bytes(32), 31, [0]) is None  # column count mismatch
+
+
+# ---- the opening's column sink (P4/P5) ------------------------------------------------------------
+
+def _combine_oracle(rows, coeffs, k):
+    """Σ_r c[g][r]·row_r per group, with the oracle's field products (Fp2 × Fp componentwise)."""
+    out = np.zeros((len(coeffs), k, 2), dtype=np.uint64)
+    for g, grp in enumerate(coeffs):
+        for r, (c0, c1) in enumerate(grp):
+            row = rows[r * k:(r + 1) * k]
+            out[g, :, 0] = O.fp_vec("add", out[g, :, 0], O.fp_vec("mul", np.full(k, c0, dtype=np.uint64), row))
+            out[g, :, 1] = O.fp_vec("add", out[g, :, 1], O.fp_vec("mul", np.full(k, c1, dtype=np.uint64), row))
+    return out
+
+
+@pytest.mark.parametrize("log_k,log_r,P,block", [(10, 1, 0, 4), (12, 1, 5, 8), (14, 2, 1, 3), (16, 1, 64, 2)])
+def test_column_sink_select_and_combine(dev, log_k, log_r, P, block):
+    """The sink's queried symbols equal the oracle's encodings at those columns (including columns
+    past n, which read 0), and its combined rows equal Σ_r c[g][r]·row_r over all blocks, added
+    into the caller's rows."""
+    from tessera_gb300.pcs import ColumnSink, RowEncoder
+
+    k, n = 1 << log_k, 1 << (log_k + log_r)
+    rng = np.random.default_rng(log_k + P)
+    cols = np.concatenate([rng.integers(0, n, 37, dtype=np.uint64), np.array([n - 1, 0, n, n + 5], dtype=np.uint64)])
+    enc = RowEncoder(k, log_r, P, device=dev)
+    sink = ColumnSink(enc, block, cols, device=dev)
+    nrows = 2 * block + 1  # two full blocks and a short one
+    rows = rand_fp(log_k * 7 + P, nrows * k)
+    masks = rand_fp(99 + P, nrows * P) if P else None
+    groups = 3
+    coeffs_all = [[tuple(int(x) for x in rand_fp(1000 * g + r, 2)) for r in range(nrows)] for g in range(groups)]
+    want = O.encode_rows(rows, log_k, log_r, masks=masks, mask_coeffs=P, threads=THREADS).reshape(nrows, n)
+    for r0 in range(0, nrows, block):
+        r1 = min(nrows, r0 + block)
+        rb = rows[r0 * k:r1 * k]
+        mb = masks[r0 * P:r1 * P] if P else None
+        if r0 == 0:
+            got = sink.select(rb, mb)  # a block without combining contributes no sums
+            coeffs_all = [[(0, 0)] * block + grp[block:] for grp in coeffs_all]
+        else:
+            got = sink.select_combining(rb, mb, [grp[r0:r1] for grp in coeffs_all])
+        for i, c in enumerate(cols):
+            expect = want[r0:r1, c] if c < n else np.zeros(r1 - r0, dtype=np.uint64)
+            assert np.array_equal(got[:, i], expect)
+    base = rng.integers(0, 2**32, (groups, k, 2), dtype=np.uint64)
+    out = sink.combined(base.copy())
+    want_sums = _combine_oracle(rows, coeffs_all, k)
+    assert np.array_equal(out, O.fp_vec("add", base.reshape(-1), want_sums.reshape(-1)).reshape(base.shape))
+    # collected sums are cleared: a second collection adds nothing
+    again = sink.combined(base.copy())
+    assert np.array_equal(again, base)
+    sink.close()
+
+
+def test_column_sink_refusals(dev):
+    from tessera_gb300 import _native as N
+    from tessera_gb300.pcs import ColumnSink, RowEncoder
+
+    enc = RowEncoder(1 << 8, 1, 0, device=dev)
+    sink = ColumnSink(enc, 2, [0, 1, 2], device=dev)
+    rows = rand_fp(5, 3 << 8)
+    with pytest.raises(N.TesseraError):
+        sink.select(rows)  # three rows in a block of two
+    sink.select_combining(rows[: 2 << 8], None, [[(1, 0), (2, 0)]])
+    with pytest.raises(N.TesseraError):
+        sink.select_combining(rows[: 2 << 8], None, [[(1, 0), (2, 0)], [(3, 0), (4, 0)]])  # another group count
+    with pytest.raises(N.TesseraError):
+        sink.combined(np.zeros((2, 1 << 8, 2), dtype=np.uint64))  # the wrong number of groups
+    sink.close()
