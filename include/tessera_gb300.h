@@ -285,6 +285,51 @@ int tg_level_bind(tg_level *l, const uint64_t r[2]);
 int tg_level_firsts(tg_level *l, uint64_t *out);
 int tg_level_free(tg_level *l);
 
+/* ---- Tree levels: product forests and LogUp fraction trees (RFC-0010 'Tree levels'; the
+ * reference's FractionTree, crates/tessera-sumcheck/src/trees.rs:260-345, prove_trees :761, and
+ * LogUp's leaf stage, crates/tessera-logup/src/prover.rs:361). Trees are listed in schedule order.
+ * kind 0: a forest of 2^s product trees of height `height` (a single tree: s = 0) from its
+ * 2^(s+height) stacked leaves (Fp2); kind 1: a fraction tree (s = 0) from 2^height numerators
+ * (Fp2; NULL: all 1) and denominators (Fp2), entering the schedule with `sent` (n, d) when given
+ * (as the roots message carried it), else its own root. Every level is built on the device when
+ * the stage opens; each tg_leaf_stage_prove_level call proves the next level on the transcript,
+ * byte for byte as the reference does, and moves every present tree's claim one level down. */
+typedef struct {
+    int kind;
+    uint32_t s, height;
+    const uint64_t *leaves;        /* forest leaves, or fraction numerators */
+    const uint64_t *denominators;  /* fraction trees */
+    const uint64_t *sent;          /* fraction trees: 2 Fp2, or NULL */
+} tg_tree;
+typedef struct {
+    int level;
+    int n_root_challenges;     /* s_max of the joining forests */
+    uint64_t *root_challenges; /* caller buffer, >= 40 Fp2 (may be NULL) */
+    uint64_t gamma[2];
+    int has_lambda;
+    uint64_t lambda[2];
+    int n_max;                 /* rounds */
+    uint64_t *rounds;          /* caller buffer: n_max x 3 Fp2 (p(0), p(2), p(3)) */
+    uint64_t *challenges;      /* n_max Fp2 */
+    uint64_t *claims;          /* n_max + 1 Fp2, as a verifier derives them */
+    int n_evals;
+    uint64_t *evals;           /* caller buffer: 2 Fp2 per forest, 4 per fraction tree */
+    uint64_t rho[2];
+    int n_present;
+    int *present;              /* caller buffer: the trees present at the level, in order */
+} tg_tree_level_proof;
+typedef struct tg_leaf_stage tg_leaf_stage;
+int tg_leaf_stage_open(tg_device *dev, const tg_tree *trees, int ntrees, int on_device, tg_leaf_stage **out);
+/* H, the tallest height (the number of levels), and the next level to prove. */
+int tg_leaf_stage_height(const tg_leaf_stage *stage, int *height, int *level);
+/* A forest's root level (2^s Fp2) or a fraction tree's root (n, d). */
+int tg_leaf_stage_root(const tg_leaf_stage *stage, int tree, uint64_t *out);
+int tg_leaf_stage_prove_level(tg_leaf_stage *stage, tg_transcript *t, tg_tree_level_proof *out);
+/* A tree's current claim: its point (npoint Fp2), the claim (a forest's value, then 0; a fraction
+ * tree's (p, q)) and its level (−1 before it joins). */
+int tg_leaf_stage_claim(const tg_leaf_stage *stage, int tree, uint64_t *point, int *npoint, uint64_t *claim, int *own);
+int tg_leaf_stage_close(tg_leaf_stage *stage);
+
 /* ---- Serving: a proof server with continuous batching (no reference counterpart: the serving
  * pattern around the hot path). A request's proof is the resident unmasked commitment of its rows
  * (commit_unmasked, crates/tessera-pcs/src/commitment.rs:343-458), the root absorbed into the

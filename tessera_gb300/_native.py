@@ -67,6 +67,19 @@ class ServerStatsC(ctypes.Structure):
                 ("peak_bytes", ctypes.c_size_t)]
 
 
+class TreeC(ctypes.Structure):
+    _fields_ = [("kind", ctypes.c_int), ("s", ctypes.c_uint32), ("height", ctypes.c_uint32), ("leaves", ctypes.c_void_p),
+                ("denominators", ctypes.c_void_p), ("sent", ctypes.c_void_p)]
+
+
+class TreeLevelProofC(ctypes.Structure):
+    _fields_ = [("level", ctypes.c_int), ("n_root_challenges", ctypes.c_int), ("root_challenges", ctypes.c_void_p),
+                ("gamma", ctypes.c_uint64 * 2), ("has_lambda", ctypes.c_int), ("lambda_", ctypes.c_uint64 * 2),
+                ("n_max", ctypes.c_int), ("rounds", ctypes.c_void_p), ("challenges", ctypes.c_void_p),
+                ("claims", ctypes.c_void_p), ("n_evals", ctypes.c_int), ("evals", ctypes.c_void_p),
+                ("rho", ctypes.c_uint64 * 2), ("n_present", ctypes.c_int), ("present", ctypes.c_void_p)]
+
+
 class SumcheckJobC(ctypes.Structure):
     _fields_ = [("transcript", ctypes.c_void_p), ("prefix", ctypes.c_char_p), ("degree", ctypes.c_int),
                 ("instances", ctypes.POINTER(InstanceC)), ("ninstances", ctypes.c_int),
@@ -132,6 +145,12 @@ SIGNATURES = {
     "tg_column_sink_select_combining": [V, V, SZ, V, V, SZ, V],
     "tg_column_sink_combined": [V, V, SZ],
     "tg_column_sink_close": [V],
+    "tg_leaf_stage_open": [V, V, INT, INT, V],
+    "tg_leaf_stage_height": [V, V, V],
+    "tg_leaf_stage_root": [V, INT, V],
+    "tg_leaf_stage_prove_level": [V, V, V],
+    "tg_leaf_stage_claim": [V, INT, V, V, V, V],
+    "tg_leaf_stage_close": [V],
     "tg_server_open": [V, SZ, INT, V],
     "tg_server_submit": [V, V, V, V],
     "tg_server_wait": [V, U64, INT],

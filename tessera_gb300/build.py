@@ -15,7 +15,7 @@ PKG = Path(__file__).resolve().parent
 CSRC = PKG / "csrc"
 OUT = PKG / "_build"
 LIB = OUT / "libtessera_gb300.so"
-SOURCES = ["lde.cu", "hash.cu", "host.cu", "capi.cu", "sumcheck.cu", "level.cu", "noalloc.cu", "peaks.cu", "batch.cu", "workload.cu", "serve.cu", "opening.cu"]
+SOURCES = ["lde.cu", "hash.cu", "host.cu", "capi.cu", "sumcheck.cu", "level.cu", "noalloc.cu", "peaks.cu", "batch.cu", "workload.cu", "serve.cu", "opening.cu", "trees.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
          "-I", str(PKG.parent / "include")]

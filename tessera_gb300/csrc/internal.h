@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "../../include/tessera_gb300.h"
+#include "gl.cuh"
 
 namespace tg {
 
@@ -130,8 +131,18 @@ int column_merge(Device* d, const uint8_t* segs, size_t nseg, uint64_t n, uint8_
 // (sc_arena_bytes of device memory) and copies the results into `host_out` (sc_host_bytes; pinned
 // memory for the copy to stay asynchronous); once the stream has run, sc_finish updates the
 // transcripts and outputs. sc_restore puts the transcripts back as they were before sc_prepare.
+// Options for callers that run their own protocol around a sumcheck (the tree levels): with
+// `weights` (one job only) γ is not drawn and instance i weighs weights[i]; without
+// `absorb_evals` the final evaluations are returned but not absorbed.
+struct ScOptions {
+    const std::vector<fp2>* weights = nullptr;
+    bool absorb_evals = true;
+};
 struct ScRun;
-ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device, int* status);
+ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device, int* status,
+                  const ScOptions& opts = ScOptions());
+// The blocking form: prepare, enqueue on the device stream, wait, finish.
+int prove_many_opts(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device, const ScOptions& opts);
 size_t sc_arena_bytes(const ScRun* r);
 size_t sc_host_bytes(const ScRun* r);
 int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out);

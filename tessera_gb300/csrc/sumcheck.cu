@@ -455,6 +455,7 @@ struct Plan {
 // One prove_many call in flight: planned on the host (γ drawn), then enqueued on a stream over
 // a device arena, then finished on the host once the stream has run.
 struct ScRun {
+    ScOptions opts;
     tg_sumcheck_job* jobs = nullptr;
     int njobs = 0, tables_on_device = 0;
     std::vector<tg_transcript> saved;
@@ -490,7 +491,8 @@ int sc_restore(ScRun* r, int rc) {
     return rc;
 }
 
-ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device, int* status) {
+ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device, int* status,
+                  const ScOptions& opts) {
     *status = TG_OK;
     if (njobs < 1 || !jobs) {
         *status = fail(TG_ERR_INVALID, "no sumcheck jobs");
@@ -500,7 +502,12 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
         *status = check_job(jobs[b], b);
         if (*status) return nullptr;
     }
+    if (opts.weights && njobs != 1) {
+        *status = fail(TG_ERR_INVALID, "caller weights are for one job");
+        return nullptr;
+    }
     ScRun* r = new ScRun();
+    r->opts = opts;
     r->jobs = jobs;
     r->njobs = njobs;
     r->tables_on_device = tables_on_device;
@@ -515,15 +522,21 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
     // per job: γ (host transcript), weights; per instance: padding
     for (int b = 0; b < njobs; b++) {
         tg_sumcheck_job& jb = jobs[b];
-        uint64_t g[2];
-        int rc = tg_transcript_challenge_fp2(jb.transcript, (std::string(jb.prefix) + "/gamma").c_str(), g);
-        if (rc) {
-            *status = sc_restore(r, rc);
+        uint64_t g[2] = {jb.gamma[0], jb.gamma[1]};
+        if (!opts.weights) {
+            int rc = tg_transcript_challenge_fp2(jb.transcript, (std::string(jb.prefix) + "/gamma").c_str(), g);
+            if (rc) {
+                *status = sc_restore(r, rc);
+                delete r;
+                return nullptr;
+            }
+            jb.gamma[0] = g[0];
+            jb.gamma[1] = g[1];
+        } else if ((int)opts.weights->size() != jb.ninstances) {
+            *status = sc_restore(r, fail(TG_ERR_INVALID, "one weight per instance"));
             delete r;
             return nullptr;
         }
-        jb.gamma[0] = g[0];
-        jb.gamma[1] = g[1];
         const fp2 gam = {g[0], g[1]};
         r->D = std::max(r->D, jb.degree);
         r->inst0[b] = (int)r->inst.size();
@@ -549,7 +562,7 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
                 is.tables.push_back(ts);
             }
             r->inst.push_back(std::move(is));
-            r->weights.push_back(acc);
+            r->weights.push_back(opts.weights ? (*opts.weights)[i] : acc);
             acc = e_mul(acc, gam);
         }
         r->rounds_off[b] = r->rounds_words;
@@ -836,6 +849,7 @@ int sc_finish(ScRun* r) {
         const size_t ne = (b + 1 < njobs ? r->evals_off[b + 1] : (uint64_t)2 * r->nevals) - r->evals_off[b];
         jb.n_evals = ne / 2;
         if (jb.final_evals && ne) memcpy(jb.final_evals, he + r->evals_off[b], ne * 8);
+        if (!r->opts.absorb_evals) continue;
         const int rc = tg_transcript_absorb_fp2s(jb.transcript, (std::string(jb.prefix) + "/evals").c_str(),
                                                  he + r->evals_off[b], ne / 2);
         if (rc) return rc;
@@ -843,9 +857,9 @@ int sc_finish(ScRun* r) {
     return TG_OK;
 }
 
-static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device) {
+int prove_many_opts(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device, const ScOptions& opts) {
     int rc;
-    ScRun* r = sc_prepare(d, jobs, njobs, tables_on_device, &rc);
+    ScRun* r = sc_prepare(d, jobs, njobs, tables_on_device, &rc, opts);
     if (!r) return rc;
     std::vector<uint8_t> host(r->host_bytes);
     {
@@ -861,6 +875,10 @@ static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on
     else sc_restore(r, rc);
     sc_free(r);
     return rc;
+}
+
+static int prove_many(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_device) {
+    return prove_many_opts(d, jobs, njobs, tables_on_device, ScOptions());
 }
 
 }  // namespace tg

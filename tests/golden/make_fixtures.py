@@ -10,7 +10,8 @@ transcript, pcs-streaming, sumcheck}) into gzip files here, trimmed to what the 
 sumcheck stages whose tables the JSON does not record (more than 5 variables), it runs the
 reference's own stdlib-Python oracle (spec/vectors/sumcheck/generate.py) and records where each
 stage's tables start in its SplitMix64 stream, so the tests regenerate the tables exactly; the
-script checks that rerun against the JSON before writing anything.
+script checks that rerun against the JSON before writing anything. The tree-level batches
+(product trees, product forests and LogUp leaf stages, every level record) are copied whole.
 
 The tests read only the files this script writes; nothing reads the reference at test time.
 """
@@ -109,6 +110,8 @@ def main() -> None:
             stages.append(stage)
         sessions.append({"name": session["name"], "context": session["context"], "stages": stages})
     write("sumcheck.json.gz", {"seed": hex(seed), "sessions": sessions})
+    # tree levels: product trees, product forests and LogUp leaf stages, with every level record
+    write("trees.json.gz", {k: sc[k] for k in ("tree_batches", "forest_batches", "logup_batches")})
 
 
 if __name__ == "__main__":

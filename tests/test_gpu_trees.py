@@ -1,0 +1,198 @@
+"""Tree levels on the GPU against the reference's golden vectors: every product-tree batch,
+product-forest batch and LogUp leaf stage of sumcheck.json, level by level — root challenges, γ, λ,
+round messages, challenges, the verifier's claims, final evaluations, ρ, the claims each tree
+carries to the next level, and the transcript state after every level."""
+import gzip
+import json
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+P = 0xFFFFFFFF00000001
+W = 7
+TREES = json.load(gzip.open(Path(__file__).parent / "golden" / "trees.json.gz"))
+
+
+@pytest.fixture(scope="module")
+def dev():
+    from tessera_gb300.device import default_device
+
+    return default_device()
+
+
+def num(x):
+    return int(x, 16)
+
+
+def f2(pair):
+    return (num(pair[0]), num(pair[1]))
+
+
+def f2s(items):
+    return [f2(p) for p in items]
+
+
+def add(a, b):
+    return ((a[0] + b[0]) % P, (a[1] + b[1]) % P)
+
+
+def sub(a, b):
+    return ((a[0] - b[0]) % P, (a[1] - b[1]) % P)
+
+
+def mul(a, b):
+    return ((a[0] * b[0] + W * a[1] * b[1]) % P, (a[0] * b[1] + a[1] * b[0]) % P)
+
+
+def words(elems):
+    return np.array([w for e in elems for w in e], dtype=np.uint64)
+
+
+def transcript(ctx):
+    from golden_data import context_tce
+    from tessera_gb300.hash import Transcript
+
+    return Transcript(context_tce(ctx))
+
+
+def check_level(rec, want, stage, label):
+    assert rec.prefix == want["prefix"], label
+    assert rec.root_challenges == f2s(want.get("root_challenges", [])), label
+    assert rec.gamma == f2(want["gamma"]), label
+    if "lambda" in want:
+        assert rec.lambda_ == (None if want["lambda"] is None else f2(want["lambda"])), label
+    assert rec.rounds == [f2s(m) for m in want["rounds"]], label
+    assert rec.challenges == f2s(want["challenges"]), label
+    assert rec.claims == f2s(want["claims"]), label
+    assert rec.final_evals == f2s(want["final_evals"]), label
+    assert rec.rho == f2(want["rho"]), label
+    assert rec.state.hex() == want["state"] and rec.counter == want["counter"], label
+    key = "tree" if "tree" in want["next"][0] else "forest"
+    assert [n[key] for n in want["next"]] == rec.present, label
+    for n in want["next"]:
+        point, claim, _ = stage.claim(n[key])
+        assert point == f2s(n["point"]), label
+        if "value" in n:
+            assert claim == f2(n["value"]), label
+        else:
+            assert claim == (f2(n["numerator"]), f2(n["denominator"])), label
+
+
+def forest_of(spec):
+    from tessera_gb300.trees import Forest, lift
+
+    return Forest(spec["rows_log"], lift([num(x) for x in spec["leaves"]]))
+
+
+def test_tree_batches(dev):
+    from tessera_gb300.trees import Forest, LeafStage, lift
+
+    for b in TREES["tree_batches"]:
+        t = transcript(b["context"])
+        with LeafStage([Forest(0, lift([num(x) for x in tr["leaves"]])) for tr in b["trees"]], dev) as st:
+            for k, tr in enumerate(b["trees"]):
+                assert st.root(k) == [(num(tr["root"]), 0)], b["name"]
+            assert st.height == len(b["levels"])
+            for want in b["levels"]:
+                check_level(st.prove_level(t), want, st, b["name"])
+
+
+def test_forest_batches(dev):
+    from tessera_gb300.trees import LeafStage
+
+    for b in TREES["forest_batches"]:
+        t = transcript(b["context"])
+        with LeafStage([forest_of(f) for f in b["forests"]], dev) as st:
+            for k, f in enumerate(b["forests"]):
+                assert st.root(k) == [(num(x), 0) for x in f["roots"]], b["name"]
+            for want in b["levels"]:
+                check_level(st.prove_level(t), want, st, b["name"])
+
+
+def compress(beta, row):
+    return add((row[0], 0), mul(beta, (row[1], 0)))
+
+
+def mle(values, point):
+    """Σ_x v[x]·eq(point, x), x_1 the lowest bit."""
+    out = (0, 0)
+    for x, v in enumerate(values):
+        e = (1, 0)
+        for i, r in enumerate(point):
+            e = mul(e, r if (x >> i) & 1 else sub((1, 0), r))
+        out = add(out, mul(v, e))
+    return out
+
+
+def logup_trees(alpha, beta, inst):
+    """The honest prover's two fraction trees of an instance, from its description."""
+    from tessera_gb300.trees import Fraction
+
+    rows = [(num(k), num(v)) for k, v in inst["rows"]]
+    tuples = [rows[j] if isinstance(j, int) else (num(j[0]), num(j[1])) for j in inst["lookups"]]
+    h_a, h_t = inst["h_a"], inst["h_t"]
+    slots = tuples + [rows[0]] * ((1 << h_a) - len(tuples))
+    lookup_d = [sub(alpha, compress(beta, tp)) for tp in slots]
+    m = [num(x) for x in inst["multiplicities"]]
+    table_rows = rows + [rows[0]] * ((1 << h_t) - len(rows))
+    table_n = [((P - mj) % P, 0) for mj in m]
+    table_d = [sub(alpha, compress(beta, r)) for r in table_rows]
+    values = [(tp[1], 0) for tp in slots]
+    return Fraction(words(lookup_d)), Fraction(words(table_d), words(table_n)), values
+
+
+HONEST_OR_DESCRIBED = ("accept", "roots", "level")
+
+
+def test_logup_leaf_stages(dev):
+    """Every LogUp batch whose prover data the vectors describe (the honest ones, and the cheats
+    that change only lookups, multiplicities or the roots message): α and β, the roots message,
+    each level of the leaf stage, the values message and the final transcript state."""
+    from tessera_gb300.trees import LeafStage
+
+    checked = 0
+    for b in TREES["logup_batches"]:
+        exp = b["expected"]
+        kind = "accept" if exp == "accept" else ("roots" if exp.get("check") == "roots" else
+                                                  "level" if str(exp.get("check", "")).startswith("level") else "other")
+        if kind not in HONEST_OR_DESCRIBED:
+            continue  # cheats on numerators, the table or its padding: the vectors do not describe that prover
+        t = transcript(b["context"])
+        alpha = t.challenge_fp2("logup/alpha")
+        beta = t.challenge_fp2("logup/beta")
+        assert (alpha, beta) == (f2(b["alpha"]), f2(b["beta"])), b["name"]
+        built = [logup_trees(alpha, beta, inst) for inst in b["instances"]]
+        sent = f2s(b["roots"])
+        t.absorb_fp2s("logup/roots", sent)
+        schedule = []
+        for entry in b["trees"]:
+            if entry["kind"] == "forest":
+                schedule.append(forest_of(b["forests"][entry["index"]]))
+            else:
+                i, side = entry["index"], 0 if entry["kind"] == "lookup" else 1
+                tree = built[i][side]
+                tree.sent = (sent[4 * i + 2 * side], sent[4 * i + 2 * side + 1])
+                schedule.append(tree)
+        with LeafStage(schedule, dev) as st:
+            for want in b["levels"]:
+                check_level(st.prove_level(t), want, st, b["name"])
+            place = {(e["kind"], e["index"]): k for k, e in enumerate(b["trees"])}
+            values = []
+            for i, inst in enumerate(b["instances"]):
+                point_a, (p_a, q_a), _ = st.claim(place[("lookup", i)])
+                point_t, (p_t, q_t), _ = st.claim(place[("table", i)])
+                lc = b["leaf_checks"][i]
+                assert point_a == f2s(lc["lookup"]["point"]) and (p_a, q_a) == (f2(lc["lookup"]["numerator"]),
+                                                                              f2(lc["lookup"]["denominator"])), b["name"]
+                assert point_t == f2s(lc["table"]["point"]) and (p_t, q_t) == (f2(lc["table"]["numerator"]),
+                                                                             f2(lc["table"]["denominator"])), b["name"]
+                if inst["has_values"]:
+                    values.append(mle(built[i][2], point_a))
+        assert values == f2s(b["values"]), b["name"]
+        t.absorb_fp2s("logup/values", values)
+        assert t.state.hex() == b["state"] and t.counter == b["counter"], b["name"]
+        checked += 1
+    assert checked >= 12
