@@ -559,6 +559,60 @@ def run_serve(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_logup(args) -> None:
+    """LogUp fraction trees, the reference benchmark's c_ℓ measurement shape: a lookup tree of 2^A
+    generated leaves (1, α − (k + β·v)) and a table tree of 2^T leaves (−m, α − (k + β·v)), each
+    built on the device and proven level by level as its own leaf stage on a transcript; the time
+    per lookup is the two trees' time over 2^A."""
+    import torch
+
+    from tessera_gb300.device import Device
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.trees import LeafStage, generated_fraction
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = Device(local)
+    ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([0x65]) * 32, bytes([0x65]) * 16)
+
+    def one(height, mult_seed):
+        start = time.perf_counter()
+        t = Transcript(ctx)
+        alpha, beta = t.challenge_fp2("logup/alpha"), t.challenge_fp2("logup/beta")
+        tree = generated_fraction(height, 0x6B6579, 0x76616C, mult_seed, alpha, beta, dev)
+        with LeafStage([tree], dev) as st:
+            st.prove(t)
+        torch.cuda.synchronize()
+        return time.perf_counter() - start
+
+    for _ in range(args.warmup):
+        one(min(args.lookups_log, 20), None)
+    times = {"lookup": [], "table": []}
+    dev.profile(True)
+    for _ in range(args.steps):
+        times["lookup"].append(one(args.lookups_log, None))
+        times["table"].append(one(args.rows_log, 0x6D756C))
+    dev.profile(False)
+    prof = dev.profile_read()
+    kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps} for k, v in prof.items()}
+    med = {k: statistics.median(v) for k, v in times.items()}
+    ps = (med["lookup"] + med["table"]) / (1 << args.lookups_log) * 1e12
+    dev.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": "LogUp ps per lookup (fraction-tree build + level sumchecks, lookup and table trees)",
+        "value": ps, "unit": "ps/lookup", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks Fp2)",
+        "data": "synthetic (counter-generated keys, values and multiplicities)",
+        "config": {"workload": f"2^{args.lookups_log} lookups into 2^{args.rows_log} rows, each tree its own leaf stage",
+                   "timing": "host wall clock per tree, median over steps, leaves generated on the device inside"},
+        "lookup_tree_ms": med["lookup"] * 1e3, "table_tree_ms": med["table"] * 1e3,
+        "reference_h100_ps_per_lookup": 297.0, "kernels": kernels,
+    }
+    print(json.dumps(line), flush=True)
+
+
 SEED_SERVE = 0x00650005
 
 
@@ -568,10 +622,12 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["large", "batched", "serve"], default="large",
+    ap.add_argument("--workload", choices=["large", "batched", "serve", "logup"], default="large",
                     help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain; "
                          "serve: the proof server against one-at-a-time proofs")
     ap.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
+    ap.add_argument("--lookups-log", type=int, default=26, help="logup: log2 of the lookups")
+    ap.add_argument("--rows-log", type=int, default=20, help="logup: log2 of the table rows")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: mean Poisson arrivals per second")
     ap.add_argument("--slots", type=int, default=8, help="serve: requests in flight at most")
     ap.add_argument("--serve-budget-gib", type=int, default=64, help="serve: HBM budget for admitted requests")
@@ -594,6 +650,8 @@ def main():
         run_batched(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "logup":
+        run_logup(args)
     else:
         run_gpu(args)
 

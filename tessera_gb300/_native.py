@@ -151,6 +151,7 @@ SIGNATURES = {
     "tg_leaf_stage_prove_level": [V, V, V],
     "tg_leaf_stage_claim": [V, INT, V, V, V, V],
     "tg_leaf_stage_close": [V],
+    "tg_logup_leaves": [V, U64, U64, INT, U64, V, V, SZ, V, V],
     "tg_server_open": [V, SZ, INT, V],
     "tg_server_submit": [V, V, V, V],
     "tg_server_wait": [V, U64, INT],

@@ -109,6 +109,35 @@ __global__ void tr_eq(const ulonglong2* r, int nl, const ulonglong2* hi, ulonglo
     }
 }
 
+// SplitMix64 of a counter, reduced once below p: the reference benchmark's counter-based input
+// generator (its counter_value, crates/tessera-gpu/src/fraction.rs:61-70).
+__device__ __forceinline__ uint64_t counter_value(uint64_t c) {
+    uint64_t z = c * 0x9E3779B97F4A7C15ull + 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    z ^= z >> 31;
+    return z >= P ? z - P : z;
+}
+
+// Generated LogUp leaves: leaf j is (n_j, α − (k_j + β·v_j)) with k_j = counter(key_seed + j),
+// v_j = counter(value_seed + j), and n_j = 1 (a lookup tree) or −m_j, m_j = counter(mult_seed + j)
+// mod 2^16 (a table tree).
+__global__ void tr_logup_leaves(uint64_t key_seed, uint64_t value_seed, uint64_t mult_seed, int unit, fp2 alpha,
+                                fp2 beta, ulonglong2* n_out, ulonglong2* d_out, uint64_t count) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
+        const uint64_t k = counter_value(key_seed + j), v = counter_value(value_seed + j);
+        const fp2 d = {sub(sub(alpha.c0, k), mul(beta.c0, v)), sub(alpha.c1, mul(beta.c1, v))};
+        d_out[j] = make_ulonglong2(d.c0, d.c1);
+        uint64_t nn = 1;
+        if (!unit) {
+            const uint64_t m = counter_value(mult_seed + j) & 0xFFFF;
+            nn = m == 0 ? 0 : P - m;
+        }
+        n_out[j] = make_ulonglong2(nn, 0);
+    }
+}
+
 static unsigned grid_of(const Device* d, uint64_t items) {
     return (unsigned)std::max<uint64_t>(1, std::min<uint64_t>((items + 255) / 256, (uint64_t)d->sm_count * 16));
 }
@@ -589,5 +618,24 @@ extern "C" int tg_leaf_stage_close(tg_leaf_stage* st) {
                 if (b->ptr) cudaMemsetAsync(b->ptr, 0, b->bytes, s);
     cudaStreamSynchronize(s);
     delete st;
+    return TG_OK;
+}
+
+extern "C" int tg_logup_leaves(tg_device* dev, uint64_t key_seed, uint64_t value_seed, int unit, uint64_t mult_seed,
+                               const uint64_t alpha[2], const uint64_t beta[2], size_t count, uint64_t* numerators,
+                               uint64_t* denominators) {
+    Device* d = reinterpret_cast<Device*>(dev);
+    if (!d || !alpha || !beta || (count && (!numerators || !denominators)))
+        return fail(TG_ERR_INVALID, "tg_logup_leaves: null argument");
+    if (count == 0) return TG_OK;
+    cudaStream_t s = d->stream;
+    {
+        Launch L(d, s, "logup_leaves", 1, count);
+        tr_logup_leaves<<<grid_of(d, count), 256, 0, s>>>(key_seed, value_seed, mult_seed, unit, fp2{alpha[0], alpha[1]},
+                                                          fp2{beta[0], beta[1]}, (ulonglong2*)numerators,
+                                                          (ulonglong2*)denominators, count);
+    }
+    TG_CUDA(cudaGetLastError());
+    TG_CUDA(cudaStreamSynchronize(s));
     return TG_OK;
 }

@@ -12,7 +12,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _native as N
-from .device import Device, host_u64, resolve
+from .device import Device, host_u64, is_device_tensor, resolve
 from .hash import Transcript
 
 P = 0xFFFFFFFF00000001
@@ -26,6 +26,10 @@ def lift(values) -> np.ndarray:
     return out
 
 
+def _entries(x) -> int:
+    return x.numel() if hasattr(x, "numel") else np.asarray(x).size
+
+
 @dataclass
 class Forest:
     """2^s product trees of one height, from their stacked leaves (2^(s+h) Fp2 entries)."""
@@ -34,7 +38,7 @@ class Forest:
 
     @property
     def height(self) -> int:
-        return (self.leaves.size // 2).bit_length() - 1 - self.s
+        return (_entries(self.leaves) // 2).bit_length() - 1 - self.s
 
 
 @dataclass
@@ -46,7 +50,7 @@ class Fraction:
 
     @property
     def height(self) -> int:
-        return (self.denominators.size // 2).bit_length() - 1
+        return (_entries(self.denominators) // 2).bit_length() - 1
 
 
 @dataclass
@@ -76,28 +80,38 @@ class LeafStage:
         self.device = resolve(device)
         self.trees = trees
         self._keep = []
+        on_device = any(is_device_tensor(getattr(t, f, None)) for t in trees for f in ("leaves", "denominators"))
+
+        def words(x):
+            """The address of a table: a device tensor's, or a host copy's."""
+            if on_device:
+                if not is_device_tensor(x):
+                    raise ValueError("a stage's leaves are all in host memory or all on the device")
+                return x.data_ptr()
+            a = host_u64(x).reshape(-1)
+            self._keep.append(a)
+            return a.ctypes.data
+
         arr = (N.TreeC * len(trees))()
         for k, t in enumerate(trees):
             if isinstance(t, Forest):
-                leaves = host_u64(t.leaves).reshape(-1)
                 arr[k].kind, arr[k].s, arr[k].height = 0, t.s, t.height
-                arr[k].leaves = leaves.ctypes.data
-                self._keep.append(leaves)
+                arr[k].leaves = words(t.leaves)
             else:
-                den = host_u64(t.denominators).reshape(-1)
                 arr[k].kind, arr[k].s, arr[k].height = 1, 0, t.height
-                arr[k].denominators = den.ctypes.data
-                self._keep.append(den)
+                arr[k].denominators = words(t.denominators)
                 if t.numerators is not None:
-                    num = host_u64(t.numerators).reshape(-1)
-                    arr[k].leaves = num.ctypes.data
-                    self._keep.append(num)
+                    arr[k].leaves = words(t.numerators)
                 if t.sent is not None:
                     sent = host_u64([t.sent[0][0], t.sent[0][1], t.sent[1][0], t.sent[1][1]])
                     arr[k].sent = sent.ctypes.data
                     self._keep.append(sent)
         self._h = ctypes.c_void_p()
-        N.call("tg_leaf_stage_open", self.device.handle, arr, len(trees), 0, ctypes.byref(self._h))
+        if on_device:
+            import torch
+
+            torch.cuda.current_stream().synchronize()
+        N.call("tg_leaf_stage_open", self.device.handle, arr, len(trees), int(on_device), ctypes.byref(self._h))
         hh, lv = ctypes.c_int(), ctypes.c_int()
         N.call("tg_leaf_stage_height", self._h, ctypes.byref(hh), ctypes.byref(lv))
         self.height = hh.value
@@ -161,3 +175,21 @@ def prove_trees(transcript: Transcript, leaves: list, device: Device | None = No
 def prove_forests(transcript: Transcript, forests: list[Forest], device: Device | None = None) -> list[LevelRecord]:
     with LeafStage(forests, device) as st:
         return st.prove(transcript)
+
+
+def generated_fraction(height: int, key_seed: int, value_seed: int, mult_seed: int | None, alpha, beta,
+                       device: Device | None = None) -> Fraction:
+    """A fraction tree of 2^height generated leaves on the device (the reference benchmark's LogUp
+    inputs): leaf j is (1 or −m_j, α − (k_j + β·v_j)) from the counter generator."""
+    import torch
+
+    d = resolve(device)
+    count = 1 << height
+    num = torch.empty(2 * count, dtype=torch.int64, device=f"cuda:{d.ordinal}")
+    den = torch.empty(2 * count, dtype=torch.int64, device=f"cuda:{d.ordinal}")
+    torch.cuda.current_stream().synchronize()
+    a = (ctypes.c_uint64 * 2)(*alpha)
+    b = (ctypes.c_uint64 * 2)(*beta)
+    N.call("tg_logup_leaves", d.handle, key_seed, value_seed, int(mult_seed is None), mult_seed or 0, a, b, count,
+           num.data_ptr(), den.data_ptr())
+    return Fraction(den, num)

@@ -196,3 +196,40 @@ def test_logup_leaf_stages(dev):
         assert t.state.hex() == b["state"] and t.counter == b["counter"], b["name"]
         checked += 1
     assert checked >= 12
+
+
+def counter_value(c):
+    m = 2**64 - 1
+    z = (c * 0x9E3779B97F4A7C15 + 0x9E3779B97F4A7C15) & m
+    z = ((z ^ (z >> 30)) * 0xBF58476D1CE4E5B9) & m
+    z = ((z ^ (z >> 27)) * 0x94D049BB133111EB) & m
+    z ^= z >> 31
+    return z - P if z >= P else z
+
+
+@pytest.mark.parametrize("unit", [True, False])
+def test_generated_leaves_and_leaf_claims(dev, unit):
+    """Generated LogUp leaves equal the counter generator's on the host, and after every level of
+    the tree the final claims are the leaves' numerators' and denominators' MLEs at the final point
+    (the verifier's leaf check, a size-independent property of an honest proof)."""
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.trees import LeafStage, generated_fraction
+
+    h, ks, vs, ms = 9, 1000, 2000000, 77
+    alpha, beta = (123456789, 987654321), (55555, 4444444)
+    tree = generated_fraction(h, ks, vs, None if unit else ms, alpha, beta, dev)
+    n = tree.numerators.cpu().numpy().view(np.uint64)
+    d = tree.denominators.cpu().numpy().view(np.uint64)
+    for j in range(1 << h):
+        k, v = counter_value(ks + j), counter_value(vs + j)
+        assert (int(d[2 * j]), int(d[2 * j + 1])) == sub(alpha, add((k, 0), mul(beta, (v, 0))))
+        m = counter_value(ms + j) & 0xFFFF
+        assert (int(n[2 * j]), int(n[2 * j + 1])) == ((1, 0) if unit else ((P - m) % P, 0))
+    t = Transcript(SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes(32), bytes(16)))
+    with LeafStage([tree], dev) as st:
+        st.prove(t)
+        point, (p, q), own = st.claim(0)
+    assert own == h and len(point) == h
+    nums = [(int(n[2 * j]), int(n[2 * j + 1])) for j in range(1 << h)]
+    dens = [(int(d[2 * j]), int(d[2 * j + 1])) for j in range(1 << h)]
+    assert (p, q) == (mle(nums, point), mle(dens, point))
