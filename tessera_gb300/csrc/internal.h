@@ -125,6 +125,21 @@ int column_absorb(Device* d, uint8_t* chains, uint64_t ncols, const uint64_t* ro
 int merkle_tree(Device* d, const uint8_t* leaves, size_t n, uint8_t* nodes, cudaStream_t s);
 int column_merge(Device* d, const uint8_t* segs, size_t nseg, uint64_t n, uint8_t* leaves, cudaStream_t s);
 
+// A bump allocator over one device buffer, 256-byte aligned pieces.
+struct Arena {
+    size_t used = 0;
+    uint8_t* base = nullptr;
+    size_t take(size_t bytes) {
+        const size_t at = used;
+        used += (bytes + 255) & ~(size_t)255;
+        return at;
+    }
+    template <typename T>
+    T* at(size_t off) const {
+        return reinterpret_cast<T*>(base + off);
+    }
+};
+
 // ---- sumcheck in phases (sumcheck.cu), for callers with their own streams and memory --------
 // sc_prepare validates the jobs and draws each job's γ on its host transcript (NULL and *status
 // on refusal, transcripts untouched); sc_enqueue launches everything on stream s over `arena`

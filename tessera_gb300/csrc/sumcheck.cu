@@ -28,6 +28,7 @@
 
 #include "b3.cuh"
 #include "gl.cuh"
+#include "fs.cuh"
 #include "internal.h"
 
 namespace tg {
@@ -37,27 +38,6 @@ constexpr int SC_MAX_DEGREE = 7;
 constexpr int SC_THREADS = 256;
 constexpr int SC_MAX_SEG_BLOCKS = 1024;
 constexpr int SC_MSG_WORDS = 2 * SC_MAX_DEGREE;  // one instance's round sums, as Fp2 words
-constexpr int FS_MAX_TRIES = 64;  // squeezes per challenge before giving up (each retries with p < 2^-31)
-
-// A job's transcript while it lives on the device.
-struct FsState {
-    uint8_t state[32];
-    uint64_t counter;
-    uint64_t r[2];  // the latest challenge
-    uint32_t err;   // 1: a challenge found no canonical pair in FS_MAX_TRIES squeezes
-    uint32_t pad_;
-};
-
-struct FsKeys {
-    uint32_t absorb[8], squeeze[8], ratchet[8];
-};
-
-struct FsJob {
-    char label[168];  // the job's prefix
-    int label_len;
-    int degree, ninst, n_max, inst0;  // inst0: the job's first instance in the per-instance arrays
-    uint64_t rounds_off, chal_off;    // word offsets of the job's rounds and challenges
-};
 
 // One instance's share of one launch.
 struct Seg {
@@ -278,65 +258,24 @@ __global__ void sc_gather_evals(const EvalRef* refs, int n, uint64_t* out) {
 
 // ---- the transcripts on the device (one thread per job) -----------------------------------------
 
-__device__ void fs_hash(const uint32_t key[8], const uint8_t* msg, uint32_t len, uint8_t out[32]) {
-    uint32_t h[8];
-    for (int i = 0; i < 8; i++) h[i] = key[i];
-    const uint32_t nb = len == 0 ? 1 : (len + 63) / 64;
-    for (uint32_t b = 0; b < nb; b++) {
-        uint32_t m[16];
-        for (int i = 0; i < 16; i++) {
-            uint32_t w = 0;
-            for (int k = 0; k < 4; k++) {
-                const uint32_t at = 64 * b + 4 * i + k;
-                if (at < len) w |= (uint32_t)msg[at] << (8 * k);
-            }
-            m[i] = w;
-        }
-        const bool last = b + 1 == nb;
-        b3::compress_cv(h, m, 0, last ? len - 64 * b : 64,
-                        b3::DERIVE_KEY_MATERIAL | (b == 0 ? b3::CHUNK_START : 0) | (last ? (b3::CHUNK_END | b3::ROOT) : 0));
-    }
-    for (int i = 0; i < 32; i++) out[i] = (uint8_t)(h[i / 4] >> (8 * (i % 4)));
-}
-
-__device__ __forceinline__ void put64(uint8_t* p, uint64_t v) {
-    for (int i = 0; i < 8; i++) p[i] = (uint8_t)(v >> (8 * i));
-}
-
-// state ‖ u64 len(label) ‖ label, label = prefix ‖ tail ‖ decimal j; returns the length.
-__device__ uint32_t fs_begin(const FsState* t, const FsJob& jb, const char* tail, int j, uint8_t* buf) {
-    char lab[200];
-    int n = 0;
-    for (int i = 0; i < jb.label_len; i++) lab[n++] = jb.label[i];
-    for (const char* c = tail; *c; c++) lab[n++] = *c;
-    char digits[12];
-    int nd = 0;
-    do {
-        digits[nd++] = (char)('0' + j % 10);
-        j /= 10;
-    } while (j > 0);
-    while (nd > 0) lab[n++] = digits[--nd];
-    for (int i = 0; i < 32; i++) buf[i] = t->state[i];
-    put64(buf + 32, (uint64_t)n);
-    for (int i = 0; i < n; i++) buf[40 + i] = (uint8_t)lab[i];
-    return 40 + n;
-}
-
 // Round j's message of each job: Σ over its instances of w_i·(own sums, or 2^{pad_i − j − 1}·S_i
 // while padded), absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
 // <prefix>/r/j.
-__global__ void sc_fs_many(FsState* states, const FsJob* jobs, int njobs, int j, FsKeys keys, const uint64_t* w,
-                           const int* pad, const uint64_t* S, const uint64_t* msgbuf, uint64_t* rounds_out,
-                           uint64_t* chal_out) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= njobs) return;
+__global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const FsJob* jobs, int njobs, int j,
+                                                         FsKeys keys, const uint64_t* w, const int* pad,
+                                                         const uint64_t* S, const uint64_t* msgbuf,
+                                                         uint64_t* rounds_out, uint64_t* chal_out) {
+    __shared__ uint32_t sbuf[FS_THREADS / 32][FS_BUF_WORDS];
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x & 31;
+    if (t >= njobs) return;  // whole warps leave together
     const FsJob& jb = jobs[t];
     if (j >= jb.n_max) return;
     FsState* st = states + t;
+    uint32_t* buf = sbuf[threadIdx.x / 32];
     const int degree = jb.degree;
     fp2 msg[SC_MAX_DEGREE];
     for (int x = 0; x < degree; x++) msg[x] = {0, 0};
-    for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {
+    for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {  // every lane forms the message
         const fp2 wi = {w[2 * i], w[2 * i + 1]};
         if (j < pad[i]) {
             const fp2 v = e_mul(wi, e_scale(fp2{S[2 * i], S[2 * i + 1]}, (1ull << (pad[i] - j - 1)) % P));
@@ -346,63 +285,43 @@ __global__ void sc_fs_many(FsState* states, const FsJob* jobs, int njobs, int j,
             for (int x = 0; x < degree; x++) msg[x] = e_add(msg[x], e_mul(wi, fp2{m[2 * x], m[2 * x + 1]}));
         }
     }
-    uint8_t buf[40 + 200 + 8 + 16 * SC_MAX_DEGREE];
-    uint32_t len = fs_begin(st, jb, "/round/", j, buf);
-    put64(buf + len, (uint64_t)degree);
-    len += 8;
-    uint64_t* rj = rounds_out + jb.rounds_off + (size_t)j * 2 * degree;
-    for (int x = 0; x < degree; x++) {
-        put64(buf + len, msg[x].c0);
-        put64(buf + len + 8, msg[x].c1);
-        len += 16;
-        rj[2 * x] = msg[x].c0;
-        rj[2 * x + 1] = msg[x].c1;
-    }
-    fs_hash(keys.absorb, buf, len, st->state);
-    for (int tries = 0; tries < FS_MAX_TRIES; tries++) {
-        len = fs_begin(st, jb, "/r/", j, buf);
-        put64(buf + len, st->counter);
-        uint8_t out[32];
-        fs_hash(keys.squeeze, buf, len + 8, out);
-        st->counter += 1;
-        uint8_t rb[64];
-        for (int i = 0; i < 32; i++) {
-            rb[i] = st->state[i];
-            rb[32 + i] = out[i];
-        }
-        fs_hash(keys.ratchet, rb, 64, st->state);
-        uint64_t c0 = 0, c1 = 0;
-        for (int i = 7; i >= 0; i--) {
-            c0 = (c0 << 8) | out[i];
-            c1 = (c1 << 8) | out[8 + i];
-        }
-        if (c0 < P && c1 < P) {
-            st->r[0] = c0;
-            st->r[1] = c1;
-            chal_out[jb.chal_off + 2 * j] = c0;
-            chal_out[jb.chal_off + 2 * j + 1] = c1;
-            return;
+    uint32_t state[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) state[i] = reinterpret_cast<const uint32_t*>(st->state)[i];
+    uint64_t counter = st->counter;
+    uint32_t len = 0;
+    if (lane == 0) {
+        uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
+        len = fs_begin(state, jb, "/round/", j, buf);
+        put64(bytes + len, (uint64_t)degree);
+        len += 8;
+        uint64_t* rj = rounds_out + jb.rounds_off + (size_t)j * 2 * degree;
+        for (int x = 0; x < degree; x++) {
+            put64(bytes + len, msg[x].c0);
+            put64(bytes + len + 8, msg[x].c1);
+            len += 16;
+            rj[2 * x] = msg[x].c0;
+            rj[2 * x + 1] = msg[x].c1;
         }
     }
-    st->err = 1;
+    len = __shfl_sync(0xFFFFFFFFu, len, 0);
+    uint64_t c0, c1;
+    const bool ok = fs_round_warp(keys, jb, j, buf, len, state, &counter, &c0, &c1);
+    if (lane != 0) return;
+    if (!ok) {
+        st->err = 1;
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < 8; i++) reinterpret_cast<uint32_t*>(st->state)[i] = state[i];
+    st->counter = counter;
+    st->r[0] = c0;
+    st->r[1] = c1;
+    chal_out[jb.chal_off + 2 * j] = c0;
+    chal_out[jb.chal_off + 2 * j + 1] = c1;
 }
 
 // ---- host driver -----------------------------------------------------------------------------
-
-// A bump allocator over one device buffer, 256-byte aligned pieces.
-struct Arena {
-    size_t used = 0;
-    uint8_t* base = nullptr;
-    size_t take(size_t bytes) {
-        const size_t at = used;
-        used += (bytes + 255) & ~(size_t)255;
-        return at;
-    }
-    template <typename T>
-    T* at(size_t off) const {
-        return reinterpret_cast<T*>(base + off);
-    }
-};
 
 template <typename F>
 static void with_degree(int degree, F&& f) {
@@ -796,7 +715,7 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         if (rc) return rc;
         {
             Launch L(d, s, "sumcheck_transcript", 1, njobs);
-            sc_fs_many<<<(njobs + 63) / 64, 64, 0, s>>>(dfs, ar.at<FsJob>(r->off_jobs), njobs, j, keys,
+            sc_fs_many<<<(njobs * 32 + FS_THREADS - 1) / FS_THREADS, FS_THREADS, 0, s>>>(dfs, ar.at<FsJob>(r->off_jobs), njobs, j, keys,
                                                         ar.at<uint64_t>(r->off_w), ar.at<int>(r->off_pad), dS, dmsg,
                                                         drounds, dchal);
         }

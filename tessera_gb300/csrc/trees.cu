@@ -28,6 +28,7 @@
 #include <string>
 #include <vector>
 
+#include "fs.cuh"
 #include "internal.h"
 
 namespace tg {
@@ -147,6 +148,7 @@ struct TreeLevels {
     uint32_t s = 0, h = 0;
     std::vector<std::unique_ptr<DevBuf>> n, d;  // level l, l = 0..h (fractions use both)
     fp2 sent_n = {0, 0}, sent_d = {0, 0};
+    bool unit = false;      // a fraction tree whose leaf numerators are all 1
     std::vector<fp2> root;  // forest: the root level; fraction: (n, d)
     int own = -1;           // the tree's level of its current claim; −1 before it joins
     std::vector<fp2> point;
@@ -184,6 +186,296 @@ static int challenge2(tg_transcript* t, const std::string& label, fp2* out) {
     return TG_OK;
 }
 
+// ---- the level sumcheck, specialised for tree levels ----------------------------------------------
+//
+// A present tree on n variables proves Σ_x eq(p, x)·g(x) with g = L·R (forest) or
+// N0·D1 + N1·D0 + λ·D0·D1 (fraction tree) over the halves of the level below. eq is never
+// tabulated or bound: at the tree's own round j the message is
+//   p_j(X) = C_j · eq1(p_j, X) · q_j(X),   q_j(X) = Σ_{x'} eq(p_{>j}, x')·g(X, x')
+// with C_j = Π_{i<j} eq1(p_i, r_i) a running scalar and eq1(t, X) = (1 − t)(1 − X) + t·X, and the
+// weights eq(p_{>j}, x') = lo_j[x' mod 2^L]·hi_j[x' >> L] come from small per-round tables built
+// once per level from the point. Round 0 reads the level below directly (the halves are its even
+// and odd entries); each later round binds the previous challenge into the tables as it sums.
+
+constexpr int TL_THREADS = 256;
+constexpr int TL_LOW = 10;
+
+struct TlSeg {
+    const ulonglong2* src[4];  // table T's entry x is src[T][x·stride]
+    ulonglong2* dst[4];        // bound tables (when bind)
+    const ulonglong2* lo;      // this round's eq weights over the remaining variables
+    const ulonglong2* hi;
+    const uint64_t* r;         // the challenge to bind
+    ulonglong2* out;           // q at the nodes 0, 1, 2, 3 (node 1 only in a tree's round 0)
+    uint64_t n;                // pairs
+    uint64_t lam[2];
+    int kind, stride, bind, lbits;
+    int block0, nblocks, part0, pad_;
+};
+static_assert(sizeof(TlSeg) % 8 == 0, "TlSeg copies as words");
+
+struct TlTree {  // one present tree, as the transcript kernel sees it
+    uint64_t w[2];   // γ^i
+    uint64_t C[2];   // the running eq scalar
+    uint64_t S[2];   // the tree's full sum, for its padding rounds
+    const uint64_t* point;  // n Fp2
+    const ulonglong2* lvl_n;  // the level below (a tree on no variable sums its two or four entries)
+    const ulonglong2* lvl_d;
+    int n, pad, kind, pad_;
+};
+
+__device__ __forceinline__ fp2 ld2(const ulonglong2* p) {
+    const ulonglong2 v = *p;
+    return {v.x, v.y};
+}
+
+// Fp2 on lazy words (any 64-bit representative; canonical only where results leave the kernel).
+__device__ __forceinline__ fp2 l2_add(fp2 a, fp2 b) { return {lz::add(a.c0, b.c0), lz::add(a.c1, b.c1)}; }
+__device__ __forceinline__ fp2 l2_sub(fp2 a, fp2 b) { return {lz::sub(a.c0, b.c0), lz::sub(a.c1, b.c1)}; }
+__device__ __forceinline__ fp2 l2_mul(fp2 a, fp2 b) {  // Karatsuba, X^2 = 7
+    const uint64_t t0 = lz::mul(a.c0, b.c0), t1 = lz::mul(a.c1, b.c1);
+    const uint64_t t2 = lz::mul(lz::add(a.c0, a.c1), lz::add(b.c0, b.c1));
+    return {lz::add(t0, lz::sub(lz::mulp2<3>(t1), t1)), lz::sub(lz::sub(t2, t0), t1)};
+}
+__device__ __forceinline__ fp2 l2_canon(fp2 a) { return {lz::canon(a.c0), lz::canon(a.c1)}; }
+
+// Σ over the segment's pairs handled by this thread of w(x')·g(X, x') at the nodes X = 0, 1, 2, 3
+// (node 1 only without a bind); NT tables (2: L, R; 4: N0, N1, D0, D1).
+template <int NT, int KIND>
+__device__ __forceinline__ void tl_pairs(const TlSeg& g, uint64_t first, uint64_t stride, fp2 (&acc)[4]) {
+    const uint64_t mask = (1ull << g.lbits) - 1;
+    const fp2 r = g.bind ? fp2{g.r[0], g.r[1]} : fp2{0, 0};
+    const fp2 lam = {g.lam[0], g.lam[1]};
+    const int st = g.stride;
+    for (uint64_t p = first; p < g.n; p += stride) {
+        fp2 u[NT], d[NT];
+#pragma unroll
+        for (int k = 0; k < NT; k++) {
+            const ulonglong2* src = g.src[k];
+            if (g.bind) {
+                const fp2 a0 = ld2(src + (4 * p) * st), a1 = ld2(src + (4 * p + 1) * st);
+                const fp2 b0 = ld2(src + (4 * p + 2) * st), b1 = ld2(src + (4 * p + 3) * st);
+                const fp2 uu = l2_add(a0, l2_mul(r, l2_sub(a1, a0)));
+                const fp2 vv = l2_add(b0, l2_mul(r, l2_sub(b1, b0)));
+                g.dst[k][2 * p] = make_ulonglong2(uu.c0, uu.c1);
+                g.dst[k][2 * p + 1] = make_ulonglong2(vv.c0, vv.c1);
+                u[k] = uu;
+                d[k] = l2_sub(vv, uu);
+            } else {
+                u[k] = ld2(src + (2 * p) * st);
+                d[k] = l2_sub(ld2(src + (2 * p + 1) * st), u[k]);
+            }
+        }
+        const fp2 w = l2_mul(ld2(g.lo + (p & mask)), ld2(g.hi + (p >> g.lbits)));
+#pragma unroll
+        for (int node = 0; node < 4; node++) {
+            if (!(node == 1 && g.bind)) {
+                fp2 gx;
+                if constexpr (KIND == 0)  // L·R
+                    gx = l2_mul(u[0], u[1]);
+                else if constexpr (KIND == 1)  // N0·D1 + N1·D0 + λ·D0·D1
+                    gx = l2_add(l2_add(l2_mul(u[0], u[3]), l2_mul(u[1], u[2])), l2_mul(lam, l2_mul(u[2], u[3])));
+                else  // numerators of 1: D1 + D0 + λ·D0·D1 over the tables D0, D1
+                    gx = l2_add(l2_add(u[0], u[1]), l2_mul(lam, l2_mul(u[0], u[1])));
+                acc[node] = l2_add(acc[node], l2_mul(w, gx));
+            }
+            if (node < 3)
+#pragma unroll
+                for (int k = 0; k < NT; k++) u[k] = l2_add(u[k], d[k]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(TL_THREADS, 2) tl_rounds(const TlSeg* segs, int nseg, uint64_t* partials,
+                                                           unsigned* counters) {
+    __shared__ TlSeg g;
+    __shared__ int si;
+    __shared__ uint64_t red[TL_THREADS / 32][8];
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (segs[mid].block0 <= (int)blockIdx.x)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        si = lo;
+    }
+    __syncthreads();
+    {
+        const uint64_t* from = reinterpret_cast<const uint64_t*>(segs + si);
+        uint64_t* to = reinterpret_cast<uint64_t*>(&g);
+        for (int w = threadIdx.x; w < (int)(sizeof(TlSeg) / 8); w += blockDim.x) to[w] = from[w];
+    }
+    __syncthreads();
+    fp2 acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
+    const uint64_t first = (uint64_t)(blockIdx.x - g.block0) * blockDim.x + threadIdx.x;
+    const uint64_t stride = (uint64_t)g.nblocks * blockDim.x;
+    if (g.kind == 0)
+        tl_pairs<2, 0>(g, first, stride, acc);
+    else if (g.kind == 1)
+        tl_pairs<4, 1>(g, first, stride, acc);
+    else
+        tl_pairs<2, 2>(g, first, stride, acc);
+    // block sums, then the segment's last block reduces the partial rows
+    uint64_t words[8];
+    for (int i = 0; i < 4; i++) {
+        const fp2 c = l2_canon(acc[i]);
+        words[2 * i] = c.c0, words[2 * i + 1] = c.c1;
+    }
+#pragma unroll
+    for (int w = 0; w < 8; w++)
+        for (int o = 16; o > 0; o >>= 1) words[w] = add(words[w], __shfl_down_sync(0xFFFFFFFFu, words[w], o));
+    if ((threadIdx.x & 31) == 0)
+        for (int w = 0; w < 8; w++) red[threadIdx.x >> 5][w] = words[w];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        for (int k = 1; k < (int)(blockDim.x >> 5); k++)
+            for (int w = 0; w < 8; w++) words[w] = add(words[w], red[k][w]);
+        for (int w = 0; w < 8; w++) partials[(size_t)(g.part0 + blockIdx.x - g.block0) * 8 + w] = words[w];
+        __threadfence();
+        last = atomicAdd(&counters[si], 1u) == (unsigned)g.nblocks - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    if (threadIdx.x < 8) {
+        uint64_t t = 0;
+        for (int b = 0; b < g.nblocks; b++) t = add(t, __ldcg(&partials[(size_t)(g.part0 + b) * 8 + threadIdx.x]));
+        reinterpret_cast<uint64_t*>(g.out)[threadIdx.x] = t;
+    }
+    if (threadIdx.x == 0) counters[si] = 0;
+}
+
+// The eq weight tables of every round of every present tree: entry e of table t is
+// Π_i eq1(c_i, bit_i(e)) over the table's coordinates c (lo: the first L of the round's remaining
+// coordinates, hi: the rest).
+struct TlEqJob {
+    const uint64_t* coords;  // Fp2 coordinates
+    int ncoords;
+    ulonglong2* out;
+    uint64_t entries;
+};
+__global__ void tl_eq_tables(const TlEqJob* jobs, int njobs, uint64_t total) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        uint64_t at = i;
+        int jb = 0;
+        while (jb < njobs && at >= jobs[jb].entries) at -= jobs[jb++].entries;
+        if (jb >= njobs) return;
+        const TlEqJob& J = jobs[jb];
+        fp2 pr = {1, 0};
+        for (int c = 0; c < J.ncoords; c++) {
+            const fp2 t = {J.coords[2 * c], J.coords[2 * c + 1]};
+            pr = e_mul(pr, (at >> c) & 1 ? t : e_sub(fp2{1, 0}, t));
+        }
+        J.out[at] = make_ulonglong2(pr.c0, pr.c1);
+    }
+}
+
+// eq1(t, X) = (1 − t)(1 − X) + t·X
+__device__ __forceinline__ fp2 eq1(fp2 t, fp2 x) {
+    const fp2 one = {1, 0};
+    return e_add(e_mul(e_sub(one, t), e_sub(one, x)), e_mul(t, x));
+}
+
+// Round j of a level: the message Σ_i γ^i·(2^{pad_i − j − 1}·S_i while padded, else
+// C_i·eq1(p_i[j'], X)·q_i(X)), absorbed under <prefix>/round/j; r_j drawn under <prefix>/r/j;
+// then each tree in its own rounds takes C_i ← C_i·eq1(p_i[j'], r_j). At j = 0 each padded tree's
+// S_i = Σ_{X∈{0,1}} eq1(p_i[0], X)·q_i(X) is taken from its round-0 sums first.
+__global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, int ntrees, const ulonglong2* q,
+                      fp2 lam, uint64_t* rounds_out, uint64_t* chal_out) {
+    __shared__ uint32_t sbuf[FS_BUF_WORDS];
+    const int lane = threadIdx.x & 31;
+    const fp2 X[3] = {{0, 0}, {2, 0}, {3, 0}};
+    fp2 msg[3] = {{0, 0}, {0, 0}, {0, 0}};
+    for (int i = 0; i < ntrees; i++) {  // every lane forms the message (the same reads)
+        TlTree& T = trees[i];
+        const fp2 w = {T.w[0], T.w[1]};
+        fp2 S = {T.S[0], T.S[1]};
+        if (j == 0 && T.pad > 0) {
+            if (T.n == 0) {  // g at the level below's single entry
+                if (T.kind == 0)
+                    S = e_mul(ld2(T.lvl_n), ld2(T.lvl_n + 1));
+                else {
+                    const fp2 n0 = ld2(T.lvl_n), n1 = ld2(T.lvl_n + 1), d0 = ld2(T.lvl_d), d1 = ld2(T.lvl_d + 1);
+                    S = e_add(e_add(e_mul(n0, d1), e_mul(n1, d0)), e_mul(lam, e_mul(d0, d1)));
+                }
+            } else {
+                const fp2 t = {T.point[0], T.point[1]};
+                S = e_add(e_mul(eq1(t, fp2{0, 0}), ld2(q + 4 * i)), e_mul(eq1(t, fp2{1, 0}), ld2(q + 4 * i + 1)));
+            }
+            __syncwarp();
+            if (lane == 0) T.S[0] = S.c0, T.S[1] = S.c1;
+        }
+        const int jj = j - T.pad;
+        if (jj < 0) {
+            const fp2 v = e_mul(w, e_scale(S, (1ull << (T.pad - j - 1)) % P));
+            for (int x = 0; x < 3; x++) msg[x] = e_add(msg[x], v);
+        } else {
+            const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
+            const fp2 wc = e_mul(w, fp2{T.C[0], T.C[1]});
+            const int node[3] = {0, 2, 3};
+            for (int x = 0; x < 3; x++)
+                msg[x] = e_add(msg[x], e_mul(wc, e_mul(eq1(t, X[x]), ld2(q + 4 * i + node[x]))));
+        }
+    }
+    uint32_t state[8];
+    for (int i = 0; i < 8; i++) state[i] = reinterpret_cast<const uint32_t*>(st->state)[i];
+    uint64_t counter = st->counter;
+    uint32_t len = 0;
+    if (lane == 0) {
+        uint8_t* bytes = reinterpret_cast<uint8_t*>(sbuf);
+        len = fs_begin(state, jb, "/round/", j, sbuf);
+        put64(bytes + len, 3);
+        len += 8;
+        for (int x = 0; x < 3; x++) {
+            put64(bytes + len, msg[x].c0);
+            put64(bytes + len + 8, msg[x].c1);
+            len += 16;
+            rounds_out[6 * j + 2 * x] = msg[x].c0;
+            rounds_out[6 * j + 2 * x + 1] = msg[x].c1;
+        }
+    }
+    len = __shfl_sync(0xFFFFFFFFu, len, 0);
+    uint64_t c0, c1;
+    const bool ok = fs_round_warp(keys, jb, j, sbuf, len, state, &counter, &c0, &c1);
+    if (lane != 0) return;
+    if (!ok) {
+        st->err = 1;
+        return;
+    }
+    for (int i = 0; i < 8; i++) reinterpret_cast<uint32_t*>(st->state)[i] = state[i];
+    st->counter = counter;
+    st->r[0] = c0, st->r[1] = c1;
+    chal_out[2 * j] = c0, chal_out[2 * j + 1] = c1;
+    const fp2 r = {c0, c1};
+    for (int i = 0; i < ntrees; i++) {
+        TlTree& T = trees[i];
+        const int jj = j - T.pad;
+        if (jj < 0) continue;
+        const fp2 C = e_mul(fp2{T.C[0], T.C[1]}, eq1(fp2{T.point[2 * jj], T.point[2 * jj + 1]}, r));
+        T.C[0] = C.c0, T.C[1] = C.c1;
+    }
+}
+
+// The last bind: each table of two entries (2·stride apart) into one, by r, as the evaluations.
+struct TlFinal {
+    const ulonglong2* src;
+    int stride, pad_;
+    ulonglong2* out;
+};
+__global__ void tl_bind_last(const TlFinal* f, int n, const uint64_t* r) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const fp2 rr = {r[0], r[1]};
+    const fp2 a = l2_canon(ld2(f[i].src)), b = l2_canon(ld2(f[i].src + f[i].stride));
+    const fp2 v = e_add(a, e_mul(rr, e_sub(b, a)));
+    *f[i].out = make_ulonglong2(v.c0, v.c1);
+}
+
 }  // namespace tg
 
 using namespace tg;
@@ -192,6 +484,10 @@ struct tg_leaf_stage {
     Device* d = nullptr;
     std::vector<TreeLevels> trees;
     int H = 0, level = 0;
+    // per tree: the eq table, its point and high part, and the halves of the level below, sized
+    // once for the tree's deepest level so that no level allocates
+    std::vector<std::vector<std::unique_ptr<DevBuf>>> pool;
+    DevBuf misc;  // a level's points, eq tables, segments, transcript and outputs
 };
 
 extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntrees, int on_device, tg_leaf_stage** out) {
@@ -237,6 +533,7 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
             rc = tr.d[spec.height]->ensure(leaves * 16);
             if (rc) return bail(rc);
             TG_CUDA(cudaMemcpyAsync(tr.d[spec.height]->ptr, spec.denominators, leaves * 16, kind, s));
+            tr.unit = !spec.leaves;
             if (spec.leaves) {
                 TG_CUDA(cudaMemcpyAsync(tr.n[spec.height]->ptr, spec.leaves, leaves * 16, kind, s));
             } else {  // numerators of 1
@@ -276,6 +573,21 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
                 tr.sent_d = {spec.sent[2], spec.sent[3]};
             }
         }
+    }
+    // per tree and table, the bound tables of its deepest level (n = s + h − 1 variables): A holds
+    // 2^(n−1) entries (own rounds 1, 3, …), B 2^(n−2) (own rounds 2, 4, …)
+    st->pool.resize(ntrees);
+    for (int k = 0; k < ntrees; k++) {
+        const TreeLevels& tr = st->trees[k];
+        const int n = (int)(tr.s + tr.h) - 1;
+        const int nt = tr.kind ? 4 : 2;
+        for (int t2 = 0; t2 < nt; t2++)
+            for (int ab = 0; ab < 2; ab++) {
+                st->pool[k].emplace_back(new DevBuf());
+                const size_t entries = n - 1 - ab >= 0 ? (1ull << (n - 1 - ab)) : 1;
+                const int rc = st->pool[k].back()->ensure(entries * 16);
+                if (rc) return bail(rc);
+            }
     }
     *out = st;
     return TG_OK;
@@ -388,137 +700,246 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         if (rc) return bail(rc);
     }
 
-    // the level's tables on the device: an eq table and the halves of the level below per tree
+    // ---- the level's sumcheck on the device (TlSeg rounds, tl_fs transcript, tl_bind_last)
     cudaStream_t s = d->stream;
-    std::vector<std::unique_ptr<DevBuf>> bufs;
-    auto buf = [&](size_t bytes) -> ulonglong2* {
-        bufs.emplace_back(new DevBuf());
-        return bufs.back()->ensure(std::max<size_t>(bytes, 16)) ? nullptr : (ulonglong2*)bufs.back()->ptr;
-    };
-    std::vector<tg_table> tabs;
-    tabs.reserve(9 * present.size());
-    std::vector<tg_instance> insts;
-    std::vector<fp2> weights;
-    std::vector<int> nvars;
-    fp2 gi = {1, 0};
+    const int np = (int)present.size();
+    std::vector<int> nvars(np), pads(np);
     int n_max = 0;
+    for (int i = 0; i < np; i++) n_max = std::max(n_max, nvars[i] = (int)jpoint[present[i]].size());
+    for (int i = 0; i < np; i++) pads[i] = n_max - nvars[i];
+    const int seg_cap = std::min(1024, 4 * d->sm_count);
+    auto blocks_for = [&](uint64_t n) {
+        return (int)std::max<uint64_t>(1, std::min<uint64_t>((n + TL_THREADS - 1) / TL_THREADS, seg_cap));
+    };
+    // the level block: points | eq tables | eq jobs | trees | q | segments | finals | partials |
+    // counters | FsState | rounds | challenges | evaluations
+    Arena ar;
+    std::vector<size_t> off_point(np), off_eq(np);
+    std::vector<std::vector<std::pair<uint64_t, uint64_t>>> eqtab(np);  // per own round: (lo offset, hi offset) in entries
+    std::vector<TlEqJob> eqjobs;
+    uint64_t eq_total = 0;
+    for (int i = 0; i < np; i++) {
+        const int n = nvars[i];
+        off_point[i] = ar.take((size_t)std::max(n, 1) * 16);
+        uint64_t entries = 0;
+        for (int jj = 0; jj < n; jj++) {
+            const int rem = n - jj - 1, nl = std::min(rem, TL_LOW), nh = rem - nl;
+            eqtab[i].push_back({entries, entries + (1ull << nl)});
+            entries += (1ull << nl) + (1ull << nh);
+        }
+        off_eq[i] = entries;  // the entry count for now; the tables go after everything uploaded
+        eq_total += entries;
+    }
+    const size_t off_jobs = ar.take(sizeof(TlEqJob) * std::max<size_t>(2 * np * 64, 1));
+    const size_t off_trees = ar.take(sizeof(TlTree) * np);
+    const size_t off_q = ar.take((size_t)64 * np);
+    // segments: launch 0 is every tree's own round 0, launch j (1 ≤ j < n_max) the trees in own rounds ≥ 1
+    std::vector<std::vector<TlSeg>> launches(std::max(n_max, 1));
+    std::vector<std::vector<std::pair<int, int>>> owners(std::max(n_max, 1));  // (tree i, own round jj)
+    std::vector<TlFinal> finals;
+    auto table_src = [&](int i, int jj, int k, int* stride) -> const ulonglong2* {
+        // the tables own round jj reads: the level below (jj ≤ 1), else round jj − 1's bound output
+        TreeLevels& tr = st->trees[present[i]];
+        const int own = tr.own >= 0 ? tr.own : 0;
+        if (jj <= 1) {
+            *stride = 2;
+            const DevBuf& lv = (tr.kind == 1 && k >= 2) ? *tr.d[own + 1] : *tr.n[own + 1];
+            return (const ulonglong2*)lv.ptr + (k & 1);
+        }
+        *stride = 1;
+        return (const ulonglong2*)st->pool[present[i]][2 * k + ((jj - 2) & 1)]->ptr;
+    };
+    // a fraction tree whose leaves have numerators of 1, at the level right above its leaves:
+    // N0 and N1 stay 1 through every bind, so only D0 and D1 are tables
+    auto unit_level = [&](int i) {
+        const TreeLevels& tr = st->trees[present[i]];
+        const int own = tr.own >= 0 ? tr.own : 0;
+        return tr.kind == 1 && tr.unit && own + 1 == (int)tr.h;
+    };
+    size_t total_segs = 0, max_blocks = 1, max_segs = 1;
+    for (int j = 0; j < std::max(n_max, 1); j++) {
+        int block0 = 0;
+        for (int i = 0; i < np; i++) {
+            const int jj = j == 0 ? 0 : j - pads[i];
+            if (j > 0 && jj < 1) continue;
+            if (nvars[i] == 0 || jj >= nvars[i]) continue;
+            TreeLevels& tr = st->trees[present[i]];
+            const bool unit = unit_level(i);
+            const int nt = unit ? 2 : tr.kind ? 4 : 2;
+            TlSeg g;
+            memset(&g, 0, sizeof g);
+            g.kind = unit ? 2 : tr.kind;
+            g.bind = jj >= 1;
+            for (int k = 0; k < nt; k++) {
+                const int tk = unit ? k + 2 : k;  // the unit kind's tables are D0 and D1
+                g.src[k] = table_src(i, jj, tk, &g.stride);
+                if (g.bind) g.dst[k] = (ulonglong2*)st->pool[present[i]][2 * tk + ((jj - 1) & 1)]->ptr;
+            }
+            g.n = 1ull << (nvars[i] - jj - 1);
+            g.lam[0] = lambda.c0, g.lam[1] = lambda.c1;
+            g.lbits = std::min(nvars[i] - jj - 1, TL_LOW);
+            g.block0 = block0;
+            g.nblocks = blocks_for(g.n);
+            g.part0 = block0;
+            block0 += g.nblocks;
+            launches[j].push_back(g);
+            owners[j].push_back({i, jj});
+        }
+        total_segs += launches[j].size();
+        max_segs = std::max(max_segs, launches[j].size());
+        max_blocks = std::max(max_blocks, (size_t)block0);
+    }
+    const size_t off_segs = ar.take(sizeof(TlSeg) * std::max<size_t>(total_segs, 1));
+    const size_t off_finals = ar.take(sizeof(TlFinal) * 4 * np);
+    const size_t off_partials = ar.take(max_blocks * 64);
+    const size_t off_counters = ar.take(4 * max_segs);
+    const size_t off_fs = ar.take(sizeof(FsState));
+    const size_t off_rounds = ar.take((size_t)std::max(n_max, 1) * 48);
+    const size_t off_chal = ar.take((size_t)std::max(n_max, 1) * 16);
+    const size_t off_evals = ar.take((size_t)64 * np);
+    const size_t upload_bytes = ar.used;  // the eq tables, built on the device, follow
+    for (int i = 0; i < np; i++) off_eq[i] = ar.take(std::max<uint64_t>(off_eq[i], 1) * 16);
+    if (ar.used > st->misc.bytes) {  // grows geometrically: the levels grow one after another
+        const int rc2 = st->misc.ensure(std::max(ar.used, 2 * st->misc.bytes));
+        if (rc2) return bail(rc2);
+    }
+    ar.base = (uint8_t*)st->misc.ptr;
+
+    // host staging of everything the level uploads
+    std::vector<uint8_t> up(upload_bytes, 0);
+    auto host_at = [&](size_t off) { return up.data() + off; };
+    std::vector<TlTree> ttrees(np);
+    fp2 gi = {1, 0};
+    for (int i = 0; i < np; i++) {
+        const std::vector<fp2>& pt = jpoint[present[i]];
+        uint64_t* pw = (uint64_t*)host_at(off_point[i]);
+        for (size_t c = 0; c < pt.size(); c++) pw[2 * c] = pt[c].c0, pw[2 * c + 1] = pt[c].c1;
+        const uint64_t* dpt = ar.at<uint64_t>(off_point[i]);
+        for (int jj = 0; jj < nvars[i]; jj++) {  // round jj's weights over p[jj+1 ..]
+            const int rem = nvars[i] - jj - 1, nl = std::min(rem, TL_LOW), nh = rem - nl;
+            ulonglong2* base = ar.at<ulonglong2>(off_eq[i]);
+            eqjobs.push_back({dpt + 2 * (jj + 1), nl, base + eqtab[i][jj].first, 1ull << nl});
+            eqjobs.push_back({dpt + 2 * (jj + 1 + nl), nh, base + eqtab[i][jj].second, 1ull << nh});
+        }
+        TlTree& T = ttrees[i];
+        memset(&T, 0, sizeof T);
+        T.w[0] = gi.c0, T.w[1] = gi.c1;
+        T.C[0] = 1;
+        T.point = dpt;
+        T.n = nvars[i];
+        T.pad = pads[i];
+        {
+            TreeLevels& trl = st->trees[present[i]];
+            const int own = trl.own >= 0 ? trl.own : 0;
+            T.kind = trl.kind;
+            T.lvl_n = (const ulonglong2*)trl.n[own + 1]->ptr;
+            T.lvl_d = trl.kind ? (const ulonglong2*)trl.d[own + 1]->ptr : nullptr;
+        }
+        gi = e_mul(gi, gamma);
+        // the final evaluations of its tables
+        TreeLevels& tr = st->trees[present[i]];
+        const int nt = tr.kind ? 4 : 2;
+        for (int k = 0; k < nt; k++) {
+            TlFinal f;
+            memset(&f, 0, sizeof f);
+            const int n = nvars[i];
+            const bool copy = n == 0 || (unit_level(i) && k < 2);  // an entry itself (numerators of 1 stay 1)
+            f.src = copy ? table_src(i, 0, k, &f.stride) : table_src(i, n - 1 >= 1 ? n : 1, k, &f.stride);
+            if (copy) f.stride = 0;
+            f.out = ar.at<ulonglong2>(off_evals) + finals.size();
+            finals.push_back(f);
+        }
+    }
+    // segments' eq tables, outputs and challenge pointers, now that the block's addresses are known
+    {
+        size_t at = 0;
+        FsState* dfs = ar.at<FsState>(off_fs);
+        for (int j = 0; j < (int)launches.size(); j++)
+            for (size_t q = 0; q < launches[j].size(); q++) {
+                TlSeg& g = launches[j][q];
+                const int i = owners[j][q].first, jj = owners[j][q].second;
+                ulonglong2* base = ar.at<ulonglong2>(off_eq[i]);
+                g.lo = base + eqtab[i][jj].first;
+                g.hi = base + eqtab[i][jj].second;
+                g.out = ar.at<ulonglong2>(off_q) + 4 * i;
+                g.r = dfs->r;
+                memcpy(host_at(off_segs) + sizeof(TlSeg) * at++, &g, sizeof g);
+            }
+    }
+    if (!eqjobs.empty()) memcpy(host_at(off_jobs), eqjobs.data(), sizeof(TlEqJob) * eqjobs.size());
+    memcpy(host_at(off_trees), ttrees.data(), sizeof(TlTree) * np);
+    if (!finals.empty()) memcpy(host_at(off_finals), finals.data(), sizeof(TlFinal) * finals.size());
+    {
+        FsState fs0;
+        memset(&fs0, 0, sizeof fs0);
+        memcpy(fs0.state, t->state, 32);
+        fs0.counter = t->counter;
+        memcpy(host_at(off_fs), &fs0, sizeof fs0);
+    }
+    FsJob jb;
+    memset(&jb, 0, sizeof jb);
+    jb.label_len = (int)prefix.size();
+    memcpy(jb.label, prefix.data(), prefix.size());
+    FsKeys keys;
+    context_key("transcript-absorb", keys.absorb);
+    context_key("transcript-squeeze", keys.squeeze);
+    context_key("transcript-ratchet", keys.ratchet);
+
+    std::vector<uint64_t> rounds((size_t)std::max(n_max, 1) * 6), chal((size_t)std::max(n_max, 1) * 2),
+        fevals(8 * (size_t)np);
+    FsState fs1;
     {
         std::lock_guard<std::mutex> lock(d->mu);
-        for (int k : present) {
-            TreeLevels& tr = st->trees[k];
-            const int own = tr.own >= 0 ? tr.own : 0;
-            const int n = (int)jpoint[k].size();
-            n_max = std::max(n_max, n);
-            nvars.push_back(n);
-            const uint64_t m = 1ull << n;
-            // eq(point, ·)
-            ulonglong2* eq = buf(m * 16);
-            ulonglong2* r = buf(std::max<size_t>(n, 1) * 16);
-            if (!eq || !r) return bail(fail(TG_ERR_NOMEM, "level tables"));
-            std::vector<uint64_t> rw(2 * std::max(n, 1), 0);
-            for (int i = 0; i < n; i++) {
-                rw[2 * i] = jpoint[k][i].c0;
-                rw[2 * i + 1] = jpoint[k][i].c1;
-            }
-            TG_CUDA(cudaMemcpyAsync(r, rw.data(), rw.size() * 8, cudaMemcpyHostToDevice, s));
-            const int nl = std::min(n, EQ_LOW), nh = n - nl;
-            ulonglong2* hi = nullptr;
-            if (nh > 0) {
-                hi = buf((1ull << nh) * 16);
-                if (!hi) return bail(fail(TG_ERR_NOMEM, "level tables"));
-                Launch L(d, s, "tree_eq", 1, 1ull << nh);
-                tr_eq_high<<<grid_of(d, 1ull << nh), 256, 0, s>>>(r + nl, nh, hi);
-            }
-            {
-                Launch L(d, s, "tree_eq", 1, m);
-                tr_eq<<<grid_of(d, m), 256, 0, s>>>(r, nl, hi, eq, m);
-            }
-            TG_CUDA(cudaStreamSynchronize(s));  // rw is a host temporary
-            // halves of the level below
-            auto split = [&](DevBuf& lv, ulonglong2** e, ulonglong2** o) -> int {
-                *e = buf(m * 16);
-                *o = buf(m * 16);
-                if (!*e || !*o) return fail(TG_ERR_NOMEM, "level tables");
-                Launch L(d, s, "tree_split", 1, m);
-                tr_split<<<grid_of(d, m), 256, 0, s>>>((const ulonglong2*)lv.ptr, *e, *o, m);
-                TG_CUDA(cudaGetLastError());
-                return TG_OK;
-            };
-            auto table = [&](const void* p, int pub) {
-                tg_table tb;
-                tb.values = (const uint64_t*)p;
-                tb.is_ext = 1;
-                tb.is_public = pub;
-                tabs.push_back(tb);
-            };
-            auto instance = [&](fp2 w) {
-                tg_instance in;
-                in.tables = &tabs[tabs.size() - 3];
-                in.ntables = 3;
-                in.vars = n;
-                insts.push_back(in);
-                weights.push_back(w);
-            };
-            if (tr.kind == 0) {
-                ulonglong2 *lt, *rt;
-                rc = split(*tr.n[own + 1], &lt, &rt);
-                if (rc) return bail(rc);
-                table(eq, 1), table(lt, 0), table(rt, 0);
-                instance(gi);
-            } else {
-                ulonglong2 *n0, *n1, *d0, *d1;
-                rc = split(*tr.n[own + 1], &n0, &n1);
-                if (!rc) rc = split(*tr.d[own + 1], &d0, &d1);
-                if (rc) return bail(rc);
-                table(eq, 1), table(n0, 0), table(d1, 0);
-                instance(gi);
-                table(eq, 1), table(n1, 0), table(d0, 0);
-                instance(gi);
-                table(eq, 1), table(d0, 0), table(d1, 0);
-                instance(e_mul(gi, lambda));
-            }
-            gi = e_mul(gi, gamma);
+        TG_CUDA(cudaMemcpyAsync(ar.base, up.data(), up.size(), cudaMemcpyHostToDevice, s));
+        if (eq_total) {
+            Launch L(d, s, "tree_eq", 1, eq_total);
+            tl_eq_tables<<<grid_of(d, eq_total), 256, 0, s>>>(ar.at<TlEqJob>(off_jobs), (int)eqjobs.size(), eq_total);
+            TG_CUDA(cudaGetLastError());
         }
+        size_t seg0 = 0;
+        auto run = [&](int j) -> int {
+            const auto& L0 = launches[j];
+            if (L0.empty()) return TG_OK;
+            int blocks = 0;
+            for (const TlSeg& g : L0) blocks += g.nblocks;
+            uint64_t units = 0;
+            for (const TlSeg& g : L0) units += g.n;
+            Launch L(d, s, "tree_level_round", 1, units);
+            tl_rounds<<<blocks, TL_THREADS, 0, s>>>(ar.at<TlSeg>(off_segs) + seg0, (int)L0.size(),
+                                                    ar.at<uint64_t>(off_partials), ar.at<unsigned>(off_counters));
+            seg0 += L0.size();
+            TG_CUDA(cudaGetLastError());
+            return TG_OK;
+        };
+        TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(off_counters), 0, 4 * max_segs, s));
+        rc = run(0);
+        if (rc) return bail(rc);
+        for (int j = 0; j < n_max; j++) {
+            if (j > 0) {
+                rc = run(j);
+                if (rc) return bail(rc);
+            }
+            Launch L(d, s, "tree_level_transcript", 1, 1);
+            tl_fs<<<1, 32, 0, s>>>(ar.at<FsState>(off_fs), jb, j, keys, ar.at<TlTree>(off_trees), np,
+                                   ar.at<ulonglong2>(off_q), lambda, ar.at<uint64_t>(off_rounds), ar.at<uint64_t>(off_chal));
+            TG_CUDA(cudaGetLastError());
+        }
+        if (!finals.empty()) {
+            Launch L(d, s, "tree_level_evals", 1, finals.size());
+            tl_bind_last<<<1, 128, 0, s>>>(ar.at<TlFinal>(off_finals), (int)finals.size(), ar.at<FsState>(off_fs)->r);
+            TG_CUDA(cudaGetLastError());
+        }
+        TG_CUDA(cudaMemcpyAsync(&fs1, ar.at<FsState>(off_fs), sizeof fs1, cudaMemcpyDeviceToHost, s));
+        TG_CUDA(cudaMemcpyAsync(rounds.data(), ar.at<uint64_t>(off_rounds), rounds.size() * 8, cudaMemcpyDeviceToHost, s));
+        TG_CUDA(cudaMemcpyAsync(chal.data(), ar.at<uint64_t>(off_chal), chal.size() * 8, cudaMemcpyDeviceToHost, s));
+        TG_CUDA(cudaMemcpyAsync(fevals.data(), ar.at<uint64_t>(off_evals), finals.size() * 16, cudaMemcpyDeviceToHost, s));
+        TG_CUDA(cudaStreamSynchronize(s));
     }
-
-    // the batched level sumcheck (γ and λ already drawn; the evaluations absorbed below)
-    std::vector<uint64_t> rounds((size_t)std::max(n_max, 1) * 6), chal((size_t)std::max(n_max, 1) * 2),
-        fevals(insts.size() * 4);
-    tg_sumcheck_job jb;
-    memset(&jb, 0, sizeof jb);
-    jb.transcript = t;
-    jb.prefix = prefix.c_str();
-    jb.degree = 3;
-    jb.instances = insts.data();
-    jb.ninstances = (int)insts.size();
-    jb.gamma[0] = gamma.c0;
-    jb.gamma[1] = gamma.c1;
-    jb.rounds = rounds.data();
-    jb.challenges = chal.data();
-    jb.final_evals = fevals.data();
-    ScOptions opts;
-    opts.weights = &weights;
-    opts.absorb_evals = false;
-    rc = prove_many_opts(d, &jb, 1, 1, opts);
-    if (rc) return bail(rc);
-
-    // the evaluations: (L, R) per forest, (N0, N1, D0, D1) per fraction tree
+    if (fs1.err) return bail(fail(TG_ERR_STATE, "a level challenge found no canonical Fp2 in %d squeezes", FS_MAX_TRIES));
+    memcpy(t->state, fs1.state, 32);
+    t->counter = fs1.counter;
     std::vector<fp2> evals;
-    auto fe = [&](size_t inst, int which) { return fp2{fevals[4 * inst + 2 * which], fevals[4 * inst + 2 * which + 1]}; };
-    size_t ii = 0;
-    for (int k : present) {
-        if (st->trees[k].kind == 0) {
-            evals.push_back(fe(ii, 0));
-            evals.push_back(fe(ii, 1));
-            ii += 1;
-        } else {
-            evals.push_back(fe(ii, 0));      // N0 (instance 0: eq, n0, d1)
-            evals.push_back(fe(ii + 1, 0));  // N1 (instance 1: eq, n1, d0)
-            evals.push_back(fe(ii + 1, 1));  // D0
-            evals.push_back(fe(ii, 1));      // D1
-            ii += 3;
-        }
-    }
+    for (size_t i = 0; i < finals.size(); i++) evals.push_back({fevals[2 * i], fevals[2 * i + 1]});
     std::vector<uint64_t> ew(2 * evals.size());
     for (size_t i = 0; i < evals.size(); i++) {
         ew[2 * i] = evals[i].c0;
