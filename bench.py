@@ -613,6 +613,79 @@ def run_logup(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_cc(args) -> None:
+    """The reference benchmark's c_c measurement shape: rows of k = 2^cc_log_k values with P mask
+    coefficients, generated on the device 32 rows at a time, encoded at rate 1/2 and absorbed into
+    the 2k column chains (B = 32); the cost per committed element is (generate + encode + hash −
+    generate) ÷ rows·k, as the reference reports it."""
+    import ctypes
+
+    import torch
+
+    from tessera_gb300 import _native as N
+    from tessera_gb300.device import Device
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    cuda = f"cuda:{local}"
+    dev = Device(local)
+    lgk, lgr, P_, B = args.cc_log_k, 1, args.cc_masks, ROW_BLOCK
+    k, n = 1 << lgk, 1 << (lgk + lgr)
+    blocks = args.cc_rows // B
+    rows = torch.empty(B * k, dtype=torch.int64, device=cuda)
+    masks = torch.empty(max(B * P_, 1), dtype=torch.int64, device=cuda)
+    cw = torch.empty(B * n, dtype=torch.int64, device=cuda)
+    chains = torch.empty(n * 32, dtype=torch.uint8, device=cuda)
+    cid = (ctypes.c_uint8 * 32)(*([0x65] * 32))
+    torch.cuda.synchronize()
+    v = ctypes.c_void_p
+    stream = torch.cuda.ExternalStream(dev.stream_ptr(), device=cuda)
+
+    def generate(b):
+        N.call("tg_fill_splitmix", dev.handle, v(rows.data_ptr()), B * k, SEED_CC + b, None)
+        if P_:
+            N.call("tg_fill_splitmix", dev.handle, v(masks.data_ptr()), B * P_, SEED_CC ^ (0x6D61736B << 16) ^ b, None)
+
+    def run(encode):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        if encode:
+            N.call("tg_column_init_dev", dev.handle, cid, n, v(chains.data_ptr()), None)
+        for b in range(blocks):
+            generate(b)
+            if encode:
+                N.call("tg_encode_rows_dev", dev.handle, lgk, lgr, P_, v(rows.data_ptr()), B,
+                       v(masks.data_ptr()) if P_ else None, v(cw.data_ptr()), None)
+                N.call("tg_column_absorb_dev", dev.handle, v(chains.data_ptr()), n, v(cw.data_ptr()), B, B, None)
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3
+
+    for _ in range(args.warmup):
+        run(True)
+    full = [run(True) for _ in range(args.steps)]
+    gen = [run(False) for _ in range(args.steps)]
+    elems = blocks * B * k
+    ps_full, ps_gen = statistics.median(full) / elems * 1e12, statistics.median(gen) / elems * 1e12
+    dev.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": "c_c: ps per committed element (encode at rate 1/2 with masks + BLAKE3 column chains)",
+        "value": ps_full - ps_gen, "unit": "ps/element", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)",
+        "data": "synthetic (SplitMix64 rows and masks generated on the device, 32 rows at a time)",
+        "config": {"workload": f"{blocks * B} rows of k = 2^{lgk}, P = {P_} masks, rate 1/2, B = {B}",
+                   "timing": "CUDA events over all blocks, median over steps"},
+        "generate_encode_hash_ps": ps_full, "generate_ps": ps_gen,
+        "reference_h100_ps": 134.8,
+    }
+    print(json.dumps(line), flush=True)
+
+
+SEED_CC = 0x00650007
+
+
 SEED_SERVE = 0x00650005
 
 
@@ -622,11 +695,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["large", "batched", "serve", "logup"], default="large",
+    ap.add_argument("--workload", choices=["large", "batched", "serve", "logup", "cc"], default="large",
                     help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain; "
                          "serve: the proof server against one-at-a-time proofs")
     ap.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
     ap.add_argument("--lookups-log", type=int, default=26, help="logup: log2 of the lookups")
+    ap.add_argument("--cc-log-k", type=int, default=22, help="cc: log2 of the row length")
+    ap.add_argument("--cc-masks", type=int, default=200, help="cc: mask coefficients per row")
+    ap.add_argument("--cc-rows", type=int, default=4096, help="cc: rows committed per run")
     ap.add_argument("--rows-log", type=int, default=20, help="logup: log2 of the table rows")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: mean Poisson arrivals per second")
     ap.add_argument("--slots", type=int, default=8, help="serve: requests in flight at most")
@@ -652,6 +728,8 @@ def main():
         run_serve(args)
     elif args.workload == "logup":
         run_logup(args)
+    elif args.workload == "cc":
+        run_cc(args)
     else:
         run_gpu(args)
 

@@ -342,13 +342,18 @@ static int fast_pass(int which, int lg, dim3 grid, const fast::Args& a, cudaStre
         TG_FAST_CASE(8, 16, 16)
         TG_FAST_CASE(9, 32, 16)
         TG_FAST_CASE(10, 32, 32)
+        TG_FAST_CASE(11, 64, 32)
         default:
             return fail(TG_ERR_INVALID, "no register-resident transform of length 2^%d", lg);
     }
 #undef TG_FAST_CASE
 }
 
-static bool fast_shape(uint32_t lgk) { return lgk >= 13 && lgk <= 20; }
+static bool fast_shape(uint32_t lgk) { return lgk >= 13 && lgk <= 22; }
+
+// Words of one CTA's tile for a column length 2^lg: 8,192 (32 elements per thread) up to 2^10,
+// 16,384 for columns of 2^11 (64 per thread).
+static uint64_t fast_tile(int lg) { return lg <= 10 ? 8192 : 16384; }
 
 // Encodes rows in groups through the three register-resident passes; y/z hold `group` rows.
 static int fast_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_t* rows, size_t npolys,
@@ -378,7 +383,7 @@ static int fast_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const
         a.sstep[e] = mul(pow(7, m), pow(w_n, ((uint64_t)e * m) & ((1ull << lgn) - 1)));
         we = mul(we, w_r);
     }
-    const size_t tiles = k / fast::TILE;
+    const size_t tiles_k2 = k / fast_tile(a.lgk2), tiles_k1 = k / fast_tile(a.lgk1);
     group = std::min<size_t>(std::max<size_t>(group, 1), 65535);
     for (size_t r0 = 0; r0 < npolys; r0 += group) {
         const unsigned g = (unsigned)std::min(group, npolys - r0);
@@ -388,12 +393,12 @@ static int fast_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const
         int rc;
         {
             Launch L(d, s, "lde_pass_a", 1, g);
-            rc = fast_pass(0, a.lgk2, dim3((unsigned)tiles, g), a, s);
+            rc = fast_pass(0, a.lgk2, dim3((unsigned)tiles_k2, g), a, s);
         }
         if (rc) return rc;
         {
             Launch L(d, s, "lde_pass_m1", 1, g);
-            rc = fast_pass(1, a.lgk1, dim3((unsigned)tiles, g), a, s);
+            rc = fast_pass(1, a.lgk1, dim3((unsigned)tiles_k1, g), a, s);
         }
         if (rc) return rc;
         if (P_ > 0 && masks) {
@@ -403,12 +408,12 @@ static int fast_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const
         }
         {
             Launch L(d, s, "lde_pass_m2", 1, g);
-            rc = fast_pass(2, a.lgk1, dim3((unsigned)(tiles << lgr), g), a, s);
+            rc = fast_pass(2, a.lgk1, dim3((unsigned)(tiles_k1 << lgr), g), a, s);
         }
         if (rc) return rc;
         {
             Launch L(d, s, "lde_pass_c", 1, g);
-            rc = fast_pass(3, a.lgk2, dim3((unsigned)(tiles << lgr), g), a, s);
+            rc = fast_pass(3, a.lgk2, dim3((unsigned)(tiles_k2 << lgr), g), a, s);
         }
         if (rc) return rc;
     }

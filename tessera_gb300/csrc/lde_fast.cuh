@@ -159,11 +159,14 @@ __device__ __forceinline__ uint64_t rootp(const uint64_t* pw, int lgn, int lg, u
 template <int RA, int RB>
 struct Shape {
     static constexpr int L = RA * RB;
-    static constexpr int T = L / 32;    // threads per column
-    static constexpr int W = TILE / L;  // columns per CTA
-    static constexpr int NA = RA / T;   // round-1 sub-transforms per thread (length RB)
-    static constexpr int NB = RB / T;   // round-2 sub-transforms per thread (length RA)
-    static_assert(L >= 32 && L <= 1024 && NA >= 1 && NB >= 1, "column length");
+    static constexpr int E = L > 1024 ? 64 : 32;  // elements per thread: 64 for columns of 2048
+    static constexpr int T = L / E;               // threads per column
+    static constexpr int W = THREADS / T;         // columns per CTA
+    static constexpr int TILE_WORDS = W * L;      // 8,192 (32 KiB... 64 KiB) or 16,384 for E = 64
+    static constexpr int MINB = E == 64 ? 1 : 2;  // CTAs per SM the registers allow
+    static constexpr int NA = RA / T;             // round-1 sub-transforms per thread (length RB)
+    static constexpr int NB = RB / T;             // round-2 sub-transforms per thread (length RA)
+    static_assert(L >= 32 && L <= 2048 && NA >= 1 && NB >= 1 && NA * RB == E && NB * RA == E, "column length");
     static_assert(W >= 8, "at least 8 columns per tile");
     // Exchange slots. With W ≥ 16 columns a row of the tile spans every bank and the column is
     // XORed with ta: a warp along a column (fixed c, 32 ta) and a warp across columns both hit
@@ -192,24 +195,28 @@ __device__ __forceinline__ void fill_inner(uint64_t* tw, const uint64_t* pw, int
 // A tile whose columns are adjacent words, copied cooperatively into shared memory as rows of W
 // words (element t of column c at sm[t·W + c]) with 16-byte loads, then read by each thread in its
 // round-1 pattern: fewer live addresses than loading every strided element into registers.
-template <int RA, int RB, bool STREAM>
-__device__ __forceinline__ void load_staged(uint64_t (&v)[32], uint64_t* sm, const uint64_t* src, size_t es, int c,
+template <int RA, int RB, bool STREAM, int N>
+__device__ __forceinline__ void load_staged(uint64_t (&v)[N], uint64_t* sm, const uint64_t* src, size_t es, int c,
                                             int q) {
     using S = Shape<RA, RB>;
     constexpr int VPR = S::W / 2;                    // 16-byte vectors per row
-    constexpr int ITERS = S::L * VPR / THREADS;      // vectors per thread, all in flight at once
-    static_assert(S::L * VPR % THREADS == 0, "whole vectors per thread");
-    ulonglong2 x[ITERS];
-    static_for<ITERS>([&](auto it_) {
-        constexpr int it = decltype(it_)::value;
-        const int i = threadIdx.x + it * THREADS;
-        const uint64_t* g = src + (size_t)(i / VPR) * es + 2 * (i % VPR);
-        x[it] = STREAM ? ld_stream(g) : *reinterpret_cast<const ulonglong2*>(g);
-    });
-    static_for<ITERS>([&](auto it_) {
-        constexpr int it = decltype(it_)::value;
-        const int i = threadIdx.x + it * THREADS;
-        *reinterpret_cast<ulonglong2*>(sm + (i / VPR) * S::W + 2 * (i % VPR)) = x[it];
+    constexpr int ITERS = S::L * VPR / THREADS;      // vectors per thread
+    constexpr int BATCH = ITERS > 16 ? 16 : ITERS;   // in flight at once
+    static_assert(S::L * VPR % THREADS == 0 && ITERS % BATCH == 0, "whole vectors per thread");
+    static_for<ITERS / BATCH>([&](auto b_) {
+        constexpr int b = decltype(b_)::value;
+        ulonglong2 x[BATCH];
+        static_for<BATCH>([&](auto it_) {
+            constexpr int it = decltype(it_)::value;
+            const int i = threadIdx.x + (b * BATCH + it) * THREADS;
+            const uint64_t* g = src + (size_t)(i / VPR) * es + 2 * (i % VPR);
+            x[it] = STREAM ? ld_stream(g) : *reinterpret_cast<const ulonglong2*>(g);
+        });
+        static_for<BATCH>([&](auto it_) {
+            constexpr int it = decltype(it_)::value;
+            const int i = threadIdx.x + (b * BATCH + it) * THREADS;
+            *reinterpret_cast<ulonglong2*>(sm + (i / VPR) * S::W + 2 * (i % VPR)) = x[it];
+        });
     });
     __syncthreads();
     static_for<S::NA>([&](auto i_) {
@@ -225,23 +232,27 @@ __device__ __forceinline__ void load_staged(uint64_t (&v)[32], uint64_t* sm, con
 
 // A tile of W columns whose elements are adjacent (column c at src + c·cs), copied into shared
 // memory as sm[c·L + t] with 16-byte loads, then read by each thread in its round-1 pattern.
-template <int RA, int RB>
-__device__ __forceinline__ void load_staged_q(uint64_t (&v)[32], uint64_t* sm, const uint64_t* src, size_t cs, int c,
+template <int RA, int RB, int N>
+__device__ __forceinline__ void load_staged_q(uint64_t (&v)[N], uint64_t* sm, const uint64_t* src, size_t cs, int c,
                                               int q) {
     using S = Shape<RA, RB>;
     constexpr int VPC = S::L / 2;                    // 16-byte vectors per column
-    constexpr int ITERS = S::W * VPC / THREADS;      // vectors per thread, all in flight at once
-    static_assert(S::W * VPC % THREADS == 0, "whole vectors per thread");
-    ulonglong2 x[ITERS];
-    static_for<ITERS>([&](auto it_) {
-        constexpr int it = decltype(it_)::value;
-        const int i = threadIdx.x + it * THREADS;
-        x[it] = *reinterpret_cast<const ulonglong2*>(src + (size_t)(i / VPC) * cs + 2 * (i % VPC));
-    });
-    static_for<ITERS>([&](auto it_) {
-        constexpr int it = decltype(it_)::value;
-        const int i = threadIdx.x + it * THREADS;
-        *reinterpret_cast<ulonglong2*>(sm + (i / VPC) * S::L + 2 * (i % VPC)) = x[it];
+    constexpr int ITERS = S::W * VPC / THREADS;      // vectors per thread
+    constexpr int BATCH = ITERS > 16 ? 16 : ITERS;   // in flight at once
+    static_assert(S::W * VPC % THREADS == 0 && ITERS % BATCH == 0, "whole vectors per thread");
+    static_for<ITERS / BATCH>([&](auto b_) {
+        constexpr int b = decltype(b_)::value;
+        ulonglong2 x[BATCH];
+        static_for<BATCH>([&](auto it_) {
+            constexpr int it = decltype(it_)::value;
+            const int i = threadIdx.x + (b * BATCH + it) * THREADS;
+            x[it] = *reinterpret_cast<const ulonglong2*>(src + (size_t)(i / VPC) * cs + 2 * (i % VPC));
+        });
+        static_for<BATCH>([&](auto it_) {
+            constexpr int it = decltype(it_)::value;
+            const int i = threadIdx.x + (b * BATCH + it) * THREADS;
+            *reinterpret_cast<ulonglong2*>(sm + (i / VPC) * S::L + 2 * (i % VPC)) = x[it];
+        });
     });
     __syncthreads();
     static_for<S::NA>([&](auto i_) {
@@ -256,8 +267,8 @@ __device__ __forceinline__ void load_staged_q(uint64_t (&v)[32], uint64_t* sm, c
 }
 
 // Round-1 loads. q-fast: column c starts at src + c·cs and its elements are adjacent.
-template <int RA, int RB>
-__device__ __forceinline__ void load_qfast(uint64_t (&v)[32], const uint64_t* src, size_t cs, int c, int q) {
+template <int RA, int RB, int N>
+__device__ __forceinline__ void load_qfast(uint64_t (&v)[N], const uint64_t* src, size_t cs, int c, int q) {
     using S = Shape<RA, RB>;
     const uint64_t* col = src + (size_t)c * cs;
     static_for<S::NA>([&](auto i_) {
@@ -271,8 +282,8 @@ __device__ __forceinline__ void load_qfast(uint64_t (&v)[32], const uint64_t* sr
 }
 
 // Round 1: DIF of length RB on each loaded sub-transform, inner twiddle, park in shared memory.
-template <int RA, int RB, bool INV>
-__device__ __forceinline__ void round1_store(uint64_t (&v)[32], uint64_t* sm, const uint64_t* tw, int c, int q) {
+template <int RA, int RB, bool INV, int N>
+__device__ __forceinline__ void round1_store(uint64_t (&v)[N], uint64_t* sm, const uint64_t* tw, int c, int q) {
     using S = Shape<RA, RB>;
     static_for<S::NA>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
@@ -289,8 +300,8 @@ __device__ __forceinline__ void round1_store(uint64_t (&v)[32], uint64_t* sm, co
 
 // Round 2 (c-fast): v[i·RA + ta] = Y[ta][kb_i], kb_i = q + T·i, then DIF of length RA:
 // v[i·RA + p] holds output kb_i + RB·rev(p).
-template <int RA, int RB, bool INV>
-__device__ __forceinline__ void round2(uint64_t (&v)[32], const uint64_t* sm, int c, int q) {
+template <int RA, int RB, bool INV, int N>
+__device__ __forceinline__ void round2(uint64_t (&v)[N], const uint64_t* sm, int c, int q) {
     using S = Shape<RA, RB>;
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
@@ -305,7 +316,7 @@ __device__ __forceinline__ void round2(uint64_t (&v)[32], const uint64_t* sm, in
 
 // ---- pass A ------------------------------------------------------------------------------------
 template <int RA, int RB>
-__global__ void __launch_bounds__(THREADS, 2) pass_a(Args a) {
+__global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_a(Args a) {
     using S = Shape<RA, RB>;
     extern __shared__ uint64_t sm[];
     uint64_t* tw = sm + S::WORDS;
@@ -323,7 +334,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_a(Args a) {
         constexpr int i = decltype(i_)::value;
         t0[i] = rootp(a.pw, lgn, a.lgk, (uint64_t)(q + S::T * i) * t1, true);
     });
-    uint64_t v[32];
+    uint64_t v[S::E];
     load_staged<RA, RB, true>(v, sm, a.rows + (row << a.lgk) + t1_0, K1, c, q);  // its syncs cover the twiddles
     round1_store<RA, RB, true>(v, sm, tw, c, q);
     __syncthreads();
@@ -344,7 +355,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_a(Args a) {
 
 // ---- pass M1 -----------------------------------------------------------------------------------
 template <int RA, int RB>
-__global__ void __launch_bounds__(THREADS, 2) pass_m1(Args a) {
+__global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_m1(Args a) {
     using S = Shape<RA, RB>;
     extern __shared__ uint64_t sm[];
     uint64_t* tw = sm + S::WORDS;
@@ -364,7 +375,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m1(Args a) {
         p7[i] = a.pow7k[idx0];
         w1[i] = a.pw[idx0];
     });
-    uint64_t v[32];
+    uint64_t v[S::E];
     {
         const int qq = threadIdx.x % S::T, cc = threadIdx.x / S::T;  // q-fast: a column's t1 are adjacent
         load_staged_q<RA, RB>(v, sm, a.y + (row << a.lgk) + ((size_t)j2_0 << a.lgk1), S::L, cc, qq);
@@ -416,7 +427,7 @@ static __global__ void mask_fixup(Args a) {
 
 // ---- pass M2 -----------------------------------------------------------------------------------
 template <int RA, int RB>
-__global__ void __launch_bounds__(THREADS, 2) pass_m2(Args a) {
+__global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_m2(Args a) {
     using S = Shape<RA, RB>;
     extern __shared__ uint64_t sm[];
     uint64_t* tw = sm + S::WORDS;
@@ -437,7 +448,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m2(Args a) {
         constexpr int i = decltype(i_)::value;
         t0[i] = rootp(a.pw, lgn, a.lgk, (uint64_t)(q + S::T * i) * j2, false);
     });
-    uint64_t v[32];
+    uint64_t v[S::E];
     load_staged<RA, RB, false>(v, sm, z, K2, c, q);  // every load of this tile is done before any store below
     round1_store<RA, RB, false>(v, sm, tw, c, q);
     __syncthreads();
@@ -457,7 +468,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_m2(Args a) {
 
 // ---- pass C ------------------------------------------------------------------------------------
 template <int RA, int RB>
-__global__ void __launch_bounds__(THREADS, 2) pass_c(Args a) {
+__global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_c(Args a) {
     using S = Shape<RA, RB>;
     extern __shared__ uint64_t sm[];
     uint64_t* tw = sm + S::WORDS;
@@ -468,7 +479,7 @@ __global__ void __launch_bounds__(THREADS, 2) pass_c(Args a) {
     const int col0 = blockIdx.x * S::W;  // columns are (v2, e) pairs, e fastest
     const int K1 = 1 << a.lgk1;
     const uint64_t* z = a.z + (row << lgn);
-    uint64_t v[32];
+    uint64_t v[S::E];
     {
         const int q = threadIdx.x % S::T, c = threadIdx.x / S::T;  // q-fast
         const int colid = col0 + c;

@@ -68,6 +68,7 @@ def test_encode_matches_oracle(dev, log_k, log_r):
 
 
 @pytest.mark.parametrize("log_k,log_r,nrows,P", [(20, 1, 2, 0), (20, 1, 1, 200), (21, 1, 1, 0), (22, 1, 1, 200),
+                                                 (21, 2, 2, 7), (22, 3, 1, 0), (22, 1, 3, 1),
                                                  (18, 2, 2, 0), (23, 1, 1, 0), (24, 1, 1, 5)])
 def test_encode_large_matches_oracle(dev, log_k, log_r, nrows, P):
     from tessera_gb300.pcs import RowEncoder
