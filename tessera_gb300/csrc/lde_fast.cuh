@@ -96,8 +96,43 @@ __device__ __forceinline__ void bf_ct(uint64_t& a, uint64_t& b) {
 
 // Length-R transform of x[BASE + i], i < R, with root ω_R^{±1}: natural order in, bit-reversed
 // order out (position p holds X[rev(p)]).
+// Swaps x[BASE .. BASE + H) with x[BASE + H .. BASE + 2H) (register moves).
+template <int H, int BASE, int N>
+__device__ __forceinline__ void swap_halves(uint64_t (&x)[N]) {
+    static_for<H>([&](auto t_) {
+        constexpr int t = decltype(t_)::value;
+        const uint64_t y = x[BASE + t];
+        x[BASE + t] = x[BASE + H + t];
+        x[BASE + H + t] = y;
+    });
+}
+
+template <int R, bool INV, int BASE, int N>
+__device__ __forceinline__ void dft_dif(uint64_t (&x)[N]);
+
+// Length 64 as its first stage and then the two independent length-32 halves (a DIF's later
+// stages never cross the halves, and their twiddles ω_64^{2m} are ω_32^m), the halves run by one
+// copy of the length-32 code in a rolled loop that swaps them: half the instruction footprint of
+// the unrolled transform, which otherwise misses the instruction cache.
+template <bool INV, int BASE, int N>
+__device__ __forceinline__ void dft_dif64(uint64_t (&x)[N]) {
+    static_for<32>([&](auto b_) {
+        constexpr int b = decltype(b_)::value;
+        bf_gs<tw_exp(64, b, INV)>(x[BASE + b], x[BASE + b + 32]);
+    });
+#pragma unroll 1
+    for (int h = 0; h < 2; h++) {
+        dft_dif<32, INV, BASE>(x);
+        swap_halves<32, BASE>(x);
+    }
+}
+
 template <int R, bool INV, int BASE, int N>
 __device__ __forceinline__ void dft_dif(uint64_t (&x)[N]) {
+    if constexpr (R == 64) {
+        dft_dif64<INV, BASE>(x);
+        return;
+    }
     static_for<ilog2(R)>([&](auto s_) {
         constexpr int s = decltype(s_)::value;
         constexpr int h = R >> (s + 1);
@@ -285,17 +320,33 @@ __device__ __forceinline__ void load_qfast(uint64_t (&v)[N], const uint64_t* src
 template <int RA, int RB, bool INV, int N>
 __device__ __forceinline__ void round1_store(uint64_t (&v)[N], uint64_t* sm, const uint64_t* tw, int c, int q) {
     using S = Shape<RA, RB>;
-    static_for<S::NA>([&](auto i_) {
-        constexpr int i = decltype(i_)::value;
-        dft_dif<RB, INV, i * RB>(v);
-        const int ta = q + S::T * i;
-        static_for<RB>([&](auto p_) {
-            constexpr int p = decltype(p_)::value;
-            constexpr int kb = brev_c(p, ilog2(RB));
-            const uint64_t val = kb == 0 ? v[i * RB + p] : lz::mul(v[i * RB + p], tw[kb * RA + ta]);
-            sm[S::slot(c, ta, kb)] = val;
+    if constexpr (S::NA == 2) {
+        // two sub-transforms: one copy of the code in a rolled loop, the second half swapped in
+#pragma unroll 1
+        for (int i = 0; i < 2; i++) {
+            dft_dif<RB, INV, 0>(v);
+            const int ta = q + S::T * i;
+            static_for<RB>([&](auto p_) {
+                constexpr int p = decltype(p_)::value;
+                constexpr int kb = brev_c(p, ilog2(RB));
+                const uint64_t val = kb == 0 ? v[p] : lz::mul(v[p], tw[kb * RA + ta]);
+                sm[S::slot(c, ta, kb)] = val;
+            });
+            swap_halves<RB, 0>(v);
+        }
+    } else {
+        static_for<S::NA>([&](auto i_) {
+            constexpr int i = decltype(i_)::value;
+            dft_dif<RB, INV, i * RB>(v);
+            const int ta = q + S::T * i;
+            static_for<RB>([&](auto p_) {
+                constexpr int p = decltype(p_)::value;
+                constexpr int kb = brev_c(p, ilog2(RB));
+                const uint64_t val = kb == 0 ? v[i * RB + p] : lz::mul(v[i * RB + p], tw[kb * RA + ta]);
+                sm[S::slot(c, ta, kb)] = val;
+            });
         });
-    });
+    }
 }
 
 // Round 2 (c-fast): v[i·RA + ta] = Y[ta][kb_i], kb_i = q + T·i, then DIF of length RA:
