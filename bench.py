@@ -683,6 +683,61 @@ def run_cc(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+def run_forest(args) -> None:
+    """The reference benchmark's c_π measurement shape: one forest of 2^s product trees of 2^h
+    leaves (Fp2 leaves generated on the device), its levels built bottom-up and its h degree-3
+    level sumchecks proven on a transcript (root challenges, γ, rounds, evals, ρ per level); the
+    cost per leaf is the whole proof's time over 2^(s+h)."""
+    import torch
+
+    from tessera_gb300.device import Device
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.trees import Forest, LeafStage
+
+    world, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = Device(local)
+    ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([0x65]) * 32, bytes([0x65]) * 16)
+    s_, h_ = args.forest_trees_log, args.forest_leaves_log
+    leaves = torch.empty(2 << (s_ + h_), dtype=torch.int64, device=f"cuda:{local}")
+
+    def one(s, h):
+        from tessera_gb300.workloads import fill_device
+
+        lv = leaves[: 2 << (s + h)]
+        fill_device(lv, SEED_CC ^ 0x666F72, dev)
+        torch.cuda.synchronize()
+        start = time.perf_counter()
+        t = Transcript(ctx)
+        with LeafStage([Forest(s, lv)], dev) as st:
+            st.prove(t)
+        torch.cuda.synchronize()
+        return time.perf_counter() - start
+
+    for _ in range(args.warmup):
+        one(min(s_, 8), min(h_, 10))
+    dev.profile(True)
+    times = [one(s_, h_) for _ in range(args.steps)]
+    dev.profile(False)
+    prof = dev.profile_read()
+    kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps} for k, v in prof.items()}
+    med = statistics.median(times)
+    del leaves
+    dev.close()
+    if rank != 0:
+        return
+    line = {
+        "metric": "c_pi: ps per product-forest leaf (level build + level sumchecks on a transcript)",
+        "value": med / (1 << (s_ + h_)) * 1e12, "unit": "ps/leaf", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u64 (Goldilocks Fp2)", "data": "synthetic (SplitMix64 Fp2 leaves generated on the device)",
+        "config": {"workload": f"one forest of 2^{s_} trees of 2^{h_} leaves",
+                   "timing": "host wall clock per proof (leaves already on the device), median over steps"},
+        "proof_ms": med * 1e3, "reference_h100_ps_per_leaf": 84.6, "kernels": kernels,
+    }
+    print(json.dumps(line), flush=True)
+
+
 SEED_CC = 0x00650007
 
 
@@ -695,12 +750,14 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
-    ap.add_argument("--workload", choices=["large", "batched", "serve", "logup", "cc"], default="large",
+    ap.add_argument("--workload", choices=["large", "batched", "serve", "logup", "cc", "forest"], default="large",
                     help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain; "
                          "serve: the proof server against one-at-a-time proofs")
     ap.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
     ap.add_argument("--lookups-log", type=int, default=26, help="logup: log2 of the lookups")
     ap.add_argument("--cc-log-k", type=int, default=22, help="cc: log2 of the row length")
+    ap.add_argument("--forest-trees-log", type=int, default=16, help="forest: log2 of the trees")
+    ap.add_argument("--forest-leaves-log", type=int, default=14, help="forest: log2 of each tree's leaves")
     ap.add_argument("--cc-masks", type=int, default=200, help="cc: mask coefficients per row")
     ap.add_argument("--cc-rows", type=int, default=4096, help="cc: rows committed per run")
     ap.add_argument("--rows-log", type=int, default=20, help="logup: log2 of the table rows")
@@ -730,6 +787,8 @@ def main():
         run_logup(args)
     elif args.workload == "cc":
         run_cc(args)
+    elif args.workload == "forest":
+        run_forest(args)
     else:
         run_gpu(args)
 
