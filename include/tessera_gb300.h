@@ -61,6 +61,10 @@ int tg_device_sync(tg_device *dev);
 int tg_device_stream(tg_device *dev, void **stream);
 /* Kernels launched through this handle so far (the library's own, counted at launch). */
 int tg_device_launches(tg_device *dev, uint64_t *launches);
+/* Returns the workspace memory that closed leaf stages left for reuse (levels and bound tables,
+ * pooled as the reference's ForestWorkspace is, crates/tessera-gpu/src/trees.rs:124-160) to the
+ * driver, zeroed first. tg_device_close does the same. */
+int tg_device_trim(tg_device *dev);
 
 /* Integer-pipe peaks of the device, measured with register-only microbenchmarks (no reference
  * counterpart: these are the denominators of the integer-bound kernels' rooflines). Rates per
@@ -79,6 +83,9 @@ int tg_measure_int_peaks(tg_device *dev, tg_int_peaks *out);
  * (i + 1)-th SplitMix64 output from `seed`, reduced once below p. Enqueued on `stream` (NULL:
  * the device's stream). */
 int tg_fill_splitmix(tg_device *dev, uint64_t *out, size_t n, uint64_t seed, void *stream);
+/* Replaces Device::fill_counter (crates/tessera-gpu/src/commit.rs:401-414): out[i] = counter(base + i),
+ * counter(c) the SplitMix64 output for state (c + 1)·0x9E3779B97F4A7C15 reduced once below p. */
+int tg_fill_counter(tg_device *dev, uint64_t *out, size_t n, uint64_t base, void *stream);
 /* Per-kernel timing (no counterpart in the reference; its GPU timing lives in benchmark
  * harnesses, crates/tessera-bench/examples/gpu_unit_costs.rs): while enabled, every launch is
  * bracketed by CUDA events on its own stream. tg_profile_read sums the elapsed times by kernel
@@ -289,17 +296,21 @@ int tg_level_free(tg_level *l);
  * reference's FractionTree, crates/tessera-sumcheck/src/trees.rs:260-345, prove_trees :761, and
  * LogUp's leaf stage, crates/tessera-logup/src/prover.rs:361). Trees are listed in schedule order.
  * kind 0: a forest of 2^s product trees of height `height` (a single tree: s = 0) from its
- * 2^(s+height) stacked leaves (Fp2); kind 1: a fraction tree (s = 0) from 2^height numerators
+ * 2^(s+height) stacked leaves (Fp2, or prime-field words with base_leaves, as the reference's GPU
+ * forest takes them, crates/tessera-gpu/src/trees.rs:163-185); kind 1: a fraction tree (s = 0) from 2^height numerators
  * (Fp2; NULL: all 1) and denominators (Fp2), entering the schedule with `sent` (n, d) when given
  * (as the roots message carried it), else its own root. Every level is built on the device when
  * the stage opens; each tg_leaf_stage_prove_level call proves the next level on the transcript,
- * byte for byte as the reference does, and moves every present tree's claim one level down. */
+ * byte for byte as the reference does, and moves every present tree's claim one level down.
+ * With on_device, the leaves are read in place (they must stay unchanged until the stage closes);
+ * the other levels and the bound tables come from the device's workspace cache. */
 typedef struct {
     int kind;
     uint32_t s, height;
     const uint64_t *leaves;        /* forest leaves, or fraction numerators */
     const uint64_t *denominators;  /* fraction trees */
     const uint64_t *sent;          /* fraction trees: 2 Fp2, or NULL */
+    uint32_t base_leaves;          /* forests: 1 when the leaves are prime-field words (one per leaf) */
 } tg_tree;
 typedef struct {
     int level;

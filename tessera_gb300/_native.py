@@ -69,7 +69,7 @@ class ServerStatsC(ctypes.Structure):
 
 class TreeC(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("s", ctypes.c_uint32), ("height", ctypes.c_uint32), ("leaves", ctypes.c_void_p),
-                ("denominators", ctypes.c_void_p), ("sent", ctypes.c_void_p)]
+                ("denominators", ctypes.c_void_p), ("sent", ctypes.c_void_p), ("base_leaves", ctypes.c_uint32)]
 
 
 class TreeLevelProofC(ctypes.Structure):
@@ -102,6 +102,8 @@ SIGNATURES = {
     "tg_device_launches": [V, V],
     "tg_measure_int_peaks": [V, V],
     "tg_fill_splitmix": [V, V, SZ, U64, V],
+    "tg_fill_counter": [V, V, SZ, U64, V],
+    "tg_device_trim": [V],
     "tg_device_stream": [V, V],
     "tg_profile_enable": [V, INT],
     "tg_profile_read": [V, V, SZ, V, V, V, SZ, V],

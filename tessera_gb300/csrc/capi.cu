@@ -51,9 +51,51 @@ int DevBuf::ensure(size_t want) {
 }
 
 void DevBuf::release() {
-    if (ptr) cudaFree(ptr);
+    if (ptr && owned) cudaFree(ptr);
     ptr = nullptr;
     bytes = 0;
+    owned = true;
+}
+
+int spare_take(Device* d, DevBuf& b, size_t want) {
+    if (want == 0) want = 16;
+    {
+        std::lock_guard<std::mutex> lock(d->spare_mu);
+        auto it = d->spare.lower_bound(want);
+        if (it != d->spare.end() && it->first / 2 <= want) {
+            b.release();
+            b.ptr = it->second;
+            b.bytes = it->first;
+            d->spare.erase(it);
+            return TG_OK;
+        }
+    }
+    if (b.ensure(want) == TG_OK) return TG_OK;
+    spare_trim(d);  // the cache gives way to a new allocation
+    return b.ensure(want);
+}
+
+void spare_give(Device* d, DevBuf& b) {
+    if (b.ptr && b.owned) {
+        std::lock_guard<std::mutex> lock(d->spare_mu);
+        d->spare.emplace(b.bytes, b.ptr);
+    }
+    b.ptr = nullptr;
+    b.bytes = 0;
+    b.owned = true;
+}
+
+void spare_trim(Device* d) {
+    std::multimap<size_t, void*> drop;
+    {
+        std::lock_guard<std::mutex> lock(d->spare_mu);
+        drop.swap(d->spare);
+    }
+    if (drop.empty()) return;
+    for (auto& kv : drop) cudaMemsetAsync(kv.second, 0, kv.first, d->stream);
+    cudaStreamSynchronize(d->stream);
+    for (auto& kv : drop) cudaFree(kv.second);
+    cudaGetLastError();
 }
 
 cudaStream_t pick_stream(Device* d, void* stream) { return stream ? (cudaStream_t)stream : d->stream; }
@@ -250,6 +292,7 @@ int tg_device_close(tg_device* dev) {
     }
     if (d->fork) cudaEventDestroy(d->fork);
     d->batch_roots.release();
+    spare_trim(d);
     d->scratch_y.release();
     d->scratch_z.release();
     d->scratch_misc.release();
@@ -324,6 +367,13 @@ int tg_device_launches(tg_device* dev, uint64_t* launches) {
     Device* d = reinterpret_cast<Device*>(dev);
     if (!d || !launches) return fail(TG_ERR_INVALID, "tg_device_launches: null argument");
     *launches = d->launches.load();
+    return TG_OK;
+}
+
+int tg_device_trim(tg_device* dev) {
+    Device* d = reinterpret_cast<Device*>(dev);
+    if (!d) return fail(TG_ERR_INVALID, "null device");
+    spare_trim(d);
     return TG_OK;
 }
 

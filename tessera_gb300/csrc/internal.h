@@ -30,6 +30,7 @@ int cuda_fail(cudaError_t e, const char* what);
 struct DevBuf {
     void* ptr = nullptr;
     size_t bytes = 0;
+    bool owned = true;  // false: a caller's memory, read in place and never freed here
     int ensure(size_t want);
     void release();
     ~DevBuf() { release(); }
@@ -86,11 +87,23 @@ struct Device {
     std::mutex prof_mu;
     std::vector<ProfRec> prof;
     std::vector<cudaEvent_t> event_pool;
+    // Workspace memory released by leaf stages (levels, bound tables), kept for the next stage as
+    // a prover pools its device memory: a stage takes the smallest spare buffer that fits before
+    // it allocates, and what the next stage's open leaves untaken goes back to the driver (zeroed).
+    std::mutex spare_mu;
+    std::multimap<size_t, void*> spare;
     // Returns the tables for (lgn, lgk), building them on first use.
     int get_tables(uint32_t lgn, uint32_t lgk, const Tables** out);
 };
 
 cudaStream_t pick_stream(Device* d, void* stream);
+
+// The workspace cache: b (empty) gets a spare buffer of at least `want` bytes (at most twice that)
+// or a new one; spare_give returns b's memory to the cache (a borrowed buffer is only dropped);
+// spare_trim zeroes and frees every spare buffer.
+int spare_take(Device* d, DevBuf& b, size_t want);
+void spare_give(Device* d, DevBuf& b);
+void spare_trim(Device* d);
 
 // Brackets the kernel launches of one logical kernel on stream s: counts them, and records
 // events around them while profiling is on.

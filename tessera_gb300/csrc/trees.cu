@@ -33,8 +33,7 @@
 
 namespace tg {
 
-constexpr int EQ_LOW = 10;  // variables of an eq table kept in shared memory per block
-
+// Level l from level l + 1: entry x is the product of entries 2x and 2x + 1, in Fp2.
 __global__ void tr_product_level(const ulonglong2* below, ulonglong2* above, uint64_t m) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < m; x += stride) {
@@ -44,69 +43,33 @@ __global__ void tr_product_level(const ulonglong2* below, ulonglong2* above, uin
     }
 }
 
+// The same in the prime field: a forest of prime-field leaves keeps every level there, one word
+// an entry (the pair is one 16-byte load).
+__global__ void tr_product_level_base(const ulonglong2* below, uint64_t* above, uint64_t m) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < m; x += stride) {
+        const ulonglong2 v = below[x];
+        above[x] = mul(v.x, v.y);
+    }
+}
+
+// (n, d) of level l from level l + 1; n null: every numerator below is 1, so n_out = d_L + d_R.
 __global__ void tr_fraction_level(const ulonglong2* n, const ulonglong2* d, ulonglong2* n_out, ulonglong2* d_out,
                                   uint64_t m) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < m; x += stride) {
-        const ulonglong2 nl = n[2 * x], nr = n[2 * x + 1], dl = d[2 * x], dr = d[2 * x + 1];
-        const fp2 a = {nl.x, nl.y}, b = {nr.x, nr.y}, c = {dl.x, dl.y}, e = {dr.x, dr.y};
-        const fp2 nn = e_add(e_mul(a, e), e_mul(b, c)), dd = e_mul(c, e);
+        const ulonglong2 dl = d[2 * x], dr = d[2 * x + 1];
+        const fp2 c = {dl.x, dl.y}, e = {dr.x, dr.y};
+        fp2 nn;
+        if (n) {
+            const ulonglong2 nl = n[2 * x], nr = n[2 * x + 1];
+            nn = e_add(e_mul(fp2{nl.x, nl.y}, e), e_mul(fp2{nr.x, nr.y}, c));
+        } else {
+            nn = e_add(c, e);
+        }
+        const fp2 dd = e_mul(c, e);
         n_out[x] = make_ulonglong2(nn.c0, nn.c1);
         d_out[x] = make_ulonglong2(dd.c0, dd.c1);
-    }
-}
-
-// even[x] = level[2x], odd[x] = level[2x + 1] for x < m.
-__global__ void tr_split(const ulonglong2* level, ulonglong2* even, ulonglong2* odd, uint64_t m) {
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < m; x += stride) {
-        even[x] = level[2 * x];
-        odd[x] = level[2 * x + 1];
-    }
-}
-
-// The high part of an eq table: hi[y] = Π_i (bit_i(y) ? r_i : 1 − r_i) over the point's
-// coordinates from EQ_LOW on (r holds those coordinates).
-__global__ void tr_eq_high(const ulonglong2* r, int nh, ulonglong2* hi) {
-    const uint64_t m = 1ull << nh;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t y = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; y < m; y += stride) {
-        fp2 p = {1, 0};
-        for (int i = 0; i < nh; i++) {
-            const fp2 ri = {r[i].x, r[i].y};
-            p = e_mul(p, (y >> i) & 1 ? ri : e_sub(fp2{1, 0}, ri));
-        }
-        hi[y] = make_ulonglong2(p.c0, p.c1);
-    }
-}
-
-// eq(r, x) for x < 2^n, x_1 the lowest bit: the low EQ_LOW coordinates' table is built in shared
-// memory by each block, and entry x is low[x mod 2^L]·hi[x >> L].
-__global__ void tr_eq(const ulonglong2* r, int nl, const ulonglong2* hi, ulonglong2* out, uint64_t total) {
-    __shared__ ulonglong2 low[1 << EQ_LOW];
-    if (threadIdx.x == 0) low[0] = make_ulonglong2(1, 0);
-    __syncthreads();
-    for (int i = 0; i < nl; i++) {  // doubling: low[x + 2^i] = low[x]·r_i, low[x] ·= (1 − r_i)
-        const fp2 ri = {r[i].x, r[i].y}, si = e_sub(fp2{1, 0}, ri);
-        const int half = 1 << i;
-        for (int x = threadIdx.x; x < half; x += blockDim.x) {
-            const fp2 v = {low[x].x, low[x].y};
-            const fp2 a = e_mul(v, si), b = e_mul(v, ri);
-            low[x] = make_ulonglong2(a.c0, a.c1);
-            low[x + half] = make_ulonglong2(b.c0, b.c1);
-        }
-        __syncthreads();
-    }
-    const uint64_t mask = (1ull << nl) - 1;
-    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
-    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < total; x += stride) {
-        const ulonglong2 a = low[x & mask];
-        fp2 v = {a.x, a.y};
-        if (hi) {
-            const ulonglong2 h = hi[x >> nl];
-            v = e_mul(v, fp2{h.x, h.y});
-        }
-        out[x] = make_ulonglong2(v.c0, v.c1);
     }
 }
 
@@ -146,6 +109,7 @@ static unsigned grid_of(const Device* d, uint64_t items) {
 struct TreeLevels {
     int kind = 0;  // 0 forest, 1 fraction
     uint32_t s = 0, h = 0;
+    bool base = false;  // a forest of prime-field leaves: every level one word an entry
     std::vector<std::unique_ptr<DevBuf>> n, d;  // level l, l = 0..h (fractions use both)
     fp2 sent_n = {0, 0}, sent_d = {0, 0};
     bool unit = false;      // a fraction tree whose leaf numerators are all 1
@@ -186,6 +150,15 @@ static int challenge2(tg_transcript* t, const std::string& label, fp2* out) {
     return TG_OK;
 }
 
+// 1/a in Fp2 as conj(a)/N(a), N(a) = a0^2 − 7·a1^2 (nonzero for a ≠ 0: 7 is no square mod p);
+// 0 for a = 0.
+static fp2 host_inv2(fp2 a) {
+    const uint64_t nrm = sub(mul(a.c0, a.c0), mul7(mul(a.c1, a.c1)));
+    if (nrm == 0) return {0, 0};
+    const uint64_t ni = inv(nrm);
+    return {mul(a.c0, ni), mul(sub(0, a.c1), ni)};
+}
+
 // ---- the level sumcheck, specialised for tree levels ----------------------------------------------
 //
 // A present tree on n variables proves Σ_x eq(p, x)·g(x) with g = L·R (forest) or
@@ -196,32 +169,38 @@ static int challenge2(tg_transcript* t, const std::string& label, fp2* out) {
 // weights eq(p_{>j}, x') = lo_j[x' mod 2^L]·hi_j[x' >> L] come from small per-round tables built
 // once per level from the point. Round 0 reads the level below directly (the halves are its even
 // and odd entries); each later round binds the previous challenge into the tables as it sums.
+//
+// q_j has degree 2, and the device sums only q_j(0) and its leading coefficient q_j(∞): the round's
+// claim gives q_j(1) = (Q_j − (1 − p_j)·q_j(0))/p_j with Q_j = claim_j/C_j, which is the tree's
+// claim in its first round and q_{j−1}(r_{j−1}) after, as the reference's CPU prover derives v(1)
+// from its claim (crates/tessera-sumcheck/src/level.rs:317-347). Where p_j = 0 nothing divides, and
+// that round's launch sums q_j(1) as well.
 
 constexpr int TL_THREADS = 256;
-constexpr int TL_LOW = 10;
+constexpr int TL_LOW = 11;  // the low eq table's variables: the pairs of one chunk share a high weight
 
 struct TlSeg {
-    const ulonglong2* src[4];  // table T's entry x is src[T][x·stride]
-    ulonglong2* dst[4];        // bound tables (when bind)
-    const ulonglong2* lo;      // this round's eq weights over the remaining variables
+    const void* src[4];  // table T's entry x is src[T][x·stride]: Fp2, or prime-field words when base
+    ulonglong2* dst[4];  // bound tables (when bind)
+    const ulonglong2* lo;  // this round's eq weights over the remaining variables
     const ulonglong2* hi;
-    const uint64_t* r;         // the challenge to bind
-    ulonglong2* out;           // q at the nodes 0, 1, 2, 3 (node 1 only in a tree's round 0)
-    uint64_t n;                // pairs
+    const uint64_t* r;     // the challenge to bind
+    ulonglong2* out;       // the round's sums: q(0), q(1) (launches that form it), q(∞)
+    uint64_t n;            // pairs: 2^lbits a chunk
     uint64_t lam[2];
     int kind, stride, bind, lbits;
-    int block0, nblocks, part0, pad_;
+    int block0, nblocks, part0, base;
 };
 static_assert(sizeof(TlSeg) % 8 == 0, "TlSeg copies as words");
 
 struct TlTree {  // one present tree, as the transcript kernel sees it
-    uint64_t w[2];   // γ^i
-    uint64_t C[2];   // the running eq scalar
-    uint64_t S[2];   // the tree's full sum, for its padding rounds
+    uint64_t w[2];  // γ^i
+    uint64_t C[2];  // the running eq scalar
+    uint64_t Q[2];  // the sum its current own round proves, over C
+    uint64_t S[2];  // its claim, which its padding rounds carry
     const uint64_t* point;  // n Fp2
-    const ulonglong2* lvl_n;  // the level below (a tree on no variable sums its two or four entries)
-    const ulonglong2* lvl_d;
-    int n, pad, kind, pad_;
+    const uint64_t* tinv;   // n Fp2: 1/point[j], or 0 where point[j] = 0
+    int n, pad;
 };
 
 __device__ __forceinline__ fp2 ld2(const ulonglong2* p) {
@@ -237,60 +216,115 @@ __device__ __forceinline__ fp2 l2_mul(fp2 a, fp2 b) {  // Karatsuba, X^2 = 7
     const uint64_t t2 = lz::mul(lz::add(a.c0, a.c1), lz::add(b.c0, b.c1));
     return {lz::add(t0, lz::sub(lz::mulp2<3>(t1), t1)), lz::sub(lz::sub(t2, t0), t1)};
 }
+__device__ __forceinline__ fp2 l2_scale(fp2 a, uint64_t b) { return {lz::mul(a.c0, b), lz::mul(a.c1, b)}; }
 __device__ __forceinline__ fp2 l2_canon(fp2 a) { return {lz::canon(a.c0), lz::canon(a.c1)}; }
 
-// Σ over the segment's pairs handled by this thread of w(x')·g(X, x') at the nodes X = 0, 1, 2, 3
-// (node 1 only without a bind); NT tables (2: L, R; 4: N0, N1, D0, D1).
-template <int NT, int KIND>
-__device__ __forceinline__ void tl_pairs(const TlSeg& g, uint64_t first, uint64_t stride, fp2 (&acc)[4]) {
-    const uint64_t mask = (1ull << g.lbits) - 1;
-    const fp2 r = g.bind ? fp2{g.r[0], g.r[1]} : fp2{0, 0};
-    const fp2 lam = {g.lam[0], g.lam[1]};
-    const int st = g.stride;
-    for (uint64_t p = first; p < g.n; p += stride) {
-        fp2 u[NT], d[NT];
-#pragma unroll
-        for (int k = 0; k < NT; k++) {
-            const ulonglong2* src = g.src[k];
-            if (g.bind) {
-                const fp2 a0 = ld2(src + (4 * p) * st), a1 = ld2(src + (4 * p + 1) * st);
-                const fp2 b0 = ld2(src + (4 * p + 2) * st), b1 = ld2(src + (4 * p + 3) * st);
-                const fp2 uu = l2_add(a0, l2_mul(r, l2_sub(a1, a0)));
-                const fp2 vv = l2_add(b0, l2_mul(r, l2_sub(b1, b0)));
-                g.dst[k][2 * p] = make_ulonglong2(uu.c0, uu.c1);
-                g.dst[k][2 * p + 1] = make_ulonglong2(vv.c0, vv.c1);
-                u[k] = uu;
-                d[k] = l2_sub(vv, uu);
-            } else {
-                u[k] = ld2(src + (2 * p) * st);
-                d[k] = l2_sub(ld2(src + (2 * p + 1) * st), u[k]);
-            }
-        }
-        const fp2 w = l2_mul(ld2(g.lo + (p & mask)), ld2(g.hi + (p >> g.lbits)));
-#pragma unroll
-        for (int node = 0; node < 4; node++) {
-            if (!(node == 1 && g.bind)) {
-                fp2 gx;
-                if constexpr (KIND == 0)  // L·R
-                    gx = l2_mul(u[0], u[1]);
-                else if constexpr (KIND == 1)  // N0·D1 + N1·D0 + λ·D0·D1
-                    gx = l2_add(l2_add(l2_mul(u[0], u[3]), l2_mul(u[1], u[2])), l2_mul(lam, l2_mul(u[2], u[3])));
-                else  // numerators of 1: D1 + D0 + λ·D0·D1 over the tables D0, D1
-                    gx = l2_add(l2_add(u[0], u[1]), l2_mul(lam, l2_mul(u[0], u[1])));
-                acc[node] = l2_add(acc[node], l2_mul(w, gx));
-            }
-            if (node < 3)
-#pragma unroll
-                for (int k = 0; k < NT; k++) u[k] = l2_add(u[k], d[k]);
+// g at X = 0, at X = 1 (ONE) and its leading coefficient in X, over one pair whose tables take the
+// values u at X = 0 and slopes d: KIND 0 L·R; 1 N0·D1 + N1·D0 + λ·D0·D1 = N0·D1 + D0·(N1 + λ·D1);
+// 2 D0 + D1 + λ·D0·D1, whose leading coefficient λ·dD0·dD1 is returned without the λ (the kernel
+// applies it once to the sum).
+template <int KIND, bool ONE>
+__device__ __forceinline__ void tl_nodes(const fp2* u, const fp2* d, fp2 lam, fp2& g0, fp2& g1, fp2& gi) {
+    if constexpr (KIND == 0) {
+        g0 = l2_mul(u[0], u[1]);
+        gi = l2_mul(d[0], d[1]);
+        if constexpr (ONE) g1 = l2_mul(l2_add(u[0], d[0]), l2_add(u[1], d[1]));
+    } else if constexpr (KIND == 1) {
+        auto f = [&](fp2 n0, fp2 n1, fp2 d0, fp2 d1) {
+            return l2_add(l2_mul(n0, d1), l2_mul(d0, l2_add(n1, l2_mul(lam, d1))));
+        };
+        g0 = f(u[0], u[1], u[2], u[3]);
+        gi = f(d[0], d[1], d[2], d[3]);
+        if constexpr (ONE)
+            g1 = f(l2_add(u[0], d[0]), l2_add(u[1], d[1]), l2_add(u[2], d[2]), l2_add(u[3], d[3]));
+    } else {
+        g0 = l2_add(l2_add(u[0], u[1]), l2_mul(lam, l2_mul(u[0], u[1])));
+        gi = l2_mul(d[0], d[1]);
+        if constexpr (ONE) {
+            const fp2 a = l2_add(u[0], d[0]), b = l2_add(u[1], d[1]);
+            g1 = l2_add(l2_add(a, b), l2_mul(lam, l2_mul(a, b)));
         }
     }
 }
 
+// This block's share of a segment: chunks c = b, b + nblocks, … of 2^lbits pairs, each summed with
+// its low weights and then scaled once by its high weight, into acc = (q(0), q(1), q(∞)). NT tables;
+// MODE 0 reads Fp2 tables (binding the previous challenge when bind), 1 binds prime-field tables
+// into Fp2 (a prime-field forest's round 1), 2 sums prime-field tables (its round 0).
+template <int NT, int KIND, int MODE, bool ONE>
+__device__ __forceinline__ void tl_sum(const TlSeg& g, uint64_t b, fp2 (&acc)[3]) {
+    const int lb = g.lbits;
+    const uint64_t span = 1ull << lb, chunks = g.n >> lb;
+    const fp2 r = g.bind ? fp2{g.r[0], g.r[1]} : fp2{0, 0};
+    const fp2 lam = {g.lam[0], g.lam[1]};
+    const uint64_t st = (uint64_t)g.stride;
+    for (uint64_t c = b; c < chunks; c += (uint64_t)g.nblocks) {
+        fp2 part[3] = {{0, 0}, {0, 0}, {0, 0}};
+#pragma unroll 2
+        for (uint64_t e = threadIdx.x; e < span; e += TL_THREADS) {
+            const uint64_t p = (c << lb) + e;
+            const fp2 w = ld2(g.lo + e);
+            if constexpr (MODE == 2) {
+                const uint64_t* L = static_cast<const uint64_t*>(g.src[0]);
+                const uint64_t* R = static_cast<const uint64_t*>(g.src[1]);
+                const uint64_t l0 = L[2 * p * st], l1 = L[(2 * p + 1) * st];
+                const uint64_t r0 = R[2 * p * st], r1 = R[(2 * p + 1) * st];
+                const uint64_t v0 = lz::mul(l0, r0), vi = lz::mul(lz::sub(l1, l0), lz::sub(r1, r0));
+                part[0] = l2_add(part[0], l2_scale(w, v0));
+                part[2] = l2_add(part[2], l2_scale(w, vi));
+                if constexpr (ONE) part[1] = l2_add(part[1], l2_scale(w, lz::mul(l1, r1)));
+            } else {
+                fp2 u[NT], d[NT];
+#pragma unroll
+                for (int k = 0; k < NT; k++) {
+                    if constexpr (MODE == 1) {
+                        const uint64_t* src = static_cast<const uint64_t*>(g.src[k]);
+                        const uint64_t a0 = src[(4 * p) * st], a1 = src[(4 * p + 1) * st];
+                        const uint64_t b0 = src[(4 * p + 2) * st], b1 = src[(4 * p + 3) * st];
+                        const uint64_t da = lz::sub(a1, a0), db = lz::sub(b1, b0);
+                        const fp2 uu = {lz::add(a0, lz::mul(r.c0, da)), lz::mul(r.c1, da)};
+                        const fp2 vv = {lz::add(b0, lz::mul(r.c0, db)), lz::mul(r.c1, db)};
+                        g.dst[k][2 * p] = make_ulonglong2(uu.c0, uu.c1);
+                        g.dst[k][2 * p + 1] = make_ulonglong2(vv.c0, vv.c1);
+                        u[k] = uu;
+                        d[k] = l2_sub(vv, uu);
+                    } else {
+                        const ulonglong2* src = static_cast<const ulonglong2*>(g.src[k]);
+                        if (g.bind) {
+                            const fp2 a0 = ld2(src + (4 * p) * st), a1 = ld2(src + (4 * p + 1) * st);
+                            const fp2 b0 = ld2(src + (4 * p + 2) * st), b1 = ld2(src + (4 * p + 3) * st);
+                            const fp2 uu = l2_add(a0, l2_mul(r, l2_sub(a1, a0)));
+                            const fp2 vv = l2_add(b0, l2_mul(r, l2_sub(b1, b0)));
+                            g.dst[k][2 * p] = make_ulonglong2(uu.c0, uu.c1);
+                            g.dst[k][2 * p + 1] = make_ulonglong2(vv.c0, vv.c1);
+                            u[k] = uu;
+                            d[k] = l2_sub(vv, uu);
+                        } else {
+                            u[k] = ld2(src + (2 * p) * st);
+                            d[k] = l2_sub(ld2(src + (2 * p + 1) * st), u[k]);
+                        }
+                    }
+                }
+                fp2 g0, g1, gi;
+                tl_nodes<KIND, ONE>(u, d, lam, g0, g1, gi);
+                part[0] = l2_add(part[0], l2_mul(w, g0));
+                part[2] = l2_add(part[2], l2_mul(w, gi));
+                if constexpr (ONE) part[1] = l2_add(part[1], l2_mul(w, g1));
+            }
+        }
+        const fp2 h = ld2(g.hi + c);
+        acc[0] = l2_add(acc[0], l2_mul(h, part[0]));
+        acc[2] = l2_add(acc[2], l2_mul(h, part[2]));
+        if constexpr (ONE) acc[1] = l2_add(acc[1], l2_mul(h, part[1]));
+    }
+}
+
+template <bool ONE>
 __global__ void __launch_bounds__(TL_THREADS, 2) tl_rounds(const TlSeg* segs, int nseg, uint64_t* partials,
                                                            unsigned* counters) {
     __shared__ TlSeg g;
     __shared__ int si;
-    __shared__ uint64_t red[TL_THREADS / 32][8];
+    __shared__ uint64_t red[TL_THREADS / 32][6];
     __shared__ bool last;
     if (threadIdx.x == 0) {
         int lo = 0, hi = nseg - 1;
@@ -310,40 +344,46 @@ __global__ void __launch_bounds__(TL_THREADS, 2) tl_rounds(const TlSeg* segs, in
         for (int w = threadIdx.x; w < (int)(sizeof(TlSeg) / 8); w += blockDim.x) to[w] = from[w];
     }
     __syncthreads();
-    fp2 acc[4] = {{0, 0}, {0, 0}, {0, 0}, {0, 0}};
-    const uint64_t first = (uint64_t)(blockIdx.x - g.block0) * blockDim.x + threadIdx.x;
-    const uint64_t stride = (uint64_t)g.nblocks * blockDim.x;
-    if (g.kind == 0)
-        tl_pairs<2, 0>(g, first, stride, acc);
-    else if (g.kind == 1)
-        tl_pairs<4, 1>(g, first, stride, acc);
-    else
-        tl_pairs<2, 2>(g, first, stride, acc);
+    fp2 acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+    const uint64_t b = (uint64_t)(blockIdx.x - g.block0);
+    if (g.kind == 0) {
+        if (!g.base)
+            tl_sum<2, 0, 0, ONE>(g, b, acc);
+        else if (g.bind)
+            tl_sum<2, 0, 1, ONE>(g, b, acc);
+        else
+            tl_sum<2, 0, 2, ONE>(g, b, acc);
+    } else if (g.kind == 1) {
+        tl_sum<4, 1, 0, ONE>(g, b, acc);
+    } else {
+        tl_sum<2, 2, 0, ONE>(g, b, acc);
+        acc[2] = l2_mul(fp2{g.lam[0], g.lam[1]}, acc[2]);
+    }
     // block sums, then the segment's last block reduces the partial rows
-    uint64_t words[8];
-    for (int i = 0; i < 4; i++) {
+    uint64_t words[6];
+    for (int i = 0; i < 3; i++) {
         const fp2 c = l2_canon(acc[i]);
         words[2 * i] = c.c0, words[2 * i + 1] = c.c1;
     }
 #pragma unroll
-    for (int w = 0; w < 8; w++)
+    for (int w = 0; w < 6; w++)
         for (int o = 16; o > 0; o >>= 1) words[w] = add(words[w], __shfl_down_sync(0xFFFFFFFFu, words[w], o));
     if ((threadIdx.x & 31) == 0)
-        for (int w = 0; w < 8; w++) red[threadIdx.x >> 5][w] = words[w];
+        for (int w = 0; w < 6; w++) red[threadIdx.x >> 5][w] = words[w];
     __syncthreads();
     if (threadIdx.x == 0) {
         for (int k = 1; k < (int)(blockDim.x >> 5); k++)
-            for (int w = 0; w < 8; w++) words[w] = add(words[w], red[k][w]);
-        for (int w = 0; w < 8; w++) partials[(size_t)(g.part0 + blockIdx.x - g.block0) * 8 + w] = words[w];
+            for (int w = 0; w < 6; w++) words[w] = add(words[w], red[k][w]);
+        for (int w = 0; w < 6; w++) partials[(size_t)(g.part0 + b) * 8 + w] = words[w];
         __threadfence();
         last = atomicAdd(&counters[si], 1u) == (unsigned)g.nblocks - 1;
     }
     __syncthreads();
     if (!last) return;
     __threadfence();
-    if (threadIdx.x < 8) {
+    if (threadIdx.x < 6) {
         uint64_t t = 0;
-        for (int b = 0; b < g.nblocks; b++) t = add(t, __ldcg(&partials[(size_t)(g.part0 + b) * 8 + threadIdx.x]));
+        for (int k = 0; k < g.nblocks; k++) t = add(t, __ldcg(&partials[(size_t)(g.part0 + k) * 8 + threadIdx.x]));
         reinterpret_cast<uint64_t*>(g.out)[threadIdx.x] = t;
     }
     if (threadIdx.x == 0) counters[si] = 0;
@@ -381,45 +421,45 @@ __device__ __forceinline__ fp2 eq1(fp2 t, fp2 x) {
     return e_add(e_mul(e_sub(one, t), e_sub(one, x)), e_mul(t, x));
 }
 
+// Own round jj's q(X) = a + b·X + c·X², from its sums q(0), q(∞) and q(1) = (Q − (1 − t)·q(0))/t
+// (t = point[jj]), or the summed q(1) where t = 0.
+__device__ void tl_quad(const TlTree& T, int jj, const ulonglong2* q, fp2& a, fp2& b, fp2& c) {
+    a = ld2(q);
+    c = ld2(q + 2);
+    const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]}, ti = {T.tinv[2 * jj], T.tinv[2 * jj + 1]};
+    fp2 q1;
+    if (ti.c0 == 0 && ti.c1 == 0)
+        q1 = ld2(q + 1);
+    else
+        q1 = e_mul(e_sub(fp2{T.Q[0], T.Q[1]}, e_mul(e_sub(fp2{1, 0}, t), a)), ti);
+    b = e_sub(e_sub(q1, a), c);
+}
+
 // Round j of a level: the message Σ_i γ^i·(2^{pad_i − j − 1}·S_i while padded, else
-// C_i·eq1(p_i[j'], X)·q_i(X)), absorbed under <prefix>/round/j; r_j drawn under <prefix>/r/j;
-// then each tree in its own rounds takes C_i ← C_i·eq1(p_i[j'], r_j). At j = 0 each padded tree's
-// S_i = Σ_{X∈{0,1}} eq1(p_i[0], X)·q_i(X) is taken from its round-0 sums first.
+// C_i·eq1(p_i[j'], X)·q_i(X)) at X = 0, 2, 3, absorbed under <prefix>/round/j; r_j drawn under
+// <prefix>/r/j; then each tree in its own rounds takes Q_i ← q_i(r_j) and C_i ← C_i·eq1(p_i[j'], r_j).
 __global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, int ntrees, const ulonglong2* q,
-                      fp2 lam, uint64_t* rounds_out, uint64_t* chal_out) {
+                      uint64_t* rounds_out, uint64_t* chal_out) {
     __shared__ uint32_t sbuf[FS_BUF_WORDS];
     const int lane = threadIdx.x & 31;
-    const fp2 X[3] = {{0, 0}, {2, 0}, {3, 0}};
     fp2 msg[3] = {{0, 0}, {0, 0}, {0, 0}};
     for (int i = 0; i < ntrees; i++) {  // every lane forms the message (the same reads)
-        TlTree& T = trees[i];
+        const TlTree& T = trees[i];
         const fp2 w = {T.w[0], T.w[1]};
-        fp2 S = {T.S[0], T.S[1]};
-        if (j == 0 && T.pad > 0) {
-            if (T.n == 0) {  // g at the level below's single entry
-                if (T.kind == 0)
-                    S = e_mul(ld2(T.lvl_n), ld2(T.lvl_n + 1));
-                else {
-                    const fp2 n0 = ld2(T.lvl_n), n1 = ld2(T.lvl_n + 1), d0 = ld2(T.lvl_d), d1 = ld2(T.lvl_d + 1);
-                    S = e_add(e_add(e_mul(n0, d1), e_mul(n1, d0)), e_mul(lam, e_mul(d0, d1)));
-                }
-            } else {
-                const fp2 t = {T.point[0], T.point[1]};
-                S = e_add(e_mul(eq1(t, fp2{0, 0}), ld2(q + 4 * i)), e_mul(eq1(t, fp2{1, 0}), ld2(q + 4 * i + 1)));
-            }
-            __syncwarp();
-            if (lane == 0) T.S[0] = S.c0, T.S[1] = S.c1;
-        }
         const int jj = j - T.pad;
         if (jj < 0) {
-            const fp2 v = e_mul(w, e_scale(S, (1ull << (T.pad - j - 1)) % P));
+            const fp2 v = e_mul(w, e_scale(fp2{T.S[0], T.S[1]}, (1ull << (T.pad - j - 1)) % P));
             for (int x = 0; x < 3; x++) msg[x] = e_add(msg[x], v);
         } else {
+            fp2 a, b, c;
+            tl_quad(T, jj, q + 4 * i, a, b, c);
             const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
             const fp2 wc = e_mul(w, fp2{T.C[0], T.C[1]});
-            const int node[3] = {0, 2, 3};
-            for (int x = 0; x < 3; x++)
-                msg[x] = e_add(msg[x], e_mul(wc, e_mul(eq1(t, X[x]), ld2(q + 4 * i + node[x]))));
+            const fp2 q2 = e_add(a, e_add(e_scale(b, 2), e_scale(c, 4)));
+            const fp2 q3 = e_add(a, e_add(e_scale(b, 3), e_scale(c, 9)));
+            msg[0] = e_add(msg[0], e_mul(wc, e_mul(eq1(t, fp2{0, 0}), a)));
+            msg[1] = e_add(msg[1], e_mul(wc, e_mul(eq1(t, fp2{2, 0}), q2)));
+            msg[2] = e_add(msg[2], e_mul(wc, e_mul(eq1(t, fp2{3, 0}), q3)));
         }
     }
     uint32_t state[8];
@@ -456,22 +496,36 @@ __global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, 
         TlTree& T = trees[i];
         const int jj = j - T.pad;
         if (jj < 0) continue;
+        fp2 a, b, c;
+        tl_quad(T, jj, q + 4 * i, a, b, c);
+        const fp2 Q = e_add(a, e_mul(r, e_add(b, e_mul(r, c))));
         const fp2 C = e_mul(fp2{T.C[0], T.C[1]}, eq1(fp2{T.point[2 * jj], T.point[2 * jj + 1]}, r));
+        T.Q[0] = Q.c0, T.Q[1] = Q.c1;
         T.C[0] = C.c0, T.C[1] = C.c1;
     }
 }
 
-// The last bind: each table of two entries (2·stride apart) into one, by r, as the evaluations.
+// The last bind: each table of two entries (2·stride apart) into one, by r, as the evaluations
+// (src null: the constant 1 of numerators of 1).
 struct TlFinal {
-    const ulonglong2* src;
-    int stride, pad_;
+    const void* src;
+    int stride, base;
     ulonglong2* out;
 };
 __global__ void tl_bind_last(const TlFinal* f, int n, const uint64_t* r) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const fp2 rr = {r[0], r[1]};
-    const fp2 a = l2_canon(ld2(f[i].src)), b = l2_canon(ld2(f[i].src + f[i].stride));
+    fp2 a = {1, 0}, b = {1, 0};
+    if (f[i].src && f[i].base) {
+        const uint64_t* w = static_cast<const uint64_t*>(f[i].src);
+        a = {lz::canon(w[0]), 0};
+        b = {lz::canon(w[f[i].stride]), 0};
+    } else if (f[i].src) {
+        const ulonglong2* v = static_cast<const ulonglong2*>(f[i].src);
+        a = l2_canon(ld2(v));
+        b = l2_canon(ld2(v + f[i].stride));
+    }
     const fp2 v = e_add(a, e_mul(rr, e_sub(b, a)));
     *f[i].out = make_ulonglong2(v.c0, v.c1);
 }
@@ -499,6 +553,7 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
         if (t.kind != 0 && t.kind != 1) return fail(TG_ERR_INVALID, "tree %d: kind %d", k, t.kind);
         if (t.height > 40 || t.s > 40 || t.s + t.height > 40) return fail(TG_ERR_INVALID, "tree %d: too large", k);
         if (t.kind == 1 && t.s) return fail(TG_ERR_INVALID, "tree %d: a fraction tree stands alone (s = 0)", k);
+        if (t.kind == 1 && t.base_leaves) return fail(TG_ERR_INVALID, "tree %d: prime-field leaves are a forest's", k);
         if (t.kind == 0 && !t.leaves) return fail(TG_ERR_INVALID, "tree %d: null leaves", k);
         if (t.kind == 1 && !t.denominators) return fail(TG_ERR_INVALID, "tree %d: null denominators", k);
     }
@@ -507,7 +562,7 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
     st->trees.resize(ntrees);
     cudaStream_t s = d->stream;
     auto bail = [&](int rc) {
-        delete st;
+        tg_leaf_stage_close(st);
         return rc;
     };
     std::lock_guard<std::mutex> lock(d->mu);
@@ -517,52 +572,64 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
         tr.kind = spec.kind;
         tr.s = spec.s;
         tr.h = spec.height;
+        tr.base = spec.kind == 0 && spec.base_leaves;
         st->H = std::max<int>(st->H, (int)spec.height);
         const uint32_t lg = spec.s + spec.height;
+        const size_t es = tr.base ? 8 : 16;  // bytes an entry
         for (uint32_t l = 0; l <= spec.height; l++) {
             tr.n.emplace_back(new DevBuf());
             tr.d.emplace_back(new DevBuf());
         }
         const uint64_t leaves = 1ull << lg;
-        const cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-        int rc = tr.n[spec.height]->ensure(leaves * 16);
-        if (rc) return bail(rc);
-        if (spec.kind == 0) {
-            TG_CUDA(cudaMemcpyAsync(tr.n[spec.height]->ptr, spec.leaves, leaves * 16, kind, s));
-        } else {
-            rc = tr.d[spec.height]->ensure(leaves * 16);
-            if (rc) return bail(rc);
-            TG_CUDA(cudaMemcpyAsync(tr.d[spec.height]->ptr, spec.denominators, leaves * 16, kind, s));
-            tr.unit = !spec.leaves;
-            if (spec.leaves) {
-                TG_CUDA(cudaMemcpyAsync(tr.n[spec.height]->ptr, spec.leaves, leaves * 16, kind, s));
-            } else {  // numerators of 1
-                std::vector<uint64_t> ones(2 * leaves, 0);
-                for (uint64_t i = 0; i < leaves; i++) ones[2 * i] = 1;
-                TG_CUDA(cudaMemcpyAsync(tr.n[spec.height]->ptr, ones.data(), leaves * 16, cudaMemcpyHostToDevice, s));
-                TG_CUDA(cudaStreamSynchronize(s));
+        // the leaf level: device leaves in place (when 16-byte aligned), else a copy
+        auto place = [&](DevBuf& b, const uint64_t* src) -> int {
+            if (on_device && ((uintptr_t)src & 15) == 0) {
+                b.ptr = (void*)src;
+                b.bytes = leaves * es;
+                b.owned = false;
+                return TG_OK;
             }
+            const int rc = spare_take(d, b, leaves * es);
+            if (rc) return rc;
+            TG_CUDA(cudaMemcpyAsync(b.ptr, src, leaves * es, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+            return TG_OK;
+        };
+        int rc = TG_OK;
+        if (spec.kind == 0) {
+            rc = place(*tr.n[spec.height], spec.leaves);
+        } else {
+            rc = place(*tr.d[spec.height], spec.denominators);
+            tr.unit = !spec.leaves;
+            if (!rc && spec.leaves) rc = place(*tr.n[spec.height], spec.leaves);
         }
+        if (rc) return bail(rc);
         for (int l = (int)spec.height - 1; l >= 0; l--) {
             const uint64_t m = 1ull << (spec.s + l);
-            rc = tr.n[l]->ensure(m * 16);
-            if (!rc && spec.kind == 1) rc = tr.d[l]->ensure(m * 16);
+            rc = spare_take(d, *tr.n[l], m * es);
+            if (!rc && spec.kind == 1) rc = spare_take(d, *tr.d[l], m * es);
             if (rc) return bail(rc);
             Launch L(d, s, spec.kind ? "tree_fraction_level" : "tree_product_level", 1, m);
-            if (spec.kind == 0)
+            if (spec.kind == 0 && tr.base)
+                tr_product_level_base<<<grid_of(d, m), 256, 0, s>>>((const ulonglong2*)tr.n[l + 1]->ptr,
+                                                                   (uint64_t*)tr.n[l]->ptr, m);
+            else if (spec.kind == 0)
                 tr_product_level<<<grid_of(d, m), 256, 0, s>>>((const ulonglong2*)tr.n[l + 1]->ptr, (ulonglong2*)tr.n[l]->ptr, m);
             else
-                tr_fraction_level<<<grid_of(d, m), 256, 0, s>>>((const ulonglong2*)tr.n[l + 1]->ptr,
-                                                               (const ulonglong2*)tr.d[l + 1]->ptr,
-                                                               (ulonglong2*)tr.n[l]->ptr, (ulonglong2*)tr.d[l]->ptr, m);
+                tr_fraction_level<<<grid_of(d, m), 256, 0, s>>>(
+                    tr.unit && l + 1 == (int)spec.height ? nullptr : (const ulonglong2*)tr.n[l + 1]->ptr,
+                    (const ulonglong2*)tr.d[l + 1]->ptr, (ulonglong2*)tr.n[l]->ptr, (ulonglong2*)tr.d[l]->ptr, m);
             TG_CUDA(cudaGetLastError());
         }
         // the root level on the host
         const uint64_t r = 1ull << spec.s;
         std::vector<uint64_t> w(2 * r);
-        TG_CUDA(cudaMemcpyAsync(w.data(), tr.n[0]->ptr, r * 16, cudaMemcpyDeviceToHost, s));
-        TG_CUDA(cudaStreamSynchronize(s));
-        for (uint64_t i = 0; i < r; i++) tr.root.push_back({w[2 * i], w[2 * i + 1]});
+        if (spec.kind == 1 && spec.height == 0 && tr.unit) {  // a single leaf of numerator 1
+            w[0] = 1, w[1] = 0;
+        } else {
+            TG_CUDA(cudaMemcpyAsync(w.data(), tr.n[0]->ptr, r * es, cudaMemcpyDeviceToHost, s));
+            TG_CUDA(cudaStreamSynchronize(s));
+        }
+        for (uint64_t i = 0; i < r; i++) tr.root.push_back(tr.base ? fp2{w[i], 0} : fp2{w[2 * i], w[2 * i + 1]});
         if (spec.kind == 1) {
             TG_CUDA(cudaMemcpy(w.data(), tr.d[0]->ptr, 16, cudaMemcpyDeviceToHost));
             tr.root.push_back({w[0], w[1]});
@@ -585,10 +652,11 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
             for (int ab = 0; ab < 2; ab++) {
                 st->pool[k].emplace_back(new DevBuf());
                 const size_t entries = n - 1 - ab >= 0 ? (1ull << (n - 1 - ab)) : 1;
-                const int rc = st->pool[k].back()->ensure(entries * 16);
+                const int rc = spare_take(d, *st->pool[k].back(), entries * 16);
                 if (rc) return bail(rc);
             }
     }
+    spare_trim(d);  // what this stage did not reuse
     *out = st;
     return TG_OK;
 }
@@ -700,9 +768,20 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         if (rc) return bail(rc);
     }
 
+    // each present tree's claim on the level: a forest's value, a fraction tree's p + λ·q, as the
+    // verifier holds it (held: a joining fraction tree's from its sent root) and as the prover
+    // sums it (own: from the tree's own root, which the rounds' q(1) and padding derive from)
+    const int np = (int)present.size();
+    std::vector<fp2> held(np), own_claim(np);
+    for (int i = 0; i < np; i++) {
+        const int k = present[i];
+        const TreeLevels& tr = st->trees[k];
+        held[i] = tr.kind == 0 ? jvalue[k] : e_add(jp[k], e_mul(lambda, jq[k]));
+        own_claim[i] = tr.kind == 1 && tr.own < 0 ? e_add(tr.root[0], e_mul(lambda, tr.root[1])) : held[i];
+    }
+
     // ---- the level's sumcheck on the device (TlSeg rounds, tl_fs transcript, tl_bind_last)
     cudaStream_t s = d->stream;
-    const int np = (int)present.size();
     std::vector<int> nvars(np), pads(np);
     int n_max = 0;
     for (int i = 0; i < np; i++) n_max = std::max(n_max, nvars[i] = (int)jpoint[present[i]].size());
@@ -714,13 +793,14 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
     // the level block: points | eq tables | eq jobs | trees | q | segments | finals | partials |
     // counters | FsState | rounds | challenges | evaluations
     Arena ar;
-    std::vector<size_t> off_point(np), off_eq(np);
+    std::vector<size_t> off_point(np), off_tinv(np), off_eq(np);
     std::vector<std::vector<std::pair<uint64_t, uint64_t>>> eqtab(np);  // per own round: (lo offset, hi offset) in entries
     std::vector<TlEqJob> eqjobs;
     uint64_t eq_total = 0;
     for (int i = 0; i < np; i++) {
         const int n = nvars[i];
         off_point[i] = ar.take((size_t)std::max(n, 1) * 16);
+        off_tinv[i] = ar.take((size_t)std::max(n, 1) * 16);
         uint64_t entries = 0;
         for (int jj = 0; jj < n; jj++) {
             const int rem = n - jj - 1, nl = std::min(rem, TL_LOW), nh = rem - nl;
@@ -737,18 +817,29 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
     std::vector<std::vector<TlSeg>> launches(std::max(n_max, 1));
     std::vector<std::vector<std::pair<int, int>>> owners(std::max(n_max, 1));  // (tree i, own round jj)
     std::vector<TlFinal> finals;
-    auto table_src = [&](int i, int jj, int k, int* stride) -> const ulonglong2* {
-        // the tables own round jj reads: the level below (jj ≤ 1), else round jj − 1's bound output
+    auto table_src = [&](int i, int jj, int k, int* stride, int* base) -> const void* {
+        // the tables own round jj reads: the level below (jj ≤ 1; prime-field words for a
+        // prime-field forest), else round jj − 1's bound output
         TreeLevels& tr = st->trees[present[i]];
         const int own = tr.own >= 0 ? tr.own : 0;
         if (jj <= 1) {
             *stride = 2;
+            *base = tr.base;
             const DevBuf& lv = (tr.kind == 1 && k >= 2) ? *tr.d[own + 1] : *tr.n[own + 1];
+            if (tr.base) return (const uint64_t*)lv.ptr + (k & 1);
             return (const ulonglong2*)lv.ptr + (k & 1);
         }
         *stride = 1;
-        return (const ulonglong2*)st->pool[present[i]][2 * k + ((jj - 2) & 1)]->ptr;
+        *base = 0;
+        return st->pool[present[i]][2 * k + ((jj - 2) & 1)]->ptr;
     };
+    // where a point coordinate is 0, q(1) has no derivation from the claim: that round's launch sums it
+    std::vector<char> one(std::max(n_max, 1), 0);
+    for (int i = 0; i < np; i++)
+        for (int jj = 0; jj < nvars[i]; jj++) {
+            const fp2 c = jpoint[present[i]][jj];
+            if (c.c0 == 0 && c.c1 == 0) one[jj == 0 ? 0 : jj + pads[i]] = 1;
+        }
     // a fraction tree whose leaves have numerators of 1, at the level right above its leaves:
     // N0 and N1 stay 1 through every bind, so only D0 and D1 are tables
     auto unit_level = [&](int i) {
@@ -772,14 +863,14 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
             g.bind = jj >= 1;
             for (int k = 0; k < nt; k++) {
                 const int tk = unit ? k + 2 : k;  // the unit kind's tables are D0 and D1
-                g.src[k] = table_src(i, jj, tk, &g.stride);
+                g.src[k] = table_src(i, jj, tk, &g.stride, &g.base);
                 if (g.bind) g.dst[k] = (ulonglong2*)st->pool[present[i]][2 * tk + ((jj - 1) & 1)]->ptr;
             }
             g.n = 1ull << (nvars[i] - jj - 1);
             g.lam[0] = lambda.c0, g.lam[1] = lambda.c1;
             g.lbits = std::min(nvars[i] - jj - 1, TL_LOW);
             g.block0 = block0;
-            g.nblocks = blocks_for(g.n);
+            g.nblocks = (int)std::min<uint64_t>(blocks_for(g.n), g.n >> g.lbits);
             g.part0 = block0;
             block0 += g.nblocks;
             launches[j].push_back(g);
@@ -813,7 +904,12 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
     for (int i = 0; i < np; i++) {
         const std::vector<fp2>& pt = jpoint[present[i]];
         uint64_t* pw = (uint64_t*)host_at(off_point[i]);
-        for (size_t c = 0; c < pt.size(); c++) pw[2 * c] = pt[c].c0, pw[2 * c + 1] = pt[c].c1;
+        uint64_t* iw = (uint64_t*)host_at(off_tinv[i]);
+        for (size_t c = 0; c < pt.size(); c++) {
+            pw[2 * c] = pt[c].c0, pw[2 * c + 1] = pt[c].c1;
+            const fp2 ti = host_inv2(pt[c]);
+            iw[2 * c] = ti.c0, iw[2 * c + 1] = ti.c1;
+        }
         const uint64_t* dpt = ar.at<uint64_t>(off_point[i]);
         for (int jj = 0; jj < nvars[i]; jj++) {  // round jj's weights over p[jj+1 ..]
             const int rem = nvars[i] - jj - 1, nl = std::min(rem, TL_LOW), nh = rem - nl;
@@ -825,16 +921,12 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         memset(&T, 0, sizeof T);
         T.w[0] = gi.c0, T.w[1] = gi.c1;
         T.C[0] = 1;
+        T.Q[0] = own_claim[i].c0, T.Q[1] = own_claim[i].c1;
+        T.S[0] = own_claim[i].c0, T.S[1] = own_claim[i].c1;
         T.point = dpt;
+        T.tinv = ar.at<uint64_t>(off_tinv[i]);
         T.n = nvars[i];
         T.pad = pads[i];
-        {
-            TreeLevels& trl = st->trees[present[i]];
-            const int own = trl.own >= 0 ? trl.own : 0;
-            T.kind = trl.kind;
-            T.lvl_n = (const ulonglong2*)trl.n[own + 1]->ptr;
-            T.lvl_d = trl.kind ? (const ulonglong2*)trl.d[own + 1]->ptr : nullptr;
-        }
         gi = e_mul(gi, gamma);
         // the final evaluations of its tables
         TreeLevels& tr = st->trees[present[i]];
@@ -843,9 +935,14 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
             TlFinal f;
             memset(&f, 0, sizeof f);
             const int n = nvars[i];
-            const bool copy = n == 0 || (unit_level(i) && k < 2);  // an entry itself (numerators of 1 stay 1)
-            f.src = copy ? table_src(i, 0, k, &f.stride) : table_src(i, n - 1 >= 1 ? n : 1, k, &f.stride);
-            if (copy) f.stride = 0;
+            if (unit_level(i) && k < 2) {  // numerators of 1 stay 1
+                f.src = nullptr;
+            } else if (n == 0) {  // the entry itself
+                f.src = table_src(i, 0, k, &f.stride, &f.base);
+                f.stride = 0;
+            } else {
+                f.src = table_src(i, n - 1 >= 1 ? n : 1, k, &f.stride, &f.base);
+            }
             f.out = ar.at<ulonglong2>(off_evals) + finals.size();
             finals.push_back(f);
         }
@@ -905,8 +1002,12 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
             uint64_t units = 0;
             for (const TlSeg& g : L0) units += g.n;
             Launch L(d, s, "tree_level_round", 1, units);
-            tl_rounds<<<blocks, TL_THREADS, 0, s>>>(ar.at<TlSeg>(off_segs) + seg0, (int)L0.size(),
-                                                    ar.at<uint64_t>(off_partials), ar.at<unsigned>(off_counters));
+            if (one[j])
+                tl_rounds<true><<<blocks, TL_THREADS, 0, s>>>(ar.at<TlSeg>(off_segs) + seg0, (int)L0.size(),
+                                                              ar.at<uint64_t>(off_partials), ar.at<unsigned>(off_counters));
+            else
+                tl_rounds<false><<<blocks, TL_THREADS, 0, s>>>(ar.at<TlSeg>(off_segs) + seg0, (int)L0.size(),
+                                                               ar.at<uint64_t>(off_partials), ar.at<unsigned>(off_counters));
             seg0 += L0.size();
             TG_CUDA(cudaGetLastError());
             return TG_OK;
@@ -921,7 +1022,7 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
             }
             Launch L(d, s, "tree_level_transcript", 1, 1);
             tl_fs<<<1, 32, 0, s>>>(ar.at<FsState>(off_fs), jb, j, keys, ar.at<TlTree>(off_trees), np,
-                                   ar.at<ulonglong2>(off_q), lambda, ar.at<uint64_t>(off_rounds), ar.at<uint64_t>(off_chal));
+                                   ar.at<ulonglong2>(off_q), ar.at<uint64_t>(off_rounds), ar.at<uint64_t>(off_chal));
             TG_CUDA(cudaGetLastError());
         }
         if (!finals.empty()) {
@@ -956,13 +1057,9 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
     std::vector<fp2> claims;
     {
         fp2 c = {0, 0}, g = {1, 0};
-        size_t i = 0;
-        for (int k : present) {
-            const TreeLevels& tr = st->trees[k];
-            const fp2 held = tr.kind == 0 ? jvalue[k] : e_add(jp[k], e_mul(lambda, jq[k]));
-            c = e_add(c, e_mul(g, e_scale(held, (1ull << (n_max - nvars[i])) % P)));
+        for (int i = 0; i < np; i++) {
+            c = e_add(c, e_mul(g, e_scale(held[i], (1ull << (n_max - nvars[i])) % P)));
             g = e_mul(g, gamma);
-            i++;
         }
         claims.push_back(c);
         for (int j = 0; j < n_max; j++) {
@@ -994,8 +1091,8 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         }
         tr.point = pt;
         tr.own = own + 1;
-        tr.n[own]->release();  // the level above is no longer needed
-        tr.d[own]->release();
+        spare_give(d, *tr.n[own]);  // the level above is no longer needed
+        spare_give(d, *tr.d[own]);
     }
     st->level++;
 
@@ -1032,12 +1129,15 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
 
 extern "C" int tg_leaf_stage_close(tg_leaf_stage* st) {
     if (!st) return TG_OK;
-    cudaStream_t s = st->d->stream;
-    for (auto& tr : st->trees)  // secret-class levels are zeroed before release
+    Device* d = st->d;
+    cudaStreamSynchronize(d->stream);  // nothing of the stage in flight
+    // the workspace goes back to the device's cache (zeroed when the cache returns it to the driver)
+    for (auto& tr : st->trees)
         for (auto* v : {&tr.n, &tr.d})
-            for (auto& b : *v)
-                if (b->ptr) cudaMemsetAsync(b->ptr, 0, b->bytes, s);
-    cudaStreamSynchronize(s);
+            for (auto& b : *v) spare_give(d, *b);
+    for (auto& tables : st->pool)
+        for (auto& b : tables) spare_give(d, *b);
+    spare_give(d, st->misc);
     delete st;
     return TG_OK;
 }

@@ -40,3 +40,10 @@ extern "C" int tg_fill_splitmix(tg_device* dev, uint64_t* out, size_t n, uint64_
     TG_CUDA(cudaGetLastError());
     return TG_OK;
 }
+
+// The reference's fill_counter (crates/tessera-gpu/kernels/commit.cu:27-33): out[i] is
+// counter(base + i), the SplitMix64 output for state (base + i + 1)·0x9E3779B97F4A7C15 reduced
+// once below p, which is the stream above started at base·0x9E3779B97F4A7C15.
+extern "C" int tg_fill_counter(tg_device* dev, uint64_t* out, size_t n, uint64_t base, void* stream) {
+    return tg_fill_splitmix(dev, out, n, base * 0x9E3779B97F4A7C15ull, stream);
+}

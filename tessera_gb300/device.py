@@ -38,6 +38,10 @@ class Device:
             N.lib().tg_device_close(self.handle)
             self.handle = None
 
+    def trim(self):
+        """Returns the workspace memory closed leaf stages left for reuse to the driver."""
+        N.call("tg_device_trim", self.handle)
+
     def sync(self):
         N.call("tg_device_sync", self.handle)
 

@@ -32,13 +32,16 @@ def _entries(x) -> int:
 
 @dataclass
 class Forest:
-    """2^s product trees of one height, from their stacked leaves (2^(s+h) Fp2 entries)."""
+    """2^s product trees of one height, from their stacked leaves: 2^(s+h) Fp2 entries, or
+    prime-field words with `base` (the reference's GPU forest takes those, and keeps every level in
+    the prime field)."""
     s: int
     leaves: np.ndarray
+    base: bool = False
 
     @property
     def height(self) -> int:
-        return (_entries(self.leaves) // 2).bit_length() - 1 - self.s
+        return (_entries(self.leaves) // (1 if self.base else 2)).bit_length() - 1 - self.s
 
 
 @dataclass
@@ -97,6 +100,7 @@ class LeafStage:
             if isinstance(t, Forest):
                 arr[k].kind, arr[k].s, arr[k].height = 0, t.s, t.height
                 arr[k].leaves = words(t.leaves)
+                arr[k].base_leaves = int(t.base)
             else:
                 arr[k].kind, arr[k].s, arr[k].height = 1, 0, t.height
                 arr[k].denominators = words(t.denominators)

@@ -43,6 +43,25 @@ def fill_device(tensor, seed: int, device=None):
     return tensor
 
 
+def counter_words(base: int, n: int) -> np.ndarray:
+    """The reference's counter generator: word i is counter(base + i), the SplitMix64 output for
+    state (base + i + 1)·0x9E3779B97F4A7C15 reduced once below p, i.e. the stream above started at
+    base·0x9E3779B97F4A7C15."""
+    return splitmix_words((base * GOLDEN) & (2**64 - 1), n)
+
+
+def fill_counter(tensor, base: int, device=None):
+    """Fills an int64 CUDA tensor in place with counter_words(base, numel), on the GPU (the
+    reference's Device::fill_counter)."""
+    from . import _native as N
+    from .device import resolve
+
+    d = resolve(device)
+    N.call("tg_fill_counter", d.handle, tensor.data_ptr(), tensor.numel(), base & (2**64 - 1), None)
+    d.sync()
+    return tensor
+
+
 class _Stream:
     def __init__(self, seed: int):
         self.state = seed & (2**64 - 1)

@@ -81,18 +81,37 @@ def check_level(rec, want, stage, label):
             assert claim == (f2(n["numerator"]), f2(n["denominator"])), label
 
 
-def forest_of(spec):
-    from tessera_gb300.trees import Forest, lift
+def leaf_table(values, base, on_device):
+    """Prime-field leaves as Fp2 pairs, or as words (base); on the device when asked."""
+    from tessera_gb300.trees import lift
 
-    return Forest(spec["rows_log"], lift([num(x) for x in spec["leaves"]]))
+    a = np.array(values, dtype=np.uint64) if base else lift(values)
+    if not on_device:
+        return a
+    import torch
+
+    return torch.from_numpy(a.view(np.int64)).cuda()
 
 
-def test_tree_batches(dev):
-    from tessera_gb300.trees import Forest, LeafStage, lift
+def forest_of(spec, base=False, on_device=False):
+    from tessera_gb300.trees import Forest
+
+    return Forest(spec["rows_log"], leaf_table([num(x) for x in spec["leaves"]], base, on_device), base)
+
+
+# Fp2 leaves from the host; prime-field leaves (the forest's levels stay in the prime field) from
+# the host and read in place on the device
+LEAF_FORMS = [(False, False), (True, False), (True, True)]
+
+
+@pytest.mark.parametrize("base,on_device", LEAF_FORMS)
+def test_tree_batches(dev, base, on_device):
+    from tessera_gb300.trees import Forest, LeafStage
 
     for b in TREES["tree_batches"]:
         t = transcript(b["context"])
-        with LeafStage([Forest(0, lift([num(x) for x in tr["leaves"]])) for tr in b["trees"]], dev) as st:
+        trees = [Forest(0, leaf_table([num(x) for x in tr["leaves"]], base, on_device), base) for tr in b["trees"]]
+        with LeafStage(trees, dev) as st:
             for k, tr in enumerate(b["trees"]):
                 assert st.root(k) == [(num(tr["root"]), 0)], b["name"]
             assert st.height == len(b["levels"])
@@ -100,12 +119,13 @@ def test_tree_batches(dev):
                 check_level(st.prove_level(t), want, st, b["name"])
 
 
-def test_forest_batches(dev):
+@pytest.mark.parametrize("base,on_device", LEAF_FORMS)
+def test_forest_batches(dev, base, on_device):
     from tessera_gb300.trees import LeafStage
 
     for b in TREES["forest_batches"]:
         t = transcript(b["context"])
-        with LeafStage([forest_of(f) for f in b["forests"]], dev) as st:
+        with LeafStage([forest_of(f, base, on_device) for f in b["forests"]], dev) as st:
             for k, f in enumerate(b["forests"]):
                 assert st.root(k) == [(num(x), 0) for x in f["roots"]], b["name"]
             for want in b["levels"]:
@@ -233,3 +253,52 @@ def test_generated_leaves_and_leaf_claims(dev, unit):
     nums = [(int(n[2 * j]), int(n[2 * j + 1])) for j in range(1 << h)]
     dens = [(int(d[2 * j]), int(d[2 * j + 1])) for j in range(1 << h)]
     assert (p, q) == (mle(nums, point), mle(dens, point))
+
+
+def fold_mle(values, point):
+    """The MLE of a table at a point by binding one coordinate at a time (x_1 the lowest bit)."""
+    v = list(values)
+    for r in point:
+        v = [add(v[2 * i], mul(r, sub(v[2 * i + 1], v[2 * i]))) for i in range(len(v) // 2)]
+    assert len(v) == 1
+    return v[0]
+
+
+def test_counter_fill(dev):
+    """The device counter generator equals the host's, word for word (the reference's fill_counter)."""
+    import torch
+
+    from tessera_gb300.workloads import counter_words, fill_counter
+
+    base = 1 << 61
+    got = fill_counter(torch.empty(5000, dtype=torch.int64, device="cuda"), base, dev).cpu().numpy().view(np.uint64)
+    assert np.array_equal(got, counter_words(base, 5000))
+    assert [int(x) for x in got[:3]] == [counter_value(base + j) for j in range(3)]
+
+
+@pytest.mark.parametrize("s,h", [(4, 8), (0, 11), (7, 3)])
+def test_prime_field_forest_matches_fp2_and_leaf_claim(dev, s, h):
+    """A forest of counter leaves proven from prime-field words (read in place on the device) and
+    from Fp2 pairs gives the same records level by level, and the final claim is the leaves' MLE at
+    the final point; a second stage of the same shape, from the device's workspace cache, repeats
+    the proof exactly."""
+    import torch
+
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.trees import Forest, LeafStage, lift
+    from tessera_gb300.workloads import fill_counter
+
+    ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([7]) * 32, bytes([9]) * 16)
+    leaves = fill_counter(torch.empty(1 << (s + h), dtype=torch.int64, device="cuda"), 1 << 61, dev)
+    host = leaves.cpu().numpy().view(np.uint64)
+    runs = []
+    for forest in (Forest(s, leaves, True), Forest(s, lift(host)), Forest(s, leaves, True)):
+        t = Transcript(ctx)
+        with LeafStage([forest], dev) as st:
+            recs = st.prove(t)
+            runs.append(([(r.rounds, r.challenges, r.final_evals, r.rho) for r in recs], st.claim(0), t.state))
+    assert runs[0] == runs[1] == runs[2]
+    point, value, own = runs[0][1]
+    assert own == h and len(point) == s + h
+    assert value == fold_mle([(int(x), 0) for x in host], point)
+    dev.trim()
