@@ -119,25 +119,27 @@ struct TreeLevels {
     fp2 value = {0, 0}, p = {0, 0}, q = {0, 0};
 };
 
-static fp2 host_eq(const std::vector<fp2>& r, uint64_t y) {
-    fp2 out = {1, 0};
-    for (size_t i = 0; i < r.size(); i++) out = e_mul(out, (y >> i) & 1 ? r[i] : e_sub(fp2{1, 0}, r[i]));
-    return out;
+// Σ_y v[y]·eq(r, y) (y_1 the lowest bit) by binding one coordinate at a time: 2^n products for
+// 2^n values, where a fresh eq product per y would cost n·2^n.
+static fp2 host_mle(std::vector<fp2> v, const std::vector<fp2>& r) {
+    for (size_t i = 0; i < r.size(); i++) {
+        const size_t half = v.size() / 2;
+        for (size_t k = 0; k < half; k++) v[k] = e_add(v[2 * k], e_mul(r[i], e_sub(v[2 * k + 1], v[2 * k])));
+        v.resize(half);
+    }
+    return v.empty() ? fp2{0, 0} : v[0];
 }
 
-// p(r) for the polynomial through (k, v_k), k = 0..3 (Lagrange).
+// p(r) for the polynomial through (k, v_k), k = 0..3 (Lagrange; the denominators' inverses are
+// those of −6, 2, −2 and 6, computed once).
 static fp2 lagrange4(const fp2 v[4], fp2 r) {
+    static const uint64_t dinv[4] = {inv(P - 6), inv(2), inv(P - 2), inv(6)};
     fp2 out = {0, 0};
     for (int i = 0; i < 4; i++) {
         fp2 num = {1, 0};
-        int64_t den = 1;
         for (int m = 0; m < 4; m++)
-            if (m != i) {
-                num = e_mul(num, e_sub(r, fp2{(uint64_t)m, 0}));
-                den *= (i - m);
-            }
-        const uint64_t dd = den < 0 ? P - (uint64_t)(-den) : (uint64_t)den;
-        out = e_add(out, e_mul(v[i], e_scale(num, inv(dd))));
+            if (m != i) num = e_mul(num, e_sub(r, fp2{(uint64_t)m, 0}));
+        out = e_add(out, e_mul(v[i], e_scale(num, dinv[i])));
     }
     return out;
 }
@@ -178,6 +180,7 @@ static fp2 host_inv2(fp2 a) {
 
 constexpr int TL_THREADS = 256;
 constexpr int TL_LOW = 11;  // the low eq table's variables: the pairs of one chunk share a high weight
+constexpr uint64_t TL_TAIL_PAIRS = 2048;  // rounds of at most this many pairs a segment run in one block
 
 struct TlSeg {
     const void* src[4];  // table T's entry x is src[T][x·stride]: Fp2, or prime-field words when base
@@ -189,7 +192,7 @@ struct TlSeg {
     uint64_t n;            // pairs: 2^lbits a chunk
     uint64_t lam[2];
     int kind, stride, bind, lbits;
-    int block0, nblocks, part0, base;
+    int block0, nblocks, part0, mode;
 };
 static_assert(sizeof(TlSeg) % 8 == 0, "TlSeg copies as words");
 
@@ -247,69 +250,122 @@ __device__ __forceinline__ void tl_nodes(const fp2* u, const fp2* d, fp2 lam, fp
     }
 }
 
+// The modes of a segment's tables in a round: Fp2 tables summed as they are (a tree's round 0),
+// prime-field tables bound into Fp2 (a prime-field forest's round 1), prime-field tables summed (its
+// round 0), and Fp2 tables bound by the previous challenge as they are summed (every later round).
+enum : int { TL_SUM = 0, TL_BIND_BASE = 1, TL_SUM_BASE = 2, TL_BIND = 3 };
+
+// Pairs a thread loads before it computes any: enough bytes in flight per thread to cover the
+// latency of HBM at two or three resident blocks per SM, within the register budget.
+template <int KIND, int MODE>
+__host__ __device__ constexpr int tl_batch() {
+    return MODE == TL_SUM_BASE ? 4 : (KIND == 1 || (KIND == 2 && MODE == TL_BIND)) ? 1 : 2;
+}
+
+// One pair's values as loaded: E entries of each of NT tables (E = 4 when binding, else 2),
+// prime-field words in .x for the base modes.
+template <int NT, int MODE>
+struct TlRaw {
+    static constexpr int E = (MODE == TL_BIND || MODE == TL_BIND_BASE) ? 4 : 2;
+    ulonglong2 v[NT][E];
+};
+
+// The loads of pair p. Prime-field levels hold L and R interleaved (L[x], R[x]) as one 16-byte
+// word pair, so a pair's 2E words come in E vector loads.
+template <int NT, int MODE>
+__device__ __forceinline__ void tl_load(const TlSeg& g, uint64_t p, TlRaw<NT, MODE>& raw) {
+    constexpr int E = TlRaw<NT, MODE>::E;
+    if constexpr (MODE == TL_SUM_BASE || MODE == TL_BIND_BASE) {
+        const ulonglong2* lv = static_cast<const ulonglong2*>(g.src[0]) + E * p;
+#pragma unroll
+        for (int e = 0; e < E; e++) raw.v[0][e] = lv[e];
+    } else {
+        const uint64_t st = (uint64_t)g.stride;
+#pragma unroll
+        for (int k = 0; k < NT; k++) {
+            const ulonglong2* src = static_cast<const ulonglong2*>(g.src[k]);
+#pragma unroll
+            for (int e = 0; e < E; e++) raw.v[k][e] = src[(E * p + e) * st];
+        }
+    }
+}
+
+// A pair's contribution: binds (writing the bound entries), forms g at the nodes and adds w·g to
+// the chunk's part sums.
+template <int NT, int KIND, int MODE, bool ONE>
+__device__ __forceinline__ void tl_pair(const TlSeg& g, uint64_t p, const TlRaw<NT, MODE>& raw, fp2 w, fp2 r, fp2 lam,
+                                        fp2 (&part)[3]) {
+    if constexpr (MODE == TL_SUM_BASE) {
+        const uint64_t l0 = raw.v[0][0].x, r0 = raw.v[0][0].y, l1 = raw.v[0][1].x, r1 = raw.v[0][1].y;
+        const uint64_t v0 = lz::mul(l0, r0), vi = lz::mul(lz::sub(l1, l0), lz::sub(r1, r0));
+        part[0] = l2_add(part[0], l2_scale(w, v0));
+        part[2] = l2_add(part[2], l2_scale(w, vi));
+        if constexpr (ONE) part[1] = l2_add(part[1], l2_scale(w, lz::mul(l1, r1)));
+    } else {
+        fp2 u[NT], d[NT];
+        if constexpr (MODE == TL_BIND_BASE) {
+#pragma unroll
+            for (int k = 0; k < 2; k++) {  // table k's entries 4p..4p+3 are raw.v[0][e] .x (L) or .y (R)
+                const uint64_t a0 = k ? raw.v[0][0].y : raw.v[0][0].x, a1 = k ? raw.v[0][1].y : raw.v[0][1].x;
+                const uint64_t b0 = k ? raw.v[0][2].y : raw.v[0][2].x, b1 = k ? raw.v[0][3].y : raw.v[0][3].x;
+                const uint64_t da = lz::sub(a1, a0), db = lz::sub(b1, b0);
+                const fp2 uu = {lz::add(a0, lz::mul(r.c0, da)), lz::mul(r.c1, da)};
+                const fp2 vv = {lz::add(b0, lz::mul(r.c0, db)), lz::mul(r.c1, db)};
+                g.dst[k][2 * p] = make_ulonglong2(uu.c0, uu.c1);
+                g.dst[k][2 * p + 1] = make_ulonglong2(vv.c0, vv.c1);
+                u[k] = uu;
+                d[k] = l2_sub(vv, uu);
+            }
+        } else if constexpr (MODE == TL_BIND) {
+#pragma unroll
+            for (int k = 0; k < NT; k++) {
+                const fp2 a0 = {raw.v[k][0].x, raw.v[k][0].y}, a1 = {raw.v[k][1].x, raw.v[k][1].y};
+                const fp2 b0 = {raw.v[k][2].x, raw.v[k][2].y}, b1 = {raw.v[k][3].x, raw.v[k][3].y};
+                const fp2 uu = l2_add(a0, l2_mul(r, l2_sub(a1, a0)));
+                const fp2 vv = l2_add(b0, l2_mul(r, l2_sub(b1, b0)));
+                g.dst[k][2 * p] = make_ulonglong2(uu.c0, uu.c1);
+                g.dst[k][2 * p + 1] = make_ulonglong2(vv.c0, vv.c1);
+                u[k] = uu;
+                d[k] = l2_sub(vv, uu);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < NT; k++) {
+                u[k] = {raw.v[k][0].x, raw.v[k][0].y};
+                d[k] = l2_sub(fp2{raw.v[k][1].x, raw.v[k][1].y}, u[k]);
+            }
+        }
+        fp2 g0, g1, gi;
+        tl_nodes<KIND, ONE>(u, d, lam, g0, g1, gi);
+        part[0] = l2_add(part[0], l2_mul(w, g0));
+        part[2] = l2_add(part[2], l2_mul(w, gi));
+        if constexpr (ONE) part[1] = l2_add(part[1], l2_mul(w, g1));
+    }
+}
+
 // This block's share of a segment: chunks c = b, b + nblocks, … of 2^lbits pairs, each summed with
-// its low weights and then scaled once by its high weight, into acc = (q(0), q(1), q(∞)). NT tables;
-// MODE 0 reads Fp2 tables (binding the previous challenge when bind), 1 binds prime-field tables
-// into Fp2 (a prime-field forest's round 1), 2 sums prime-field tables (its round 0).
+// its low weights and then scaled once by its high weight, into acc = (q(0), q(1), q(∞)). A thread
+// loads tl_batch pairs (TL_THREADS apart) before it computes them.
 template <int NT, int KIND, int MODE, bool ONE>
 __device__ __forceinline__ void tl_sum(const TlSeg& g, uint64_t b, fp2 (&acc)[3]) {
+    constexpr int U = tl_batch<KIND, MODE>();
     const int lb = g.lbits;
     const uint64_t span = 1ull << lb, chunks = g.n >> lb;
-    const fp2 r = g.bind ? fp2{g.r[0], g.r[1]} : fp2{0, 0};
+    const fp2 r = (MODE == TL_BIND || MODE == TL_BIND_BASE) ? fp2{g.r[0], g.r[1]} : fp2{0, 0};
     const fp2 lam = {g.lam[0], g.lam[1]};
-    const uint64_t st = (uint64_t)g.stride;
     for (uint64_t c = b; c < chunks; c += (uint64_t)g.nblocks) {
         fp2 part[3] = {{0, 0}, {0, 0}, {0, 0}};
-#pragma unroll 2
-        for (uint64_t e = threadIdx.x; e < span; e += TL_THREADS) {
-            const uint64_t p = (c << lb) + e;
-            const fp2 w = ld2(g.lo + e);
-            if constexpr (MODE == 2) {
-                const uint64_t* L = static_cast<const uint64_t*>(g.src[0]);
-                const uint64_t* R = static_cast<const uint64_t*>(g.src[1]);
-                const uint64_t l0 = L[2 * p * st], l1 = L[(2 * p + 1) * st];
-                const uint64_t r0 = R[2 * p * st], r1 = R[(2 * p + 1) * st];
-                const uint64_t v0 = lz::mul(l0, r0), vi = lz::mul(lz::sub(l1, l0), lz::sub(r1, r0));
-                part[0] = l2_add(part[0], l2_scale(w, v0));
-                part[2] = l2_add(part[2], l2_scale(w, vi));
-                if constexpr (ONE) part[1] = l2_add(part[1], l2_scale(w, lz::mul(l1, r1)));
-            } else {
-                fp2 u[NT], d[NT];
+        for (uint64_t e0 = threadIdx.x; e0 < span; e0 += (uint64_t)U * TL_THREADS) {
+            TlRaw<NT, MODE> raw[U];
 #pragma unroll
-                for (int k = 0; k < NT; k++) {
-                    if constexpr (MODE == 1) {
-                        const uint64_t* src = static_cast<const uint64_t*>(g.src[k]);
-                        const uint64_t a0 = src[(4 * p) * st], a1 = src[(4 * p + 1) * st];
-                        const uint64_t b0 = src[(4 * p + 2) * st], b1 = src[(4 * p + 3) * st];
-                        const uint64_t da = lz::sub(a1, a0), db = lz::sub(b1, b0);
-                        const fp2 uu = {lz::add(a0, lz::mul(r.c0, da)), lz::mul(r.c1, da)};
-                        const fp2 vv = {lz::add(b0, lz::mul(r.c0, db)), lz::mul(r.c1, db)};
-                        g.dst[k][2 * p] = make_ulonglong2(uu.c0, uu.c1);
-                        g.dst[k][2 * p + 1] = make_ulonglong2(vv.c0, vv.c1);
-                        u[k] = uu;
-                        d[k] = l2_sub(vv, uu);
-                    } else {
-                        const ulonglong2* src = static_cast<const ulonglong2*>(g.src[k]);
-                        if (g.bind) {
-                            const fp2 a0 = ld2(src + (4 * p) * st), a1 = ld2(src + (4 * p + 1) * st);
-                            const fp2 b0 = ld2(src + (4 * p + 2) * st), b1 = ld2(src + (4 * p + 3) * st);
-                            const fp2 uu = l2_add(a0, l2_mul(r, l2_sub(a1, a0)));
-                            const fp2 vv = l2_add(b0, l2_mul(r, l2_sub(b1, b0)));
-                            g.dst[k][2 * p] = make_ulonglong2(uu.c0, uu.c1);
-                            g.dst[k][2 * p + 1] = make_ulonglong2(vv.c0, vv.c1);
-                            u[k] = uu;
-                            d[k] = l2_sub(vv, uu);
-                        } else {
-                            u[k] = ld2(src + (2 * p) * st);
-                            d[k] = l2_sub(ld2(src + (2 * p + 1) * st), u[k]);
-                        }
-                    }
-                }
-                fp2 g0, g1, gi;
-                tl_nodes<KIND, ONE>(u, d, lam, g0, g1, gi);
-                part[0] = l2_add(part[0], l2_mul(w, g0));
-                part[2] = l2_add(part[2], l2_mul(w, gi));
-                if constexpr (ONE) part[1] = l2_add(part[1], l2_mul(w, g1));
+            for (int u = 0; u < U; u++) {
+                const uint64_t e = e0 + (uint64_t)u * TL_THREADS;
+                if (U == 1 || e < span) tl_load<NT, MODE>(g, (c << lb) + e, raw[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; u++) {
+                const uint64_t e = e0 + (uint64_t)u * TL_THREADS;
+                if (U == 1 || e < span) tl_pair<NT, KIND, MODE, ONE>(g, (c << lb) + e, raw[u], ld2(g.lo + e), r, lam, part);
             }
         }
         const fp2 h = ld2(g.hi + c);
@@ -319,7 +375,23 @@ __device__ __forceinline__ void tl_sum(const TlSeg& g, uint64_t b, fp2 (&acc)[3]
     }
 }
 
-template <bool ONE>
+// The block's six-word sum, into thread 0's words (red: a row per warp; the call ends with every
+// thread past a barrier after the last use of red but thread 0's reads).
+__device__ __forceinline__ void tl_block_sum(uint64_t (&words)[6], uint64_t (*red)[6]) {
+#pragma unroll
+    for (int w = 0; w < 6; w++)
+        for (int o = 16; o > 0; o >>= 1) words[w] = add(words[w], __shfl_down_sync(0xFFFFFFFFu, words[w], o));
+    if ((threadIdx.x & 31) == 0)
+        for (int w = 0; w < 6; w++) red[threadIdx.x >> 5][w] = words[w];
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int k = 1; k < (int)(blockDim.x >> 5); k++)
+            for (int w = 0; w < 6; w++) words[w] = add(words[w], red[k][w]);
+}
+
+// One round's segments of one kind and mode: each block sums its share of its segment, and the
+// segment's last block adds the blocks' rows into the segment's q.
+template <int NT, int KIND, int MODE, bool ONE>
 __global__ void __launch_bounds__(TL_THREADS, 2) tl_rounds(const TlSeg* segs, int nseg, uint64_t* partials,
                                                            unsigned* counters) {
     __shared__ TlSeg g;
@@ -346,34 +418,17 @@ __global__ void __launch_bounds__(TL_THREADS, 2) tl_rounds(const TlSeg* segs, in
     __syncthreads();
     fp2 acc[3] = {{0, 0}, {0, 0}, {0, 0}};
     const uint64_t b = (uint64_t)(blockIdx.x - g.block0);
-    if (g.kind == 0) {
-        if (!g.base)
-            tl_sum<2, 0, 0, ONE>(g, b, acc);
-        else if (g.bind)
-            tl_sum<2, 0, 1, ONE>(g, b, acc);
-        else
-            tl_sum<2, 0, 2, ONE>(g, b, acc);
-    } else if (g.kind == 1) {
-        tl_sum<4, 1, 0, ONE>(g, b, acc);
-    } else {
-        tl_sum<2, 2, 0, ONE>(g, b, acc);
-        acc[2] = l2_mul(fp2{g.lam[0], g.lam[1]}, acc[2]);
-    }
-    // block sums, then the segment's last block reduces the partial rows
+    tl_sum<NT, KIND, MODE, ONE>(g, b, acc);
+    if constexpr (KIND == 2) acc[2] = l2_mul(fp2{g.lam[0], g.lam[1]}, acc[2]);
+    // block sums, then the segment's last block reduces the partial rows (every thread a share)
     uint64_t words[6];
     for (int i = 0; i < 3; i++) {
         const fp2 c = l2_canon(acc[i]);
         words[2 * i] = c.c0, words[2 * i + 1] = c.c1;
     }
-#pragma unroll
-    for (int w = 0; w < 6; w++)
-        for (int o = 16; o > 0; o >>= 1) words[w] = add(words[w], __shfl_down_sync(0xFFFFFFFFu, words[w], o));
-    if ((threadIdx.x & 31) == 0)
-        for (int w = 0; w < 6; w++) red[threadIdx.x >> 5][w] = words[w];
-    __syncthreads();
+    auto block_sum = [&]() { tl_block_sum(words, red); };
+    block_sum();
     if (threadIdx.x == 0) {
-        for (int k = 1; k < (int)(blockDim.x >> 5); k++)
-            for (int w = 0; w < 6; w++) words[w] = add(words[w], red[k][w]);
         for (int w = 0; w < 6; w++) partials[(size_t)(g.part0 + b) * 8 + w] = words[w];
         __threadfence();
         last = atomicAdd(&counters[si], 1u) == (unsigned)g.nblocks - 1;
@@ -381,13 +436,46 @@ __global__ void __launch_bounds__(TL_THREADS, 2) tl_rounds(const TlSeg* segs, in
     __syncthreads();
     if (!last) return;
     __threadfence();
-    if (threadIdx.x < 6) {
-        uint64_t t = 0;
-        for (int k = 0; k < g.nblocks; k++) t = add(t, __ldcg(&partials[(size_t)(g.part0 + k) * 8 + threadIdx.x]));
-        reinterpret_cast<uint64_t*>(g.out)[threadIdx.x] = t;
+    for (int w = 0; w < 6; w++) words[w] = 0;
+    for (int k = threadIdx.x; k < g.nblocks; k += blockDim.x)
+        for (int w = 0; w < 6; w++) words[w] = add(words[w], __ldcg(&partials[(size_t)(g.part0 + k) * 8 + w]));
+    __syncthreads();  // red is reused
+    block_sum();
+    if (threadIdx.x == 0) {
+        for (int w = 0; w < 6; w++) reinterpret_cast<uint64_t*>(g.out)[w] = words[w];
+        counters[si] = 0;
     }
-    if (threadIdx.x == 0) counters[si] = 0;
 }
+
+// A segment's kernel key: its kind and mode (the launches of a round go one per key).
+__host__ __device__ constexpr int tl_key(int kind, int mode) { return kind * 4 + mode; }
+
+template <bool ONE>
+static void tl_launch(int key, int blocks, cudaStream_t s, const TlSeg* segs, int nseg, uint64_t* partials,
+                      unsigned* counters) {
+    switch (key) {
+#define TL_CASE(NT, KIND, MODE)                                                                          \
+    case KIND * 4 + MODE:                                                                                \
+        tl_rounds<NT, KIND, MODE, ONE><<<blocks, TL_THREADS, 0, s>>>(segs, nseg, partials, counters); \
+        break;
+        TL_CASE(2, 0, TL_SUM)
+        TL_CASE(2, 0, TL_BIND_BASE)
+        TL_CASE(2, 0, TL_SUM_BASE)
+        TL_CASE(2, 0, TL_BIND)
+        TL_CASE(4, 1, TL_SUM)
+        TL_CASE(4, 1, TL_BIND)
+        TL_CASE(2, 2, TL_SUM)
+        TL_CASE(2, 2, TL_BIND)
+#undef TL_CASE
+        default:
+            break;
+    }
+}
+
+// The low eq table's variables for a round over 2^rem pairs: TL_LOW for large rounds (one high
+// weight per chunk of 2^TL_LOW pairs), fewer where that would leave too few chunks to fill the GPU,
+// but at least a block's worth of pairs a chunk.
+inline int tl_low_bits(int rem) { return std::min(rem, std::max(8, std::min(TL_LOW, rem - 10))); }
 
 // The eq weight tables of every round of every present tree: entry e of table t is
 // Π_i eq1(c_i, bit_i(e)) over the table's coordinates c (lo: the first L of the round's remaining
@@ -438,9 +526,9 @@ __device__ void tl_quad(const TlTree& T, int jj, const ulonglong2* q, fp2& a, fp
 // Round j of a level: the message Σ_i γ^i·(2^{pad_i − j − 1}·S_i while padded, else
 // C_i·eq1(p_i[j'], X)·q_i(X)) at X = 0, 2, 3, absorbed under <prefix>/round/j; r_j drawn under
 // <prefix>/r/j; then each tree in its own rounds takes Q_i ← q_i(r_j) and C_i ← C_i·eq1(p_i[j'], r_j).
-__global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, int ntrees, const ulonglong2* q,
-                      uint64_t* rounds_out, uint64_t* chal_out) {
-    __shared__ uint32_t sbuf[FS_BUF_WORDS];
+// One warp runs it (sbuf: FS_BUF_WORDS of shared memory).
+__device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& keys, TlTree* trees, int ntrees,
+                            const ulonglong2* q, uint64_t* rounds_out, uint64_t* chal_out, uint32_t* sbuf) {
     const int lane = threadIdx.x & 31;
     fp2 msg[3] = {{0, 0}, {0, 0}, {0, 0}};
     for (int i = 0; i < ntrees; i++) {  // every lane forms the message (the same reads)
@@ -502,6 +590,84 @@ __global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, 
         const fp2 C = e_mul(fp2{T.C[0], T.C[1]}, eq1(fp2{T.point[2 * jj], T.point[2 * jj + 1]}, r));
         T.Q[0] = Q.c0, T.Q[1] = Q.c1;
         T.C[0] = C.c0, T.C[1] = C.c1;
+    }
+}
+
+__global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, int ntrees, const ulonglong2* q,
+                      uint64_t* rounds_out, uint64_t* chal_out) {
+    __shared__ uint32_t sbuf[FS_BUF_WORDS];
+    tl_fs_round(st, jb, j, keys, trees, ntrees, q, rounds_out, chal_out, sbuf);
+}
+
+// A segment's whole sum by one block (its chunks one after another); each variant is its own
+// function, so that the tail kernel's registers are those of the variant it calls.
+template <int NT, int KIND, int MODE, bool ONE>
+__device__ __noinline__ void tl_sum_block(const TlSeg& g, fp2 (&acc)[3]) {
+    tl_sum<NT, KIND, MODE, ONE>(g, 0, acc);
+}
+
+template <bool ONE>
+__device__ void tl_sum_any(const TlSeg& g, fp2 (&acc)[3]) {
+    switch (tl_key(g.kind, g.mode)) {
+        case tl_key(0, TL_SUM): tl_sum_block<2, 0, TL_SUM, ONE>(g, acc); break;
+        case tl_key(0, TL_BIND_BASE): tl_sum_block<2, 0, TL_BIND_BASE, ONE>(g, acc); break;
+        case tl_key(0, TL_SUM_BASE): tl_sum_block<2, 0, TL_SUM_BASE, ONE>(g, acc); break;
+        case tl_key(0, TL_BIND): tl_sum_block<2, 0, TL_BIND, ONE>(g, acc); break;
+        case tl_key(1, TL_SUM): tl_sum_block<4, 1, TL_SUM, ONE>(g, acc); break;
+        case tl_key(1, TL_BIND): tl_sum_block<4, 1, TL_BIND, ONE>(g, acc); break;
+        case tl_key(2, TL_SUM): tl_sum_block<2, 2, TL_SUM, ONE>(g, acc); break;
+        case tl_key(2, TL_BIND): tl_sum_block<2, 2, TL_BIND, ONE>(g, acc); break;
+        default: break;
+    }
+}
+
+// A level's small rounds, j0 to the last, run by one block with no launch between them.
+struct TlTail {
+    FsJob jb;
+    FsKeys keys;
+    FsState* st;
+    TlTree* trees;
+    const ulonglong2* q;
+    uint64_t* rounds_out;
+    uint64_t* chal_out;
+    const TlSeg* segs;     // the tail rounds' segments, in round order (one block each: nblocks = 1)
+    const int* first;      // round j0 + t's segments are segs[first[t] .. first[t + 1])
+    const uint8_t* one;    // round j0 + t sums q(1)
+    int ntrees, j0, rounds, pad_;
+};
+
+// Each round sums its segments with the whole block, then warp 0 runs the round's transcript,
+// whose challenge the next round binds (the barrier between them orders the block's memory).
+__global__ void __launch_bounds__(TL_THREADS, 1) tl_tail(const TlTail* A) {
+    __shared__ TlSeg g;
+    __shared__ uint64_t red[TL_THREADS / 32][6];
+    __shared__ uint32_t sbuf[FS_BUF_WORDS];
+    const int rounds = A->rounds;
+    for (int t = 0; t < rounds; t++) {
+        const bool one = A->one[t];
+        for (int si = A->first[t]; si < A->first[t + 1]; si++) {
+            if (threadIdx.x < (int)(sizeof(TlSeg) / 8))
+                reinterpret_cast<uint64_t*>(&g)[threadIdx.x] = reinterpret_cast<const uint64_t*>(A->segs + si)[threadIdx.x];
+            __syncthreads();
+            fp2 acc[3] = {{0, 0}, {0, 0}, {0, 0}};
+            if (one)
+                tl_sum_any<true>(g, acc);
+            else
+                tl_sum_any<false>(g, acc);
+            if (g.kind == 2) acc[2] = l2_mul(fp2{g.lam[0], g.lam[1]}, acc[2]);
+            uint64_t words[6];
+            for (int i = 0; i < 3; i++) {
+                const fp2 c = l2_canon(acc[i]);
+                words[2 * i] = c.c0, words[2 * i + 1] = c.c1;
+            }
+            tl_block_sum(words, red);
+            if (threadIdx.x == 0)
+                for (int w = 0; w < 6; w++) reinterpret_cast<uint64_t*>(g.out)[w] = words[w];
+            __syncthreads();
+        }
+        if (threadIdx.x < 32)
+            tl_fs_round(A->st, A->jb, A->j0 + t, A->keys, A->trees, A->ntrees, A->q, A->rounds_out, A->chal_out, sbuf);
+        __syncthreads();
     }
 }
 
@@ -750,9 +916,7 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
             jq[k] = tr.q;
         } else if (tr.kind == 0) {
             jpoint[k].assign(rootc.begin() + (s_max - tr.s), rootc.end());
-            fp2 v = {0, 0};
-            for (uint64_t y = 0; y < tr.root.size(); y++) v = e_add(v, e_mul(tr.root[y], host_eq(jpoint[k], y)));
-            jvalue[k] = v;
+            jvalue[k] = host_mle(tr.root, jpoint[k]);
         } else {
             jp[k] = tr.sent_n;
             jq[k] = tr.sent_d;
@@ -803,7 +967,7 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         off_tinv[i] = ar.take((size_t)std::max(n, 1) * 16);
         uint64_t entries = 0;
         for (int jj = 0; jj < n; jj++) {
-            const int rem = n - jj - 1, nl = std::min(rem, TL_LOW), nh = rem - nl;
+            const int rem = n - jj - 1, nl = tl_low_bits(rem), nh = rem - nl;
             eqtab[i].push_back({entries, entries + (1ull << nl)});
             entries += (1ull << nl) + (1ull << nh);
         }
@@ -861,25 +1025,62 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
             memset(&g, 0, sizeof g);
             g.kind = unit ? 2 : tr.kind;
             g.bind = jj >= 1;
+            int base = 0;
             for (int k = 0; k < nt; k++) {
                 const int tk = unit ? k + 2 : k;  // the unit kind's tables are D0 and D1
-                g.src[k] = table_src(i, jj, tk, &g.stride, &g.base);
+                g.src[k] = table_src(i, jj, tk, &g.stride, &base);
                 if (g.bind) g.dst[k] = (ulonglong2*)st->pool[present[i]][2 * tk + ((jj - 1) & 1)]->ptr;
             }
+            g.mode = base ? (g.bind ? TL_BIND_BASE : TL_SUM_BASE) : (g.bind ? TL_BIND : TL_SUM);
             g.n = 1ull << (nvars[i] - jj - 1);
             g.lam[0] = lambda.c0, g.lam[1] = lambda.c1;
-            g.lbits = std::min(nvars[i] - jj - 1, TL_LOW);
-            g.block0 = block0;
+            g.lbits = tl_low_bits(nvars[i] - jj - 1);
             g.nblocks = (int)std::min<uint64_t>(blocks_for(g.n), g.n >> g.lbits);
-            g.part0 = block0;
-            block0 += g.nblocks;
             launches[j].push_back(g);
             owners[j].push_back({i, jj});
         }
+        // one kernel per kind and mode: the round's segments grouped by key, blocks numbered
+        // within each group (the groups run one after another and share partials and counters)
+        {
+            std::vector<size_t> order(launches[j].size());
+            for (size_t q = 0; q < order.size(); q++) order[q] = q;
+            std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+                return tl_key(launches[j][x].kind, launches[j][x].mode) < tl_key(launches[j][y].kind, launches[j][y].mode);
+            });
+            std::vector<TlSeg> segs2;
+            std::vector<std::pair<int, int>> own2;
+            for (size_t q : order) segs2.push_back(launches[j][q]), own2.push_back(owners[j][q]);
+            launches[j].swap(segs2);
+            owners[j].swap(own2);
+            for (size_t q = 0; q < launches[j].size(); q++) {
+                TlSeg& g = launches[j][q];
+                if (q == 0 || tl_key(g.kind, g.mode) != tl_key(launches[j][q - 1].kind, launches[j][q - 1].mode))
+                    block0 = 0;
+                g.block0 = g.part0 = block0;
+                block0 += g.nblocks;
+                max_blocks = std::max(max_blocks, (size_t)block0);
+            }
+        }
         total_segs += launches[j].size();
         max_segs = std::max(max_segs, launches[j].size());
-        max_blocks = std::max(max_blocks, (size_t)block0);
     }
+    // the tail: the last rounds, from the first whose segments all have at most TL_TAIL_PAIRS pairs,
+    // run in one block (each segment one block's work)
+    int j0 = std::max(n_max, 1);
+    for (int j = (int)launches.size() - 1; j >= 0; j--) {
+        uint64_t most = 0;
+        for (const TlSeg& g : launches[j]) most = std::max(most, g.n);
+        if (most > TL_TAIL_PAIRS) break;
+        j0 = j;
+    }
+    size_t tail_seg0 = 0;
+    for (int j = 0; j < j0 && j < (int)launches.size(); j++) tail_seg0 += launches[j].size();
+    for (int j = j0; j < (int)launches.size(); j++)
+        for (TlSeg& g : launches[j]) g.nblocks = 1, g.block0 = g.part0 = 0;
+    const int tail_rounds = n_max > 0 ? n_max - j0 : 0;
+    const size_t off_tail = ar.take(sizeof(TlTail));
+    const size_t off_tail_first = ar.take(4 * ((size_t)tail_rounds + 1));
+    const size_t off_tail_one = ar.take((size_t)tail_rounds + 1);
     const size_t off_segs = ar.take(sizeof(TlSeg) * std::max<size_t>(total_segs, 1));
     const size_t off_finals = ar.take(sizeof(TlFinal) * 4 * np);
     const size_t off_partials = ar.take(max_blocks * 64);
@@ -912,7 +1113,7 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         }
         const uint64_t* dpt = ar.at<uint64_t>(off_point[i]);
         for (int jj = 0; jj < nvars[i]; jj++) {  // round jj's weights over p[jj+1 ..]
-            const int rem = nvars[i] - jj - 1, nl = std::min(rem, TL_LOW), nh = rem - nl;
+            const int rem = nvars[i] - jj - 1, nl = tl_low_bits(rem), nh = rem - nl;
             ulonglong2* base = ar.at<ulonglong2>(off_eq[i]);
             eqjobs.push_back({dpt + 2 * (jj + 1), nl, base + eqtab[i][jj].first, 1ull << nl});
             eqjobs.push_back({dpt + 2 * (jj + 1 + nl), nh, base + eqtab[i][jj].second, 1ull << nh});
@@ -981,6 +1182,31 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
     context_key("transcript-absorb", keys.absorb);
     context_key("transcript-squeeze", keys.squeeze);
     context_key("transcript-ratchet", keys.ratchet);
+    if (tail_rounds > 0) {
+        TlTail tl;
+        memset(&tl, 0, sizeof tl);
+        tl.jb = jb;
+        tl.keys = keys;
+        tl.st = ar.at<FsState>(off_fs);
+        tl.trees = ar.at<TlTree>(off_trees);
+        tl.q = ar.at<ulonglong2>(off_q);
+        tl.rounds_out = ar.at<uint64_t>(off_rounds);
+        tl.chal_out = ar.at<uint64_t>(off_chal);
+        tl.segs = ar.at<TlSeg>(off_segs) + tail_seg0;
+        tl.first = ar.at<int>(off_tail_first);
+        tl.one = ar.at<uint8_t>(off_tail_one);
+        tl.ntrees = np;
+        tl.j0 = j0;
+        tl.rounds = tail_rounds;
+        memcpy(host_at(off_tail), &tl, sizeof tl);
+        int* first = (int*)host_at(off_tail_first);
+        uint8_t* onef = host_at(off_tail_one);
+        first[0] = 0;
+        for (int t2 = 0; t2 < tail_rounds; t2++) {
+            first[t2 + 1] = first[t2] + (int)launches[j0 + t2].size();
+            onef[t2] = (uint8_t)one[j0 + t2];
+        }
+    }
 
     std::vector<uint64_t> rounds((size_t)std::max(n_max, 1) * 6), chal((size_t)std::max(n_max, 1) * 2),
         fevals(8 * (size_t)np);
@@ -996,33 +1222,42 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         size_t seg0 = 0;
         auto run = [&](int j) -> int {
             const auto& L0 = launches[j];
-            if (L0.empty()) return TG_OK;
-            int blocks = 0;
-            for (const TlSeg& g : L0) blocks += g.nblocks;
-            uint64_t units = 0;
-            for (const TlSeg& g : L0) units += g.n;
-            Launch L(d, s, "tree_level_round", 1, units);
-            if (one[j])
-                tl_rounds<true><<<blocks, TL_THREADS, 0, s>>>(ar.at<TlSeg>(off_segs) + seg0, (int)L0.size(),
-                                                              ar.at<uint64_t>(off_partials), ar.at<unsigned>(off_counters));
-            else
-                tl_rounds<false><<<blocks, TL_THREADS, 0, s>>>(ar.at<TlSeg>(off_segs) + seg0, (int)L0.size(),
-                                                               ar.at<uint64_t>(off_partials), ar.at<unsigned>(off_counters));
+            size_t q0 = 0;
+            while (q0 < L0.size()) {  // one launch per group of one key
+                const int key = tl_key(L0[q0].kind, L0[q0].mode);
+                size_t q1 = q0;
+                int blocks = 0;
+                uint64_t units = 0;
+                while (q1 < L0.size() && tl_key(L0[q1].kind, L0[q1].mode) == key) blocks += L0[q1].nblocks, units += L0[q1].n, q1++;
+                Launch L(d, s, "tree_level_round", 1, units);
+                const TlSeg* segs = ar.at<TlSeg>(off_segs) + seg0 + q0;
+                if (one[j])
+                    tl_launch<true>(key, blocks, s, segs, (int)(q1 - q0), ar.at<uint64_t>(off_partials),
+                                    ar.at<unsigned>(off_counters));
+                else
+                    tl_launch<false>(key, blocks, s, segs, (int)(q1 - q0), ar.at<uint64_t>(off_partials),
+                                     ar.at<unsigned>(off_counters));
+                TG_CUDA(cudaGetLastError());
+                q0 = q1;
+            }
             seg0 += L0.size();
-            TG_CUDA(cudaGetLastError());
             return TG_OK;
         };
         TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(off_counters), 0, 4 * max_segs, s));
-        rc = run(0);
-        if (rc) return bail(rc);
-        for (int j = 0; j < n_max; j++) {
-            if (j > 0) {
-                rc = run(j);
-                if (rc) return bail(rc);
-            }
+        for (int j = 0; j < std::min(n_max, j0); j++) {
+            rc = run(j);
+            if (rc) return bail(rc);
             Launch L(d, s, "tree_level_transcript", 1, 1);
             tl_fs<<<1, 32, 0, s>>>(ar.at<FsState>(off_fs), jb, j, keys, ar.at<TlTree>(off_trees), np,
                                    ar.at<ulonglong2>(off_q), ar.at<uint64_t>(off_rounds), ar.at<uint64_t>(off_chal));
+            TG_CUDA(cudaGetLastError());
+        }
+        if (tail_rounds > 0) {
+            uint64_t units = 0;
+            for (int j = j0; j < n_max; j++)
+                for (const TlSeg& g : launches[j]) units += g.n;
+            Launch L(d, s, "tree_level_tail", 1, units);
+            tl_tail<<<1, TL_THREADS, 0, s>>>(ar.at<TlTail>(off_tail));
             TG_CUDA(cudaGetLastError());
         }
         if (!finals.empty()) {

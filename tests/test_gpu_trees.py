@@ -276,12 +276,20 @@ def test_counter_fill(dev):
     assert [int(x) for x in got[:3]] == [counter_value(base + j) for j in range(3)]
 
 
-@pytest.mark.parametrize("s,h", [(4, 8), (0, 11), (7, 3)])
+def eq_at(p, r):
+    out = (1, 0)
+    for a, b in zip(p, r):
+        out = mul(out, add(mul(a, b), mul(sub((1, 0), a), sub((1, 0), b))))
+    return out
+
+
+@pytest.mark.parametrize("s,h", [(4, 8), (0, 11), (7, 3), (6, 9), (2, 14)])
 def test_prime_field_forest_matches_fp2_and_leaf_claim(dev, s, h):
     """A forest of counter leaves proven from prime-field words (read in place on the device) and
-    from Fp2 pairs gives the same records level by level, and the final claim is the leaves' MLE at
-    the final point; a second stage of the same shape, from the device's workspace cache, repeats
-    the proof exactly."""
+    from Fp2 pairs gives the same records level by level; every level passes the verifier's last
+    check (the last round's claim is eq(point, r)·L(r)·R(r), which fails if any round message is
+    wrong); the final claim is the leaves' MLE at the final point; and a second stage of the same
+    shape, from the device's workspace cache, repeats the proof exactly."""
     import torch
 
     from tessera_gb300.hash import Mode, SessionContext, Transcript
@@ -298,6 +306,11 @@ def test_prime_field_forest_matches_fp2_and_leaf_claim(dev, s, h):
             recs = st.prove(t)
             runs.append(([(r.rounds, r.challenges, r.final_evals, r.rho) for r in recs], st.claim(0), t.state))
     assert runs[0] == runs[1] == runs[2]
+    pt = None
+    for k, (rounds, chal, evals, rho) in enumerate(runs[0][0]):
+        pt = list(recs[k].root_challenges) if k == 0 else pt
+        assert recs[k].claims[-1] == mul(eq_at(pt, chal), mul(evals[0], evals[1])), k
+        pt = [rho] + list(chal)
     point, value, own = runs[0][1]
     assert own == h and len(point) == s + h
     assert value == fold_mle([(int(x), 0) for x in host], point)
