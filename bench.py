@@ -586,7 +586,8 @@ def run_logup(args) -> None:
         return time.perf_counter() - start
 
     for _ in range(args.warmup):
-        one(min(args.lookups_log, 20), None)
+        one(args.lookups_log, None)
+        one(args.rows_log, 0x6D756C)
     times = {"lookup": [], "table": []}
     dev.profile(True)
     for _ in range(args.steps):
@@ -753,13 +754,13 @@ def main():
                     help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain; "
                          "serve: the proof server against one-at-a-time proofs")
     ap.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
-    ap.add_argument("--lookups-log", type=int, default=26, help="logup: log2 of the lookups")
+    ap.add_argument("--lookups-log", type=int, default=30, help="logup: log2 of the lookups")
     ap.add_argument("--cc-log-k", type=int, default=22, help="cc: log2 of the row length")
     ap.add_argument("--forest-trees-log", type=int, default=16, help="forest: log2 of the trees")
     ap.add_argument("--forest-leaves-log", type=int, default=14, help="forest: log2 of each tree's leaves")
     ap.add_argument("--cc-masks", type=int, default=200, help="cc: mask coefficients per row")
     ap.add_argument("--cc-rows", type=int, default=4096, help="cc: rows committed per run")
-    ap.add_argument("--rows-log", type=int, default=20, help="logup: log2 of the table rows")
+    ap.add_argument("--rows-log", type=int, default=24, help="logup: log2 of the table rows")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: mean Poisson arrivals per second")
     ap.add_argument("--slots", type=int, default=8, help="serve: requests in flight at most")
     ap.add_argument("--serve-budget-gib", type=int, default=64, help="serve: HBM budget for admitted requests")

@@ -344,7 +344,8 @@ int tg_leaf_stage_close(tg_leaf_stage *stage);
  * crates/tessera-gpu/src/fraction.rs:61-105): leaf j is (n_j, α − (k_j + β·v_j)) with
  * k_j = counter(key_seed + j), v_j = counter(value_seed + j), counter(c) the SplitMix64 output for
  * state (c + 1)·0x9E3779B97F4A7C15 reduced once below p, and n_j = 1 (unit) or −m_j,
- * m_j = counter(mult_seed + j) mod 2^16. numerators and denominators: count Fp2 each, device. */
+ * m_j = counter(mult_seed + j) mod 2^16. numerators and denominators: count Fp2 each, device
+ * (numerators may be NULL with unit: numerators of 1 need no table). */
 int tg_logup_leaves(tg_device *dev, uint64_t key_seed, uint64_t value_seed, int unit, uint64_t mult_seed,
                     const uint64_t alpha[2], const uint64_t beta[2], size_t count, uint64_t *numerators,
                     uint64_t *denominators);

@@ -66,6 +66,7 @@ int spare_take(Device* d, DevBuf& b, size_t want) {
             b.release();
             b.ptr = it->second;
             b.bytes = it->first;
+            d->spare_bytes -= it->first;
             d->spare.erase(it);
             return TG_OK;
         }
@@ -76,13 +77,17 @@ int spare_take(Device* d, DevBuf& b, size_t want) {
 }
 
 void spare_give(Device* d, DevBuf& b) {
+    bool over = false;
     if (b.ptr && b.owned) {
         std::lock_guard<std::mutex> lock(d->spare_mu);
         d->spare.emplace(b.bytes, b.ptr);
+        d->spare_bytes += b.bytes;
+        over = d->spare_cap && d->spare_bytes > d->spare_cap;
     }
     b.ptr = nullptr;
     b.bytes = 0;
     b.owned = true;
+    if (over) spare_trim(d);
 }
 
 void spare_trim(Device* d) {
@@ -90,6 +95,7 @@ void spare_trim(Device* d) {
     {
         std::lock_guard<std::mutex> lock(d->spare_mu);
         drop.swap(d->spare);
+        d->spare_bytes = 0;
     }
     if (drop.empty()) return;
     for (auto& kv : drop) cudaMemsetAsync(kv.second, 0, kv.first, d->stream);
@@ -252,6 +258,7 @@ int tg_device_open(int ordinal, const tg_config* cfg, tg_device** out) {
     }
     d->sm_count = prop.multiProcessorCount;
     d->smem_optin = prop.sharedMemPerBlockOptin;
+    d->spare_cap = prop.totalGlobalMem / 2;
     *out = reinterpret_cast<tg_device*>(d);
     return TG_OK;
 }

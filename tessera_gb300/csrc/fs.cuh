@@ -82,7 +82,9 @@ static __device__ __forceinline__ void compress_quad(uint32_t cv[8], const uint3
     const int i = threadIdx.x & 3;
     const uint32_t iv[4] = {TG_B3_IV0, TG_B3_IV1, TG_B3_IV2, TG_B3_IV3};
     uint32_t a = cv[i], b = cv[4 + i], c = iv[i], d = i < 2 ? 0u : i == 2 ? len : flags;
-#pragma unroll
+    // rolled: the schedule's words are lane-dependent lookups either way, and one round's code stays
+    // in the instruction cache of a warp that runs alone
+#pragma unroll 1
     for (int r = 0; r < 7; r++) {
         b3_g(a, b, c, d, m[kB3Sched[r][2 * i]], m[kB3Sched[r][2 * i + 1]]);
         b = __shfl_sync(0xFFFFFFFFu, b, (i + 1) & 3, 4);
@@ -101,8 +103,9 @@ static __device__ __forceinline__ void compress_quad(uint32_t cv[8], const uint3
     }
 }
 
-// fs_hash by a whole warp; the caller has zeroed buf from len to the next block boundary.
-static __device__ void fs_hash_warp(const uint32_t key[8], const uint32_t* buf, uint32_t len, uint32_t out[8]) {
+// fs_hash by a whole warp; the caller has zeroed buf from len to the next block boundary (one copy
+// of the code for the absorb, squeeze and ratchet calls).
+static __device__ __noinline__ void fs_hash_warp(const uint32_t key[8], const uint32_t* buf, uint32_t len, uint32_t out[8]) {
     const uint32_t nb = len == 0 ? 1 : (len + 63) / 64;
     uint32_t h[8];
 #pragma unroll

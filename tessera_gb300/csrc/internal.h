@@ -87,11 +87,13 @@ struct Device {
     std::mutex prof_mu;
     std::vector<ProfRec> prof;
     std::vector<cudaEvent_t> event_pool;
-    // Workspace memory released by leaf stages (levels, bound tables), kept for the next stage as
-    // a prover pools its device memory: a stage takes the smallest spare buffer that fits before
-    // it allocates, and what the next stage's open leaves untaken goes back to the driver (zeroed).
+    // Workspace memory released by leaf stages (levels, bound tables), kept for later stages as a
+    // prover pools its device memory: a stage takes the smallest spare buffer that fits before it
+    // allocates. The cache goes back to the driver (zeroed) when it would pass spare_cap bytes
+    // (half the device's memory), when an allocation fails, and on tg_device_trim.
     std::mutex spare_mu;
     std::multimap<size_t, void*> spare;
+    size_t spare_bytes = 0, spare_cap = 0;
     // Returns the tables for (lgn, lgk), building them on first use.
     int get_tables(uint32_t lgn, uint32_t lgk, const Tables** out);
 };

@@ -93,6 +93,7 @@ __global__ void tr_logup_leaves(uint64_t key_seed, uint64_t value_seed, uint64_t
         const uint64_t k = counter_value(key_seed + j), v = counter_value(value_seed + j);
         const fp2 d = {sub(sub(alpha.c0, k), mul(beta.c0, v)), sub(alpha.c1, mul(beta.c1, v))};
         d_out[j] = make_ulonglong2(d.c0, d.c1);
+        if (!n_out) continue;  // numerators of 1, not stored
         uint64_t nn = 1;
         if (!unit) {
             const uint64_t m = counter_value(mult_seed + j) & 0xFFFF;
@@ -528,7 +529,7 @@ __device__ void tl_quad(const TlTree& T, int jj, const ulonglong2* q, fp2& a, fp
 // <prefix>/r/j; then each tree in its own rounds takes Q_i ← q_i(r_j) and C_i ← C_i·eq1(p_i[j'], r_j).
 // One warp runs it (sbuf: FS_BUF_WORDS of shared memory).
 __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& keys, TlTree* trees, int ntrees,
-                            const ulonglong2* q, uint64_t* rounds_out, uint64_t* chal_out, uint32_t* sbuf) {
+                            ulonglong2* q, uint64_t* rounds_out, uint64_t* chal_out, uint32_t* sbuf) {
     const int lane = threadIdx.x & 31;
     fp2 msg[3] = {{0, 0}, {0, 0}, {0, 0}};
     for (int i = 0; i < ntrees; i++) {  // every lane forms the message (the same reads)
@@ -536,18 +537,23 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
         const fp2 w = {T.w[0], T.w[1]};
         const int jj = j - T.pad;
         if (jj < 0) {
-            const fp2 v = e_mul(w, e_scale(fp2{T.S[0], T.S[1]}, (1ull << (T.pad - j - 1)) % P));
+            const fp2 ws = e_mul(w, fp2{T.S[0], T.S[1]});
+            const fp2 v = {mul_pow2_lt64(ws.c0, T.pad - j - 1), mul_pow2_lt64(ws.c1, T.pad - j - 1)};
             for (int x = 0; x < 3; x++) msg[x] = e_add(msg[x], v);
         } else {
             fp2 a, b, c;
             tl_quad(T, jj, q + 4 * i, a, b, c);
+            if (lane == 0) q[4 * i + 3] = make_ulonglong2(b.c0, b.c1);  // for the update after the challenge
             const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
             const fp2 wc = e_mul(w, fp2{T.C[0], T.C[1]});
-            const fp2 q2 = e_add(a, e_add(e_scale(b, 2), e_scale(c, 4)));
-            const fp2 q3 = e_add(a, e_add(e_scale(b, 3), e_scale(c, 9)));
-            msg[0] = e_add(msg[0], e_mul(wc, e_mul(eq1(t, fp2{0, 0}), a)));
-            msg[1] = e_add(msg[1], e_mul(wc, e_mul(eq1(t, fp2{2, 0}), q2)));
-            msg[2] = e_add(msg[2], e_mul(wc, e_mul(eq1(t, fp2{3, 0}), q3)));
+            // q(2) = a + 2b + 4c, q(3) = a + 3b + 9c; eq1(t, X) at 0, 2, 3: 1 − t, 3t − 1, 5t − 2
+            const fp2 b2 = e_add(b, b), c2 = e_add(c, c), c4 = e_add(c2, c2), c8 = e_add(c4, c4);
+            const fp2 q2 = e_add(a, e_add(b2, c4)), q3 = e_add(e_add(a, e_add(b2, b)), e_add(c8, c));
+            const fp2 t2 = e_add(t, t), t3 = e_add(t2, t), t5 = e_add(t3, t2);
+            const fp2 e0 = e_sub(fp2{1, 0}, t), e2 = e_sub(t3, fp2{1, 0}), e3 = e_sub(t5, fp2{2, 0});
+            msg[0] = e_add(msg[0], e_mul(wc, e_mul(e0, a)));
+            msg[1] = e_add(msg[1], e_mul(wc, e_mul(e2, q2)));
+            msg[2] = e_add(msg[2], e_mul(wc, e_mul(e3, q3)));
         }
     }
     uint32_t state[8];
@@ -584,16 +590,17 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
         TlTree& T = trees[i];
         const int jj = j - T.pad;
         if (jj < 0) continue;
-        fp2 a, b, c;
-        tl_quad(T, jj, q + 4 * i, a, b, c);
+        const fp2 a = ld2(q + 4 * i), b = ld2(q + 4 * i + 3), c = ld2(q + 4 * i + 2);  // b as the message pass left it
         const fp2 Q = e_add(a, e_mul(r, e_add(b, e_mul(r, c))));
-        const fp2 C = e_mul(fp2{T.C[0], T.C[1]}, eq1(fp2{T.point[2 * jj], T.point[2 * jj + 1]}, r));
+        const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
+        const fp2 tr = e_mul(t, r);  // eq1(t, r) = 1 − t − r + 2·t·r
+        const fp2 C = e_mul(fp2{T.C[0], T.C[1]}, e_add(e_sub(e_sub(fp2{1, 0}, t), r), e_add(tr, tr)));
         T.Q[0] = Q.c0, T.Q[1] = Q.c1;
         T.C[0] = C.c0, T.C[1] = C.c1;
     }
 }
 
-__global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, int ntrees, const ulonglong2* q,
+__global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, int ntrees, ulonglong2* q,
                       uint64_t* rounds_out, uint64_t* chal_out) {
     __shared__ uint32_t sbuf[FS_BUF_WORDS];
     tl_fs_round(st, jb, j, keys, trees, ntrees, q, rounds_out, chal_out, sbuf);
@@ -627,7 +634,7 @@ struct TlTail {
     FsKeys keys;
     FsState* st;
     TlTree* trees;
-    const ulonglong2* q;
+    ulonglong2* q;
     uint64_t* rounds_out;
     uint64_t* chal_out;
     const TlSeg* segs;     // the tail rounds' segments, in round order (one block each: nblocks = 1)
@@ -822,7 +829,6 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
                 if (rc) return bail(rc);
             }
     }
-    spare_trim(d);  // what this stage did not reuse
     *out = st;
     return TG_OK;
 }
@@ -1381,7 +1387,7 @@ extern "C" int tg_logup_leaves(tg_device* dev, uint64_t key_seed, uint64_t value
                                const uint64_t alpha[2], const uint64_t beta[2], size_t count, uint64_t* numerators,
                                uint64_t* denominators) {
     Device* d = reinterpret_cast<Device*>(dev);
-    if (!d || !alpha || !beta || (count && (!numerators || !denominators)))
+    if (!d || !alpha || !beta || (count && (!denominators || (!numerators && !unit))))
         return fail(TG_ERR_INVALID, "tg_logup_leaves: null argument");
     if (count == 0) return TG_OK;
     cudaStream_t s = d->stream;

@@ -184,16 +184,18 @@ def prove_forests(transcript: Transcript, forests: list[Forest], device: Device 
 def generated_fraction(height: int, key_seed: int, value_seed: int, mult_seed: int | None, alpha, beta,
                        device: Device | None = None) -> Fraction:
     """A fraction tree of 2^height generated leaves on the device (the reference benchmark's LogUp
-    inputs): leaf j is (1 or −m_j, α − (k_j + β·v_j)) from the counter generator."""
+    inputs): leaf j is (1 or −m_j, α − (k_j + β·v_j)) from the counter generator; numerators of 1
+    (no mult_seed) are not stored."""
     import torch
 
     d = resolve(device)
     count = 1 << height
-    num = torch.empty(2 * count, dtype=torch.int64, device=f"cuda:{d.ordinal}")
+    unit = mult_seed is None
+    num = None if unit else torch.empty(2 * count, dtype=torch.int64, device=f"cuda:{d.ordinal}")
     den = torch.empty(2 * count, dtype=torch.int64, device=f"cuda:{d.ordinal}")
     torch.cuda.current_stream().synchronize()
     a = (ctypes.c_uint64 * 2)(*alpha)
     b = (ctypes.c_uint64 * 2)(*beta)
-    N.call("tg_logup_leaves", d.handle, key_seed, value_seed, int(mult_seed is None), mult_seed or 0, a, b, count,
-           num.data_ptr(), den.data_ptr())
+    N.call("tg_logup_leaves", d.handle, key_seed, value_seed, int(unit), mult_seed or 0, a, b, count,
+           None if unit else num.data_ptr(), den.data_ptr())
     return Fraction(den, num)

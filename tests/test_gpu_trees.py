@@ -238,7 +238,8 @@ def test_generated_leaves_and_leaf_claims(dev, unit):
     h, ks, vs, ms = 9, 1000, 2000000, 77
     alpha, beta = (123456789, 987654321), (55555, 4444444)
     tree = generated_fraction(h, ks, vs, None if unit else ms, alpha, beta, dev)
-    n = tree.numerators.cpu().numpy().view(np.uint64)
+    assert (tree.numerators is None) == unit
+    n = np.tile(np.array([1, 0], dtype=np.uint64), 1 << h) if unit else tree.numerators.cpu().numpy().view(np.uint64)
     d = tree.denominators.cpu().numpy().view(np.uint64)
     for j in range(1 << h):
         k, v = counter_value(ks + j), counter_value(vs + j)
