@@ -524,11 +524,27 @@ int tg_commit_unmasked(tg_device* dev, uint32_t log_k, uint32_t log_inv_rate, ui
         const int b = (int)(c & 1);
         uint64_t* half = stage + b * chunk * k;
         TG_CUDA(cudaStreamWaitEvent(cs, d->consumed[b], 0));
-        TG_CUDA(cudaMemcpyAsync(half, rows + r0 * k, g * k * 8, cudaMemcpyHostToDevice, cs));
-        TG_CUDA(cudaEventRecord(d->staged[b], cs));
-        TG_CUDA(cudaStreamWaitEvent(s, d->staged[b], 0));
-        rc = lde_encode(d, log_k, log_inv_rate, 0, half, g, nullptr, cw, s);
-        if (rc) return rc;
+        if (c == 0 && g >= 2) {
+            // the first chunk's copy has nothing to hide behind: its first half is encoded while
+            // the second half is still in flight
+            const size_t g0 = g / 2;
+            TG_CUDA(cudaMemcpyAsync(half, rows, g0 * k * 8, cudaMemcpyHostToDevice, cs));
+            TG_CUDA(cudaEventRecord(d->staged[1], cs));  // staged[1] is free until chunk 1
+            TG_CUDA(cudaMemcpyAsync(half + g0 * k, rows + g0 * k, (g - g0) * k * 8, cudaMemcpyHostToDevice, cs));
+            TG_CUDA(cudaEventRecord(d->staged[0], cs));
+            TG_CUDA(cudaStreamWaitEvent(s, d->staged[1], 0));
+            rc = lde_encode(d, log_k, log_inv_rate, 0, half, g0, nullptr, cw, s);
+            if (rc) return rc;
+            TG_CUDA(cudaStreamWaitEvent(s, d->staged[0], 0));
+            rc = lde_encode(d, log_k, log_inv_rate, 0, half + g0 * k, g - g0, nullptr, cw + g0 * n, s);
+            if (rc) return rc;
+        } else {
+            TG_CUDA(cudaMemcpyAsync(half, rows + r0 * k, g * k * 8, cudaMemcpyHostToDevice, cs));
+            TG_CUDA(cudaEventRecord(d->staged[b], cs));
+            TG_CUDA(cudaStreamWaitEvent(s, d->staged[b], 0));
+            rc = lde_encode(d, log_k, log_inv_rate, 0, half, g, nullptr, cw, s);
+            if (rc) return rc;
+        }
         TG_CUDA(cudaEventRecord(d->consumed[b], s));
         rc = column_absorb(d, nodes, n, cw, n, g, row_block, s);
         if (rc) return rc;

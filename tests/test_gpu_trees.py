@@ -316,3 +316,29 @@ def test_prime_field_forest_matches_fp2_and_leaf_claim(dev, s, h):
     assert own == h and len(point) == s + h
     assert value == fold_mle([(int(x), 0) for x in host], point)
     dev.trim()
+
+
+def test_unaligned_device_leaves_are_copied(dev):
+    """Prime-field leaves at an address that is not 16-byte aligned (a view one word into a
+    tensor) cannot be read in place as word pairs: the stage copies them, and the proof equals the
+    one from aligned leaves."""
+    import torch
+
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.trees import Forest, LeafStage
+    from tessera_gb300.workloads import fill_counter
+
+    s, h = 3, 7
+    ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([3]) * 32, bytes([4]) * 16)
+    aligned = fill_counter(torch.empty(1 << (s + h), dtype=torch.int64, device="cuda"), 5, dev)
+    backing = torch.zeros((1 << (s + h)) + 1, dtype=torch.int64, device="cuda")
+    shifted = backing[1:]
+    shifted.copy_(aligned)
+    assert shifted.data_ptr() % 16 == 8
+    out = []
+    for leaves in (aligned, shifted):
+        t = Transcript(ctx)
+        with LeafStage([Forest(s, leaves, True)], dev) as st:
+            recs = st.prove(t)
+            out.append(([(r.rounds, r.final_evals) for r in recs], st.claim(0), t.state))
+    assert out[0] == out[1]
