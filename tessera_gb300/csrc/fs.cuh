@@ -78,13 +78,14 @@ static __device__ __forceinline__ void b3_g(uint32_t& a, uint32_t& b, uint32_t& 
     TG_B3_G(a, b, c, d, x, y)
 }
 
+// ROLLED keeps one round's code (the schedule's words are lane-dependent lookups either way): for a
+// warp that runs alone on its SM, whose unrolled rounds would miss in the instruction cache.
+template <bool ROLLED>
 static __device__ __forceinline__ void compress_quad(uint32_t cv[8], const uint32_t* m, uint32_t len, uint32_t flags) {
     const int i = threadIdx.x & 3;
     const uint32_t iv[4] = {TG_B3_IV0, TG_B3_IV1, TG_B3_IV2, TG_B3_IV3};
     uint32_t a = cv[i], b = cv[4 + i], c = iv[i], d = i < 2 ? 0u : i == 2 ? len : flags;
-    // rolled: the schedule's words are lane-dependent lookups either way, and one round's code stays
-    // in the instruction cache of a warp that runs alone
-#pragma unroll 1
+#pragma unroll(ROLLED ? 1 : 7)
     for (int r = 0; r < 7; r++) {
         b3_g(a, b, c, d, m[kB3Sched[r][2 * i]], m[kB3Sched[r][2 * i + 1]]);
         b = __shfl_sync(0xFFFFFFFFu, b, (i + 1) & 3, 4);
@@ -105,6 +106,7 @@ static __device__ __forceinline__ void compress_quad(uint32_t cv[8], const uint3
 
 // fs_hash by a whole warp; the caller has zeroed buf from len to the next block boundary (one copy
 // of the code for the absorb, squeeze and ratchet calls).
+template <bool ROLLED>
 static __device__ __noinline__ void fs_hash_warp(const uint32_t key[8], const uint32_t* buf, uint32_t len, uint32_t out[8]) {
     const uint32_t nb = len == 0 ? 1 : (len + 63) / 64;
     uint32_t h[8];
@@ -112,7 +114,7 @@ static __device__ __noinline__ void fs_hash_warp(const uint32_t key[8], const ui
     for (int i = 0; i < 8; i++) h[i] = key[i];
     for (uint32_t b = 0; b < nb; b++) {
         const bool last = b + 1 == nb;
-        compress_quad(h, buf + 16 * b, last ? len - 64 * b : 64,
+        compress_quad<ROLLED>(h, buf + 16 * b, last ? len - 64 * b : 64,
                       b3::DERIVE_KEY_MATERIAL | (b == 0 ? b3::CHUNK_START : 0) | (last ? (b3::CHUNK_END | b3::ROOT) : 0));
     }
 #pragma unroll
@@ -153,12 +155,13 @@ static __device__ uint32_t fs_begin(const uint32_t state[8], const FsJob& jb, co
 // label length ‖ <prefix>/round/j ‖ message, len bytes) into buf; every lane absorbs it, then
 // squeezes <prefix>/r/j until the first two words are a canonical Fp2 (c0, c1). state and counter
 // are the same in every lane. False after FS_MAX_TRIES squeezes.
+template <bool ROLLED = false>
 static __device__ bool fs_round_warp(const FsKeys& keys, const FsJob& jb, int j, uint32_t* buf, uint32_t len,
                                      uint32_t state[8], uint64_t* counter, uint64_t* c0, uint64_t* c1) {
     const int lane = threadIdx.x & 31;
     if (lane == 0) zero_to_block(buf, len);
     __syncwarp();
-    fs_hash_warp(keys.absorb, buf, len, state);
+    fs_hash_warp<ROLLED>(keys.absorb, buf, len, state);
     __syncwarp();
     for (int tries = 0; tries < FS_MAX_TRIES; tries++) {
         uint32_t l2 = 0;
@@ -170,13 +173,13 @@ static __device__ bool fs_round_warp(const FsKeys& keys, const FsJob& jb, int j,
         l2 = __shfl_sync(0xFFFFFFFFu, l2, 0);
         __syncwarp();
         uint32_t out[8];
-        fs_hash_warp(keys.squeeze, buf, l2 + 8, out);
+        fs_hash_warp<ROLLED>(keys.squeeze, buf, l2 + 8, out);
         __syncwarp();
         *counter += 1;
         if (lane == 0)
             for (int i = 0; i < 8; i++) buf[i] = state[i], buf[8 + i] = out[i];
         __syncwarp();
-        fs_hash_warp(keys.ratchet, buf, 64, state);
+        fs_hash_warp<ROLLED>(keys.ratchet, buf, 64, state);
         __syncwarp();
         *c0 = (uint64_t)out[0] | ((uint64_t)out[1] << 32);
         *c1 = (uint64_t)out[2] | ((uint64_t)out[3] << 32);

@@ -392,9 +392,15 @@ __device__ __forceinline__ void tl_block_sum(uint64_t (&words)[6], uint64_t (*re
 
 // One round's segments of one kind and mode: each block sums its share of its segment, and the
 // segment's last block adds the blocks' rows into the segment's q.
+// Resident blocks per SM a variant's registers allow: three for the prime-field sums, two else.
+template <int MODE>
+__host__ __device__ constexpr int tl_min_blocks() {
+    return MODE == TL_SUM_BASE ? 3 : 2;
+}
+
 template <int NT, int KIND, int MODE, bool ONE>
-__global__ void __launch_bounds__(TL_THREADS, 2) tl_rounds(const TlSeg* segs, int nseg, uint64_t* partials,
-                                                           unsigned* counters) {
+__global__ void __launch_bounds__(TL_THREADS, tl_min_blocks<MODE>()) tl_rounds(const TlSeg* segs, int nseg,
+                                                                              uint64_t* partials, unsigned* counters) {
     __shared__ TlSeg g;
     __shared__ int si;
     __shared__ uint64_t red[TL_THREADS / 32][6];
@@ -575,7 +581,7 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
     }
     len = __shfl_sync(0xFFFFFFFFu, len, 0);
     uint64_t c0, c1;
-    const bool ok = fs_round_warp(keys, jb, j, sbuf, len, state, &counter, &c0, &c1);
+    const bool ok = fs_round_warp<true>(keys, jb, j, sbuf, len, state, &counter, &c0, &c1);
     if (lane != 0) return;
     if (!ok) {
         st->err = 1;
