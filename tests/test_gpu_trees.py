@@ -227,15 +227,17 @@ def counter_value(c):
     return z - P if z >= P else z
 
 
-@pytest.mark.parametrize("unit", [True, False])
-def test_generated_leaves_and_leaf_claims(dev, unit):
-    """Generated LogUp leaves equal the counter generator's on the host, and after every level of
-    the tree the final claims are the leaves' numerators' and denominators' MLEs at the final point
-    (the verifier's leaf check, a size-independent property of an honest proof)."""
+@pytest.mark.parametrize("unit,h", [(True, 9), (False, 9), (True, 14), (False, 17)])
+def test_generated_leaves_and_leaf_claims(dev, unit, h):
+    """Generated LogUp leaves equal the counter generator's on the host; every level passes the
+    verifier's last check (its last claim is eq(point, r)·(N0·D1 + N1·D0 + λ·D0·D1) at the final
+    evaluations, which fails if any round message is wrong); and after the last level the final
+    claims are the leaves' numerators' and denominators' MLEs at the final point (the verifier's
+    leaf check). Heights past 12 run launched rounds as well as each level's single-block tail."""
     from tessera_gb300.hash import Mode, SessionContext, Transcript
     from tessera_gb300.trees import LeafStage, generated_fraction
 
-    h, ks, vs, ms = 9, 1000, 2000000, 77
+    ks, vs, ms = 1000, 2000000, 77
     alpha, beta = (123456789, 987654321), (55555, 4444444)
     tree = generated_fraction(h, ks, vs, None if unit else ms, alpha, beta, dev)
     assert (tree.numerators is None) == unit
@@ -248,12 +250,18 @@ def test_generated_leaves_and_leaf_claims(dev, unit):
         assert (int(n[2 * j]), int(n[2 * j + 1])) == ((1, 0) if unit else ((P - m) % P, 0))
     t = Transcript(SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes(32), bytes(16)))
     with LeafStage([tree], dev) as st:
-        st.prove(t)
+        recs = st.prove(t)
         point, (p, q), own = st.claim(0)
     assert own == h and len(point) == h
+    pt = []
+    for rec in recs:
+        n0, n1, d0, d1 = rec.final_evals
+        g = add(add(mul(n0, d1), mul(n1, d0)), mul(rec.lambda_, mul(d0, d1)))
+        assert rec.claims[-1] == mul(eq_at(pt, rec.challenges), g), rec.prefix
+        pt = [rec.rho] + list(rec.challenges)
     nums = [(int(n[2 * j]), int(n[2 * j + 1])) for j in range(1 << h)]
     dens = [(int(d[2 * j]), int(d[2 * j + 1])) for j in range(1 << h)]
-    assert (p, q) == (mle(nums, point), mle(dens, point))
+    assert (p, q) == (fold_mle(nums, point), fold_mle(dens, point))
 
 
 def fold_mle(values, point):
