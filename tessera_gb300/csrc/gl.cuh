@@ -220,4 +220,15 @@ __device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) {
 __device__ __forceinline__ uint64_t canon(uint64_t x) { return x >= P ? x - P : x; }
 
 }  // namespace lz
+
+// Fp2 on lazy words (any 64-bit representative; canonical only where results leave a kernel).
+__device__ __forceinline__ fp2 l2_add(fp2 a, fp2 b) { return {lz::add(a.c0, b.c0), lz::add(a.c1, b.c1)}; }
+__device__ __forceinline__ fp2 l2_sub(fp2 a, fp2 b) { return {lz::sub(a.c0, b.c0), lz::sub(a.c1, b.c1)}; }
+__device__ __forceinline__ fp2 l2_mul(fp2 a, fp2 b) {  // Karatsuba, X^2 = 7
+    const uint64_t t0 = lz::mul(a.c0, b.c0), t1 = lz::mul(a.c1, b.c1);
+    const uint64_t t2 = lz::mul(lz::add(a.c0, a.c1), lz::add(b.c0, b.c1));
+    return {lz::add(t0, lz::sub(lz::mulp2<3>(t1), t1)), lz::sub(lz::sub(t2, t0), t1)};
+}
+__device__ __forceinline__ fp2 l2_scale(fp2 a, uint64_t b) { return {lz::mul(a.c0, b), lz::mul(a.c1, b)}; }
+__device__ __forceinline__ fp2 l2_canon(fp2 a) { return {lz::canon(a.c0), lz::canon(a.c1)}; }
 }  // namespace tg

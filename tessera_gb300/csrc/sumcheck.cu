@@ -71,12 +71,13 @@ __device__ __forceinline__ fp2 load_entry(const uint64_t* t, bool base, uint64_t
     return {v.x, v.y};
 }
 
+// a + r·(b − a) on lazy words (bound tables hold lazy words; the last bind canonicalises).
 __device__ __forceinline__ fp2 bind_pair(fp2 a, fp2 b, fp2 r, bool base) {
     if (base) {  // a, b in the prime field: two base products
-        const uint64_t d = sub(b.c0, a.c0);
-        return {add(a.c0, mul(r.c0, d)), mul(r.c1, d)};
+        const uint64_t d = lz::sub(b.c0, a.c0);
+        return {lz::add(a.c0, lz::mul(r.c0, d)), lz::mul(r.c1, d)};
     }
-    return e_add(a, e_mul(r, e_sub(b, a)));
+    return l2_add(a, l2_mul(r, l2_sub(b, a)));
 }
 
 // Sums NW words across the block (warp shuffles, then one word per warp in shared memory);
@@ -133,13 +134,15 @@ __global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nse
 #pragma unroll
     for (int w = 0; w < 2 * D; w++) words[w] = 0;
 
+    // lazy arithmetic throughout; the sums are canonicalised before they are reduced
     if (g.kind == 1) {
         fp2 acc = {0, 0};
         for (uint64_t x = (uint64_t)lb * blockDim.x + threadIdx.x; x < g.n; x += stride) {
             fp2 prod = {1, 0};
-            for (int k = 0; k < nt; k++) prod = e_mul(prod, load_entry(g.src[k], (g.base_mask >> k) & 1, x));
-            acc = e_add(acc, prod);
+            for (int k = 0; k < nt; k++) prod = l2_mul(prod, load_entry(g.src[k], (g.base_mask >> k) & 1, x));
+            acc = l2_add(acc, prod);
         }
+        acc = l2_canon(acc);
         words[0] = acc.c0;
         words[1] = acc.c1;
     } else if (!g.bind && g.base_mask == (1u << nt) - 1) {
@@ -153,22 +156,22 @@ __global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nse
             for (int d = 0; d < D; d++) prod[d] = 1;
             for (int k = 0; k < nt; k++) {
                 const ulonglong2 v = reinterpret_cast<const ulonglong2*>(g.src[k])[p];
-                const uint64_t diff = sub(v.y, v.x);
+                const uint64_t diff = lz::sub(v.y, v.x);
                 uint64_t x = v.y;  // value at node 1
-                prod[0] = mul(prod[0], v.x);
+                prod[0] = lz::mul(prod[0], v.x);
 #pragma unroll
                 for (int d = 1; d < D; d++) {  // nodes 2..D
                     if (d < deg) {
-                        x = add(x, diff);
-                        prod[d] = mul(prod[d], x);
+                        x = lz::add(x, diff);
+                        prod[d] = lz::mul(prod[d], x);
                     }
                 }
             }
 #pragma unroll
-            for (int d = 0; d < D; d++) acc[d] = add(acc[d], prod[d]);
+            for (int d = 0; d < D; d++) acc[d] = lz::add(acc[d], prod[d]);
         }
 #pragma unroll
-        for (int d = 0; d < D; d++) words[2 * d] = acc[d];
+        for (int d = 0; d < D; d++) words[2 * d] = lz::canon(acc[d]);
     } else {
         fp2 acc[D];
 #pragma unroll
@@ -191,24 +194,25 @@ __global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nse
                     u = load_entry(g.src[k], base, 2 * p);
                     v = load_entry(g.src[k], base, 2 * p + 1);
                 }
-                const fp2 diff = e_sub(v, u);
+                const fp2 diff = l2_sub(v, u);
                 fp2 x = v;
-                prod[0] = e_mul(prod[0], u);
+                prod[0] = l2_mul(prod[0], u);
 #pragma unroll
                 for (int d = 1; d < D; d++) {
                     if (d < deg) {
-                        x = e_add(x, diff);
-                        prod[d] = e_mul(prod[d], x);
+                        x = l2_add(x, diff);
+                        prod[d] = l2_mul(prod[d], x);
                     }
                 }
             }
 #pragma unroll
-            for (int d = 0; d < D; d++) acc[d] = e_add(acc[d], prod[d]);
+            for (int d = 0; d < D; d++) acc[d] = l2_add(acc[d], prod[d]);
         }
 #pragma unroll
         for (int d = 0; d < D; d++) {
-            words[2 * d] = acc[d].c0;
-            words[2 * d + 1] = acc[d].c1;
+            const fp2 c = l2_canon(acc[d]);
+            words[2 * d] = c.c0;
+            words[2 * d + 1] = c.c1;
         }
     }
     block_sum<2 * D>(words);
@@ -243,7 +247,7 @@ __global__ void sc_bind_last(const BindLast* b, int n) {
     if (i >= n) return;
     const BindLast t = b[i];
     const fp2 r = {t.r[0], t.r[1]};
-    const fp2 u = bind_pair(load_entry(t.src, t.base, 0), load_entry(t.src, t.base, 1), r, t.base);
+    const fp2 u = l2_canon(bind_pair(load_entry(t.src, t.base, 0), load_entry(t.src, t.base, 1), r, t.base));
     reinterpret_cast<ulonglong2*>(t.dst)[0] = make_ulonglong2(u.c0, u.c1);
 }
 

@@ -212,16 +212,6 @@ __device__ __forceinline__ fp2 ld2(const ulonglong2* p) {
     return {v.x, v.y};
 }
 
-// Fp2 on lazy words (any 64-bit representative; canonical only where results leave the kernel).
-__device__ __forceinline__ fp2 l2_add(fp2 a, fp2 b) { return {lz::add(a.c0, b.c0), lz::add(a.c1, b.c1)}; }
-__device__ __forceinline__ fp2 l2_sub(fp2 a, fp2 b) { return {lz::sub(a.c0, b.c0), lz::sub(a.c1, b.c1)}; }
-__device__ __forceinline__ fp2 l2_mul(fp2 a, fp2 b) {  // Karatsuba, X^2 = 7
-    const uint64_t t0 = lz::mul(a.c0, b.c0), t1 = lz::mul(a.c1, b.c1);
-    const uint64_t t2 = lz::mul(lz::add(a.c0, a.c1), lz::add(b.c0, b.c1));
-    return {lz::add(t0, lz::sub(lz::mulp2<3>(t1), t1)), lz::sub(lz::sub(t2, t0), t1)};
-}
-__device__ __forceinline__ fp2 l2_scale(fp2 a, uint64_t b) { return {lz::mul(a.c0, b), lz::mul(a.c1, b)}; }
-__device__ __forceinline__ fp2 l2_canon(fp2 a) { return {lz::canon(a.c0), lz::canon(a.c1)}; }
 
 // g at X = 0, at X = 1 (ONE) and its leading coefficient in X, over one pair whose tables take the
 // values u at X = 0 and slopes d: KIND 0 L·R; 1 N0·D1 + N1·D0 + λ·D0·D1 = N0·D1 + D0·(N1 + λ·D1);
