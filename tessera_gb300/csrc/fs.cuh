@@ -67,11 +67,24 @@ static __device__ void fs_hash(const uint32_t key[8], uint32_t* buf, uint32_t le
 // value.
 
 // Word k of round r's message is m[kB3Sched[r][k]] (the message permutation applied r times).
-static __constant__ uint8_t kB3Sched[7][16] = {
+constexpr uint8_t kB3Sched[7][16] = {
     {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15},  {2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8},
     {3, 4, 10, 12, 13, 2, 7, 14, 6, 5, 9, 0, 11, 15, 8, 1},  {10, 7, 12, 9, 14, 3, 13, 15, 4, 0, 11, 2, 5, 8, 1, 6},
     {12, 13, 9, 11, 15, 10, 14, 8, 7, 2, 5, 3, 0, 1, 6, 4},  {9, 14, 11, 5, 8, 12, 15, 1, 13, 3, 0, 10, 2, 6, 4, 7},
     {11, 15, 5, 0, 1, 9, 8, 6, 14, 10, 2, 12, 3, 4, 7, 13}};
+
+// The four schedule indices lane i of a quad reads in round r (column words 2i, 2i + 1, diagonal
+// words 8 + 2i, 9 + 2i), four bits each; rounds 0–3 in the low word, 4–6 in the high word, so a
+// lane keeps its whole schedule in two registers instead of loading lane-divergent table entries.
+__host__ __device__ constexpr uint64_t b3_lane_sched(int i, int half) {
+    uint64_t v = 0;
+    for (int r = 4 * half; r < 7 && r < 4 * half + 4; r++) {
+        const uint64_t q = (uint64_t)kB3Sched[r][2 * i] | ((uint64_t)kB3Sched[r][2 * i + 1] << 4) |
+                           ((uint64_t)kB3Sched[r][8 + 2 * i] << 8) | ((uint64_t)kB3Sched[r][9 + 2 * i] << 12);
+        v |= q << (16 * (r - 4 * half));
+    }
+    return v;
+}
 
 static __device__ __forceinline__ void b3_g(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d, uint32_t x, uint32_t y) {
     using namespace b3;
@@ -85,13 +98,20 @@ static __device__ __forceinline__ void compress_quad(uint32_t cv[8], const uint3
     const int i = threadIdx.x & 3;
     const uint32_t iv[4] = {TG_B3_IV0, TG_B3_IV1, TG_B3_IV2, TG_B3_IV3};
     uint32_t a = cv[i], b = cv[4 + i], c = iv[i], d = i < 2 ? 0u : i == 2 ? len : flags;
+    constexpr uint64_t L0 = b3_lane_sched(0, 0), L1 = b3_lane_sched(1, 0), L2 = b3_lane_sched(2, 0), L3 = b3_lane_sched(3, 0);
+    constexpr uint64_t H0 = b3_lane_sched(0, 1), H1 = b3_lane_sched(1, 1), H2 = b3_lane_sched(2, 1), H3 = b3_lane_sched(3, 1);
+    uint64_t slo = i == 0 ? L0 : i == 1 ? L1 : i == 2 ? L2 : L3;
+    uint64_t shi = i == 0 ? H0 : i == 1 ? H1 : i == 2 ? H2 : H3;
 #pragma unroll(ROLLED ? 1 : 7)
     for (int r = 0; r < 7; r++) {
-        b3_g(a, b, c, d, m[kB3Sched[r][2 * i]], m[kB3Sched[r][2 * i + 1]]);
+        const uint32_t q = (uint32_t)slo & 0xFFFFu;  // this round's four indices
+        slo = (slo >> 16) | (shi << 48);
+        shi >>= 16;
+        b3_g(a, b, c, d, m[q & 15], m[(q >> 4) & 15]);
         b = __shfl_sync(0xFFFFFFFFu, b, (i + 1) & 3, 4);
         c = __shfl_sync(0xFFFFFFFFu, c, (i + 2) & 3, 4);
         d = __shfl_sync(0xFFFFFFFFu, d, (i + 3) & 3, 4);
-        b3_g(a, b, c, d, m[kB3Sched[r][8 + 2 * i]], m[kB3Sched[r][9 + 2 * i]]);
+        b3_g(a, b, c, d, m[(q >> 8) & 15], m[q >> 12]);
         b = __shfl_sync(0xFFFFFFFFu, b, (i + 3) & 3, 4);
         c = __shfl_sync(0xFFFFFFFFu, c, (i + 2) & 3, 4);
         d = __shfl_sync(0xFFFFFFFFu, d, (i + 1) & 3, 4);
@@ -127,6 +147,13 @@ static __device__ __forceinline__ void zero_to_block(uint32_t* buf, uint32_t len
     for (uint32_t i = len; i < end; i++) bytes[i] = 0;
 }
 
+// zero_to_block by a whole warp (the caller syncs the warp after it).
+static __device__ __forceinline__ void zero_to_block_warp(uint32_t* buf, uint32_t len) {
+    uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
+    const uint32_t end = (len == 0 ? 1 : (len + 63) / 64) * 64;
+    for (uint32_t i = len + (threadIdx.x & 31); i < end; i += 32) bytes[i] = 0;
+}
+
 static __device__ __forceinline__ void put64(uint8_t* p, uint64_t v) {
     for (int i = 0; i < 8; i++) p[i] = (uint8_t)(v >> (8 * i));
 }
@@ -159,7 +186,7 @@ template <bool ROLLED = false>
 static __device__ bool fs_round_warp(const FsKeys& keys, const FsJob& jb, int j, uint32_t* buf, uint32_t len,
                                      uint32_t state[8], uint64_t* counter, uint64_t* c0, uint64_t* c1) {
     const int lane = threadIdx.x & 31;
-    if (lane == 0) zero_to_block(buf, len);
+    zero_to_block_warp(buf, len);
     __syncwarp();
     fs_hash_warp<ROLLED>(keys.absorb, buf, len, state);
     __syncwarp();
@@ -168,9 +195,10 @@ static __device__ bool fs_round_warp(const FsKeys& keys, const FsJob& jb, int j,
         if (lane == 0) {
             l2 = fs_begin(state, jb, "/r/", j, buf);
             put64(reinterpret_cast<uint8_t*>(buf) + l2, *counter);
-            zero_to_block(buf, l2 + 8);
         }
         l2 = __shfl_sync(0xFFFFFFFFu, l2, 0);
+        __syncwarp();
+        zero_to_block_warp(buf, l2 + 8);
         __syncwarp();
         uint32_t out[8];
         fs_hash_warp<ROLLED>(keys.squeeze, buf, l2 + 8, out);

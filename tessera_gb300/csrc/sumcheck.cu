@@ -38,6 +38,9 @@ constexpr int SC_MAX_DEGREE = 7;
 constexpr int SC_THREADS = 256;
 constexpr int SC_MAX_SEG_BLOCKS = 1024;
 constexpr int SC_MSG_WORDS = 2 * SC_MAX_DEGREE;  // one instance's round sums, as Fp2 words
+// The last rounds run in one block (sc_tail) from the first whose segments hold this many pairs in
+// all, when every job has a warp of that block for its transcript.
+constexpr uint64_t SC_TAIL_PAIRS = 4096;
 
 // One instance's share of one launch.
 struct Seg {
@@ -101,36 +104,12 @@ __device__ __forceinline__ void block_sum(uint64_t (&v)[NW]) {
     __syncthreads();
 }
 
-// One launch of round sums (and product sums) over all segments: a block finds its segment, runs
-// a grid-stride loop over the segment's pairs, and the segment's last block to finish reduces the
-// segment's partial rows into seg.out.
+// Block lb's share of a segment's sums (a grid-stride loop over the segment's nblocks blocks),
+// canonical, in this thread's words: the d node sums as Fp2 words (kind 0), or the product sum.
 template <int D>
-__global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nseg, uint64_t* partials,
-                                                        unsigned* counters) {
-    __shared__ Seg g;
-    __shared__ int si;
-    if (threadIdx.x == 0) {
-        int lo = 0, hi = nseg - 1;
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) / 2;
-            if (segs[mid].block0 <= (int)blockIdx.x)
-                lo = mid;
-            else
-                hi = mid - 1;
-        }
-        si = lo;
-    }
-    __syncthreads();
-    {
-        const uint64_t* from = reinterpret_cast<const uint64_t*>(segs + si);
-        uint64_t* to = reinterpret_cast<uint64_t*>(&g);
-        for (int w = threadIdx.x; w < (int)(sizeof(Seg) / 8); w += blockDim.x) to[w] = from[w];
-    }
-    __syncthreads();
-    const int lb = blockIdx.x - g.block0;
+__device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&words)[2 * D]) {
     const uint64_t stride = (uint64_t)g.nblocks * blockDim.x;
     const int deg = g.degree, nt = g.nt;
-    uint64_t words[2 * D];
 #pragma unroll
     for (int w = 0; w < 2 * D; w++) words[w] = 0;
 
@@ -215,6 +194,38 @@ __global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nse
             words[2 * d + 1] = c.c1;
         }
     }
+}
+
+// One launch of round sums (and product sums) over all segments: a block finds its segment, runs
+// a grid-stride loop over the segment's pairs, and the segment's last block to finish reduces the
+// segment's partial rows into seg.out.
+template <int D>
+__global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nseg, uint64_t* partials,
+                                                        unsigned* counters) {
+    __shared__ Seg g;
+    __shared__ int si;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nseg - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) / 2;
+            if (segs[mid].block0 <= (int)blockIdx.x)
+                lo = mid;
+            else
+                hi = mid - 1;
+        }
+        si = lo;
+    }
+    __syncthreads();
+    {
+        const uint64_t* from = reinterpret_cast<const uint64_t*>(segs + si);
+        uint64_t* to = reinterpret_cast<uint64_t*>(&g);
+        for (int w = threadIdx.x; w < (int)(sizeof(Seg) / 8); w += blockDim.x) to[w] = from[w];
+    }
+    __syncthreads();
+    const int lb = blockIdx.x - g.block0;
+    const int deg = g.degree;
+    uint64_t words[2 * D];
+    sc_seg_sums<D>(g, lb, words);
     block_sum<2 * D>(words);
 
     // the segment's last block reduces its partial rows
@@ -265,17 +276,15 @@ __global__ void sc_gather_evals(const EvalRef* refs, int n, uint64_t* out) {
 // Round j's message of each job: Σ over its instances of w_i·(own sums, or 2^{pad_i − j − 1}·S_i
 // while padded), absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
 // <prefix>/r/j.
-__global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const FsJob* jobs, int njobs, int j,
-                                                         FsKeys keys, const uint64_t* w, const int* pad,
-                                                         const uint64_t* S, const uint64_t* msgbuf,
-                                                         uint64_t* rounds_out, uint64_t* chal_out) {
-    __shared__ uint32_t sbuf[FS_THREADS / 32][FS_BUF_WORDS];
-    const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32, lane = threadIdx.x & 31;
-    if (t >= njobs) return;  // whole warps leave together
+// One warp runs job t's round (buf: FS_BUF_WORDS of the warp's shared memory).
+template <bool ROLLED>
+__device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, const FsKeys& keys, const uint64_t* w,
+                          const int* pad, const uint64_t* S, const uint64_t* msgbuf, uint64_t* rounds_out,
+                          uint64_t* chal_out, uint32_t* buf) {
+    const int lane = threadIdx.x & 31;
     const FsJob& jb = jobs[t];
     if (j >= jb.n_max) return;
     FsState* st = states + t;
-    uint32_t* buf = sbuf[threadIdx.x / 32];
     const int degree = jb.degree;
     fp2 msg[SC_MAX_DEGREE];
     for (int x = 0; x < degree; x++) msg[x] = {0, 0};
@@ -310,7 +319,7 @@ __global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const 
     }
     len = __shfl_sync(0xFFFFFFFFu, len, 0);
     uint64_t c0, c1;
-    const bool ok = fs_round_warp(keys, jb, j, buf, len, state, &counter, &c0, &c1);
+    const bool ok = fs_round_warp<ROLLED>(keys, jb, j, buf, len, state, &counter, &c0, &c1);
     if (lane != 0) return;
     if (!ok) {
         st->err = 1;
@@ -323,6 +332,60 @@ __global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const 
     st->r[1] = c1;
     chal_out[jb.chal_off + 2 * j] = c0;
     chal_out[jb.chal_off + 2 * j + 1] = c1;
+}
+
+__global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const FsJob* jobs, int njobs, int j,
+                                                         FsKeys keys, const uint64_t* w, const int* pad,
+                                                         const uint64_t* S, const uint64_t* msgbuf,
+                                                         uint64_t* rounds_out, uint64_t* chal_out) {
+    __shared__ uint32_t sbuf[FS_THREADS / 32][FS_BUF_WORDS];
+    const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
+    if (t >= njobs) return;  // whole warps leave together
+    sc_fs_job<false>(states, jobs, t, j, keys, w, pad, S, msgbuf, rounds_out, chal_out, sbuf[threadIdx.x / 32]);
+}
+
+// The small last rounds of a batch, j0 to J − 1, in one block with no launch between them: each
+// round sums its segments (every segment one block's work: nblocks = 1) with the whole block, then
+// the block's warps run the jobs' transcripts, whose challenges the next round binds.
+struct ScTail {
+    FsKeys keys;
+    FsState* states;
+    const FsJob* jobs;
+    const uint64_t* w;
+    const int* pad;
+    const uint64_t* S;
+    uint64_t* msgbuf;
+    uint64_t* rounds_out;
+    uint64_t* chal_out;
+    const Seg* segs;   // the tail rounds' segments in round order
+    const int* first;  // round j0 + t's segments are segs[first[t] .. first[t + 1])
+    int njobs, j0, rounds, pad_;
+};
+
+template <int D>
+__global__ void __launch_bounds__(SC_THREADS, 1) sc_tail(const ScTail* A) {
+    __shared__ Seg g;
+    __shared__ uint32_t sbuf[SC_THREADS / 32][FS_BUF_WORDS];
+    const int warp = threadIdx.x >> 5;
+    for (int t = 0; t < A->rounds; t++) {
+        for (int si = A->first[t]; si < A->first[t + 1]; si++) {
+            if (threadIdx.x < (int)(sizeof(Seg) / 8))
+                reinterpret_cast<uint64_t*>(&g)[threadIdx.x] = reinterpret_cast<const uint64_t*>(A->segs + si)[threadIdx.x];
+            __syncthreads();
+            uint64_t words[2 * D];
+            sc_seg_sums<D>(g, 0, words);
+            block_sum<2 * D>(words);  // ends with a barrier
+            if (threadIdx.x == 0) {
+                const int nout = g.kind == 1 ? 2 : 2 * g.degree;
+                for (int w = 0; w < nout; w++) g.out[w] = words[w];
+            }
+            __syncthreads();
+        }
+        for (int job = warp; job < A->njobs; job += SC_THREADS / 32)
+            sc_fs_job<true>(A->states, A->jobs, job, A->j0 + t, A->keys, A->w, A->pad, A->S, A->msgbuf, A->rounds_out,
+                            A->chal_out, sbuf[warp]);
+        __syncthreads();
+    }
 }
 
 // ---- host driver -----------------------------------------------------------------------------
@@ -391,9 +454,13 @@ struct ScRun {
     std::vector<Plan> plans;
     size_t max_segs = 1, max_blocks = 1, total_segs = 0, nbind = 0;
     int seg_cap = 1;
+    int j0 = 0;  // rounds j0 … J − 1 run in sc_tail
+    ScTail tail_h;
+    std::vector<int> tail_first;
     // arena layout (offsets from the arena's base)
     size_t off_fs = 0, off_jobs = 0, off_w = 0, off_pad = 0, off_S = 0, off_msg = 0, off_rounds = 0, off_chal = 0,
-           off_partials = 0, off_counters = 0, off_segs = 0, off_bind = 0, off_erefs = 0, off_evals = 0;
+           off_partials = 0, off_counters = 0, off_segs = 0, off_bind = 0, off_erefs = 0, off_evals = 0, off_tail = 0,
+           off_first = 0;
     size_t arena_bytes = 0;
     // host-side staging that the enqueued copies read (kept until finish)
     std::vector<FsState> fs0;
@@ -519,6 +586,14 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
         r->max_blocks = std::max(r->max_blocks, (size_t)p.blocks);
         r->total_segs += p.who.size();
     }
+    r->j0 = r->J;
+    if (njobs <= SC_THREADS / 32)
+        for (int j = r->J - 1; j >= 0; j--) {
+            uint64_t pairs = 0;
+            for (auto& w : r->plans[1 + j].who) pairs += 1ull << (r->inst[w.first].vars - w.second - 1);
+            if (pairs > SC_TAIL_PAIRS) break;
+            r->j0 = j;
+        }
 
     // the arena: tables, transcripts, plans and outputs
     Arena ar;
@@ -541,6 +616,8 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
     r->off_partials = ar.take(r->max_blocks * 2 * SC_MAX_DEGREE * 8);
     r->off_counters = ar.take(4 * r->max_segs);
     r->off_segs = ar.take(sizeof(Seg) * std::max<size_t>(r->total_segs, 1));
+    r->off_tail = ar.take(sizeof(ScTail));
+    r->off_first = ar.take(4 * ((size_t)(r->J - r->j0) + 1));
     for (auto& is : r->inst)
         if (is.vars >= 1) r->nbind += is.tables.size();
     r->off_bind = ar.take(sizeof(BindLast) * std::max<size_t>(r->nbind, 1));
@@ -614,9 +691,10 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
                     for (int k = 0; k < g.nt; k++) g.dst[k] = ar.at<uint64_t>(is.tables[k].buf_off[(own - 1) & 1]);
                 }
             }
-            g.block0 = block0;
-            g.nblocks = blocks_for(g.n);
-            g.part0 = block0;
+            const bool tail = &p - r->plans.data() >= 1 + r->j0;  // one block's work in sc_tail
+            g.block0 = tail ? 0 : block0;
+            g.nblocks = tail ? 1 : blocks_for(g.n);
+            g.part0 = g.block0;
             block0 += g.nblocks;
             r->all_segs.push_back(g);
         }
@@ -692,6 +770,29 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         TG_CUDA(cudaMemcpyAsync(ar.at<EvalRef>(r->off_erefs), r->erefs.data(), sizeof(EvalRef) * r->erefs.size(),
                                 cudaMemcpyHostToDevice, s));
     TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(r->off_counters), 0, 4 * r->max_segs, s));
+    if (r->j0 < r->J) {
+        ScTail& t = r->tail_h;
+        memset(&t, 0, sizeof t);
+        t.keys = keys;
+        t.states = dfs;
+        t.jobs = ar.at<FsJob>(r->off_jobs);
+        t.w = ar.at<uint64_t>(r->off_w);
+        t.pad = ar.at<int>(r->off_pad);
+        t.S = dS;
+        t.msgbuf = dmsg;
+        t.rounds_out = ar.at<uint64_t>(r->off_rounds);
+        t.chal_out = ar.at<uint64_t>(r->off_chal);
+        t.segs = ar.at<Seg>(r->off_segs) + r->plan_seg0[1 + r->j0];
+        t.first = ar.at<int>(r->off_first);
+        t.njobs = njobs;
+        t.j0 = r->j0;
+        t.rounds = r->J - r->j0;
+        r->tail_first.assign(1, 0);
+        for (int j = r->j0; j < r->J; j++) r->tail_first.push_back(r->tail_first.back() + (int)r->plans[1 + j].who.size());
+        TG_CUDA(cudaMemcpyAsync(ar.at<ScTail>(r->off_tail), &t, sizeof t, cudaMemcpyHostToDevice, s));
+        TG_CUDA(cudaMemcpyAsync(ar.at<int>(r->off_first), r->tail_first.data(), 4 * r->tail_first.size(),
+                                cudaMemcpyHostToDevice, s));
+    }
 
     // the launches
     uint64_t* partials = ar.at<uint64_t>(r->off_partials);
@@ -714,7 +815,7 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
     };
     int rc = run_plan(0, "sumcheck_product_sum");
     if (rc) return rc;
-    for (int j = 0; j < r->J; j++) {
+    for (int j = 0; j < r->j0; j++) {
         rc = run_plan(1 + j, "sumcheck_round");
         if (rc) return rc;
         {
@@ -723,6 +824,17 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
                                                         ar.at<uint64_t>(r->off_w), ar.at<int>(r->off_pad), dS, dmsg,
                                                         drounds, dchal);
         }
+        TG_CUDA(cudaGetLastError());
+    }
+    if (r->j0 < r->J) {
+        uint64_t units = 0;
+        for (int j = r->j0; j < r->J; j++)
+            for (size_t q = 0; q < r->plans[1 + j].who.size(); q++) units += r->all_segs[r->plan_seg0[1 + j] + q].n;
+        Launch L(d, s, "sumcheck_tail", 1, units);
+        with_degree(r->D, [&](auto D_) {
+            constexpr int DD = decltype(D_)::value;
+            sc_tail<DD><<<1, SC_THREADS, 0, s>>>(ar.at<ScTail>(r->off_tail));
+        });
         TG_CUDA(cudaGetLastError());
     }
     if (!r->binds.empty()) {
