@@ -15,9 +15,11 @@
 //   pass C  per v2 and coset: forward size-K2 transform, written interleaved into the codeword.
 //
 // The inverse transform's last step and the forward transform's first step share their data
-// grouping (fixed j2, all j1), which is why they fuse into pass M. Rows go through in groups
-// whose scratch (k + n words per row) fits in L2, so passes M and C read their inputs from L2.
-// Rows of k ≤ 2^11 take one CTA each, all in shared memory.
+// grouping (fixed j2, all j1), which is why they fuse into pass M. Rows go through in groups of
+// scratch (k + n words per row, lde_group_bytes in all: 32 rows at k = 2^20), so that every pass's
+// grid spans many waves; the scratch is written with an L2 evict-last hint, and the part still in
+// L2 when the next pass reads it saves HBM reads. Rows of k ≤ 2^11 take one CTA each, all in
+// shared memory.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
