@@ -118,7 +118,10 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
         fp2 acc = {0, 0};
         for (uint64_t x = (uint64_t)lb * blockDim.x + threadIdx.x; x < g.n; x += stride) {
             fp2 prod = {1, 0};
-            for (int k = 0; k < nt; k++) prod = l2_mul(prod, load_entry(g.src[k], (g.base_mask >> k) & 1, x));
+            for (int k = 0; k < nt; k++) {
+                const fp2 e = load_entry(g.src[k], (g.base_mask >> k) & 1, x);
+                prod = k ? l2_mul(prod, e) : e;
+            }
             acc = l2_add(acc, prod);
         }
         acc = l2_canon(acc);
@@ -133,16 +136,16 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
             uint64_t prod[D];
 #pragma unroll
             for (int d = 0; d < D; d++) prod[d] = 1;
-            for (int k = 0; k < nt; k++) {
+            for (int k = 0; k < nt; k++) {  // the first table's values start the products
                 const ulonglong2 v = reinterpret_cast<const ulonglong2*>(g.src[k])[p];
                 const uint64_t diff = lz::sub(v.y, v.x);
                 uint64_t x = v.y;  // value at node 1
-                prod[0] = lz::mul(prod[0], v.x);
+                prod[0] = k ? lz::mul(prod[0], v.x) : v.x;
 #pragma unroll
                 for (int d = 1; d < D; d++) {  // nodes 2..D
                     if (d < deg) {
                         x = lz::add(x, diff);
-                        prod[d] = lz::mul(prod[d], x);
+                        prod[d] = k ? lz::mul(prod[d], x) : x;
                     }
                 }
             }
@@ -175,12 +178,12 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
                 }
                 const fp2 diff = l2_sub(v, u);
                 fp2 x = v;
-                prod[0] = l2_mul(prod[0], u);
+                prod[0] = k ? l2_mul(prod[0], u) : u;  // the first table's values start the products
 #pragma unroll
                 for (int d = 1; d < D; d++) {
                     if (d < deg) {
                         x = l2_add(x, diff);
-                        prod[d] = l2_mul(prod[d], x);
+                        prod[d] = k ? l2_mul(prod[d], x) : x;
                     }
                 }
             }
