@@ -53,6 +53,30 @@ __global__ void tr_product_level_base(const ulonglong2* below, uint64_t* above, 
     }
 }
 
+// Two levels in one pass: level l (m2 = 2m entries) and level l − 1 (m entries) from level l + 1,
+// so that level l is written but not read back. Thread x reads entries 4x … 4x + 3 below.
+__global__ void tr_product_level2(const ulonglong2* below, ulonglong2* mid, ulonglong2* above, uint64_t m) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < m; x += stride) {
+        const ulonglong2 a = below[4 * x], b = below[4 * x + 1], c = below[4 * x + 2], d = below[4 * x + 3];
+        const fp2 p = l2_canon(l2_mul(fp2{a.x, a.y}, fp2{b.x, b.y})), q = l2_canon(l2_mul(fp2{c.x, c.y}, fp2{d.x, d.y}));
+        const fp2 r = l2_canon(l2_mul(p, q));
+        mid[2 * x] = make_ulonglong2(p.c0, p.c1);
+        mid[2 * x + 1] = make_ulonglong2(q.c0, q.c1);
+        above[x] = make_ulonglong2(r.c0, r.c1);
+    }
+}
+
+__global__ void tr_product_level2_base(const ulonglong2* below, ulonglong2* mid, uint64_t* above, uint64_t m) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < m; x += stride) {
+        const ulonglong2 a = below[2 * x], b = below[2 * x + 1];
+        const uint64_t p = lz::canon(lz::mul(a.x, a.y)), q = lz::canon(lz::mul(b.x, b.y));
+        mid[x] = make_ulonglong2(p, q);
+        above[x] = lz::canon(lz::mul(p, q));
+    }
+}
+
 // (n, d) of level l from level l + 1; n null: every numerator below is 1, so n_out = d_L + d_R.
 __global__ void tr_fraction_level(const ulonglong2* n, const ulonglong2* d, ulonglong2* n_out, ulonglong2* d_out,
                                   uint64_t m) {
@@ -70,6 +94,32 @@ __global__ void tr_fraction_level(const ulonglong2* n, const ulonglong2* d, ulon
         const fp2 dd = e_mul(c, e);
         n_out[x] = make_ulonglong2(nn.c0, nn.c1);
         d_out[x] = make_ulonglong2(dd.c0, dd.c1);
+    }
+}
+
+// Two fraction levels in one pass, as tr_product_level2 (n null: numerators of 1 below).
+__global__ void tr_fraction_level2(const ulonglong2* n, const ulonglong2* d, ulonglong2* n_mid, ulonglong2* d_mid,
+                                   ulonglong2* n_out, ulonglong2* d_out, uint64_t m) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < m; x += stride) {
+        fp2 nn[2], dd[2];
+        for (int h = 0; h < 2; h++) {
+            const ulonglong2 dl = d[4 * x + 2 * h], dr = d[4 * x + 2 * h + 1];
+            const fp2 c = {dl.x, dl.y}, e = {dr.x, dr.y};
+            if (n) {
+                const ulonglong2 nl = n[4 * x + 2 * h], nr = n[4 * x + 2 * h + 1];
+                nn[h] = l2_canon(l2_add(l2_mul(fp2{nl.x, nl.y}, e), l2_mul(fp2{nr.x, nr.y}, c)));
+            } else {
+                nn[h] = l2_canon(l2_add(c, e));
+            }
+            dd[h] = l2_canon(l2_mul(c, e));
+            n_mid[2 * x + h] = make_ulonglong2(nn[h].c0, nn[h].c1);
+            d_mid[2 * x + h] = make_ulonglong2(dd[h].c0, dd[h].c1);
+        }
+        // (lazy arithmetic, every stored entry canonical)
+        const fp2 no = l2_canon(l2_add(l2_mul(nn[0], dd[1]), l2_mul(nn[1], dd[0]))), dn = l2_canon(l2_mul(dd[0], dd[1]));
+        n_out[x] = make_ulonglong2(no.c0, no.c1);
+        d_out[x] = make_ulonglong2(dn.c0, dn.c1);
     }
 }
 
@@ -772,22 +822,41 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
             if (!rc && spec.leaves) rc = place(*tr.n[spec.height], spec.leaves);
         }
         if (rc) return bail(rc);
-        for (int l = (int)spec.height - 1; l >= 0; l--) {
-            const uint64_t m = 1ull << (spec.s + l);
-            rc = spare_take(d, *tr.n[l], m * es);
-            if (!rc && spec.kind == 1) rc = spare_take(d, *tr.d[l], m * es);
-            if (rc) return bail(rc);
+        // levels two at a time (l and l − 1 from l + 1), the last one alone when the count is odd
+        for (int l = (int)spec.height - 1; l >= 0;) {
+            const bool two = l >= 1;
+            const uint64_t m = 1ull << (spec.s + l);  // entries of level l
+            for (int t = 0; t < (two ? 2 : 1); t++) {
+                const uint64_t mt = m >> t;
+                rc = spare_take(d, *tr.n[l - t], mt * es);
+                if (!rc && spec.kind == 1) rc = spare_take(d, *tr.d[l - t], mt * es);
+                if (rc) return bail(rc);
+            }
+            const ulonglong2* nb = tr.unit && l + 1 == (int)spec.height ? nullptr : (const ulonglong2*)tr.n[l + 1]->ptr;
             Launch L(d, s, spec.kind ? "tree_fraction_level" : "tree_product_level", 1, m);
-            if (spec.kind == 0 && tr.base)
+            if (two) {
+                const uint64_t mo = m / 2;  // entries of level l − 1, one per thread
+                if (spec.kind == 0 && tr.base)
+                    tr_product_level2_base<<<grid_of(d, mo), 256, 0, s>>>(
+                        (const ulonglong2*)tr.n[l + 1]->ptr, (ulonglong2*)tr.n[l]->ptr, (uint64_t*)tr.n[l - 1]->ptr, mo);
+                else if (spec.kind == 0)
+                    tr_product_level2<<<grid_of(d, mo), 256, 0, s>>>((const ulonglong2*)tr.n[l + 1]->ptr,
+                                                                    (ulonglong2*)tr.n[l]->ptr, (ulonglong2*)tr.n[l - 1]->ptr, mo);
+                else
+                    tr_fraction_level2<<<grid_of(d, mo), 256, 0, s>>>(
+                        nb, (const ulonglong2*)tr.d[l + 1]->ptr, (ulonglong2*)tr.n[l]->ptr, (ulonglong2*)tr.d[l]->ptr,
+                        (ulonglong2*)tr.n[l - 1]->ptr, (ulonglong2*)tr.d[l - 1]->ptr, mo);
+            } else if (spec.kind == 0 && tr.base) {
                 tr_product_level_base<<<grid_of(d, m), 256, 0, s>>>((const ulonglong2*)tr.n[l + 1]->ptr,
                                                                    (uint64_t*)tr.n[l]->ptr, m);
-            else if (spec.kind == 0)
+            } else if (spec.kind == 0) {
                 tr_product_level<<<grid_of(d, m), 256, 0, s>>>((const ulonglong2*)tr.n[l + 1]->ptr, (ulonglong2*)tr.n[l]->ptr, m);
-            else
-                tr_fraction_level<<<grid_of(d, m), 256, 0, s>>>(
-                    tr.unit && l + 1 == (int)spec.height ? nullptr : (const ulonglong2*)tr.n[l + 1]->ptr,
-                    (const ulonglong2*)tr.d[l + 1]->ptr, (ulonglong2*)tr.n[l]->ptr, (ulonglong2*)tr.d[l]->ptr, m);
+            } else {
+                tr_fraction_level<<<grid_of(d, m), 256, 0, s>>>(nb, (const ulonglong2*)tr.d[l + 1]->ptr,
+                                                               (ulonglong2*)tr.n[l]->ptr, (ulonglong2*)tr.d[l]->ptr, m);
+            }
             TG_CUDA(cudaGetLastError());
+            l -= two ? 2 : 1;
         }
         // the root level on the host
         const uint64_t r = 1ull << spec.s;
