@@ -589,13 +589,15 @@ def run_logup(args) -> None:
         one(args.lookups_log, None)
         one(args.rows_log, 0x6D756C)
     times = {"lookup": [], "table": []}
-    dev.profile(True)
-    for _ in range(args.steps):
+    for _ in range(args.steps):  # timed without per-launch events
         times["lookup"].append(one(args.lookups_log, None))
         times["table"].append(one(args.rows_log, 0x6D756C))
+    dev.profile(True)  # one more step, profiled, for the kernel breakdown
+    one(args.lookups_log, None)
+    one(args.rows_log, 0x6D756C)
     dev.profile(False)
     prof = dev.profile_read()
-    kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps} for k, v in prof.items()}
+    kernels = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in prof.items()}
     med = {k: statistics.median(v) for k, v in times.items()}
     ps = (med["lookup"] + med["table"]) / (1 << args.lookups_log) * 1e12
     dev.close()
@@ -607,7 +609,8 @@ def run_logup(args) -> None:
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks Fp2)",
         "data": "synthetic (counter-generated keys, values and multiplicities)",
         "config": {"workload": f"2^{args.lookups_log} lookups into 2^{args.rows_log} rows, each tree its own leaf stage",
-                   "timing": "host wall clock per tree, median over steps, leaves generated on the device inside"},
+                   "timing": "host wall clock per tree, median over steps, leaves generated on the device inside; "
+                             "kernels from one more profiled step"},
         "lookup_tree_ms": med["lookup"] * 1e3, "table_tree_ms": med["table"] * 1e3,
         "reference_h100_ps_per_lookup": 297.0, "kernels": kernels,
     }
@@ -715,11 +718,12 @@ def run_forest(args) -> None:
 
     for _ in range(args.warmup):
         one()
-    dev.profile(True)
-    times = [one() for _ in range(args.steps)]
+    times = [one() for _ in range(args.steps)]  # timed without per-launch events
+    dev.profile(True)  # one more proof, profiled, for the kernel breakdown
+    one()
     dev.profile(False)
     prof = dev.profile_read()
-    kernels = {k: {"ms_per_step": v[0] / args.steps, "launches_per_step": v[1] / args.steps} for k, v in prof.items()}
+    kernels = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in prof.items()}
     med = statistics.median(times)
     del leaves
     dev.close()
@@ -732,7 +736,8 @@ def run_forest(args) -> None:
         "dtype": "u64 (Goldilocks; Fp2 after the first bind)",
         "data": "synthetic (counter-generated prime-field leaves on the device, as the reference benchmark)",
         "config": {"workload": f"one forest of 2^{s_} trees of 2^{h_} leaves",
-                   "timing": "host wall clock per proof (leaves already on the device), median over steps"},
+                   "timing": "host wall clock per proof (leaves already on the device), median over steps; "
+                             "kernels from one more profiled proof"},
         "proof_ms": med * 1e3, "reference_h100_ps_per_leaf": 84.6, "kernels": kernels,
     }
     print(json.dumps(line), flush=True)
