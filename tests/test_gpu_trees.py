@@ -350,3 +350,40 @@ def test_unaligned_device_leaves_are_copied(dev):
             recs = st.prove(t)
             out.append(([(r.rounds, r.final_evals) for r in recs], st.claim(0), t.state))
     assert out[0] == out[1]
+
+
+def test_workspace_cache_reuse_and_trim(dev):
+    """Stages of alternating shapes take their levels and bound tables from the device's workspace
+    cache (buffers a closed stage left, possibly written by another shape) and prove exactly as the
+    first time; tg_device_trim returns the cached memory to the driver."""
+    import torch
+
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.trees import Forest, LeafStage, generated_fraction
+    from tessera_gb300.workloads import fill_counter
+
+    ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([5]) * 32, bytes([6]) * 16)
+    big = fill_counter(torch.empty(1 << 22, dtype=torch.int64, device="cuda"), 11, dev)
+    small = fill_counter(torch.empty(1 << 16, dtype=torch.int64, device="cuda"), 12, dev)
+
+    def forest(leaves, s):
+        t = Transcript(ctx)
+        with LeafStage([Forest(s, leaves, True)], dev) as st:
+            recs = st.prove(t)
+            return [(r.rounds, r.final_evals) for r in recs], st.claim(0), t.state
+
+    def fraction():
+        t = Transcript(ctx)
+        tree = generated_fraction(15, 3, 4, 5, (7, 8), (9, 10), dev)
+        with LeafStage([tree], dev) as st:
+            recs = st.prove(t)
+            return [(r.rounds, r.final_evals) for r in recs], st.claim(0), t.state
+
+    first = (forest(big, 8), forest(small, 4), fraction())
+    for _ in range(2):
+        assert (forest(big, 8), forest(small, 4), fraction()) == first
+    torch.cuda.synchronize()
+    free_before = torch.cuda.mem_get_info()[0]
+    dev.trim()
+    free_after = torch.cuda.mem_get_info()[0]
+    assert free_after > free_before  # the 2^22-leaf forest's levels and tables went back
