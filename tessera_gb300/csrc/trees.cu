@@ -566,14 +566,16 @@ __device__ void tl_quad(const TlTree& T, int jj, const ulonglong2* q, fp2& a, fp
     if (ti.c0 == 0 && ti.c1 == 0)
         q1 = ld2(q + 1);
     else
-        q1 = e_mul(e_sub(fp2{T.Q[0], T.Q[1]}, e_mul(e_sub(fp2{1, 0}, t), a)), ti);
-    b = e_sub(e_sub(q1, a), c);
+        q1 = l2_mul(l2_sub(fp2{T.Q[0], T.Q[1]}, l2_mul(l2_sub(fp2{1, 0}, t), a)), ti);
+    b = l2_sub(l2_sub(q1, a), c);  // lazy words, as Q and C are kept
 }
 
 // Round j of a level: the message Σ_i γ^i·(2^{pad_i − j − 1}·S_i while padded, else
 // C_i·eq1(p_i[j'], X)·q_i(X)) at X = 0, 2, 3, absorbed under <prefix>/round/j; r_j drawn under
 // <prefix>/r/j; then each tree in its own rounds takes Q_i ← q_i(r_j) and C_i ← C_i·eq1(p_i[j'], r_j).
 // One warp runs it (sbuf: FS_BUF_WORDS of shared memory).
+// ROLLED: the BLAKE3 rounds as one rolled loop (for the tail kernel, whose warp runs alone).
+template <bool ROLLED>
 __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& keys, TlTree* trees, int ntrees,
                             ulonglong2* q, uint64_t* rounds_out, uint64_t* chal_out, uint32_t* sbuf) {
     const int lane = threadIdx.x & 31;
@@ -582,26 +584,28 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
         const TlTree& T = trees[i];
         const fp2 w = {T.w[0], T.w[1]};
         const int jj = j - T.pad;
+        // lazy words throughout; the message is canonicalised once
         if (jj < 0) {
-            const fp2 ws = e_mul(w, fp2{T.S[0], T.S[1]});
+            const fp2 ws = l2_mul(w, fp2{T.S[0], T.S[1]});
             const fp2 v = {mul_pow2_lt64(ws.c0, T.pad - j - 1), mul_pow2_lt64(ws.c1, T.pad - j - 1)};
-            for (int x = 0; x < 3; x++) msg[x] = e_add(msg[x], v);
+            for (int x = 0; x < 3; x++) msg[x] = l2_add(msg[x], v);
         } else {
             fp2 a, b, c;
             tl_quad(T, jj, q + 4 * i, a, b, c);
             if (lane == 0) q[4 * i + 3] = make_ulonglong2(b.c0, b.c1);  // for the update after the challenge
             const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
-            const fp2 wc = e_mul(w, fp2{T.C[0], T.C[1]});
+            const fp2 wc = l2_mul(w, fp2{T.C[0], T.C[1]});
             // q(2) = a + 2b + 4c, q(3) = a + 3b + 9c; eq1(t, X) at 0, 2, 3: 1 − t, 3t − 1, 5t − 2
-            const fp2 b2 = e_add(b, b), c2 = e_add(c, c), c4 = e_add(c2, c2), c8 = e_add(c4, c4);
-            const fp2 q2 = e_add(a, e_add(b2, c4)), q3 = e_add(e_add(a, e_add(b2, b)), e_add(c8, c));
-            const fp2 t2 = e_add(t, t), t3 = e_add(t2, t), t5 = e_add(t3, t2);
-            const fp2 e0 = e_sub(fp2{1, 0}, t), e2 = e_sub(t3, fp2{1, 0}), e3 = e_sub(t5, fp2{2, 0});
-            msg[0] = e_add(msg[0], e_mul(wc, e_mul(e0, a)));
-            msg[1] = e_add(msg[1], e_mul(wc, e_mul(e2, q2)));
-            msg[2] = e_add(msg[2], e_mul(wc, e_mul(e3, q3)));
+            const fp2 b2 = l2_add(b, b), c2 = l2_add(c, c), c4 = l2_add(c2, c2), c8 = l2_add(c4, c4);
+            const fp2 q2 = l2_add(a, l2_add(b2, c4)), q3 = l2_add(l2_add(a, l2_add(b2, b)), l2_add(c8, c));
+            const fp2 t2 = l2_add(t, t), t3 = l2_add(t2, t), t5 = l2_add(t3, t2);
+            const fp2 e0 = l2_sub(fp2{1, 0}, t), e2 = l2_sub(t3, fp2{1, 0}), e3 = l2_sub(t5, fp2{2, 0});
+            msg[0] = l2_add(msg[0], l2_mul(wc, l2_mul(e0, a)));
+            msg[1] = l2_add(msg[1], l2_mul(wc, l2_mul(e2, q2)));
+            msg[2] = l2_add(msg[2], l2_mul(wc, l2_mul(e3, q3)));
         }
     }
+    for (int x = 0; x < 3; x++) msg[x] = l2_canon(msg[x]);
     uint32_t state[8];
     for (int i = 0; i < 8; i++) state[i] = reinterpret_cast<const uint32_t*>(st->state)[i];
     uint64_t counter = st->counter;
@@ -621,7 +625,7 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
     }
     len = __shfl_sync(0xFFFFFFFFu, len, 0);
     uint64_t c0, c1;
-    const bool ok = fs_round_warp<true>(keys, jb, j, sbuf, len, state, &counter, &c0, &c1);
+    const bool ok = fs_round_warp<ROLLED>(keys, jb, j, sbuf, len, state, &counter, &c0, &c1);
     if (lane != 0) return;
     if (!ok) {
         st->err = 1;
@@ -637,10 +641,10 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
         const int jj = j - T.pad;
         if (jj < 0) continue;
         const fp2 a = ld2(q + 4 * i), b = ld2(q + 4 * i + 3), c = ld2(q + 4 * i + 2);  // b as the message pass left it
-        const fp2 Q = e_add(a, e_mul(r, e_add(b, e_mul(r, c))));
+        const fp2 Q = l2_add(a, l2_mul(r, l2_add(b, l2_mul(r, c))));
         const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
-        const fp2 tr = e_mul(t, r);  // eq1(t, r) = 1 − t − r + 2·t·r
-        const fp2 C = e_mul(fp2{T.C[0], T.C[1]}, e_add(e_sub(e_sub(fp2{1, 0}, t), r), e_add(tr, tr)));
+        const fp2 tr = l2_mul(t, r);  // eq1(t, r) = 1 − t − r + 2·t·r
+        const fp2 C = l2_mul(fp2{T.C[0], T.C[1]}, l2_add(l2_sub(l2_sub(fp2{1, 0}, t), r), l2_add(tr, tr)));
         T.Q[0] = Q.c0, T.Q[1] = Q.c1;
         T.C[0] = C.c0, T.C[1] = C.c1;
     }
@@ -649,7 +653,7 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
 __global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, int ntrees, ulonglong2* q,
                       uint64_t* rounds_out, uint64_t* chal_out) {
     __shared__ uint32_t sbuf[FS_BUF_WORDS];
-    tl_fs_round(st, jb, j, keys, trees, ntrees, q, rounds_out, chal_out, sbuf);
+    tl_fs_round<false>(st, jb, j, keys, trees, ntrees, q, rounds_out, chal_out, sbuf);
 }
 
 // A segment's whole sum by one block (its chunks one after another); each variant is its own
@@ -719,7 +723,7 @@ __global__ void __launch_bounds__(TL_THREADS, 1) tl_tail(const TlTail* A) {
             __syncthreads();
         }
         if (threadIdx.x < 32)
-            tl_fs_round(A->st, A->jb, A->j0 + t, A->keys, A->trees, A->ntrees, A->q, A->rounds_out, A->chal_out, sbuf);
+            tl_fs_round<true>(A->st, A->jb, A->j0 + t, A->keys, A->trees, A->ntrees, A->q, A->rounds_out, A->chal_out, sbuf);
         __syncthreads();
     }
 }
