@@ -231,7 +231,7 @@ static fp2 host_inv2(fp2 a) {
 
 constexpr int TL_THREADS = 256;
 constexpr int TL_LOW = 11;  // the low eq table's variables: the pairs of one chunk share a high weight
-constexpr uint64_t TL_TAIL_PAIRS = 2048;  // rounds of at most this many pairs a segment run in one block
+constexpr uint64_t TL_TAIL_PAIRS = 512;  // rounds of at most this many pairs a segment run in one block
 
 struct TlSeg {
     const void* src[4];  // table T's entry x is src[T][x·stride]: Fp2, or prime-field words when base
