@@ -231,7 +231,8 @@ static fp2 host_inv2(fp2 a) {
 
 constexpr int TL_THREADS = 256;
 constexpr int TL_LOW = 11;  // the low eq table's variables: the pairs of one chunk share a high weight
-constexpr uint64_t TL_TAIL_PAIRS = 512;  // rounds of at most this many pairs a segment run in one block
+constexpr uint64_t TL_TAIL_PAIRS = 512;
+constexpr uint32_t TL_ROOT_DEVICE_LOG = 12;  // a joining forest of 2^s ≥ 2^12 roots folds its claim on the device  // rounds of at most this many pairs a segment run in one block
 
 struct TlSeg {
     const void* src[4];  // table T's entry x is src[T][x·stride]: Fp2, or prime-field words when base
@@ -656,6 +657,41 @@ __global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, 
     tl_fs_round<false>(st, jb, j, keys, trees, ntrees, q, rounds_out, chal_out, sbuf);
 }
 
+// A joining forest's claim Σ_y root[y]·eq(point, y) (y_1 the lowest bit) by binding one point
+// coordinate at a time, in one block: the root level (2^s prime-field words or Fp2 entries) folds
+// into the ping-pong scratch (2^(s−1) + 2^(s−2) entries). The claim becomes the tree's Q and S for
+// the rounds, and goes to out (canonical) for the host's record of the level.
+constexpr int TL_ROOT_THREADS = 1024;
+__global__ void __launch_bounds__(TL_ROOT_THREADS, 1) tl_root_claim(const void* level, int base, int s,
+                                                                  const uint64_t* point, ulonglong2* scratch,
+                                                                  TlTree* T, uint64_t* out) {
+    ulonglong2* buf[2] = {scratch, scratch + (1ull << (s - 1))};
+    for (int c = 0; c < s; c++) {
+        const uint64_t m = 1ull << (s - c - 1);  // entries after this fold
+        const fp2 t = {point[2 * c], point[2 * c + 1]};
+        const ulonglong2* src = c ? buf[(c - 1) & 1] : static_cast<const ulonglong2*>(level);
+        ulonglong2* dst = buf[c & 1];
+        for (uint64_t k = threadIdx.x; k < m; k += blockDim.x) {
+            fp2 a, b;
+            if (c == 0 && base) {
+                const ulonglong2 w = src[k];  // prime-field words 2k, 2k + 1
+                a = {w.x, 0}, b = {w.y, 0};
+            } else {
+                a = ld2(src + 2 * k), b = ld2(src + 2 * k + 1);
+            }
+            const fp2 v = l2_add(a, l2_mul(t, l2_sub(b, a)));
+            dst[k] = make_ulonglong2(v.c0, v.c1);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        const fp2 v = l2_canon(ld2(buf[(s - 1) & 1]));
+        T->Q[0] = v.c0, T->Q[1] = v.c1;
+        T->S[0] = v.c0, T->S[1] = v.c1;
+        out[0] = v.c0, out[1] = v.c1;
+    }
+}
+
 // A segment's whole sum by one block (its chunks one after another); each variant is its own
 // function, so that the tail kernel's registers are those of the variant it calls.
 template <int NT, int KIND, int MODE, bool ONE>
@@ -982,6 +1018,7 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
     // the claims the joining trees enter with (applied once the level is proven)
     std::vector<std::vector<fp2>> jpoint(ntrees);
     std::vector<fp2> jvalue(ntrees), jp(ntrees), jq(ntrees);
+    std::vector<char> root_on_device(ntrees, 0);
     for (int k : present) {
         TreeLevels& tr = st->trees[k];
         if (tr.own >= 0) {
@@ -991,7 +1028,10 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
             jq[k] = tr.q;
         } else if (tr.kind == 0) {
             jpoint[k].assign(rootc.begin() + (s_max - tr.s), rootc.end());
-            jvalue[k] = host_mle(tr.root, jpoint[k]);
+            if (tr.s >= TL_ROOT_DEVICE_LOG)
+                root_on_device[k] = 1;  // folded on the device before the rounds (tl_root_claim)
+            else
+                jvalue[k] = host_mle(tr.root, jpoint[k]);
         } else {
             jp[k] = tr.sent_n;
             jq[k] = tr.sent_d;
@@ -1164,6 +1204,12 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
     const size_t off_rounds = ar.take((size_t)std::max(n_max, 1) * 48);
     const size_t off_chal = ar.take((size_t)std::max(n_max, 1) * 16);
     const size_t off_evals = ar.take((size_t)64 * np);
+    // the device root claims: one output pair per present tree, and the fold's scratch
+    const size_t off_rootc = ar.take((size_t)16 * np);
+    uint64_t root_scratch = 1;
+    for (int i = 0; i < np; i++)
+        if (root_on_device[present[i]]) root_scratch = std::max<uint64_t>(root_scratch, (3ull << st->trees[present[i]].s) / 4);
+    const size_t off_rscratch = ar.take(root_scratch * 16);
     const size_t upload_bytes = ar.used;  // the eq tables, built on the device, follow
     for (int i = 0; i < np; i++) off_eq[i] = ar.take(std::max<uint64_t>(off_eq[i], 1) * 16);
     if (ar.used > st->misc.bytes) {  // grows geometrically: the levels grow one after another
@@ -1284,11 +1330,20 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
     }
 
     std::vector<uint64_t> rounds((size_t)std::max(n_max, 1) * 6), chal((size_t)std::max(n_max, 1) * 2),
-        fevals(8 * (size_t)np);
+        fevals(8 * (size_t)np), rootc_host(2 * (size_t)np);
     FsState fs1;
     {
         std::lock_guard<std::mutex> lock(d->mu);
         TG_CUDA(cudaMemcpyAsync(ar.base, up.data(), up.size(), cudaMemcpyHostToDevice, s));
+        for (int i = 0; i < np; i++) {
+            if (!root_on_device[present[i]]) continue;
+            const TreeLevels& tr = st->trees[present[i]];
+            Launch L(d, s, "tree_root_claim", 1, 1ull << tr.s);
+            tl_root_claim<<<1, TL_ROOT_THREADS, 0, s>>>(tr.n[0]->ptr, tr.base, (int)tr.s, ar.at<uint64_t>(off_point[i]),
+                                                        ar.at<ulonglong2>(off_rscratch), ar.at<TlTree>(off_trees) + i,
+                                                        ar.at<uint64_t>(off_rootc) + 2 * i);
+            TG_CUDA(cudaGetLastError());
+        }
         if (eq_total) {
             Launch L(d, s, "tree_eq", 1, eq_total);
             tl_eq_tables<<<grid_of(d, eq_total), 256, 0, s>>>(ar.at<TlEqJob>(off_jobs), (int)eqjobs.size(), eq_total);
@@ -1344,8 +1399,11 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         TG_CUDA(cudaMemcpyAsync(rounds.data(), ar.at<uint64_t>(off_rounds), rounds.size() * 8, cudaMemcpyDeviceToHost, s));
         TG_CUDA(cudaMemcpyAsync(chal.data(), ar.at<uint64_t>(off_chal), chal.size() * 8, cudaMemcpyDeviceToHost, s));
         TG_CUDA(cudaMemcpyAsync(fevals.data(), ar.at<uint64_t>(off_evals), finals.size() * 16, cudaMemcpyDeviceToHost, s));
+        TG_CUDA(cudaMemcpyAsync(rootc_host.data(), ar.at<uint64_t>(off_rootc), 16 * (size_t)np, cudaMemcpyDeviceToHost, s));
         TG_CUDA(cudaStreamSynchronize(s));
     }
+    for (int i = 0; i < np; i++)  // the device root claims, for the record
+        if (root_on_device[present[i]]) held[i] = jvalue[present[i]] = {rootc_host[2 * i], rootc_host[2 * i + 1]};
     if (fs1.err) return bail(fail(TG_ERR_STATE, "a level challenge found no canonical Fp2 in %d squeezes", FS_MAX_TRIES));
     memcpy(t->state, fs1.state, 32);
     t->counter = fs1.counter;

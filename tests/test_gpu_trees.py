@@ -292,7 +292,7 @@ def eq_at(p, r):
     return out
 
 
-@pytest.mark.parametrize("s,h", [(4, 8), (0, 11), (7, 3), (6, 9), (2, 14)])
+@pytest.mark.parametrize("s,h", [(4, 8), (0, 11), (7, 3), (6, 9), (2, 14), (12, 3)])
 def test_prime_field_forest_matches_fp2_and_leaf_claim(dev, s, h):
     """A forest of counter leaves proven from prime-field words (read in place on the device) and
     from Fp2 pairs gives the same records level by level; every level passes the verifier's last
