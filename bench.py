@@ -53,7 +53,9 @@ P = 0xFFFFFFFF00000001
 
 
 class Clocks:
-    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+    """Samples nvidia-smi clocks and throttle reasons every 200 ms; begin()/end() mark the timed
+    region on the host clock, and the summary keeps the samples that arrived inside it (started
+    before the warm-up, so that the sampler is running when the region starts)."""
 
     FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
               "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
@@ -61,6 +63,13 @@ class Clocks:
 
     def __init__(self, index: int):
         self.index, self.rows, self.proc = index, [], None
+        self.t0 = self.t1 = None
+
+    def begin(self):
+        self.t0 = time.time()
+
+    def end(self):
+        self.t1 = time.time()
 
     def __enter__(self):
         try:
@@ -74,7 +83,7 @@ class Clocks:
 
     def _read(self):
         for line in self.proc.stdout:
-            self.rows.append([x.strip() for x in line.split(",")])
+            self.rows.append([time.time()] + [x.strip() for x in line.split(",")])
 
     def __exit__(self, *exc):
         if self.proc:
@@ -87,12 +96,14 @@ class Clocks:
     def summary(self) -> dict:
         if not self.rows:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
-        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
-        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        inside = [r[1:] for r in self.rows if self.t0 is None or self.t0 <= r[0] <= (self.t1 or r[0]) + 0.05]
+        rows = inside or [r[1:] for r in self.rows]  # a region shorter than the sampling period
+        sm = [float(r[1]) for r in rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[i] for r in self.rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
+        reasons = sorted({names[i] for r in rows for i in range(4) if len(r) > 5 + i and r[5 + i] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
-                "reasons": reasons, "samples": len(self.rows)}
+                "reasons": reasons, "samples": len(inside)}
 
 
 def dist_env():
@@ -234,21 +245,27 @@ def run_gpu(args) -> None:
 
             dist.barrier()
 
-    for _ in range(args.warmup):
-        step()
-    barrier()
-    int_peaks = dev.int_peaks()  # register-only microbenchmarks, outside the timed region
+    clocks = Clocks(local).__enter__()  # sampling from the warm-up on; the summary keeps the timed region's
+    try:
+        for _ in range(args.warmup):
+            step()
+        barrier()
+        int_peaks = dev.int_peaks()  # register-only microbenchmarks, outside the timed region
 
-    # the timed region: K steps, inputs resident
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
-    launches0 = dev.launches()
-    dev.profile(True)
-    with Clocks(local) as clocks:
+        # the timed region: K steps, inputs resident
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+        launches0 = dev.launches()
+        dev.profile(True)
+        torch.cuda.synchronize()
+        clocks.begin()
         ev[0].record(stream)
         for i in range(args.steps):
             step()
             ev[i + 1].record(stream)
         stream.synchronize()
+        clocks.end()
+    finally:
+        clocks.__exit__(None, None, None)
     dev.profile(False)
     prof = dev.profile_read()
     launches = dev.launches() - launches0
