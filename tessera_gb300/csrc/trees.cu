@@ -1212,8 +1212,11 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
     const size_t off_rscratch = ar.take(root_scratch * 16);
     const size_t upload_bytes = ar.used;  // the eq tables, built on the device, follow
     for (int i = 0; i < np; i++) off_eq[i] = ar.take(std::max<uint64_t>(off_eq[i], 1) * 16);
-    if (ar.used > st->misc.bytes) {  // grows geometrically: the levels grow one after another
-        const int rc2 = st->misc.ensure(std::max(ar.used, 2 * st->misc.bytes));
+    if (ar.used > st->misc.bytes) {  // grows geometrically, through the workspace cache: the levels
+        // grow one after another, and a repeated proof of the same shape finds every size cached
+        const size_t want = std::max(ar.used, 2 * st->misc.bytes);
+        spare_give(d, st->misc);
+        const int rc2 = spare_take(d, st->misc, want);
         if (rc2) return bail(rc2);
     }
     ar.base = (uint8_t*)st->misc.ptr;
