@@ -243,8 +243,10 @@ struct TlSeg {
     ulonglong2* out;       // the round's sums: q(0), q(1) (launches that form it), q(∞)
     uint64_t n;            // pairs: 2^lbits a chunk
     uint64_t lam[2];
+    uint64_t mu[2];        // 1/λ, for the shifted form of numerators of 1 (shift)
     int kind, stride, bind, lbits;
     int block0, nblocks, part0, mode;
+    int shift, pad_;       // kind 2 with λ ≠ 0: g summed as (D0 + μ)(D1 + μ)
 };
 static_assert(sizeof(TlSeg) % 8 == 0, "TlSeg copies as words");
 
@@ -267,9 +269,12 @@ __device__ __forceinline__ fp2 ld2(const ulonglong2* p) {
 // g at X = 0, at X = 1 (ONE) and its leading coefficient in X, over one pair whose tables take the
 // values u at X = 0 and slopes d: KIND 0 L·R; 1 N0·D1 + N1·D0 + λ·D0·D1 = N0·D1 + D0·(N1 + λ·D1);
 // 2 D0 + D1 + λ·D0·D1, whose leading coefficient λ·dD0·dD1 is returned without the λ (the kernel
-// applies it once to the sum).
+// applies it once to the sum). With shift (λ ≠ 0, μ = 1/λ), kind 2 is λ·(D0 + μ)(D1 + μ) − μ: the
+// pair gives (D0 + μ)(D1 + μ) at the nodes, and since the eq weights sum to 1 the kernel turns the
+// segment's sums into λ·S − μ at 0 and 1 and λ·S at ∞ once — one Fp2 product fewer per node.
 template <int KIND, bool ONE>
-__device__ __forceinline__ void tl_nodes(const fp2* u, const fp2* d, fp2 lam, fp2& g0, fp2& g1, fp2& gi) {
+__device__ __forceinline__ void tl_nodes(const fp2* u, const fp2* d, fp2 lam, fp2 mu, bool shift, fp2& g0, fp2& g1,
+                                         fp2& gi) {
     if constexpr (KIND == 0) {
         g0 = l2_mul(u[0], u[1]);
         gi = l2_mul(d[0], d[1]);
@@ -282,6 +287,11 @@ __device__ __forceinline__ void tl_nodes(const fp2* u, const fp2* d, fp2 lam, fp
         gi = f(d[0], d[1], d[2], d[3]);
         if constexpr (ONE)
             g1 = f(l2_add(u[0], d[0]), l2_add(u[1], d[1]), l2_add(u[2], d[2]), l2_add(u[3], d[3]));
+    } else if (shift) {
+        const fp2 a = l2_add(u[0], mu), b = l2_add(u[1], mu);
+        g0 = l2_mul(a, b);
+        gi = l2_mul(d[0], d[1]);
+        if constexpr (ONE) g1 = l2_mul(l2_add(a, d[0]), l2_add(b, d[1]));
     } else {
         g0 = l2_add(l2_add(u[0], u[1]), l2_mul(lam, l2_mul(u[0], u[1])));
         gi = l2_mul(d[0], d[1]);
@@ -290,6 +300,19 @@ __device__ __forceinline__ void tl_nodes(const fp2* u, const fp2* d, fp2 lam, fp
             g1 = l2_add(l2_add(a, b), l2_mul(lam, l2_mul(a, b)));
         }
     }
+}
+
+// A kind-2 segment's per-thread sums under λ: all three with shift, else the leading coefficient.
+__device__ __forceinline__ void tl_unit_scale(const TlSeg& g, fp2 (&acc)[3]) {
+    const fp2 lam = {g.lam[0], g.lam[1]};
+    acc[2] = l2_mul(lam, acc[2]);
+    if (g.shift) acc[0] = l2_mul(lam, acc[0]), acc[1] = l2_mul(lam, acc[1]);
+}
+
+// A shifted kind-2 segment's reduced sums (canonical words) less μ at the nodes 0 and 1.
+__device__ __forceinline__ void tl_unit_finish(const TlSeg& g, uint64_t (&words)[6]) {
+    if (g.kind != 2 || !g.shift) return;
+    for (int n = 0; n < 2; n++) words[2 * n] = sub(words[2 * n], g.mu[0]), words[2 * n + 1] = sub(words[2 * n + 1], g.mu[1]);
 }
 
 // The modes of a segment's tables in a round: Fp2 tables summed as they are (a tree's round 0),
@@ -378,7 +401,7 @@ __device__ __forceinline__ void tl_pair(const TlSeg& g, uint64_t p, const TlRaw<
             }
         }
         fp2 g0, g1, gi;
-        tl_nodes<KIND, ONE>(u, d, lam, g0, g1, gi);
+        tl_nodes<KIND, ONE>(u, d, lam, fp2{g.mu[0], g.mu[1]}, g.shift, g0, g1, gi);
         part[0] = l2_add(part[0], l2_mul(w, g0));
         part[2] = l2_add(part[2], l2_mul(w, gi));
         if constexpr (ONE) part[1] = l2_add(part[1], l2_mul(w, g1));
@@ -467,7 +490,7 @@ __global__ void __launch_bounds__(TL_THREADS, tl_min_blocks<MODE>()) tl_rounds(c
     fp2 acc[3] = {{0, 0}, {0, 0}, {0, 0}};
     const uint64_t b = (uint64_t)(blockIdx.x - g.block0);
     tl_sum<NT, KIND, MODE, ONE>(g, b, acc);
-    if constexpr (KIND == 2) acc[2] = l2_mul(fp2{g.lam[0], g.lam[1]}, acc[2]);
+    if constexpr (KIND == 2) tl_unit_scale(g, acc);
     // block sums, then the segment's last block reduces the partial rows (every thread a share)
     uint64_t words[6];
     for (int i = 0; i < 3; i++) {
@@ -490,6 +513,7 @@ __global__ void __launch_bounds__(TL_THREADS, tl_min_blocks<MODE>()) tl_rounds(c
     __syncthreads();  // red is reused
     block_sum();
     if (threadIdx.x == 0) {
+        tl_unit_finish(g, words);
         for (int w = 0; w < 6; w++) reinterpret_cast<uint64_t*>(g.out)[w] = words[w];
         counters[si] = 0;
     }
@@ -747,15 +771,17 @@ __global__ void __launch_bounds__(TL_THREADS, 1) tl_tail(const TlTail* A) {
                 tl_sum_any<true>(g, acc);
             else
                 tl_sum_any<false>(g, acc);
-            if (g.kind == 2) acc[2] = l2_mul(fp2{g.lam[0], g.lam[1]}, acc[2]);
+            if (g.kind == 2) tl_unit_scale(g, acc);
             uint64_t words[6];
             for (int i = 0; i < 3; i++) {
                 const fp2 c = l2_canon(acc[i]);
                 words[2 * i] = c.c0, words[2 * i + 1] = c.c1;
             }
             tl_block_sum(words, red);
-            if (threadIdx.x == 0)
+            if (threadIdx.x == 0) {
+                tl_unit_finish(g, words);
                 for (int w = 0; w < 6; w++) reinterpret_cast<uint64_t*>(g.out)[w] = words[w];
+            }
             __syncthreads();
         }
         if (threadIdx.x < 32)
@@ -1149,6 +1175,11 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
             g.mode = base ? (g.bind ? TL_BIND_BASE : TL_SUM_BASE) : (g.bind ? TL_BIND : TL_SUM);
             g.n = 1ull << (nvars[i] - jj - 1);
             g.lam[0] = lambda.c0, g.lam[1] = lambda.c1;
+            if (g.kind == 2 && !(lambda.c0 == 0 && lambda.c1 == 0)) {
+                const fp2 mu = host_inv2(lambda);
+                g.mu[0] = mu.c0, g.mu[1] = mu.c1;
+                g.shift = 1;
+            }
             g.lbits = tl_low_bits(nvars[i] - jj - 1);
             g.nblocks = (int)std::min<uint64_t>(blocks_for(g.n), g.n >> g.lbits);
             launches[j].push_back(g);
