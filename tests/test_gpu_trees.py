@@ -227,7 +227,8 @@ def counter_value(c):
     return z - P if z >= P else z
 
 
-@pytest.mark.parametrize("unit,h", [(True, 9), (False, 9), (True, 14), (False, 17)])
+@pytest.mark.parametrize("unit,h", [(True, 1), (False, 2), (True, 3), (False, 5), (True, 9), (False, 9), (True, 14),
+                                    (False, 17)])
 def test_generated_leaves_and_leaf_claims(dev, unit, h):
     """Generated LogUp leaves equal the counter generator's on the host; every level passes the
     verifier's last check (its last claim is eq(point, r)·(N0·D1 + N1·D0 + λ·D0·D1) at the final
@@ -292,7 +293,7 @@ def eq_at(p, r):
     return out
 
 
-@pytest.mark.parametrize("s,h", [(4, 8), (0, 11), (7, 3), (6, 9), (2, 14), (12, 3)])
+@pytest.mark.parametrize("s,h", [(4, 8), (0, 11), (7, 3), (6, 9), (2, 14), (12, 3), (6, 14), (3, 1)])
 def test_prime_field_forest_matches_fp2_and_leaf_claim(dev, s, h):
     """A forest of counter leaves proven from prime-field words (read in place on the device) and
     from Fp2 pairs gives the same records level by level; every level passes the verifier's last
@@ -387,3 +388,41 @@ def test_workspace_cache_reuse_and_trim(dev):
     dev.trim()
     free_after = torch.cuda.mem_get_info()[0]
     assert free_after > free_before  # the 2^22-leaf forest's levels and tables went back
+
+
+def test_leaf_stage_refusals(dev):
+    """Malformed stages are refused before anything runs (unknown kind, too many variables, a
+    fraction tree with s > 0 or prime-field leaves, missing leaves), and a level past the last one
+    is refused with the transcript unchanged."""
+    import ctypes
+
+    from tessera_gb300 import _native as N
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.trees import Forest, LeafStage, lift
+
+    leaves = lift(list(range(1, 17)))
+    h = ctypes.c_void_p()
+
+    def opened(**fields):
+        spec = N.TreeC()
+        spec.kind, spec.s, spec.height = 0, 0, 4
+        spec.leaves = leaves.ctypes.data
+        for k, v in fields.items():
+            setattr(spec, k, v)
+        arr = (N.TreeC * 1)(spec)
+        return N.lib().tg_leaf_stage_open(dev.handle, arr, 1, 0, ctypes.byref(h))
+
+    assert opened(kind=2) < 0
+    assert opened(s=30, height=12) < 0  # 42 variables
+    assert opened(kind=1, s=1, denominators=leaves.ctypes.data) < 0
+    assert opened(kind=1, base_leaves=1, denominators=leaves.ctypes.data) < 0
+    assert opened(leaves=None) < 0
+    assert opened(kind=1, denominators=None) < 0
+    ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes(32), bytes(16))
+    t = Transcript(ctx)
+    with LeafStage([Forest(0, leaves)], dev) as st:
+        st.prove(t)
+        before = (t.state, t.counter)
+        with pytest.raises(N.TesseraError):
+            st.prove_level(t)
+        assert (t.state, t.counter) == before
