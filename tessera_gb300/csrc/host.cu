@@ -48,13 +48,13 @@ static Node chunk_node(const uint32_t key[8], const uint8_t* in, size_t len, uin
     for (size_t b = 0; b + 1 < nb; b++) {
         uint32_t m[16];
         words16(in + 64 * b, 64, m);
-        b3::compress_cv(n.cv, m, chunk, 64, mode | (b == 0 ? b3::CHUNK_START : 0));
+        b3::compress_cv(n.cv, m, chunk, 64, mode | (b == 0 ? (uint32_t)b3::CHUNK_START : 0u));
     }
     const size_t last = len - 64 * (nb - 1);
     words16(in + 64 * (nb - 1), last, n.m);
     n.counter = chunk;
     n.len = (uint32_t)last;
-    n.flags = mode | b3::CHUNK_END | (nb == 1 ? b3::CHUNK_START : 0);
+    n.flags = mode | b3::CHUNK_END | (nb == 1 ? (uint32_t)b3::CHUNK_START : 0u);
     return n;
 }
 

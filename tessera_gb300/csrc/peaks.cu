@@ -113,7 +113,7 @@ extern "C" int tg_measure_int_peaks(tg_device* dev, tg_int_peaks* out) {
         *sec = ms / 1e3;
         return TG_OK;
     };
-    double t;
+    double t = 0;
     const int it_w = 2048, it_m = 512, it_b = 512, it_h = 2048;
     rc = timed([&] { peak_imad_wide<<<blocks, PK_THREADS, 0, s>>>(buf, it_w, 0x9E3779B9u); }, &t);
     if (rc) return rc;
