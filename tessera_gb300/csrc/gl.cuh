@@ -219,6 +219,74 @@ __device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) {
 // The canonical representative.
 __device__ __forceinline__ uint64_t canon(uint64_t x) { return x >= P ? x - P : x; }
 
+// 7·x, the non-residue's multiple: the 67-bit product in two multiply-adds, then fold.
+__device__ __forceinline__ uint64_t mul7(uint64_t x) {
+    uint32_t l0, l1, h;
+    asm("mul.lo.u32 %0, %3, 7;\n\t"
+        "mul.hi.u32 %1, %3, 7;\n\t"
+        "mad.lo.cc.u32 %1, %4, 7, %1;\n\t"
+        "madc.hi.u32 %2, %4, 7, 0;"
+        : "=r"(l0), "=r"(l1), "=r"(h)
+        : "r"(lo32(x)), "r"(hi32(x)));
+    return fold_lo(mk64(l0, l1), h);
+}
+
+// An unreduced sum of 64 × 64-bit products (and words) in five 32-bit limbs: exact for fewer than
+// 2^32 terms, and folded to one word once, where the sum is used.
+struct Acc {
+    uint32_t w[5];
+};
+
+__device__ __forceinline__ Acc acc_zero() { return {{0, 0, 0, 0, 0}}; }
+__device__ __forceinline__ Acc acc_of(uint64_t x) { return {{lo32(x), hi32(x), 0, 0, 0}}; }
+
+// x·y as a sum
+__device__ __forceinline__ Acc acc_mul(uint64_t x, uint64_t y) {
+    Acc a;
+    asm("{\n\t"
+        "mul.lo.u32 %0, %4, %6;\n\t"
+        "mul.hi.u32 %1, %4, %6;\n\t"
+        "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
+        "madc.hi.u32 %2, %4, %7, 0;\n\t"
+        "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
+        "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
+        "madc.hi.u32 %3, %5, %7, 0;\n\t"
+        "mad.lo.cc.u32 %2, %5, %7, %2;\n\t"
+        "addc.u32 %3, %3, 0;\n\t"
+        "}"
+        : "=r"(a.w[0]), "=r"(a.w[1]), "=r"(a.w[2]), "=r"(a.w[3])
+        : "r"(lo32(x)), "r"(hi32(x)), "r"(lo32(y)), "r"(hi32(y)));
+    a.w[4] = 0;
+    return a;
+}
+
+// a += x·y: x0·y0 into limbs 0–1, x1·y1 into 2–3, the cross products into 1–2, each carry to limb 4.
+__device__ __forceinline__ void mad(Acc& a, uint64_t x, uint64_t y) {
+    asm("{\n\t"
+        "mad.lo.cc.u32 %0, %5, %7, %0;\n\t"
+        "madc.hi.cc.u32 %1, %5, %7, %1;\n\t"
+        "madc.lo.cc.u32 %2, %6, %8, %2;\n\t"
+        "madc.hi.cc.u32 %3, %6, %8, %3;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.lo.cc.u32 %1, %5, %8, %1;\n\t"
+        "madc.hi.cc.u32 %2, %5, %8, %2;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "mad.lo.cc.u32 %1, %6, %7, %1;\n\t"
+        "madc.hi.cc.u32 %2, %6, %7, %2;\n\t"
+        "addc.cc.u32 %3, %3, 0;\n\t"
+        "addc.u32 %4, %4, 0;\n\t"
+        "}"
+        : "+r"(a.w[0]), "+r"(a.w[1]), "+r"(a.w[2]), "+r"(a.w[3]), "+r"(a.w[4])
+        : "r"(lo32(x)), "r"(hi32(x)), "r"(lo32(y)), "r"(hi32(y)));
+}
+
+// The sum mod p as one word: limbs 0–1 + w2·2^64 + (w3 + w4·2^32)·2^96, with 2^64 ≡ 2^32 − 1 and
+// 2^96 ≡ −1.
+__device__ __forceinline__ uint64_t reduce(const Acc& a) {
+    return sub(fold_lo(mk64(a.w[0], a.w[1]), a.w[2]), mk64(a.w[3], a.w[4]));
+}
+
 }  // namespace lz
 
 // Fp2 on lazy words (any 64-bit representative; canonical only where results leave a kernel).
@@ -231,4 +299,50 @@ __device__ __forceinline__ fp2 l2_mul(fp2 a, fp2 b) {  // Karatsuba, X^2 = 7
 }
 __device__ __forceinline__ fp2 l2_scale(fp2 a, uint64_t b) { return {lz::mul(a.c0, b), lz::mul(a.c1, b)}; }
 __device__ __forceinline__ fp2 l2_canon(fp2 a) { return {lz::canon(a.c0), lz::canon(a.c1)}; }
+
+// Fp2 products as unreduced sums, one fold a component: a·b = (a0·b0 + a1·7b1, a0·b1 + a1·b0), the
+// 7·b1 passed in where b is a constant of many products (k7 = mul7(k.c1)).
+__device__ __forceinline__ fp2 l2_mulk(fp2 a, fp2 k, uint64_t k7) {
+    lz::Acc s0 = lz::acc_mul(a.c0, k.c0), s1 = lz::acc_mul(a.c0, k.c1);
+    lz::mad(s0, a.c1, k7);
+    lz::mad(s1, a.c1, k.c0);
+    return {lz::reduce(s0), lz::reduce(s1)};
+}
+__device__ __forceinline__ fp2 l2_muls(fp2 a, fp2 b) { return l2_mulk(a, b, lz::mul7(b.c1)); }
+// a + k·d
+__device__ __forceinline__ fp2 l2_fma(fp2 a, fp2 k, uint64_t k7, fp2 d) {
+    lz::Acc s0 = lz::acc_of(a.c0), s1 = lz::acc_of(a.c1);
+    lz::mad(s0, d.c0, k.c0);
+    lz::mad(s0, d.c1, k7);
+    lz::mad(s1, d.c0, k.c1);
+    lz::mad(s1, d.c1, k.c0);
+    return {lz::reduce(s0), lz::reduce(s1)};
+}
+// a·b + c·d
+__device__ __forceinline__ fp2 l2_dot(fp2 a, fp2 b, fp2 c, fp2 d) {
+    lz::Acc s0 = lz::acc_mul(a.c0, b.c0), s1 = lz::acc_mul(a.c0, b.c1);
+    lz::mad(s0, a.c1, lz::mul7(b.c1));
+    lz::mad(s0, c.c0, d.c0);
+    lz::mad(s0, c.c1, lz::mul7(d.c1));
+    lz::mad(s1, a.c1, b.c0);
+    lz::mad(s1, c.c0, d.c1);
+    lz::mad(s1, c.c1, d.c0);
+    return {lz::reduce(s0), lz::reduce(s1)};
+}
+// An unreduced Fp2 sum of products: s += k·g (k7 = 7·k.c1), s += k·x for a prime-field x.
+struct Acc2 {
+    lz::Acc c0, c1;
+};
+__device__ __forceinline__ Acc2 acc2_zero() { return {lz::acc_zero(), lz::acc_zero()}; }
+__device__ __forceinline__ void l2_mad(Acc2& s, fp2 k, uint64_t k7, fp2 g) {
+    lz::mad(s.c0, g.c0, k.c0);
+    lz::mad(s.c0, g.c1, k7);
+    lz::mad(s.c1, g.c0, k.c1);
+    lz::mad(s.c1, g.c1, k.c0);
+}
+__device__ __forceinline__ void l2_mad_base(Acc2& s, fp2 k, uint64_t x) {
+    lz::mad(s.c0, x, k.c0);
+    lz::mad(s.c1, x, k.c1);
+}
+__device__ __forceinline__ fp2 l2_reduce(const Acc2& s) { return {lz::reduce(s.c0), lz::reduce(s.c1)}; }
 }  // namespace tg

@@ -273,31 +273,29 @@ __device__ __forceinline__ fp2 ld2(const ulonglong2* p) {
 // pair gives (D0 + μ)(D1 + μ) at the nodes, and since the eq weights sum to 1 the kernel turns the
 // segment's sums into λ·S − μ at 0 and 1 and λ·S at ∞ once — one Fp2 product fewer per node.
 template <int KIND, bool ONE>
-__device__ __forceinline__ void tl_nodes(const fp2* u, const fp2* d, fp2 lam, fp2 mu, bool shift, fp2& g0, fp2& g1,
-                                         fp2& gi) {
+__device__ __forceinline__ void tl_nodes(const fp2* u, const fp2* d, fp2 lam, uint64_t lam7, fp2 mu, bool shift, fp2& g0,
+                                         fp2& g1, fp2& gi) {
     if constexpr (KIND == 0) {
-        g0 = l2_mul(u[0], u[1]);
-        gi = l2_mul(d[0], d[1]);
-        if constexpr (ONE) g1 = l2_mul(l2_add(u[0], d[0]), l2_add(u[1], d[1]));
+        g0 = l2_muls(u[0], u[1]);
+        gi = l2_muls(d[0], d[1]);
+        if constexpr (ONE) g1 = l2_muls(l2_add(u[0], d[0]), l2_add(u[1], d[1]));
     } else if constexpr (KIND == 1) {
-        auto f = [&](fp2 n0, fp2 n1, fp2 d0, fp2 d1) {
-            return l2_add(l2_mul(n0, d1), l2_mul(d0, l2_add(n1, l2_mul(lam, d1))));
-        };
+        auto f = [&](fp2 n0, fp2 n1, fp2 d0, fp2 d1) { return l2_dot(n0, d1, d0, l2_fma(n1, lam, lam7, d1)); };
         g0 = f(u[0], u[1], u[2], u[3]);
         gi = f(d[0], d[1], d[2], d[3]);
         if constexpr (ONE)
             g1 = f(l2_add(u[0], d[0]), l2_add(u[1], d[1]), l2_add(u[2], d[2]), l2_add(u[3], d[3]));
     } else if (shift) {
         const fp2 a = l2_add(u[0], mu), b = l2_add(u[1], mu);
-        g0 = l2_mul(a, b);
-        gi = l2_mul(d[0], d[1]);
-        if constexpr (ONE) g1 = l2_mul(l2_add(a, d[0]), l2_add(b, d[1]));
+        g0 = l2_muls(a, b);
+        gi = l2_muls(d[0], d[1]);
+        if constexpr (ONE) g1 = l2_muls(l2_add(a, d[0]), l2_add(b, d[1]));
     } else {
-        g0 = l2_add(l2_add(u[0], u[1]), l2_mul(lam, l2_mul(u[0], u[1])));
-        gi = l2_mul(d[0], d[1]);
+        g0 = l2_fma(l2_add(u[0], u[1]), lam, lam7, l2_muls(u[0], u[1]));
+        gi = l2_muls(d[0], d[1]);
         if constexpr (ONE) {
             const fp2 a = l2_add(u[0], d[0]), b = l2_add(u[1], d[1]);
-            g1 = l2_add(l2_add(a, b), l2_mul(lam, l2_mul(a, b)));
+            g1 = l2_fma(l2_add(a, b), lam, lam7, l2_muls(a, b));
         }
     }
 }
@@ -324,7 +322,7 @@ enum : int { TL_SUM = 0, TL_BIND_BASE = 1, TL_SUM_BASE = 2, TL_BIND = 3 };
 // latency of HBM at two or three resident blocks per SM, within the register budget.
 template <int KIND, int MODE>
 __host__ __device__ constexpr int tl_batch() {
-    return MODE == TL_SUM_BASE ? 4 : (KIND == 1 || (KIND == 2 && MODE == TL_BIND)) ? 1 : 2;
+    return MODE == TL_SUM_BASE ? 2 : (KIND == 1 || MODE == TL_BIND) ? 1 : 2;
 }
 
 // One pair's values as loaded: E entries of each of NT tables (E = 4 when binding, else 2),
@@ -356,16 +354,19 @@ __device__ __forceinline__ void tl_load(const TlSeg& g, uint64_t p, TlRaw<NT, MO
 }
 
 // A pair's contribution: binds (writing the bound entries), forms g at the nodes and adds w·g to
-// the chunk's part sums.
+// the chunk's unreduced part sums. k7 holds 7·c1 of the constants: r (the challenge), λ, w.
+struct TlK7 {
+    uint64_t r, lam;
+};
 template <int NT, int KIND, int MODE, bool ONE>
 __device__ __forceinline__ void tl_pair(const TlSeg& g, uint64_t p, const TlRaw<NT, MODE>& raw, fp2 w, fp2 r, fp2 lam,
-                                        fp2 (&part)[3]) {
+                                        TlK7 k7, Acc2 (&part)[3]) {
     if constexpr (MODE == TL_SUM_BASE) {
         const uint64_t l0 = raw.v[0][0].x, r0 = raw.v[0][0].y, l1 = raw.v[0][1].x, r1 = raw.v[0][1].y;
         const uint64_t v0 = lz::mul(l0, r0), vi = lz::mul(lz::sub(l1, l0), lz::sub(r1, r0));
-        part[0] = l2_add(part[0], l2_scale(w, v0));
-        part[2] = l2_add(part[2], l2_scale(w, vi));
-        if constexpr (ONE) part[1] = l2_add(part[1], l2_scale(w, lz::mul(l1, r1)));
+        l2_mad_base(part[0], w, v0);
+        l2_mad_base(part[2], w, vi);
+        if constexpr (ONE) l2_mad_base(part[1], w, lz::mul(l1, r1));
     } else {
         fp2 u[NT], d[NT];
         if constexpr (MODE == TL_BIND_BASE) {
@@ -386,8 +387,8 @@ __device__ __forceinline__ void tl_pair(const TlSeg& g, uint64_t p, const TlRaw<
             for (int k = 0; k < NT; k++) {
                 const fp2 a0 = {raw.v[k][0].x, raw.v[k][0].y}, a1 = {raw.v[k][1].x, raw.v[k][1].y};
                 const fp2 b0 = {raw.v[k][2].x, raw.v[k][2].y}, b1 = {raw.v[k][3].x, raw.v[k][3].y};
-                const fp2 uu = l2_add(a0, l2_mul(r, l2_sub(a1, a0)));
-                const fp2 vv = l2_add(b0, l2_mul(r, l2_sub(b1, b0)));
+                const fp2 uu = l2_fma(a0, r, k7.r, l2_sub(a1, a0));
+                const fp2 vv = l2_fma(b0, r, k7.r, l2_sub(b1, b0));
                 g.dst[k][2 * p] = make_ulonglong2(uu.c0, uu.c1);
                 g.dst[k][2 * p + 1] = make_ulonglong2(vv.c0, vv.c1);
                 u[k] = uu;
@@ -401,10 +402,11 @@ __device__ __forceinline__ void tl_pair(const TlSeg& g, uint64_t p, const TlRaw<
             }
         }
         fp2 g0, g1, gi;
-        tl_nodes<KIND, ONE>(u, d, lam, fp2{g.mu[0], g.mu[1]}, g.shift, g0, g1, gi);
-        part[0] = l2_add(part[0], l2_mul(w, g0));
-        part[2] = l2_add(part[2], l2_mul(w, gi));
-        if constexpr (ONE) part[1] = l2_add(part[1], l2_mul(w, g1));
+        tl_nodes<KIND, ONE>(u, d, lam, k7.lam, fp2{g.mu[0], g.mu[1]}, g.shift, g0, g1, gi);
+        const uint64_t w7 = lz::mul7(w.c1);
+        l2_mad(part[0], w, w7, g0);
+        l2_mad(part[2], w, w7, gi);
+        if constexpr (ONE) l2_mad(part[1], w, w7, g1);
     }
 }
 
@@ -418,8 +420,9 @@ __device__ __forceinline__ void tl_sum(const TlSeg& g, uint64_t b, fp2 (&acc)[3]
     const uint64_t span = 1ull << lb, chunks = g.n >> lb;
     const fp2 r = (MODE == TL_BIND || MODE == TL_BIND_BASE) ? fp2{g.r[0], g.r[1]} : fp2{0, 0};
     const fp2 lam = {g.lam[0], g.lam[1]};
+    const TlK7 k7 = {lz::mul7(r.c1), lz::mul7(lam.c1)};
     for (uint64_t c = b; c < chunks; c += (uint64_t)g.nblocks) {
-        fp2 part[3] = {{0, 0}, {0, 0}, {0, 0}};
+        Acc2 part[3] = {acc2_zero(), acc2_zero(), acc2_zero()};
         for (uint64_t e0 = threadIdx.x; e0 < span; e0 += (uint64_t)U * TL_THREADS) {
             TlRaw<NT, MODE> raw[U];
 #pragma unroll
@@ -430,13 +433,13 @@ __device__ __forceinline__ void tl_sum(const TlSeg& g, uint64_t b, fp2 (&acc)[3]
 #pragma unroll
             for (int u = 0; u < U; u++) {
                 const uint64_t e = e0 + (uint64_t)u * TL_THREADS;
-                if (U == 1 || e < span) tl_pair<NT, KIND, MODE, ONE>(g, (c << lb) + e, raw[u], ld2(g.lo + e), r, lam, part);
+                if (U == 1 || e < span) tl_pair<NT, KIND, MODE, ONE>(g, (c << lb) + e, raw[u], ld2(g.lo + e), r, lam, k7, part);
             }
         }
         const fp2 h = ld2(g.hi + c);
-        acc[0] = l2_add(acc[0], l2_mul(h, part[0]));
-        acc[2] = l2_add(acc[2], l2_mul(h, part[2]));
-        if constexpr (ONE) acc[1] = l2_add(acc[1], l2_mul(h, part[1]));
+        acc[0] = l2_add(acc[0], l2_mul(h, l2_reduce(part[0])));
+        acc[2] = l2_add(acc[2], l2_mul(h, l2_reduce(part[2])));
+        if constexpr (ONE) acc[1] = l2_add(acc[1], l2_mul(h, l2_reduce(part[1])));
     }
 }
 
