@@ -74,13 +74,14 @@ __device__ __forceinline__ fp2 load_entry(const uint64_t* t, bool base, uint64_t
     return {v.x, v.y};
 }
 
-// a + r·(b − a) on lazy words (bound tables hold lazy words; the last bind canonicalises).
-__device__ __forceinline__ fp2 bind_pair(fp2 a, fp2 b, fp2 r, bool base) {
+// a + r·(b − a) on lazy words (bound tables hold lazy words; the last bind canonicalises); r7 =
+// 7·r.c1.
+__device__ __forceinline__ fp2 bind_pair(fp2 a, fp2 b, fp2 r, uint64_t r7, bool base) {
     if (base) {  // a, b in the prime field: two base products
         const uint64_t d = lz::sub(b.c0, a.c0);
         return {lz::add(a.c0, lz::mul(r.c0, d)), lz::mul(r.c1, d)};
     }
-    return l2_add(a, l2_mul(r, l2_sub(b, a)));
+    return l2_fma(a, r, r7, l2_sub(b, a));
 }
 
 // Sums NW words across the block (warp shuffles, then one word per warp in shared memory);
@@ -120,7 +121,7 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
             fp2 prod = {1, 0};
             for (int k = 0; k < nt; k++) {
                 const fp2 e = load_entry(g.src[k], (g.base_mask >> k) & 1, x);
-                prod = k ? l2_mul(prod, e) : e;
+                prod = k ? l2_muls(prod, e) : e;
             }
             acc = l2_add(acc, prod);
         }
@@ -159,6 +160,7 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
 #pragma unroll
         for (int d = 0; d < D; d++) acc[d] = {0, 0};
         const fp2 r = g.bind ? fp2{g.r[0], g.r[1]} : fp2{0, 0};
+        const uint64_t r7 = lz::mul7(r.c1);
         for (uint64_t p = (uint64_t)lb * blockDim.x + threadIdx.x; p < g.n; p += stride) {
             fp2 prod[D];
 #pragma unroll
@@ -167,8 +169,8 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
                 const bool base = (g.base_mask >> k) & 1;
                 fp2 u, v;
                 if (g.bind) {
-                    u = bind_pair(load_entry(g.src[k], base, 4 * p), load_entry(g.src[k], base, 4 * p + 1), r, base);
-                    v = bind_pair(load_entry(g.src[k], base, 4 * p + 2), load_entry(g.src[k], base, 4 * p + 3), r, base);
+                    u = bind_pair(load_entry(g.src[k], base, 4 * p), load_entry(g.src[k], base, 4 * p + 1), r, r7, base);
+                    v = bind_pair(load_entry(g.src[k], base, 4 * p + 2), load_entry(g.src[k], base, 4 * p + 3), r, r7, base);
                     ulonglong2* out = reinterpret_cast<ulonglong2*>(g.dst[k]);
                     out[2 * p] = make_ulonglong2(u.c0, u.c1);
                     out[2 * p + 1] = make_ulonglong2(v.c0, v.c1);
@@ -178,12 +180,12 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
                 }
                 const fp2 diff = l2_sub(v, u);
                 fp2 x = v;
-                prod[0] = k ? l2_mul(prod[0], u) : u;  // the first table's values start the products
+                prod[0] = k ? l2_muls(prod[0], u) : u;  // the first table's values start the products
 #pragma unroll
                 for (int d = 1; d < D; d++) {
                     if (d < deg) {
                         x = l2_add(x, diff);
-                        prod[d] = k ? l2_mul(prod[d], x) : x;
+                        prod[d] = k ? l2_muls(prod[d], x) : x;
                     }
                 }
             }
@@ -261,7 +263,7 @@ __global__ void sc_bind_last(const BindLast* b, int n) {
     if (i >= n) return;
     const BindLast t = b[i];
     const fp2 r = {t.r[0], t.r[1]};
-    const fp2 u = l2_canon(bind_pair(load_entry(t.src, t.base, 0), load_entry(t.src, t.base, 1), r, t.base));
+    const fp2 u = l2_canon(bind_pair(load_entry(t.src, t.base, 0), load_entry(t.src, t.base, 1), r, lz::mul7(r.c1), t.base));
     reinterpret_cast<ulonglong2*>(t.dst)[0] = make_ulonglong2(u.c0, u.c1);
 }
 

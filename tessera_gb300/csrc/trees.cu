@@ -59,8 +59,8 @@ __global__ void tr_product_level2(const ulonglong2* below, ulonglong2* mid, ulon
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < m; x += stride) {
         const ulonglong2 a = below[4 * x], b = below[4 * x + 1], c = below[4 * x + 2], d = below[4 * x + 3];
-        const fp2 p = l2_canon(l2_mul(fp2{a.x, a.y}, fp2{b.x, b.y})), q = l2_canon(l2_mul(fp2{c.x, c.y}, fp2{d.x, d.y}));
-        const fp2 r = l2_canon(l2_mul(p, q));
+        const fp2 p = l2_canon(l2_muls(fp2{a.x, a.y}, fp2{b.x, b.y})), q = l2_canon(l2_muls(fp2{c.x, c.y}, fp2{d.x, d.y}));
+        const fp2 r = l2_canon(l2_muls(p, q));
         mid[2 * x] = make_ulonglong2(p.c0, p.c1);
         mid[2 * x + 1] = make_ulonglong2(q.c0, q.c1);
         above[x] = make_ulonglong2(r.c0, r.c1);
@@ -108,16 +108,16 @@ __global__ void tr_fraction_level2(const ulonglong2* n, const ulonglong2* d, ulo
             const fp2 c = {dl.x, dl.y}, e = {dr.x, dr.y};
             if (n) {
                 const ulonglong2 nl = n[4 * x + 2 * h], nr = n[4 * x + 2 * h + 1];
-                nn[h] = l2_canon(l2_add(l2_mul(fp2{nl.x, nl.y}, e), l2_mul(fp2{nr.x, nr.y}, c)));
+                nn[h] = l2_canon(l2_dot(fp2{nl.x, nl.y}, e, fp2{nr.x, nr.y}, c));
             } else {
                 nn[h] = l2_canon(l2_add(c, e));
             }
-            dd[h] = l2_canon(l2_mul(c, e));
+            dd[h] = l2_canon(l2_muls(c, e));
             n_mid[2 * x + h] = make_ulonglong2(nn[h].c0, nn[h].c1);
             d_mid[2 * x + h] = make_ulonglong2(dd[h].c0, dd[h].c1);
         }
-        // (lazy arithmetic, every stored entry canonical)
-        const fp2 no = l2_canon(l2_add(l2_mul(nn[0], dd[1]), l2_mul(nn[1], dd[0]))), dn = l2_canon(l2_mul(dd[0], dd[1]));
+        // (products as unreduced sums, every stored entry canonical)
+        const fp2 no = l2_canon(l2_dot(nn[0], dd[1], nn[1], dd[0])), dn = l2_canon(l2_muls(dd[0], dd[1]));
         n_out[x] = make_ulonglong2(no.c0, no.c1);
         d_out[x] = make_ulonglong2(dn.c0, dn.c1);
     }
@@ -696,6 +696,7 @@ __global__ void __launch_bounds__(TL_ROOT_THREADS, 1) tl_root_claim(const void* 
     for (int c = 0; c < s; c++) {
         const uint64_t m = 1ull << (s - c - 1);  // entries after this fold
         const fp2 t = {point[2 * c], point[2 * c + 1]};
+        const uint64_t t7 = lz::mul7(t.c1);
         const ulonglong2* src = c ? buf[(c - 1) & 1] : static_cast<const ulonglong2*>(level);
         ulonglong2* dst = buf[c & 1];
         for (uint64_t k = threadIdx.x; k < m; k += blockDim.x) {
@@ -706,7 +707,7 @@ __global__ void __launch_bounds__(TL_ROOT_THREADS, 1) tl_root_claim(const void* 
             } else {
                 a = ld2(src + 2 * k), b = ld2(src + 2 * k + 1);
             }
-            const fp2 v = l2_add(a, l2_mul(t, l2_sub(b, a)));
+            const fp2 v = l2_fma(a, t, t7, l2_sub(b, a));
             dst[k] = make_ulonglong2(v.c0, v.c1);
         }
         __syncthreads();
