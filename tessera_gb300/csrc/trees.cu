@@ -460,13 +460,13 @@ __device__ __forceinline__ void tl_block_sum(uint64_t (&words)[6], uint64_t (*re
 // One round's segments of one kind and mode: each block sums its share of its segment, and the
 // segment's last block adds the blocks' rows into the segment's q.
 // Resident blocks per SM a variant's registers allow: three for the prime-field sums, two else.
-template <int MODE>
+template <int KIND, int MODE>
 __host__ __device__ constexpr int tl_min_blocks() {
-    return MODE == TL_SUM_BASE ? 3 : 2;
+    return MODE == TL_SUM_BASE || (KIND != 1 && MODE == TL_BIND) ? 3 : 2;
 }
 
 template <int NT, int KIND, int MODE, bool ONE>
-__global__ void __launch_bounds__(TL_THREADS, tl_min_blocks<MODE>()) tl_rounds(const TlSeg* segs, int nseg,
+__global__ void __launch_bounds__(TL_THREADS, tl_min_blocks<KIND, MODE>()) tl_rounds(const TlSeg* segs, int nseg,
                                                                               uint64_t* partials, unsigned* counters) {
     __shared__ TlSeg g;
     __shared__ int si;
