@@ -288,6 +288,8 @@ int tg_device_close(tg_device* dev) {
         if (d->staged[b]) cudaEventDestroy(d->staged[b]);
         if (d->consumed[b]) cudaEventDestroy(d->consumed[b]);
     }
+    for (cudaEvent_t& e : d->ramp)
+        if (e) cudaEventDestroy(e);
     d->stage_rows.release();
     d->stage_cw.release();
     d->stage_nodes.release();
@@ -509,6 +511,7 @@ int tg_commit_unmasked(tg_device* dev, uint32_t log_k, uint32_t log_inv_rate, ui
             TG_CUDA(cudaEventCreateWithFlags(&d->staged[b], cudaEventDisableTiming));
             TG_CUDA(cudaEventCreateWithFlags(&d->consumed[b], cudaEventDisableTiming));
         }
+        for (cudaEvent_t& e : d->ramp) TG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     }
     cudaStream_t s = d->stream, cs = d->copy_stream;
     uint64_t* stage = (uint64_t*)d->stage_rows.ptr;
@@ -525,19 +528,29 @@ int tg_commit_unmasked(tg_device* dev, uint32_t log_k, uint32_t log_inv_rate, ui
         uint64_t* half = stage + b * chunk * k;
         TG_CUDA(cudaStreamWaitEvent(cs, d->consumed[b], 0));
         if (c == 0 && g >= 2) {
-            // the first chunk's copy has nothing to hide behind: its first half is encoded while
-            // the second half is still in flight
-            const size_t g0 = g / 2;
-            TG_CUDA(cudaMemcpyAsync(half, rows, g0 * k * 8, cudaMemcpyHostToDevice, cs));
-            TG_CUDA(cudaEventRecord(d->staged[1], cs));  // staged[1] is free until chunk 1
-            TG_CUDA(cudaMemcpyAsync(half + g0 * k, rows + g0 * k, (g - g0) * k * 8, cudaMemcpyHostToDevice, cs));
-            TG_CUDA(cudaEventRecord(d->staged[0], cs));
-            TG_CUDA(cudaStreamWaitEvent(s, d->staged[1], 0));
-            rc = lde_encode(d, log_k, log_inv_rate, 0, half, g0, nullptr, cw, s);
-            if (rc) return rc;
-            TG_CUDA(cudaStreamWaitEvent(s, d->staged[0], 0));
-            rc = lde_encode(d, log_k, log_inv_rate, 0, half + g0 * k, g - g0, nullptr, cw + g0 * n, s);
-            if (rc) return rc;
+            // the first chunk's copy has nothing to hide behind: it goes in pieces of g/8, g/8,
+            // g/4 and the rest, each encoded as soon as it has landed, so that only the first
+            // piece's copy is exposed
+            size_t piece[4], np = 0, at = 0, want = std::max<size_t>(1, g / 8);
+            while (at < g) {
+                const size_t take = np == 3 ? g - at : std::min(want, g - at);
+                piece[np++] = take;
+                at += take;
+                if (np >= 2) want *= 2;
+            }
+            at = 0;
+            for (size_t q = 0; q < np; q++) {
+                TG_CUDA(cudaMemcpyAsync(half + at * k, rows + at * k, piece[q] * k * 8, cudaMemcpyHostToDevice, cs));
+                TG_CUDA(cudaEventRecord(d->ramp[q], cs));
+                at += piece[q];
+            }
+            at = 0;
+            for (size_t q = 0; q < np; q++) {
+                TG_CUDA(cudaStreamWaitEvent(s, d->ramp[q], 0));
+                rc = lde_encode(d, log_k, log_inv_rate, 0, half + at * k, piece[q], nullptr, cw + at * n, s);
+                if (rc) return rc;
+                at += piece[q];
+            }
         } else {
             TG_CUDA(cudaMemcpyAsync(half, rows + r0 * k, g * k * 8, cudaMemcpyHostToDevice, cs));
             TG_CUDA(cudaEventRecord(d->staged[b], cs));

@@ -73,6 +73,7 @@ struct Device {
     DevBuf stage_rows, stage_cw, stage_nodes;
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t staged[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
+    cudaEvent_t ramp[4] = {nullptr, nullptr, nullptr, nullptr};  // the first chunk's pieces landed
     DevBuf err;  // device error words for bounded waits
     tg_config cfg;
     std::atomic<uint64_t> launches{0};  // kernels this handle has launched

@@ -191,11 +191,12 @@ def test_commit_unmasked_shapes(dev, npolys, log_k, log_r, B):
     assert c.root() == root and b"".join(c.leaves()) == leaves.tobytes()
 
 
-@pytest.mark.parametrize("npolys,B,group_rows", [(37, 2, 5), (37, 3, 5), (20, 7, 5), (16, 4, 8), (9, 32, 2)])
+@pytest.mark.parametrize("npolys,B,group_rows", [(37, 2, 5), (37, 3, 5), (20, 7, 5), (16, 4, 8), (9, 32, 2),
+                                                 (40, 32, 40), (3, 1, 3)])
 def test_commit_unmasked_pipelined_chunks(npolys, B, group_rows):
     """The host-buffer commitment copies rows in chunks of whole row blocks while the previous
-    chunk encodes: a small encoder group forces many chunks (and a short last one); the root and
-    leaves match the oracle."""
+    chunk encodes, and the first chunk in pieces of 1/8, 1/8, 1/4 and the rest: a small encoder
+    group forces many chunks (and a short last one); the root and leaves match the oracle."""
     from tessera_gb300.device import Device
     from tessera_gb300.pcs import CommitmentParams, ReferenceCommitment
 
