@@ -40,174 +40,159 @@ struct FsJob {
 constexpr int FS_THREADS = 128;  // four warps, one job each
 constexpr int FS_BUF_WORDS = 132;  // 512 bytes of message, and 4 words that stagger the threads' banks
 
-// BLAKE3 (derive-key-material mode under `key`) of the first len bytes of buf; the bytes of buf
-// past len up to the next block boundary are overwritten with zeros.
-static __device__ void fs_hash(const uint32_t key[8], uint32_t* buf, uint32_t len, uint32_t out[8]) {
-    uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
-    const uint32_t nb = len == 0 ? 1 : (len + 63) / 64;
-    for (uint32_t i = len; i < 64 * nb; i++) bytes[i] = 0;
+// The G function with its additions on the ALU: a transcript is a dependent chain, where the shorter
+// latency counts, not the pipe the additions issue on (the column chains, bound by throughput, put
+// them on the multiply-add pipe instead; here that form is about 10 % slower).
+static __device__ __forceinline__ void b3_g_alu(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d, uint32_t x,
+                                                uint32_t y) {
+    a = a + b + x;
+    d = b3::rotr(d ^ a, 16);
+    c = c + d;
+    b = b3::rotr(b ^ c, 12);
+    a = a + b + y;
+    d = b3::rotr(d ^ a, 8);
+    c = c + d;
+    b = b3::rotr(b ^ c, 7);
+}
+
+// One compression by one thread with the additions on the ALU and the message in registers: a
+// transcript is a chain of dependent compressions, and one thread's chain is shorter than that of
+// four lanes running the G functions side by side with shuffles between the column and diagonal
+// steps (about 1,250 against 1,450 cycles a compression on GB300).
+#define FS_G(a, b, c, d, x, y) b3_g_alu(a, b, c, d, x, y);
+#define FS_ROUND(m0, m1, m2, m3, m4, m5, m6, m7, m8, m9, m10, m11, m12, m13, m14, m15) \
+    FS_G(s0, s4, s8, s12, m0, m1)                                                       \
+    FS_G(s1, s5, s9, s13, m2, m3)                                                       \
+    FS_G(s2, s6, s10, s14, m4, m5)                                                      \
+    FS_G(s3, s7, s11, s15, m6, m7)                                                      \
+    FS_G(s0, s5, s10, s15, m8, m9)                                                      \
+    FS_G(s1, s6, s11, s12, m10, m11)                                                    \
+    FS_G(s2, s7, s8, s13, m12, m13)                                                     \
+    FS_G(s3, s4, s9, s14, m14, m15)
+static __device__ __forceinline__ void compress_one(uint32_t cv[8], const uint32_t* mp, uint32_t len, uint32_t flags) {
+    uint32_t m[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) m[i] = mp[i];
+    uint32_t s0 = cv[0], s1 = cv[1], s2 = cv[2], s3 = cv[3], s4 = cv[4], s5 = cv[5], s6 = cv[6], s7 = cv[7];
+    uint32_t s8 = TG_B3_IV0, s9 = TG_B3_IV1, s10 = TG_B3_IV2, s11 = TG_B3_IV3, s12 = 0, s13 = 0, s14 = len, s15 = flags;
+    FS_ROUND(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10], m[11], m[12], m[13], m[14], m[15])
+    FS_ROUND(m[2], m[6], m[3], m[10], m[7], m[0], m[4], m[13], m[1], m[11], m[12], m[5], m[9], m[14], m[15], m[8])
+    FS_ROUND(m[3], m[4], m[10], m[12], m[13], m[2], m[7], m[14], m[6], m[5], m[9], m[0], m[11], m[15], m[8], m[1])
+    FS_ROUND(m[10], m[7], m[12], m[9], m[14], m[3], m[13], m[15], m[4], m[0], m[11], m[2], m[5], m[8], m[1], m[6])
+    FS_ROUND(m[12], m[13], m[9], m[11], m[15], m[10], m[14], m[8], m[7], m[2], m[5], m[3], m[0], m[1], m[6], m[4])
+    FS_ROUND(m[9], m[14], m[11], m[5], m[8], m[12], m[15], m[1], m[13], m[3], m[0], m[10], m[2], m[6], m[4], m[7])
+    FS_ROUND(m[11], m[15], m[5], m[0], m[1], m[9], m[8], m[6], m[14], m[10], m[2], m[12], m[3], m[4], m[7], m[13])
+    cv[0] = s0 ^ s8, cv[1] = s1 ^ s9, cv[2] = s2 ^ s10, cv[3] = s3 ^ s11;
+    cv[4] = s4 ^ s12, cv[5] = s5 ^ s13, cv[6] = s6 ^ s14, cv[7] = s7 ^ s15;
+}
+#undef FS_ROUND
+#undef FS_G
+
+// BLAKE3 in derive-key-material mode under `key` of the first len bytes of buf (zero from len to
+// the next block boundary), by lane 0 of a warp; every lane gets the output.
+static __device__ __noinline__ void fs_hash_warp(const uint32_t key[8], const uint32_t* buf, uint32_t len, uint32_t out[8]) {
     uint32_t h[8];
 #pragma unroll
     for (int i = 0; i < 8; i++) h[i] = key[i];
-    for (uint32_t b = 0; b < nb; b++) {
-        uint32_t m[16];
-#pragma unroll
-        for (int i = 0; i < 16; i++) m[i] = buf[16 * b + i];
-        const bool last = b + 1 == nb;
-        b3::compress_cv(h, m, 0, last ? len - 64 * b : 64,
-                        b3::DERIVE_KEY_MATERIAL | (b == 0 ? b3::CHUNK_START : 0) | (last ? (b3::CHUNK_END | b3::ROOT) : 0));
+    if ((threadIdx.x & 31) == 0) {
+        const uint32_t nb = len == 0 ? 1 : (len + 63) / 64;
+        for (uint32_t b = 0; b < nb; b++) {
+            const bool last = b + 1 == nb;
+            compress_one(h, buf + 16 * b, last ? len - 64 * b : 64,
+                         b3::DERIVE_KEY_MATERIAL | (b == 0 ? b3::CHUNK_START : 0) | (last ? (b3::CHUNK_END | b3::ROOT) : 0));
+        }
     }
 #pragma unroll
-    for (int i = 0; i < 8; i++) out[i] = h[i];
+    for (int i = 0; i < 8; i++) out[i] = __shfl_sync(0xFFFFFFFFu, h[i], 0);
 }
 
-// ---- one compression by a warp: the four lanes of each quad run the column and the diagonal
-// G functions of a round side by side (lane i holds column i: words i, 4 + i, 8 + i, 12 + i),
-// rotating the rows by shuffles for the diagonal step; every lane ends with the whole chaining
-// value.
-
-// Word k of round r's message is m[kB3Sched[r][k]] (the message permutation applied r times).
-constexpr uint8_t kB3Sched[7][16] = {
-    {0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 11, 12, 13, 14, 15},  {2, 6, 3, 10, 7, 0, 4, 13, 1, 11, 12, 5, 9, 14, 15, 8},
-    {3, 4, 10, 12, 13, 2, 7, 14, 6, 5, 9, 0, 11, 15, 8, 1},  {10, 7, 12, 9, 14, 3, 13, 15, 4, 0, 11, 2, 5, 8, 1, 6},
-    {12, 13, 9, 11, 15, 10, 14, 8, 7, 2, 5, 3, 0, 1, 6, 4},  {9, 14, 11, 5, 8, 12, 15, 1, 13, 3, 0, 10, 2, 6, 4, 7},
-    {11, 15, 5, 0, 1, 9, 8, 6, 14, 10, 2, 12, 3, 4, 7, 13}};
-
-// The four schedule indices lane i of a quad reads in round r (column words 2i, 2i + 1, diagonal
-// words 8 + 2i, 9 + 2i), four bits each; rounds 0–3 in the low word, 4–6 in the high word, so a
-// lane keeps its whole schedule in two registers instead of loading lane-divergent table entries.
-__host__ __device__ constexpr uint64_t b3_lane_sched(int i, int half) {
+// A label tail ("/round/", "/r/") as little-endian bytes of one word, and its length.
+constexpr uint64_t fs_pack(const char* t) {
     uint64_t v = 0;
-    for (int r = 4 * half; r < 7 && r < 4 * half + 4; r++) {
-        const uint64_t q = (uint64_t)kB3Sched[r][2 * i] | ((uint64_t)kB3Sched[r][2 * i + 1] << 4) |
-                           ((uint64_t)kB3Sched[r][8 + 2 * i] << 8) | ((uint64_t)kB3Sched[r][9 + 2 * i] << 12);
-        v |= q << (16 * (r - 4 * half));
-    }
+    for (int i = 0; i < 8 && t[i]; i++) v |= (uint64_t)(uint8_t)t[i] << (8 * i);
     return v;
 }
-
-static __device__ __forceinline__ void b3_g(uint32_t& a, uint32_t& b, uint32_t& c, uint32_t& d, uint32_t x, uint32_t y) {
-    using namespace b3;
-    TG_B3_G(a, b, c, d, x, y)
-}
-
-// ROLLED keeps one round's code (the schedule's words are lane-dependent lookups either way): for a
-// warp that runs alone on its SM, whose unrolled rounds would miss in the instruction cache.
-template <bool ROLLED>
-static __device__ __forceinline__ void compress_quad(uint32_t cv[8], const uint32_t* m, uint32_t len, uint32_t flags) {
-    const int i = threadIdx.x & 3;
-    const uint32_t iv[4] = {TG_B3_IV0, TG_B3_IV1, TG_B3_IV2, TG_B3_IV3};
-    uint32_t a = cv[i], b = cv[4 + i], c = iv[i], d = i < 2 ? 0u : i == 2 ? len : flags;
-    constexpr uint64_t L0 = b3_lane_sched(0, 0), L1 = b3_lane_sched(1, 0), L2 = b3_lane_sched(2, 0), L3 = b3_lane_sched(3, 0);
-    constexpr uint64_t H0 = b3_lane_sched(0, 1), H1 = b3_lane_sched(1, 1), H2 = b3_lane_sched(2, 1), H3 = b3_lane_sched(3, 1);
-    uint64_t slo = i == 0 ? L0 : i == 1 ? L1 : i == 2 ? L2 : L3;
-    uint64_t shi = i == 0 ? H0 : i == 1 ? H1 : i == 2 ? H2 : H3;
-#pragma unroll(ROLLED ? 1 : 7)
-    for (int r = 0; r < 7; r++) {
-        const uint32_t q = (uint32_t)slo & 0xFFFFu;  // this round's four indices
-        slo = (slo >> 16) | (shi << 48);
-        shi >>= 16;
-        b3_g(a, b, c, d, m[q & 15], m[(q >> 4) & 15]);
-        b = __shfl_sync(0xFFFFFFFFu, b, (i + 1) & 3, 4);
-        c = __shfl_sync(0xFFFFFFFFu, c, (i + 2) & 3, 4);
-        d = __shfl_sync(0xFFFFFFFFu, d, (i + 3) & 3, 4);
-        b3_g(a, b, c, d, m[(q >> 8) & 15], m[q >> 12]);
-        b = __shfl_sync(0xFFFFFFFFu, b, (i + 3) & 3, 4);
-        c = __shfl_sync(0xFFFFFFFFu, c, (i + 2) & 3, 4);
-        d = __shfl_sync(0xFFFFFFFFu, d, (i + 1) & 3, 4);
-    }
-    const uint32_t lo = a ^ c, hi = b ^ d;
-#pragma unroll
-    for (int k = 0; k < 4; k++) {
-        cv[k] = __shfl_sync(0xFFFFFFFFu, lo, k, 4);
-        cv[4 + k] = __shfl_sync(0xFFFFFFFFu, hi, k, 4);
-    }
-}
-
-// fs_hash by a whole warp; the caller has zeroed buf from len to the next block boundary (one copy
-// of the code for the absorb, squeeze and ratchet calls).
-template <bool ROLLED>
-static __device__ __noinline__ void fs_hash_warp(const uint32_t key[8], const uint32_t* buf, uint32_t len, uint32_t out[8]) {
-    const uint32_t nb = len == 0 ? 1 : (len + 63) / 64;
-    uint32_t h[8];
-#pragma unroll
-    for (int i = 0; i < 8; i++) h[i] = key[i];
-    for (uint32_t b = 0; b < nb; b++) {
-        const bool last = b + 1 == nb;
-        compress_quad<ROLLED>(h, buf + 16 * b, last ? len - 64 * b : 64,
-                      b3::DERIVE_KEY_MATERIAL | (b == 0 ? b3::CHUNK_START : 0) | (last ? (b3::CHUNK_END | b3::ROOT) : 0));
-    }
-#pragma unroll
-    for (int i = 0; i < 8; i++) out[i] = h[i];
-}
-
-static __device__ __forceinline__ void zero_to_block(uint32_t* buf, uint32_t len) {
-    uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
-    const uint32_t end = (len == 0 ? 1 : (len + 63) / 64) * 64;
-    for (uint32_t i = len; i < end; i++) bytes[i] = 0;
-}
-
-// zero_to_block by a whole warp (the caller syncs the warp after it).
-static __device__ __forceinline__ void zero_to_block_warp(uint32_t* buf, uint32_t len) {
-    uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
-    const uint32_t end = (len == 0 ? 1 : (len + 63) / 64) * 64;
-    for (uint32_t i = len + (threadIdx.x & 31); i < end; i += 32) bytes[i] = 0;
-}
-
-static __device__ __forceinline__ void put64(uint8_t* p, uint64_t v) {
-    for (int i = 0; i < 8; i++) p[i] = (uint8_t)(v >> (8 * i));
-}
-
-// state ‖ u64 len(label) ‖ label, label = prefix ‖ tail ‖ decimal j, into buf; returns the length.
-static __device__ uint32_t fs_begin(const uint32_t state[8], const FsJob& jb, const char* tail, int j, uint32_t* buf) {
-    uint8_t* b = reinterpret_cast<uint8_t*>(buf);
-#pragma unroll
-    for (int i = 0; i < 8; i++) buf[i] = state[i];
-    uint32_t n = 40;
-    for (int i = 0; i < jb.label_len; i++) b[n++] = (uint8_t)jb.label[i];
-    for (const char* c = tail; *c; c++) b[n++] = (uint8_t)*c;
-    char digits[12];
-    int nd = 0;
-    do {
-        digits[nd++] = (char)('0' + j % 10);
-        j /= 10;
-    } while (j > 0);
-    while (nd > 0) b[n++] = (uint8_t)digits[--nd];
-    buf[8] = n - 40;  // the label's length as a u64
-    buf[9] = 0;
+constexpr int fs_len(const char* t) {
+    int n = 0;
+    while (t[n]) n++;
     return n;
 }
 
-// Round j's transcript step by a whole warp: lane 0 has written the round's absorb input (state ‖
-// label length ‖ <prefix>/round/j ‖ message, len bytes) into buf; every lane absorbs it, then
-// squeezes <prefix>/r/j until the first two words are a canonical Fp2 (c0, c1). state and counter
-// are the same in every lane. False after FS_MAX_TRIES squeezes.
-template <bool ROLLED = false>
+// state ‖ u64 len(label) ‖ label ‖ payload into buf by a whole warp, label = prefix ‖ tail ‖
+// decimal j and payload np little-endian u64 words (np ≤ NP; the same state, j and payload in every
+// lane), then zeros to the next block boundary; returns the length in every lane. Each lane writes
+// its own bytes (the caller syncs the warp before buf is read).
+template <int NP>
+static __device__ uint32_t fs_msg_warp(const uint32_t state[8], const FsJob& jb, uint64_t tail, int tail_len, int j,
+                                       const uint64_t (&pay)[NP], int np, uint32_t* buf) {
+    const int lane = threadIdx.x & 31;
+    uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
+    int nd = 1;  // decimal digits of j
+    for (uint32_t q = (uint32_t)j; q >= 10; q /= 10) nd++;
+    const int pre = jb.label_len, L = pre + tail_len + nd;
+    const uint32_t len = 40 + (uint32_t)L + 8 * (uint32_t)np;
+    if (lane < 10) {  // words 0–9: the state and the label's length
+        uint32_t v = lane == 8 ? (uint32_t)L : 0u;
+#pragma unroll
+        for (int i = 0; i < 8; i++)
+            if (lane == i) v = state[i];
+        buf[lane] = v;
+    }
+    for (int k = lane; k < L; k += 32) {
+        uint32_t c;
+        if (k < pre) {
+            c = (uint8_t)jb.label[k];
+        } else if (k < pre + tail_len) {
+            c = (uint32_t)(tail >> (8 * (k - pre))) & 0xFFu;
+        } else {
+            uint32_t q = (uint32_t)j;
+            for (int t = k - pre - tail_len + 1; t < nd; t++) q /= 10;
+            c = '0' + q % 10;
+        }
+        bytes[40 + k] = (uint8_t)c;
+    }
+    for (int k = lane; k < 8 * np; k += 32) {
+        uint64_t v = 0;
+#pragma unroll
+        for (int i = 0; i < NP; i++)
+            if ((k >> 3) == i) v = pay[i];
+        bytes[40 + L + k] = (uint8_t)(v >> (8 * (k & 7)));
+    }
+    const uint32_t end = (len + 63) / 64 * 64;
+    for (uint32_t i = len + lane; i < end; i += 32) bytes[i] = 0;
+    return len;
+}
+
+// Round j's transcript step by a whole warp, its absorb input (state ‖ label length ‖
+// <prefix>/round/j ‖ message) already in buf and zero padded (fs_msg_warp): absorbs it, then
+// squeezes <prefix>/r/j until the first two words are a canonical Fp2 (c0, c1), every lane building
+// the squeeze and ratchet inputs. state and counter are the same in every lane. False after
+// FS_MAX_TRIES squeezes.
 static __device__ bool fs_round_warp(const FsKeys& keys, const FsJob& jb, int j, uint32_t* buf, uint32_t len,
                                      uint32_t state[8], uint64_t* counter, uint64_t* c0, uint64_t* c1) {
     const int lane = threadIdx.x & 31;
-    zero_to_block_warp(buf, len);
     __syncwarp();
-    fs_hash_warp<ROLLED>(keys.absorb, buf, len, state);
+    fs_hash_warp(keys.absorb, buf, len, state);
     __syncwarp();
     for (int tries = 0; tries < FS_MAX_TRIES; tries++) {
-        uint32_t l2 = 0;
-        if (lane == 0) {
-            l2 = fs_begin(state, jb, "/r/", j, buf);
-            put64(reinterpret_cast<uint8_t*>(buf) + l2, *counter);
-        }
-        l2 = __shfl_sync(0xFFFFFFFFu, l2, 0);
-        __syncwarp();
-        zero_to_block_warp(buf, l2 + 8);
+        const uint64_t pay[1] = {*counter};
+        const uint32_t l2 = fs_msg_warp<1>(state, jb, fs_pack("/r/"), fs_len("/r/"), j, pay, 1, buf);
         __syncwarp();
         uint32_t out[8];
-        fs_hash_warp<ROLLED>(keys.squeeze, buf, l2 + 8, out);
+        fs_hash_warp(keys.squeeze, buf, l2, out);
         __syncwarp();
         *counter += 1;
-        if (lane == 0)
-            for (int i = 0; i < 8; i++) buf[i] = state[i], buf[8 + i] = out[i];
+        if (lane < 16) {  // the ratchet's input: state ‖ squeezed block
+            uint32_t v = 0;
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                if (lane == i) v = state[i];
+                if (lane == 8 + i) v = out[i];
+            }
+            buf[lane] = v;
+        }
         __syncwarp();
-        fs_hash_warp<ROLLED>(keys.ratchet, buf, 64, state);
+        fs_hash_warp(keys.ratchet, buf, 64, state);
         __syncwarp();
         *c0 = (uint64_t)out[0] | ((uint64_t)out[1] << 32);
         *c1 = (uint64_t)out[2] | ((uint64_t)out[3] << 32);

@@ -282,7 +282,6 @@ __global__ void sc_gather_evals(const EvalRef* refs, int n, uint64_t* out) {
 // while padded), absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
 // <prefix>/r/j.
 // One warp runs job t's round (buf: FS_BUF_WORDS of the warp's shared memory).
-template <bool ROLLED>
 __device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, const FsKeys& keys, const uint64_t* w,
                           const int* pad, const uint64_t* S, const uint64_t* msgbuf, uint64_t* rounds_out,
                           uint64_t* chal_out, uint32_t* buf) {
@@ -292,7 +291,7 @@ __device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, cons
     FsState* st = states + t;
     const int degree = jb.degree;
     fp2 msg[SC_MAX_DEGREE];
-    for (int x = 0; x < degree; x++) msg[x] = {0, 0};
+    for (int x = 0; x < SC_MAX_DEGREE; x++) msg[x] = {0, 0};
     for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {  // every lane forms the message
         const fp2 wi = {w[2 * i], w[2 * i + 1]};
         if (j < pad[i]) {
@@ -307,24 +306,19 @@ __device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, cons
 #pragma unroll
     for (int i = 0; i < 8; i++) state[i] = reinterpret_cast<const uint32_t*>(st->state)[i];
     uint64_t counter = st->counter;
-    uint32_t len = 0;
     if (lane == 0) {
-        uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
-        len = fs_begin(state, jb, "/round/", j, buf);
-        put64(bytes + len, (uint64_t)degree);
-        len += 8;
         uint64_t* rj = rounds_out + jb.rounds_off + (size_t)j * 2 * degree;
-        for (int x = 0; x < degree; x++) {
-            put64(bytes + len, msg[x].c0);
-            put64(bytes + len + 8, msg[x].c1);
-            len += 16;
-            rj[2 * x] = msg[x].c0;
-            rj[2 * x + 1] = msg[x].c1;
-        }
+        for (int x = 0; x < degree; x++) rj[2 * x] = msg[x].c0, rj[2 * x + 1] = msg[x].c1;
     }
-    len = __shfl_sync(0xFFFFFFFFu, len, 0);
+    // the message as TCE Vec<Fp2>: its length, then the values
+    uint64_t pay[1 + 2 * SC_MAX_DEGREE];
+    pay[0] = (uint64_t)degree;
+#pragma unroll
+    for (int x = 0; x < SC_MAX_DEGREE; x++) pay[1 + 2 * x] = msg[x].c0, pay[2 + 2 * x] = msg[x].c1;
+    const uint32_t len = fs_msg_warp<1 + 2 * SC_MAX_DEGREE>(state, jb, fs_pack("/round/"), fs_len("/round/"), j, pay,
+                                                            1 + 2 * degree, buf);
     uint64_t c0, c1;
-    const bool ok = fs_round_warp<ROLLED>(keys, jb, j, buf, len, state, &counter, &c0, &c1);
+    const bool ok = fs_round_warp(keys, jb, j, buf, len, state, &counter, &c0, &c1);
     if (lane != 0) return;
     if (!ok) {
         st->err = 1;
@@ -346,7 +340,7 @@ __global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const 
     __shared__ uint32_t sbuf[FS_THREADS / 32][FS_BUF_WORDS];
     const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
     if (t >= njobs) return;  // whole warps leave together
-    sc_fs_job<false>(states, jobs, t, j, keys, w, pad, S, msgbuf, rounds_out, chal_out, sbuf[threadIdx.x / 32]);
+    sc_fs_job(states, jobs, t, j, keys, w, pad, S, msgbuf, rounds_out, chal_out, sbuf[threadIdx.x / 32]);
 }
 
 // The small last rounds of a batch, j0 to J − 1, in one block with no launch between them: each
@@ -387,7 +381,7 @@ __global__ void __launch_bounds__(SC_THREADS, 1) sc_tail(const ScTail* A) {
             __syncthreads();
         }
         for (int job = warp; job < A->njobs; job += SC_THREADS / 32)
-            sc_fs_job<true>(A->states, A->jobs, job, A->j0 + t, A->keys, A->w, A->pad, A->S, A->msgbuf, A->rounds_out,
+            sc_fs_job(A->states, A->jobs, job, A->j0 + t, A->keys, A->w, A->pad, A->S, A->msgbuf, A->rounds_out,
                             A->chal_out, sbuf[warp]);
         __syncthreads();
     }

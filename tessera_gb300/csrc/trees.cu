@@ -602,8 +602,6 @@ __device__ void tl_quad(const TlTree& T, int jj, const ulonglong2* q, fp2& a, fp
 // C_i·eq1(p_i[j'], X)·q_i(X)) at X = 0, 2, 3, absorbed under <prefix>/round/j; r_j drawn under
 // <prefix>/r/j; then each tree in its own rounds takes Q_i ← q_i(r_j) and C_i ← C_i·eq1(p_i[j'], r_j).
 // One warp runs it (sbuf: FS_BUF_WORDS of shared memory).
-// ROLLED: the BLAKE3 rounds as one rolled loop (for the tail kernel, whose warp runs alone).
-template <bool ROLLED>
 __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& keys, TlTree* trees, int ntrees,
                             ulonglong2* q, uint64_t* rounds_out, uint64_t* chal_out, uint32_t* sbuf) {
     const int lane = threadIdx.x & 31;
@@ -637,23 +635,13 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
     uint32_t state[8];
     for (int i = 0; i < 8; i++) state[i] = reinterpret_cast<const uint32_t*>(st->state)[i];
     uint64_t counter = st->counter;
-    uint32_t len = 0;
-    if (lane == 0) {
-        uint8_t* bytes = reinterpret_cast<uint8_t*>(sbuf);
-        len = fs_begin(state, jb, "/round/", j, sbuf);
-        put64(bytes + len, 3);
-        len += 8;
-        for (int x = 0; x < 3; x++) {
-            put64(bytes + len, msg[x].c0);
-            put64(bytes + len + 8, msg[x].c1);
-            len += 16;
-            rounds_out[6 * j + 2 * x] = msg[x].c0;
-            rounds_out[6 * j + 2 * x + 1] = msg[x].c1;
-        }
-    }
-    len = __shfl_sync(0xFFFFFFFFu, len, 0);
+    if (lane == 0)
+        for (int x = 0; x < 3; x++) rounds_out[6 * j + 2 * x] = msg[x].c0, rounds_out[6 * j + 2 * x + 1] = msg[x].c1;
+    // the message as TCE Vec<Fp2>: its length, then the values
+    const uint64_t pay[7] = {3, msg[0].c0, msg[0].c1, msg[1].c0, msg[1].c1, msg[2].c0, msg[2].c1};
+    const uint32_t len = fs_msg_warp<7>(state, jb, fs_pack("/round/"), fs_len("/round/"), j, pay, 7, sbuf);
     uint64_t c0, c1;
-    const bool ok = fs_round_warp<ROLLED>(keys, jb, j, sbuf, len, state, &counter, &c0, &c1);
+    const bool ok = fs_round_warp(keys, jb, j, sbuf, len, state, &counter, &c0, &c1);
     if (lane != 0) return;
     if (!ok) {
         st->err = 1;
@@ -681,7 +669,7 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
 __global__ void tl_fs(FsState* st, FsJob jb, int j, FsKeys keys, TlTree* trees, int ntrees, ulonglong2* q,
                       uint64_t* rounds_out, uint64_t* chal_out) {
     __shared__ uint32_t sbuf[FS_BUF_WORDS];
-    tl_fs_round<false>(st, jb, j, keys, trees, ntrees, q, rounds_out, chal_out, sbuf);
+    tl_fs_round(st, jb, j, keys, trees, ntrees, q, rounds_out, chal_out, sbuf);
 }
 
 // A joining forest's claim Σ_y root[y]·eq(point, y) (y_1 the lowest bit) by binding one point
@@ -789,7 +777,8 @@ __global__ void __launch_bounds__(TL_THREADS, 1) tl_tail(const TlTail* A) {
             __syncthreads();
         }
         if (threadIdx.x < 32)
-            tl_fs_round<true>(A->st, A->jb, A->j0 + t, A->keys, A->trees, A->ntrees, A->q, A->rounds_out, A->chal_out, sbuf);
+            tl_fs_round(A->st, A->jb, A->j0 + t, A->keys, A->trees, A->ntrees, A->q, A->rounds_out, A->chal_out,
+                                    sbuf);
         __syncthreads();
     }
 }
