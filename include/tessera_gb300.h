@@ -78,6 +78,17 @@ typedef struct tg_int_peaks {
 } tg_int_peaks;
 int tg_measure_int_peaks(tg_device *dev, tg_int_peaks *out);
 
+/* Self-check of the device's lazy Goldilocks arithmetic, the field code of the hot kernels (no
+ * reference counterpart; its results are checked against exact integer arithmetic). Inputs are any
+ * 64-bit words, standing for their value mod p. For i < n, with a = words[i], b = words[(i+1) % n],
+ * c = words[(i+2) % n], d = words[(i+3) % n], out[TG_LAZY_CHECK_OUTS·i + t] is the canonical value
+ * of: t = 0 a + b; 1 a − b; 2 a·b; 3 7·a; 4 a·2^5; 5 a·2^40; 6 a·2^70; 7 a·b + c·d as one unreduced
+ * sum; 8 a + b·c + d·a, a sum seeded with a word; 9–10 (a + bX)(c + dX) in Fp2 = Fp[X]/(X^2 − 7);
+ * 11–12 (a + bX) + (c + dX)(b + aX); 13–14 (a + bX)(c + dX) + (b + dX)(a + cX); 15
+ * Σ_{k<64} words[(i+k) % n]·words[(i+2k+1) % n] as one unreduced sum. n ≥ 4; host buffers. */
+#define TG_LAZY_CHECK_OUTS 16
+int tg_check_lazy_arith(tg_device *dev, const uint64_t *words, size_t n, uint64_t *out);
+
 /* Synthetic inputs on the device (no reference counterpart; the reference benchmark draws the
  * same words on the host, crates/tessera-bench/benches/primitives.rs:52-69): out[i] is the
  * (i + 1)-th SplitMix64 output from `seed`, reduced once below p. Enqueued on `stream` (NULL:

@@ -123,6 +123,10 @@ __host__ __device__ __forceinline__ uint64_t mul_small(uint64_t x, uint32_t k) {
 namespace tg {
 namespace lz {
 
+// Every multi-instruction asm block below copies its inputs into registers of its own before it
+// writes an output: the compiler may give an output (or a read-write operand) the register of an
+// input that holds the same value, and a later read of that input would see the output instead.
+
 __device__ __forceinline__ uint32_t lo32(uint64_t x) { return (uint32_t)x; }
 __device__ __forceinline__ uint32_t hi32(uint64_t x) { return (uint32_t)(x >> 32); }
 __device__ __forceinline__ uint64_t mk64(uint32_t lo, uint32_t hi) { return ((uint64_t)hi << 32) | lo; }
@@ -150,9 +154,10 @@ __device__ __forceinline__ uint64_t sub(uint64_t a, uint64_t b) {
 // multiply pipe with its carry.
 __device__ __forceinline__ uint64_t fold(uint64_t lo, uint32_t hl, uint32_t hh) {
     uint32_t r0, r1, c;
-    asm("mad.lo.cc.u32 %0, %3, 0xFFFFFFFF, %4;\n\t"
-        "madc.hi.cc.u32 %1, %3, 0xFFFFFFFF, %5;\n\t"
-        "addc.u32 %2, 0, 0;"
+    asm("{\n\t.reg .u32 h, l0, l1;\n\tmov.u32 h, %3;\n\tmov.u32 l0, %4;\n\tmov.u32 l1, %5;\n\t"
+        "mad.lo.cc.u32 %0, h, 0xFFFFFFFF, l0;\n\t"
+        "madc.hi.cc.u32 %1, h, 0xFFFFFFFF, l1;\n\t"
+        "addc.u32 %2, 0, 0;\n\t}"
         : "=r"(r0), "=r"(r1), "=r"(c)
         : "r"(hl), "r"(lo32(lo)), "r"(hi32(lo)));
     uint64_t d;
@@ -165,9 +170,10 @@ __device__ __forceinline__ uint64_t fold(uint64_t lo, uint32_t hl, uint32_t hh) 
 // (lo + h·2^64) mod p for h < 2^32: lo + h·(2^32 − 1).
 __device__ __forceinline__ uint64_t fold_lo(uint64_t lo, uint32_t h) {
     uint32_t r0, r1, c;
-    asm("mad.lo.cc.u32 %0, %3, 0xFFFFFFFF, %4;\n\t"
-        "madc.hi.cc.u32 %1, %3, 0xFFFFFFFF, %5;\n\t"
-        "addc.u32 %2, 0, 0;"
+    asm("{\n\t.reg .u32 h, l0, l1;\n\tmov.u32 h, %3;\n\tmov.u32 l0, %4;\n\tmov.u32 l1, %5;\n\t"
+        "mad.lo.cc.u32 %0, h, 0xFFFFFFFF, l0;\n\t"
+        "madc.hi.cc.u32 %1, h, 0xFFFFFFFF, l1;\n\t"
+        "addc.u32 %2, 0, 0;\n\t}"
         : "=r"(r0), "=r"(r1), "=r"(c)
         : "r"(h), "r"(lo32(lo)), "r"(hi32(lo)));
     // with a carry, the word is below h·(2^32 − 1) < 2^64 − 2^33: adding 2^32 − 1 cannot wrap
@@ -201,14 +207,16 @@ __device__ __forceinline__ uint64_t mulp2(uint64_t x) {
 __device__ __forceinline__ uint64_t mul(uint64_t a, uint64_t b) {
     uint32_t r0, r1, r2, r3;
     asm("{\n\t"
-        "mul.lo.u32 %0, %4, %6;\n\t"
-        "mul.hi.u32 %1, %4, %6;\n\t"
-        "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
-        "madc.hi.u32 %2, %4, %7, 0;\n\t"
-        "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
-        "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
-        "madc.hi.u32 %3, %5, %7, 0;\n\t"
-        "mad.lo.cc.u32 %2, %5, %7, %2;\n\t"
+        ".reg .u32 x0, x1, y0, y1;\n\t"
+        "mov.u32 x0, %4;\n\tmov.u32 x1, %5;\n\tmov.u32 y0, %6;\n\tmov.u32 y1, %7;\n\t"
+        "mul.lo.u32 %0, x0, y0;\n\t"
+        "mul.hi.u32 %1, x0, y0;\n\t"
+        "mad.lo.cc.u32 %1, x0, y1, %1;\n\t"
+        "madc.hi.u32 %2, x0, y1, 0;\n\t"
+        "mad.lo.cc.u32 %1, x1, y0, %1;\n\t"
+        "madc.hi.cc.u32 %2, x1, y0, %2;\n\t"
+        "madc.hi.u32 %3, x1, y1, 0;\n\t"
+        "mad.lo.cc.u32 %2, x1, y1, %2;\n\t"
         "addc.u32 %3, %3, 0;\n\t"
         "}"
         : "=r"(r0), "=r"(r1), "=r"(r2), "=r"(r3)
@@ -250,14 +258,16 @@ __device__ __forceinline__ Acc acc_of(uint64_t x) { return {{lo32(x), hi32(x), 0
 __device__ __forceinline__ Acc acc_mul(uint64_t x, uint64_t y) {
     Acc a;
     asm("{\n\t"
-        "mul.lo.u32 %0, %4, %6;\n\t"
-        "mul.hi.u32 %1, %4, %6;\n\t"
-        "mad.lo.cc.u32 %1, %4, %7, %1;\n\t"
-        "madc.hi.u32 %2, %4, %7, 0;\n\t"
-        "mad.lo.cc.u32 %1, %5, %6, %1;\n\t"
-        "madc.hi.cc.u32 %2, %5, %6, %2;\n\t"
-        "madc.hi.u32 %3, %5, %7, 0;\n\t"
-        "mad.lo.cc.u32 %2, %5, %7, %2;\n\t"
+        ".reg .u32 x0, x1, y0, y1;\n\t"
+        "mov.u32 x0, %4;\n\tmov.u32 x1, %5;\n\tmov.u32 y0, %6;\n\tmov.u32 y1, %7;\n\t"
+        "mul.lo.u32 %0, x0, y0;\n\t"
+        "mul.hi.u32 %1, x0, y0;\n\t"
+        "mad.lo.cc.u32 %1, x0, y1, %1;\n\t"
+        "madc.hi.u32 %2, x0, y1, 0;\n\t"
+        "mad.lo.cc.u32 %1, x1, y0, %1;\n\t"
+        "madc.hi.cc.u32 %2, x1, y0, %2;\n\t"
+        "madc.hi.u32 %3, x1, y1, 0;\n\t"
+        "mad.lo.cc.u32 %2, x1, y1, %2;\n\t"
         "addc.u32 %3, %3, 0;\n\t"
         "}"
         : "=r"(a.w[0]), "=r"(a.w[1]), "=r"(a.w[2]), "=r"(a.w[3])
@@ -269,17 +279,19 @@ __device__ __forceinline__ Acc acc_mul(uint64_t x, uint64_t y) {
 // a += x·y: x0·y0 into limbs 0–1, x1·y1 into 2–3, the cross products into 1–2, each carry to limb 4.
 __device__ __forceinline__ void mad(Acc& a, uint64_t x, uint64_t y) {
     asm("{\n\t"
-        "mad.lo.cc.u32 %0, %5, %7, %0;\n\t"
-        "madc.hi.cc.u32 %1, %5, %7, %1;\n\t"
-        "madc.lo.cc.u32 %2, %6, %8, %2;\n\t"
-        "madc.hi.cc.u32 %3, %6, %8, %3;\n\t"
+        ".reg .u32 x0, x1, y0, y1;\n\t"
+        "mov.u32 x0, %5;\n\tmov.u32 x1, %6;\n\tmov.u32 y0, %7;\n\tmov.u32 y1, %8;\n\t"
+        "mad.lo.cc.u32 %0, x0, y0, %0;\n\t"
+        "madc.hi.cc.u32 %1, x0, y0, %1;\n\t"
+        "madc.lo.cc.u32 %2, x1, y1, %2;\n\t"
+        "madc.hi.cc.u32 %3, x1, y1, %3;\n\t"
         "addc.u32 %4, %4, 0;\n\t"
-        "mad.lo.cc.u32 %1, %5, %8, %1;\n\t"
-        "madc.hi.cc.u32 %2, %5, %8, %2;\n\t"
+        "mad.lo.cc.u32 %1, x0, y1, %1;\n\t"
+        "madc.hi.cc.u32 %2, x0, y1, %2;\n\t"
         "addc.cc.u32 %3, %3, 0;\n\t"
         "addc.u32 %4, %4, 0;\n\t"
-        "mad.lo.cc.u32 %1, %6, %7, %1;\n\t"
-        "madc.hi.cc.u32 %2, %6, %7, %2;\n\t"
+        "mad.lo.cc.u32 %1, x1, y0, %1;\n\t"
+        "madc.hi.cc.u32 %2, x1, y0, %2;\n\t"
         "addc.cc.u32 %3, %3, 0;\n\t"
         "addc.u32 %4, %4, 0;\n\t"
         "}"

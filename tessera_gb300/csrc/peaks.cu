@@ -130,3 +130,57 @@ extern "C" int tg_measure_int_peaks(tg_device* dev, tg_int_peaks* out) {
     d->launches += 8;
     return TG_OK;
 }
+
+// ---- a self-check of the lazy arithmetic on any 64-bit words ----------------------------------
+
+namespace tg {
+
+// Word i's outputs (canonical): see tg_check_lazy_arith in the header for the list.
+__global__ void check_lazy_kernel(const uint64_t* w, size_t n, uint64_t* out) {
+    const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const uint64_t a = w[i], b = w[(i + 1) % n], c = w[(i + 2) % n], d = w[(i + 3) % n];
+    uint64_t* o = out + (size_t)TG_LAZY_CHECK_OUTS * i;
+    o[0] = lz::canon(lz::add(a, b));
+    o[1] = lz::canon(lz::sub(a, b));
+    o[2] = lz::canon(lz::mul(a, b));
+    o[3] = lz::canon(lz::mul7(a));
+    o[4] = lz::canon(lz::mulp2<5>(a));
+    o[5] = lz::canon(lz::mulp2<40>(a));
+    o[6] = lz::canon(lz::mulp2<70>(a));
+    lz::Acc s = lz::acc_mul(a, b);
+    lz::mad(s, c, d);
+    o[7] = lz::canon(lz::reduce(s));
+    lz::Acc t = lz::acc_of(a);
+    lz::mad(t, b, c);
+    lz::mad(t, d, a);
+    o[8] = lz::canon(lz::reduce(t));
+    const fp2 x = {a, b}, y = {c, d}, u = {b, a}, v = {b, d}, z = {a, c};
+    const fp2 m = l2_canon(l2_muls(x, y)), f = l2_canon(l2_fma(x, y, lz::mul7(y.c1), u)), g = l2_canon(l2_dot(x, y, v, z));
+    o[9] = m.c0, o[10] = m.c1, o[11] = f.c0, o[12] = f.c1, o[13] = g.c0, o[14] = g.c1;
+    lz::Acc big = lz::acc_zero();
+    for (size_t k = 0; k < 64; k++) lz::mad(big, w[(i + k) % n], w[(i + 2 * k + 1) % n]);
+    o[15] = lz::canon(lz::reduce(big));
+}
+
+}  // namespace tg
+
+extern "C" int tg_check_lazy_arith(tg_device* dev, const uint64_t* words, size_t n, uint64_t* out) {
+    using namespace tg;
+    Device* d = reinterpret_cast<Device*>(dev);
+    if (!d || !words || !out) return fail(TG_ERR_INVALID, "tg_check_lazy_arith: null argument");
+    if (n < 4) return fail(TG_ERR_INVALID, "tg_check_lazy_arith: %zu words, at least 4 needed", n);
+    DevBuf in, res;
+    int rc = in.ensure(n * 8);
+    if (!rc) rc = res.ensure(n * 8 * TG_LAZY_CHECK_OUTS);
+    if (rc) return rc;
+    cudaStream_t s = d->stream;
+    TG_CUDA(cudaMemcpyAsync(in.ptr, words, n * 8, cudaMemcpyHostToDevice, s));
+    check_lazy_kernel<<<(unsigned)((n + 127) / 128), 128, 0, s>>>((const uint64_t*)in.ptr, n, (uint64_t*)res.ptr);
+    TG_CUDA(cudaGetLastError());
+    d->launches += 1;
+    TG_CUDA(cudaMemcpyAsync(out, res.ptr, n * 8 * TG_LAZY_CHECK_OUTS, cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    return TG_OK;
+}
+

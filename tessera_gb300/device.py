@@ -68,6 +68,17 @@ class Device:
         N.call("tg_measure_int_peaks", self.handle, ctypes.byref(p))
         return {name: getattr(p, name) for name, _ in _Peaks._fields_}
 
+    def check_lazy_arith(self, words):
+        """The device's lazy field arithmetic on any 64-bit words (tg_check_lazy_arith): an array
+        of shape (n, 16) of canonical results, in the order the header lists."""
+        import numpy as np
+
+        w = np.ascontiguousarray(np.asarray(words, dtype=np.uint64))
+        out = np.zeros((len(w), 16), dtype=np.uint64)
+        N.call("tg_check_lazy_arith", self.handle, ctypes.c_void_p(w.ctypes.data), len(w),
+               ctypes.c_void_p(out.ctypes.data))
+        return out
+
     def profile(self, on: bool = True):
         N.call("tg_profile_enable", self.handle, int(on))
 
