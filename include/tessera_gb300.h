@@ -46,7 +46,14 @@ typedef struct {
     uint64_t level_budget_bytes; /* default 16 GiB */
     uint64_t level_min_entries;  /* default 2^14 (gpu.rs:89 LEVEL_MIN_ENTRIES) */
     uint64_t lde_group_bytes;    /* encoder scratch per group of rows; default 768 MiB */
+    uint64_t tree_flags;         /* TG_TREE_* below; default 0 */
 } tg_config;
+
+/* Tree levels: sum each round's q(1) on the device and use it, instead of deriving q(1) from the
+ * round's claim (the reference prover's derivation, crates/tessera-sumcheck/src/level.rs:317-347).
+ * The proof is the same either way; the summing path is otherwise taken only where a point
+ * coordinate is 0, so this flag exists to check it. Slower. */
+#define TG_TREE_SUM_Q1 1u
 
 /* Library version, and the message of the calling thread's last failure. */
 int tg_version(void);

@@ -28,7 +28,10 @@ class InvalidInput(TesseraError, ValueError):
 
 class Config(ctypes.Structure):
     _fields_ = [("level_budget_bytes", ctypes.c_uint64), ("level_min_entries", ctypes.c_uint64),
-                ("lde_group_bytes", ctypes.c_uint64)]
+                ("lde_group_bytes", ctypes.c_uint64), ("tree_flags", ctypes.c_uint64)]
+
+
+TG_TREE_SUM_Q1 = 1
 
 
 class TranscriptState(ctypes.Structure):

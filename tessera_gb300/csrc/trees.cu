@@ -1131,8 +1131,10 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         *base = 0;
         return st->pool[present[i]][2 * k + ((jj - 2) & 1)]->ptr;
     };
-    // where a point coordinate is 0, q(1) has no derivation from the claim: that round's launch sums it
-    std::vector<char> one(std::max(n_max, 1), 0);
+    // where a point coordinate is 0, q(1) has no derivation from the claim: that round's launch sums
+    // it (every round's does under TG_TREE_SUM_Q1, which takes the summed q(1) throughout)
+    const bool sum_q1 = (d->cfg.tree_flags & TG_TREE_SUM_Q1) != 0;
+    std::vector<char> one(std::max(n_max, 1), sum_q1 ? 1 : 0);
     for (int i = 0; i < np; i++)
         for (int jj = 0; jj < nvars[i]; jj++) {
             const fp2 c = jpoint[present[i]][jj];
@@ -1256,7 +1258,7 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
         uint64_t* iw = (uint64_t*)host_at(off_tinv[i]);
         for (size_t c = 0; c < pt.size(); c++) {
             pw[2 * c] = pt[c].c0, pw[2 * c + 1] = pt[c].c1;
-            const fp2 ti = host_inv2(pt[c]);
+            const fp2 ti = sum_q1 ? fp2{0, 0} : host_inv2(pt[c]);  // 0: tl_quad reads the summed q(1)
             iw[2 * c] = ti.c0, iw[2 * c + 1] = ti.c1;
         }
         const uint64_t* dpt = ar.at<uint64_t>(off_point[i]);

@@ -18,16 +18,18 @@ P = 0xFFFFFFFF00000001
 
 class Device:
     """An open GPU. `level_budget_bytes` and `level_min_entries` bound the level offload;
-    `lde_group_bytes` sizes the encoder's L2-resident scratch per group of rows."""
+    `lde_group_bytes` sizes the encoder's L2-resident scratch per group of rows; `tree_sum_q1`
+    makes every tree-level round sum q(1) instead of deriving it from its claim (same proofs; a
+    check of that path)."""
 
     def __init__(self, ordinal: int = 0, level_budget_bytes: int | None = None, level_min_entries: int | None = None,
-                 lde_group_bytes: int = 0):
+                 lde_group_bytes: int = 0, tree_sum_q1: bool = False):
         if level_budget_bytes is None:
             gib = os.environ.get("TESSERA_GPU_LEVEL_GIB")
             level_budget_bytes = int(float(gib) * (1 << 30)) if gib else 0
         if level_min_entries is None:
             level_min_entries = int(os.environ.get("TESSERA_GPU_LEVEL_MIN", "0"))
-        cfg = N.Config(level_budget_bytes, level_min_entries, lde_group_bytes)
+        cfg = N.Config(level_budget_bytes, level_min_entries, lde_group_bytes, N.TG_TREE_SUM_Q1 if tree_sum_q1 else 0)
         h = ctypes.c_void_p()
         N.call("tg_device_open", ordinal, ctypes.byref(cfg), ctypes.byref(h))
         self.handle = h

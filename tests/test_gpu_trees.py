@@ -426,3 +426,55 @@ def test_leaf_stage_refusals(dev):
         with pytest.raises(N.TesseraError):
             st.prove_level(t)
         assert (t.state, t.counter) == before
+
+
+@pytest.fixture(scope="module")
+def dev_q1():
+    from tessera_gb300.device import Device
+
+    d = Device(0, tree_sum_q1=True)
+    yield d
+    d.close()
+
+
+def test_summed_q1_gives_the_golden_proofs(dev_q1):
+    """With every round summing q(1) on the device (the path a point coordinate of 0 takes, else
+    out of reach: the points are transcript challenges) instead of deriving it from the round's
+    claim, the golden tree, forest and LogUp batches come out the same, level by level."""
+    for base, on_device in LEAF_FORMS[:2]:
+        test_tree_batches(dev_q1, base, on_device)
+        test_forest_batches(dev_q1, base, on_device)
+    test_logup_leaf_stages(dev_q1)
+
+
+@pytest.mark.parametrize("kind", ["unit17", "fraction14", "forest6x14", "forest_fp2_4x12"])
+def test_summed_q1_matches_derived_in_launched_rounds(dev, dev_q1, kind):
+    """Trees large enough for launched rounds of every kind and mode (numerators of 1, fractions,
+    prime-field and Fp2 products) before each level's tail: the proof with q(1) summed equals the
+    proof with q(1) derived, every record, the final claim and the transcript state."""
+    import torch
+
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.trees import Forest, LeafStage, generated_fraction, lift
+    from tessera_gb300.workloads import fill_counter
+
+    ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([3]) * 32, bytes([5]) * 16)
+    if kind.startswith("forest"):
+        s, h = (6, 14) if kind == "forest6x14" else (4, 12)
+        leaves = fill_counter(torch.empty(1 << (s + h), dtype=torch.int64, device="cuda"), 1 << 61, dev)
+        host = leaves.cpu().numpy().view(np.uint64)
+
+    def prove(d):
+        if kind.startswith("forest"):
+            tree = Forest(s, leaves, True) if kind == "forest6x14" else Forest(s, lift(host))
+        else:
+            h = 17 if kind == "unit17" else 14
+            tree = generated_fraction(h, 1000, 2000000, None if kind == "unit17" else 77, (123456789, 987654321),
+                                      (55555, 4444444), d)
+        t = Transcript(ctx)
+        with LeafStage([tree], d) as st:
+            recs = st.prove(t)
+            return ([(r.rounds, r.challenges, r.claims, r.final_evals, r.rho) for r in recs], st.claim(0),
+                    t.state.hex(), t.counter)
+
+    assert prove(dev) == prove(dev_q1)
