@@ -596,7 +596,7 @@ def run_logup(args) -> None:
         start = time.perf_counter()
         t = Transcript(ctx)
         alpha, beta = t.challenge_fp2("logup/alpha"), t.challenge_fp2("logup/beta")
-        tree = generated_fraction(height, 0x6B6579, 0x76616C, mult_seed, alpha, beta, dev)
+        tree = generated_fraction(height, 0x6B6579, 0x76616C, mult_seed, alpha, beta, dev, deferred=True)
         with LeafStage([tree], dev) as st:
             st.prove(t)
         torch.cuda.synchronize()

@@ -322,6 +322,16 @@ int tg_level_free(tg_level *l);
  * byte for byte as the reference does, and moves every present tree's claim one level down.
  * With on_device, the leaves are read in place (they must stay unchanged until the stage closes);
  * the other levels and the bound tables come from the device's workspace cache. */
+/* Generated LogUp leaves, as tg_logup_leaves writes them: leaf j is (n_j, α − (k_j + β·v_j)) with
+ * k_j = counter(key_seed + j), v_j = counter(value_seed + j) and n_j = 1 (unit) or −m_j,
+ * m_j = counter(mult_seed + j) mod 2^16 (the reference benchmark's inputs,
+ * crates/tessera-gpu/src/fraction.rs:61-105). */
+typedef struct {
+    uint64_t key_seed, value_seed, mult_seed;
+    int unit;
+    uint64_t alpha[2], beta[2];
+} tg_leaf_gen;
+
 typedef struct {
     int kind;
     uint32_t s, height;
@@ -329,6 +339,10 @@ typedef struct {
     const uint64_t *denominators;  /* fraction trees */
     const uint64_t *sent;          /* fraction trees: 2 Fp2, or NULL */
     uint32_t base_leaves;          /* forests: 1 when the leaves are prime-field words (one per leaf) */
+    const tg_leaf_gen *gen;        /* fraction trees, or NULL: the stage generates the leaves into
+                                      `denominators` (and `leaves` unless gen->unit; NULL then), 16-byte
+                                      aligned device buffers of 2^height Fp2 (on_device), in the same pass
+                                      as the two levels above them */
 } tg_tree;
 typedef struct {
     int level;

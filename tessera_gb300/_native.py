@@ -70,9 +70,15 @@ class ServerStatsC(ctypes.Structure):
                 ("peak_bytes", ctypes.c_size_t)]
 
 
+class LeafGenC(ctypes.Structure):
+    _fields_ = [("key_seed", ctypes.c_uint64), ("value_seed", ctypes.c_uint64), ("mult_seed", ctypes.c_uint64),
+                ("unit", ctypes.c_int), ("alpha", ctypes.c_uint64 * 2), ("beta", ctypes.c_uint64 * 2)]
+
+
 class TreeC(ctypes.Structure):
     _fields_ = [("kind", ctypes.c_int), ("s", ctypes.c_uint32), ("height", ctypes.c_uint32), ("leaves", ctypes.c_void_p),
-                ("denominators", ctypes.c_void_p), ("sent", ctypes.c_void_p), ("base_leaves", ctypes.c_uint32)]
+                ("denominators", ctypes.c_void_p), ("sent", ctypes.c_void_p), ("base_leaves", ctypes.c_uint32),
+                ("gen", ctypes.c_void_p)]
 
 
 class TreeLevelProofC(ctypes.Structure):

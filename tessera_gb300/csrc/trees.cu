@@ -133,24 +133,69 @@ __device__ __forceinline__ uint64_t counter_value(uint64_t c) {
     return z >= P ? z - P : z;
 }
 
-// Generated LogUp leaves: leaf j is (n_j, α − (k_j + β·v_j)) with k_j = counter(key_seed + j),
+// Generated LogUp leaf j: (n_j, α − (k_j + β·v_j)) with k_j = counter(key_seed + j),
 // v_j = counter(value_seed + j), and n_j = 1 (a lookup tree) or −m_j, m_j = counter(mult_seed + j)
-// mod 2^16 (a table tree).
-__global__ void tr_logup_leaves(uint64_t key_seed, uint64_t value_seed, uint64_t mult_seed, int unit, fp2 alpha,
-                                fp2 beta, ulonglong2* n_out, ulonglong2* d_out, uint64_t count) {
+// mod 2^16 (a table tree); canonical.
+struct LeafGen {
+    uint64_t key_seed, value_seed, mult_seed;
+    int unit, pad_;
+    fp2 alpha, beta;
+};
+__device__ __forceinline__ void logup_leaf(const LeafGen& g, uint64_t j, fp2& n, fp2& d) {
+    const uint64_t k = counter_value(g.key_seed + j), v = counter_value(g.value_seed + j);
+    d = {sub(sub(g.alpha.c0, k), mul(g.beta.c0, v)), sub(g.alpha.c1, mul(g.beta.c1, v))};
+    n = {1, 0};
+    if (!g.unit) {
+        const uint64_t m = counter_value(g.mult_seed + j) & 0xFFFF;
+        n.c0 = m == 0 ? 0 : P - m;
+    }
+}
+
+__global__ void tr_logup_leaves(LeafGen g, ulonglong2* n_out, ulonglong2* d_out, uint64_t count) {
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     for (uint64_t j = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; j < count; j += stride) {
-        const uint64_t k = counter_value(key_seed + j), v = counter_value(value_seed + j);
-        const fp2 d = {sub(sub(alpha.c0, k), mul(beta.c0, v)), sub(alpha.c1, mul(beta.c1, v))};
+        fp2 n, d;
+        logup_leaf(g, j, n, d);
         d_out[j] = make_ulonglong2(d.c0, d.c1);
-        if (!n_out) continue;  // numerators of 1, not stored
-        uint64_t nn = 1;
-        if (!unit) {
-            const uint64_t m = counter_value(mult_seed + j) & 0xFFFF;
-            nn = m == 0 ? 0 : P - m;
-        }
-        n_out[j] = make_ulonglong2(nn, 0);
+        if (n_out) n_out[j] = make_ulonglong2(n.c0, n.c1);  // numerators of 1 are not stored
     }
+}
+
+// Generated leaves and the two levels above them in one pass (tr_fraction_level2 without reading
+// the leaves back): thread x generates leaves 4x … 4x + 3 and stores them for the leaf level's
+// rounds (numerators only when not all 1), then their two parents and their grandparent.
+__global__ void tr_logup_level2(LeafGen g, ulonglong2* n_leaf, ulonglong2* d_leaf, ulonglong2* n_mid,
+                                ulonglong2* d_mid, ulonglong2* n_out, ulonglong2* d_out, uint64_t m) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t x = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; x < m; x += stride) {
+        fp2 n4[4], d4[4];
+#pragma unroll
+        for (int i = 0; i < 4; i++) {
+            logup_leaf(g, 4 * x + i, n4[i], d4[i]);
+            d_leaf[4 * x + i] = make_ulonglong2(d4[i].c0, d4[i].c1);
+            if (!g.unit) n_leaf[4 * x + i] = make_ulonglong2(n4[i].c0, n4[i].c1);
+        }
+        fp2 nn[2], dd[2];
+#pragma unroll
+        for (int h = 0; h < 2; h++) {
+            const fp2 c = d4[2 * h], e = d4[2 * h + 1];
+            nn[h] = g.unit ? l2_canon(l2_add(c, e)) : l2_canon(l2_dot(n4[2 * h], e, n4[2 * h + 1], c));
+            dd[h] = l2_canon(l2_muls(c, e));
+            n_mid[2 * x + h] = make_ulonglong2(nn[h].c0, nn[h].c1);
+            d_mid[2 * x + h] = make_ulonglong2(dd[h].c0, dd[h].c1);
+        }
+        const fp2 no = l2_canon(l2_dot(nn[0], dd[1], nn[1], dd[0])), dn = l2_canon(l2_muls(dd[0], dd[1]));
+        n_out[x] = make_ulonglong2(no.c0, no.c1);
+        d_out[x] = make_ulonglong2(dn.c0, dn.c1);
+    }
+}
+
+static LeafGen leaf_gen(const tg_leaf_gen& g) {
+    LeafGen o;
+    memset(&o, 0, sizeof o);
+    o.key_seed = g.key_seed, o.value_seed = g.value_seed, o.mult_seed = g.mult_seed, o.unit = g.unit ? 1 : 0;
+    o.alpha = {g.alpha[0], g.alpha[1]}, o.beta = {g.beta[0], g.beta[1]};
+    return o;
 }
 
 static unsigned grid_of(const Device* d, uint64_t items) {
@@ -834,6 +879,17 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
         if (t.kind == 1 && t.base_leaves) return fail(TG_ERR_INVALID, "tree %d: prime-field leaves are a forest's", k);
         if (t.kind == 0 && !t.leaves) return fail(TG_ERR_INVALID, "tree %d: null leaves", k);
         if (t.kind == 1 && !t.denominators) return fail(TG_ERR_INVALID, "tree %d: null denominators", k);
+        if (t.gen) {
+            if (t.kind != 1) return fail(TG_ERR_INVALID, "tree %d: generated leaves are a fraction tree's", k);
+            if (!on_device) return fail(TG_ERR_INVALID, "tree %d: generated leaves go to device buffers", k);
+            if (((uintptr_t)t.denominators & 15) || ((uintptr_t)t.leaves & 15))
+                return fail(TG_ERR_INVALID, "tree %d: generated leaves need 16-byte aligned buffers", k);
+            if ((t.leaves == nullptr) != (t.gen->unit != 0))
+                return fail(TG_ERR_INVALID, "tree %d: numerators buffer %s for %s numerators", k, t.leaves ? "given" : "missing",
+                            t.gen->unit ? "unit" : "generated");
+            if (t.gen->alpha[0] >= P || t.gen->alpha[1] >= P || t.gen->beta[0] >= P || t.gen->beta[1] >= P)
+                return fail(TG_ERR_INVALID, "tree %d: alpha and beta must be canonical", k);
+        }
     }
     tg_leaf_stage* st = new tg_leaf_stage();
     st->d = d;
@@ -881,6 +937,16 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
             if (!rc && spec.leaves) rc = place(*tr.n[spec.height], spec.leaves);
         }
         if (rc) return bail(rc);
+        // generated leaves: in the same pass as the two levels above them, or alone for a tree of
+        // height below 2
+        const bool gen_fused = spec.gen && spec.height >= 2;
+        const LeafGen lg_spec = spec.gen ? leaf_gen(*spec.gen) : LeafGen{};
+        if (spec.gen && !gen_fused) {
+            Launch L(d, s, "logup_leaves", 1, leaves);
+            tr_logup_leaves<<<grid_of(d, leaves), 256, 0, s>>>(lg_spec, spec.leaves ? (ulonglong2*)tr.n[spec.height]->ptr : nullptr,
+                                                              (ulonglong2*)tr.d[spec.height]->ptr, leaves);
+            TG_CUDA(cudaGetLastError());
+        }
         // levels two at a time (l and l − 1 from l + 1), the last one alone when the count is odd
         for (int l = (int)spec.height - 1; l >= 0;) {
             const bool two = l >= 1;
@@ -901,6 +967,11 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
                 else if (spec.kind == 0)
                     tr_product_level2<<<grid_of(d, mo), 256, 0, s>>>((const ulonglong2*)tr.n[l + 1]->ptr,
                                                                     (ulonglong2*)tr.n[l]->ptr, (ulonglong2*)tr.n[l - 1]->ptr, mo);
+                else if (gen_fused && l + 1 == (int)spec.height)
+                    tr_logup_level2<<<grid_of(d, mo), 256, 0, s>>>(
+                        lg_spec, spec.leaves ? (ulonglong2*)tr.n[l + 1]->ptr : nullptr, (ulonglong2*)tr.d[l + 1]->ptr,
+                        (ulonglong2*)tr.n[l]->ptr, (ulonglong2*)tr.d[l]->ptr, (ulonglong2*)tr.n[l - 1]->ptr,
+                        (ulonglong2*)tr.d[l - 1]->ptr, mo);
                 else
                     tr_fraction_level2<<<grid_of(d, mo), 256, 0, s>>>(
                         nb, (const ulonglong2*)tr.d[l + 1]->ptr, (ulonglong2*)tr.n[l]->ptr, (ulonglong2*)tr.d[l]->ptr,
@@ -1549,9 +1620,12 @@ extern "C" int tg_logup_leaves(tg_device* dev, uint64_t key_seed, uint64_t value
     cudaStream_t s = d->stream;
     {
         Launch L(d, s, "logup_leaves", 1, count);
-        tr_logup_leaves<<<grid_of(d, count), 256, 0, s>>>(key_seed, value_seed, mult_seed, unit, fp2{alpha[0], alpha[1]},
-                                                          fp2{beta[0], beta[1]}, (ulonglong2*)numerators,
-                                                          (ulonglong2*)denominators, count);
+        tg_leaf_gen g;
+        memset(&g, 0, sizeof g);
+        g.key_seed = key_seed, g.value_seed = value_seed, g.mult_seed = mult_seed, g.unit = unit;
+        g.alpha[0] = alpha[0], g.alpha[1] = alpha[1], g.beta[0] = beta[0], g.beta[1] = beta[1];
+        tr_logup_leaves<<<grid_of(d, count), 256, 0, s>>>(leaf_gen(g), (ulonglong2*)numerators, (ulonglong2*)denominators,
+                                                          count);
     }
     TG_CUDA(cudaGetLastError());
     TG_CUDA(cudaStreamSynchronize(s));

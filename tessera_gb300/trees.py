@@ -45,11 +45,25 @@ class Forest:
 
 
 @dataclass
+class LeafGen:
+    """Generated LogUp leaves (tg_leaf_gen): leaf j is (1 or −m_j, α − (k_j + β·v_j)) from the
+    counter generator; mult_seed None: numerators of 1."""
+    key_seed: int
+    value_seed: int
+    mult_seed: int | None
+    alpha: tuple
+    beta: tuple
+
+
+@dataclass
 class Fraction:
-    """A LogUp fraction tree from its leaves' numerators (Fp2, or None for 1) and denominators."""
+    """A LogUp fraction tree from its leaves' numerators (Fp2, or None for 1) and denominators.
+    With `gen`, the leaf stage writes the generated leaves into these device tensors when it opens,
+    in the same pass as the two levels above them."""
     denominators: np.ndarray
     numerators: np.ndarray | None = None
     sent: tuple | None = None  # the root (n, d) as the roots message carries it
+    gen: LeafGen | None = None
 
     @property
     def height(self) -> int:
@@ -106,6 +120,12 @@ class LeafStage:
                 arr[k].denominators = words(t.denominators)
                 if t.numerators is not None:
                     arr[k].leaves = words(t.numerators)
+                if t.gen is not None:
+                    g = t.gen
+                    gc = N.LeafGenC(g.key_seed, g.value_seed, g.mult_seed or 0, int(g.mult_seed is None),
+                                    (ctypes.c_uint64 * 2)(*g.alpha), (ctypes.c_uint64 * 2)(*g.beta))
+                    self._keep.append(gc)
+                    arr[k].gen = ctypes.addressof(gc)
                 if t.sent is not None:
                     sent = host_u64([t.sent[0][0], t.sent[0][1], t.sent[1][0], t.sent[1][1]])
                     arr[k].sent = sent.ctypes.data
@@ -182,10 +202,11 @@ def prove_forests(transcript: Transcript, forests: list[Forest], device: Device 
 
 
 def generated_fraction(height: int, key_seed: int, value_seed: int, mult_seed: int | None, alpha, beta,
-                       device: Device | None = None) -> Fraction:
+                       device: Device | None = None, deferred: bool = False) -> Fraction:
     """A fraction tree of 2^height generated leaves on the device (the reference benchmark's LogUp
     inputs): leaf j is (1 or −m_j, α − (k_j + β·v_j)) from the counter generator; numerators of 1
-    (no mult_seed) are not stored."""
+    (no mult_seed) are not stored. deferred: the leaves are generated when a leaf stage opens the
+    tree, in the same pass as its two lowest levels (the tensors hold them from then on)."""
     import torch
 
     d = resolve(device)
@@ -193,6 +214,8 @@ def generated_fraction(height: int, key_seed: int, value_seed: int, mult_seed: i
     unit = mult_seed is None
     num = None if unit else torch.empty(2 * count, dtype=torch.int64, device=f"cuda:{d.ordinal}")
     den = torch.empty(2 * count, dtype=torch.int64, device=f"cuda:{d.ordinal}")
+    if deferred:
+        return Fraction(den, num, gen=LeafGen(key_seed, value_seed, mult_seed, tuple(alpha), tuple(beta)))
     torch.cuda.current_stream().synchronize()
     a = (ctypes.c_uint64 * 2)(*alpha)
     b = (ctypes.c_uint64 * 2)(*beta)

@@ -478,3 +478,60 @@ def test_summed_q1_matches_derived_in_launched_rounds(dev, dev_q1, kind):
                     t.state.hex(), t.counter)
 
     assert prove(dev) == prove(dev_q1)
+
+
+@pytest.mark.parametrize("unit,h", [(True, 0), (False, 1), (True, 2), (False, 3), (True, 9), (False, 12), (True, 14)])
+def test_deferred_generated_leaves_match(dev, unit, h):
+    """Leaves generated by the leaf stage itself, in the same pass as the two levels above them,
+    are the generator's leaves, and the proof equals the one over leaves generated beforehand."""
+    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.trees import LeafStage, generated_fraction
+
+    ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([1]) * 32, bytes([2]) * 16)
+    args = (h, 31, 4000, None if unit else 900, (987654321, 123), (77, 1 << 40))
+    runs = []
+    for deferred in (False, True):
+        tree = generated_fraction(*args, dev, deferred=deferred)
+        t = Transcript(ctx)
+        with LeafStage([tree], dev) as st:
+            recs = st.prove(t)
+            proof = ([(r.rounds, r.challenges, r.claims, r.final_evals, r.rho) for r in recs], st.claim(0), t.state.hex())
+        leaves = (tree.denominators.cpu().numpy().copy(), None if unit else tree.numerators.cpu().numpy().copy())
+        runs.append((proof, leaves))
+    assert runs[0][0] == runs[1][0]
+    assert np.array_equal(runs[0][1][0], runs[1][1][0])
+    if not unit:
+        assert np.array_equal(runs[0][1][1], runs[1][1][1])
+
+
+def test_generated_leaves_refusals(dev):
+    """A generator needs device buffers (16-byte aligned, numerators exactly when not unit) and a
+    fraction tree; anything else is refused before any work."""
+    import ctypes
+
+    import torch
+
+    from tessera_gb300 import _native as N
+    from tessera_gb300.trees import LeafGen, LeafStage
+
+    g = LeafGen(1, 2, None, (3, 4), (5, 6))
+    den = torch.empty(2 * 8, dtype=torch.int64, device="cuda")
+    num = torch.empty(2 * 8, dtype=torch.int64, device="cuda")
+    from tessera_gb300.trees import Fraction
+
+    with pytest.raises(N.InvalidInput):  # unit generator with a numerators buffer
+        LeafStage([Fraction(den, num, gen=g)], dev)
+    with pytest.raises(N.InvalidInput):  # generated numerators without a buffer
+        LeafStage([Fraction(den, None, gen=LeafGen(1, 2, 3, (3, 4), (5, 6)))], dev)
+    with pytest.raises(N.InvalidInput):  # not canonical
+        LeafStage([Fraction(den, None, gen=LeafGen(1, 2, None, (P, 4), (5, 6)))], dev)
+    arr = (N.TreeC * 1)()
+    gc = N.LeafGenC(1, 2, 0, 1, (ctypes.c_uint64 * 2)(3, 4), (ctypes.c_uint64 * 2)(5, 6))
+    host = np.zeros(16, dtype=np.uint64)
+    arr[0].kind, arr[0].height, arr[0].denominators, arr[0].gen = 1, 3, host.ctypes.data, ctypes.addressof(gc)
+    h = ctypes.c_void_p()
+    with pytest.raises(N.InvalidInput):  # host memory
+        N.call("tg_leaf_stage_open", dev.handle, arr, 1, 0, ctypes.byref(h))
+    arr[0].kind, arr[0].leaves = 0, host.ctypes.data
+    with pytest.raises(N.InvalidInput):  # a forest
+        N.call("tg_leaf_stage_open", dev.handle, arr, 1, 1, ctypes.byref(h))
