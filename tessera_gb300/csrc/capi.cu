@@ -57,6 +57,17 @@ void DevBuf::release() {
     owned = true;
 }
 
+int readback_ensure(Device* d, size_t bytes) {
+    if (d->readback_bytes >= bytes) return TG_OK;
+    if (d->readback) cudaFreeHost(d->readback);
+    d->readback = nullptr;
+    d->readback_bytes = 0;
+    const size_t want = std::max<size_t>(bytes, 64 << 10);
+    TG_CUDA(cudaHostAlloc((void**)&d->readback, want, cudaHostAllocDefault));
+    d->readback_bytes = want;
+    return TG_OK;
+}
+
 int spare_take(Device* d, DevBuf& b, size_t want) {
     if (want == 0) want = 16;
     {
@@ -290,6 +301,7 @@ int tg_device_close(tg_device* dev) {
     }
     for (cudaEvent_t& e : d->ramp)
         if (e) cudaEventDestroy(e);
+    if (d->readback) cudaFreeHost(d->readback);
     d->stage_rows.release();
     d->stage_cw.release();
     d->stage_nodes.release();

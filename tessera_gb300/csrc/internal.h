@@ -75,6 +75,11 @@ struct Device {
     cudaEvent_t staged[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
     cudaEvent_t ramp[4] = {nullptr, nullptr, nullptr, nullptr};  // the first chunk's pieces landed
     DevBuf err;  // device error words for bounded waits
+    // Pinned host memory that small results (a tree level's or a sumcheck batch's transcript
+    // states, messages, challenges, evaluations) come back through in one copy and one wait, not a
+    // synchronous copy each (readback_ensure grows it; used under mu).
+    uint8_t* readback = nullptr;
+    size_t readback_bytes = 0;
     tg_config cfg;
     std::atomic<uint64_t> launches{0};  // kernels this handle has launched
     // While a CUDA graph is captured, Launch counts kernels into `captured` instead (a replay
@@ -98,6 +103,9 @@ struct Device {
     // Returns the tables for (lgn, lgk), building them on first use.
     int get_tables(uint32_t lgn, uint32_t lgk, const Tables** out);
 };
+
+// Device::readback of at least `bytes` (caller holds d->mu).
+int readback_ensure(Device* d, size_t bytes);
 
 cudaStream_t pick_stream(Device* d, void* stream);
 

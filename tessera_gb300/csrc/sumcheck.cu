@@ -899,10 +899,17 @@ int prove_many_opts(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_d
     {
         std::lock_guard<std::mutex> lock(d->mu);
         rc = d->scratch_sc.ensure(r->arena_bytes);
-        if (!rc) rc = sc_enqueue(d, r, d->stream, d->scratch_sc.ptr, host.data());
+        if (!rc) rc = readback_ensure(d, r->host_bytes);
+        // the outputs come back through the device's pinned readback (one wait, not a synchronous
+        // copy each), then move to the run's own buffer before the lock is released
+        if (!rc) rc = sc_enqueue(d, r, d->stream, d->scratch_sc.ptr, d->readback);
         if (!rc) {
             const cudaError_t e = cudaStreamSynchronize(d->stream);
             if (e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
+        }
+        if (!rc) {
+            memcpy(host.data(), d->readback, r->host_bytes);
+            r->host_out = host.data();
         }
     }
     if (!rc) rc = sc_finish(r);

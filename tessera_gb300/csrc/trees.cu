@@ -1495,12 +1495,19 @@ extern "C" int tg_leaf_stage_prove_level(tg_leaf_stage* st, tg_transcript* t, tg
             tl_bind_last<<<1, 128, 0, s>>>(ar.at<TlFinal>(off_finals), (int)finals.size(), ar.at<FsState>(off_fs)->r);
             TG_CUDA(cudaGetLastError());
         }
-        TG_CUDA(cudaMemcpyAsync(&fs1, ar.at<FsState>(off_fs), sizeof fs1, cudaMemcpyDeviceToHost, s));
-        TG_CUDA(cudaMemcpyAsync(rounds.data(), ar.at<uint64_t>(off_rounds), rounds.size() * 8, cudaMemcpyDeviceToHost, s));
-        TG_CUDA(cudaMemcpyAsync(chal.data(), ar.at<uint64_t>(off_chal), chal.size() * 8, cudaMemcpyDeviceToHost, s));
-        TG_CUDA(cudaMemcpyAsync(fevals.data(), ar.at<uint64_t>(off_evals), finals.size() * 16, cudaMemcpyDeviceToHost, s));
-        TG_CUDA(cudaMemcpyAsync(rootc_host.data(), ar.at<uint64_t>(off_rootc), 16 * (size_t)np, cudaMemcpyDeviceToHost, s));
+        // the outputs lie back to back in the block (state, messages, challenges, evaluations, root
+        // claims): one copy into pinned memory and one wait, not a round trip each
+        const size_t out_lo = off_fs, out_bytes = off_rootc + 16 * (size_t)np - off_fs;
+        rc = readback_ensure(d, out_bytes);
+        if (rc) return bail(rc);
+        TG_CUDA(cudaMemcpyAsync(d->readback, ar.base + out_lo, out_bytes, cudaMemcpyDeviceToHost, s));
         TG_CUDA(cudaStreamSynchronize(s));
+        auto from = [&](size_t off) { return d->readback + (off - out_lo); };
+        memcpy(&fs1, from(off_fs), sizeof fs1);
+        memcpy(rounds.data(), from(off_rounds), rounds.size() * 8);
+        memcpy(chal.data(), from(off_chal), chal.size() * 8);
+        memcpy(fevals.data(), from(off_evals), finals.size() * 16);
+        memcpy(rootc_host.data(), from(off_rootc), 16 * (size_t)np);
     }
     for (int i = 0; i < np; i++)  // the device root claims, for the record
         if (root_on_device[present[i]]) held[i] = jvalue[present[i]] = {rootc_host[2 * i], rootc_host[2 * i + 1]};
