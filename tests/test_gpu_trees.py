@@ -535,3 +535,54 @@ def test_generated_leaves_refusals(dev):
     arr[0].kind, arr[0].leaves = 0, host.ctypes.data
     with pytest.raises(N.InvalidInput):  # a forest
         N.call("tg_leaf_stage_open", dev.handle, arr, 1, 1, ctypes.byref(h))
+
+
+def _random_fp2(rng, n):
+    return [(int(a), int(b)) for a, b in zip(rng.integers(0, P, size=n, dtype=np.uint64),
+                                             rng.integers(0, P, size=n, dtype=np.uint64))]
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_random_stages_match_the_oracle(dev, seed):
+    """Random mixed stages beyond the golden shapes — forests of several root counts and heights,
+    fraction trees with and without numerators of 1, trees joining at different levels — proven on
+    the device and by the oracle's restatement of the tree-level prover: every level record, the
+    claims each tree carries and the transcript state agree."""
+    from golden_data import context_tce
+    from oracle import trees as OT
+    from oracle.oracle import OracleTranscript
+    from tessera_gb300.trees import Forest, Fraction, LeafStage
+
+    rng = np.random.default_rng(seed)
+    shapes = [("forest", 2, 3), ("fraction", 0, 4), ("unit", 0, 2), ("forest", 0, 5), ("forest", 3, 1)]
+    gpu_trees, o_trees = [], []
+    for kind, s, h in shapes[: 3 + seed % 3]:
+        if kind == "forest":
+            lv = _random_fp2(rng, 1 << (s + h))
+            gpu_trees.append(Forest(s, words(lv)))
+            o_trees.append(OT.OTree(0, s, leaves=lv))
+        else:
+            den = _random_fp2(rng, 1 << h)
+            num_ = None if kind == "unit" else _random_fp2(rng, 1 << h)
+            gpu_trees.append(Fraction(words(den), None if num_ is None else words(num_)))
+            o_trees.append(OT.OTree(1, 0, numerators=num_, denominators=den))
+    ctx = {"protocol": "tessera-protocol/1", "mode": "NonInteractive", "params": "test-small/1",
+           "statement_digest": "65" * 32, "session_id": "%032x" % seed}
+    tce = context_tce(ctx)
+    from tessera_gb300.hash import Transcript
+
+    t_gpu, t_or = Transcript(tce), OracleTranscript(tce)
+    ost = OT.OStage(o_trees)
+    with LeafStage(gpu_trees, dev) as st:
+        assert st.height == ost.H
+        for _ in range(st.height):
+            rec, want = st.prove_level(t_gpu), ost.prove_level(t_or)
+            assert rec.root_challenges == want["root_challenges"]
+            assert rec.gamma == want["gamma"] and rec.lambda_ == want["lambda"]
+            assert rec.rounds == want["rounds"] and rec.challenges == want["challenges"]
+            assert rec.claims == want["claims"] and rec.final_evals == want["final_evals"]
+            assert rec.rho == want["rho"] and rec.present == want["present"]
+            assert rec.state.hex() == want["state"] and rec.counter == want["counter"]
+            for k in rec.present:
+                point, claim, _ = st.claim(k)
+                assert (point, claim) == ost.claim(k)
