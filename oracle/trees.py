@@ -50,7 +50,8 @@ def line(a, b, r):
 
 
 def mle(values, point):
-    """Σ_x values[x]·eq(point, x), x_1 the lowest bit, by binding one coordinate at a time."""
+    """Σ_x values[x]·eq(point, x), x_1 the lowest bit, by binding one coordinate at a time (a
+    joining forest's claim on its roots, crates/tessera-sumcheck/src/trees.rs:761 prove_trees)."""
     v = list(values)
     for r in point:
         v = [line(v[2 * i], v[2 * i + 1], r) for i in range(len(v) // 2)]
@@ -82,7 +83,9 @@ def lagrange4(v, r):
 class OTree:
     """One tree of a stage: a forest of 2^s product trees (kind 0) from 2^(s+h) Fp2 leaves, or a
     fraction tree (kind 1) from numerators (None: all 1) and denominators, with `sent` the root
-    the roots message carried (None: its own)."""
+    the roots message carried (None: its own). Levels are built as the reference's FractionTree
+    and product trees build them (crates/tessera-sumcheck/src/trees.rs:260-300): entry x of a level
+    from entries 2x and 2x + 1 below, (n, d) = (n_l·d_r + n_r·d_l, d_l·d_r) or the product."""
 
     def __init__(self, kind, s, leaves=None, numerators=None, denominators=None, sent=None):
         self.kind, self.s, self.sent = kind, s, sent
@@ -132,6 +135,9 @@ class OStage:
         self.level = 0
 
     def prove_level(self, t) -> dict:
+        """The stage's next level on transcript t (crates/tessera-sumcheck/src/trees.rs:761
+        prove_trees, one ProvenTreeLevel; the batched level sumcheck of level.rs:127-262 with the
+        padding of prover.rs:1122-1410), as a record of what it absorbed and drew."""
         level, H = self.level, self.H
         prefix = f"tree/{level}"
         joining = [k for k, tr in enumerate(self.trees) if H - tr.h == level]
