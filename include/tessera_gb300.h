@@ -128,7 +128,8 @@ int tg_encode_rows(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32
  * 32 MiB device array that every GPU loading the library holds until exit; shapes need
  * 2 (k + n) <= 2^22 words (k <= 2^19 at rate 1/2) and larger ones are refused. The first call on a
  * device looks up the array's address, so make it before any stream capture. Calls share the
- * array: calls that overlap on the GPU race, so order them on one stream. */
+ * array: calls that overlap on the GPU race, so order them on one stream. The handle's device
+ * must be the current device (TG_ERR_INVALID otherwise). */
 int tg_encode_rows_noalloc_dev(tg_device *dev, uint32_t log_k, uint32_t log_inv_rate, uint32_t mask_coeffs,
                                const uint64_t *rows, size_t nrows, const uint64_t *masks, uint64_t *codewords,
                                void *stream);

@@ -434,116 +434,35 @@ int lde_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_
     if ((size_t)P_ > ((size_t)1 << lgk)) return fail(TG_ERR_INVALID, "%u mask coefficients exceed k", P_);
     if (P_ > 0 && !masks) return fail(TG_ERR_INVALID, "mask coefficients requested without masks");
     if (npolys == 0) return TG_OK;
-    const uint32_t lgn = lgk + lgr;
     const Tables* t;
-    int rc = d->get_tables(lgn, lgk, &t);
+    int rc = d->get_tables(lgk + lgr, lgk, &t);
     if (rc) return rc;
-
-    LdeArgs a = {};
-    a.pw = t->pw;
-    a.pow7k = t->pow7k;
-    a.lgk = (int)lgk;
-    a.lgr = (int)lgr;
-    a.P = (int)P_;
-    const uint64_t k = 1ull << lgk;
-    const uint64_t pow7_k = pow(7, k);
-    const uint64_t w_r = root_of_unity(lgr);  // ω_{2^r}
-    uint64_t we = 1;
-    for (int e = 0; e < (1 << lgr); e++) {
-        a.mk[e] = mul(k % P, sub(mul(pow7_k, we), 1));
-        we = mul(we, w_r);
-    }
-    const int limit = smem_limit(d);
-
-    if (lgk <= 11) {
-        const size_t K = (size_t)1 << lgk;
-        const size_t smem = (2 * K + 2 * std::max<size_t>(K / 2, 1)) * 8;
-        TG_CUDA(cudaFuncSetAttribute(lde_small, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-        const int threads = (int)std::min<size_t>(512, std::max<size_t>(32, K / 2));
-        for (size_t r0 = 0; r0 < npolys; r0 += 65535) {
-            const size_t g = std::min<size_t>(65535, npolys - r0);
-            a.rows = rows + (r0 << lgk);
-            a.masks = masks ? masks + r0 * P_ : nullptr;
-            a.out = codewords + (r0 << lgn);
-            Launch L(d, s, "lde_small", 1, g);
-            lde_small<<<(unsigned)g, threads, smem, s>>>(a);
-        }
-        TG_CUDA(cudaGetLastError());
-        return TG_OK;
-    }
-
-    if (fast_shape(lgk)) {
-        const size_t per_row_fast = (k + (k << lgr)) * 8;
-        size_t gfast = std::max<size_t>(1, d->cfg.lde_group_bytes / per_row_fast);
-        gfast = std::min<size_t>(gfast, std::min<size_t>(npolys, 65535));
-        rc = d->scratch_y.ensure(gfast * k * 8);
+    // Rows of k > 2^11 go through scratch: k + n words per row, rows in groups of about the
+    // configured budget, so that every pass's grid spans many waves.
+    size_t group = 0;
+    uint64_t *y = nullptr, *z = nullptr;
+    if (lgk > 11) {
+        const size_t k = (size_t)1 << lgk;
+        group = std::max<size_t>(1, d->cfg.lde_group_bytes / ((k + (k << lgr)) * 8));
+        group = std::min<size_t>(group, std::min<size_t>(npolys, 65535));
+        rc = d->scratch_y.ensure(group * k * 8);
         if (rc) return rc;
-        rc = d->scratch_z.ensure(gfast * (k << lgr) * 8);
+        rc = d->scratch_z.ensure(group * (k << lgr) * 8);
         if (rc) return rc;
-        return fast_encode(d, lgk, lgr, P_, rows, npolys, masks, codewords, s, t->pw, t->pow7k,
-                           (uint64_t*)d->scratch_y.ptr, (uint64_t*)d->scratch_z.ptr, gfast);
+        y = (uint64_t*)d->scratch_y.ptr;
+        z = (uint64_t*)d->scratch_z.ptr;
     }
-    a.lgk1 = (int)(lgk + 1) / 2;
-    a.lgk2 = (int)lgk / 2;
-    const size_t K1 = (size_t)1 << a.lgk1, K2 = (size_t)1 << a.lgk2;
-    const size_t R = (size_t)1 << lgr;
-    // tile widths: at most 128 KiB of data per buffer
-    int lgw_a = 4, lgw_m = 3, lgw_c = 3;
-    while (lgw_a > 0 && ((K2 << lgw_a) * 8 > 128 * 1024)) lgw_a--;
-    while (lgw_m > 0 && (2 * ((K1 + 1) << lgw_m) * 8 + K1 * 8 > (size_t)limit)) lgw_m--;
-    while (lgw_c > 0 && (R * ((K2 + 1) << lgw_c) * 8 + K2 * 4 > (size_t)limit)) lgw_c--;
-    const size_t smem_a = ((K2 << lgw_a) + K2 / 2) * 8;
-    const size_t smem_m = (2 * ((K1 + 1) << lgw_m) + K1) * 8;
-    const size_t smem_c = (R * ((K2 + 1) << lgw_c) + K2 / 2) * 8;
-    if (smem_m > (size_t)limit || smem_c > (size_t)limit)
-        return fail(TG_ERR_INVALID, "row length 2^%u at rate 1/2^%u exceeds shared memory", lgk, lgr);
-    TG_CUDA(cudaFuncSetAttribute(lde_pass_a, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_a));
-    TG_CUDA(cudaFuncSetAttribute(lde_pass_m, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_m));
-    TG_CUDA(cudaFuncSetAttribute(lde_pass_c, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_c));
-
-    // rows per group: scratch of (k + n) words per row, about the configured budget
-    const size_t per_row = (k + (k << lgr)) * 8;
-    size_t group = std::max<size_t>(1, d->cfg.lde_group_bytes / per_row);
-    group = std::min<size_t>(group, std::min<size_t>(npolys, 65535));
-    rc = d->scratch_y.ensure(group * k * 8);
-    if (rc) return rc;
-    rc = d->scratch_z.ensure(group * (k << lgr) * 8);
-    if (rc) return rc;
-    a.y = (uint64_t*)d->scratch_y.ptr;
-    a.z = (uint64_t*)d->scratch_z.ptr;
-    for (size_t r0 = 0; r0 < npolys; r0 += group) {
-        const unsigned g = (unsigned)std::min(group, npolys - r0);
-        a.rows = rows + (r0 << lgk);
-        a.masks = masks ? masks + r0 * P_ : nullptr;
-        a.out = codewords + (r0 << lgn);
-        a.lgw = lgw_a;
-        {
-            Launch L(d, s, "lde_pass_a", 1, g);
-            lde_pass_a<<<dim3((unsigned)(K1 >> lgw_a), g), 512, smem_a, s>>>(a);
-        }
-        a.lgw = lgw_m;
-        {
-            Launch L(d, s, "lde_pass_m", 1, g);
-            lde_pass_m<<<dim3((unsigned)(K2 >> lgw_m), g), 512, smem_m, s>>>(a);
-        }
-        a.lgw = lgw_c;
-        {
-            Launch L(d, s, "lde_pass_c", 1, g);
-            lde_pass_c<<<dim3((unsigned)(K1 >> lgw_c), g), 512, smem_c, s>>>(a);
-        }
-    }
-    TG_CUDA(cudaGetLastError());
-    return TG_OK;
+    return lde_encode_into(d, lgk, lgr, P_, rows, npolys, masks, codewords, s, t->pw, t->pow7k, false, y, z, group);
 }
 
 }  // namespace tg
 
 namespace tg {
 
-// The encoder over caller-owned tables and scratch, for the allocation-free entry point: it
-// launches the same kernels as lde_encode but allocates nothing. When `build_tables` is set it
-// first writes pw (n words, ω_n^m) and pow7k (k words, 7^i/k) on stream s; y and z hold
-// `group` rows of scratch (k and n words per row).
+// The encoder over caller-owned tables and scratch (lde_encode's launcher, and the
+// allocation-free entry point's): it allocates nothing. When `build_tables` is set it first
+// writes pw (n words, ω_n^m) and pow7k (k words, 7^i/k) on stream s; y and z hold `group` rows
+// of scratch (k and n words per row; unused for k <= 2^11).
 int lde_encode_into(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_t* rows, size_t npolys,
                     const uint64_t* masks, uint64_t* codewords, cudaStream_t s, uint64_t* pw, uint64_t* pow7k,
                     bool build_tables, uint64_t* y, uint64_t* z, size_t group) {

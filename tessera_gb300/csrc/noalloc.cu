@@ -82,12 +82,25 @@ extern "C" int tg_encode_rows_noalloc_dev(tg_device* dev, uint32_t log_k, uint32
                     "rows of 2^%u at rate 1/2^%u need %zu words of fixed scratch; the allocation-free encoder holds %zu "
                     "(2 (k + n) <= 2^22)",
                     log_k, log_inv_rate, tables + per_row, NOALLOC_WORDS);
+    // The fixed array's address is this device's, so the kernels must launch on this device.
+    int cur = -1;
+    TG_CUDA(cudaGetDevice(&cur));
+    if (cur != d->ordinal)
+        return fail(TG_ERR_INVALID, "tg_encode_rows_noalloc_dev: device %d is current, the handle is device %d", cur,
+                    d->ordinal);
     std::lock_guard<std::mutex> lock(g_mu);
     PerDevice* pd = nullptr;
     int rc = device_base(d->ordinal, &pd);
     if (rc) return rc;
     const uint32_t lgn = log_k + log_inv_rate;
-    const bool build = !(pd->tables && pd->lgn == lgn && pd->lgk == log_k);
+    cudaStream_t s = pick_stream(d, stream);
+    // A call recorded into a CUDA graph runs its kernels only when the graph is launched, maybe
+    // after calls of other shapes have rewritten the array: such a call always writes its own
+    // tables, and leaves the array's tables marked unknown for the next direct call.
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    TG_CUDA(cudaStreamIsCapturing(s, &capture));
+    const bool captured = capture != cudaStreamCaptureStatusNone;
+    const bool build = captured || !(pd->tables && pd->lgn == lgn && pd->lgk == log_k);
     uint64_t* pw = pd->base;
     uint64_t* pow7k = pw + n;
     uint64_t* scratch = pow7k + k;
@@ -95,9 +108,9 @@ extern "C" int tg_encode_rows_noalloc_dev(tg_device* dev, uint32_t log_k, uint32
     uint64_t* y = scratch;
     uint64_t* z = scratch + group * k;
     std::lock_guard<std::mutex> dl(d->mu);
-    rc = lde_encode_into(d, log_k, log_inv_rate, mask_coeffs, rows, nrows, masks, codewords, pick_stream(d, stream), pw,
-                         pow7k, build, y, z, std::max<size_t>(group, 1));
-    if (rc) {
+    rc = lde_encode_into(d, log_k, log_inv_rate, mask_coeffs, rows, nrows, masks, codewords, s, pw, pow7k, build, y, z,
+                         std::max<size_t>(group, 1));
+    if (rc || captured) {
         pd->tables = false;
         return rc;
     }

@@ -64,3 +64,49 @@ def test_noalloc_refuses_shapes_beyond_its_array():
     out_d = torch.zeros(1 << 21, dtype=torch.int64, device="cuda")
     with pytest.raises(N.InvalidInput, match="fixed scratch"):
         _encode("tg_encode_rows_noalloc_dev", dev, 20, 1, 0, rows_d, 1, None, out_d)
+
+
+def test_noalloc_graph_replay_after_a_call_of_another_shape():
+    """A call recorded into a CUDA graph writes its own tables when the graph runs.
+
+    The fixed array keeps the tables of the last shape encoded. A graph recorded from a call of
+    shape A and replayed after a direct call of shape B must still give A's codewords.
+    """
+    import torch
+
+    from tessera_gb300.device import default_device
+
+    dev = default_device()
+    shapes = {"a": (14, 1, 0, 2), "b": (13, 2, 0, 3)}
+    bufs = {}
+    for name, (log_k, log_r, P, nrows) in shapes.items():
+        k, n = 1 << log_k, 1 << (log_k + log_r)
+        rng = np.random.default_rng(77 + log_k)
+        rows = rng.integers(0, 0xFFFFFFFF00000001, size=nrows * k, dtype=np.uint64)
+        rows_d = torch.from_numpy(rows.view(np.int64)).cuda()
+        want = torch.empty(nrows * n, dtype=torch.int64, device="cuda")
+        _encode("tg_encode_rows_dev", dev, log_k, log_r, P, rows_d, nrows, None, want)
+        bufs[name] = (rows_d, want, torch.full((nrows * n,), -1, dtype=torch.int64, device="cuda"))
+    torch.cuda.synchronize()
+    a, b = shapes["a"], shapes["b"]
+    _encode("tg_encode_rows_noalloc_dev", dev, a[0], a[1], a[2], bufs["a"][0], a[3], None, bufs["a"][2])
+    torch.cuda.synchronize()
+    graph = torch.cuda.CUDAGraph()
+    side = torch.cuda.Stream()
+    with torch.cuda.graph(graph, stream=side, capture_error_mode="relaxed"):
+        _encode("tg_encode_rows_noalloc_dev", dev, a[0], a[1], a[2], bufs["a"][0], a[3], None, bufs["a"][2])
+    bufs["a"][2].fill_(-1)
+    torch.cuda.synchronize()
+    # the direct call runs on the library's stream (torch's default stream has no handle), so the
+    # replay waits for it to end: calls that overlap on the GPU race on the array
+    _encode("tg_encode_rows_noalloc_dev", dev, b[0], b[1], b[2], bufs["b"][0], b[3], None, bufs["b"][2])
+    torch.cuda.synchronize()
+    graph.replay()
+    torch.cuda.synchronize()
+    assert torch.equal(bufs["b"][2], bufs["b"][1])
+    assert torch.equal(bufs["a"][2], bufs["a"][1])
+    # a direct call of shape A after the replay
+    bufs["a"][2].fill_(-1)
+    _encode("tg_encode_rows_noalloc_dev", dev, a[0], a[1], a[2], bufs["a"][0], a[3], None, bufs["a"][2])
+    torch.cuda.synchronize()
+    assert torch.equal(bufs["a"][2], bufs["a"][1])
