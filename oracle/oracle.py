@@ -98,6 +98,7 @@ def _declare(L):
         "or_level_sums": (None, [INT, vp, vp, SZ, vp, vp, U32, vp]),
         "or_level_bind": (None, [vp, INT, SZ, vp]),
         "or_splitmix_fill": (None, [U64, vp, SZ]),
+        "or_mle": (None, [vp, INT, U32, vp, vp]),
     }
     for name, (res, args) in sig.items():
         f = getattr(L, name)
@@ -344,6 +345,15 @@ def level_bind(tables, r):
     ra = u64(r)
     lib().or_level_bind(ptrs, len(tabs), tabs[0].size // 2, _ptr(ra))
     return [t[: t.size // 2] for t in tabs]
+
+
+def mle(values, point, is_ext: bool = False):
+    """Σ_x values[x]·eq(point, x), point a list of Fp2 pairs (x_1 the index's lowest bit)."""
+    v = u64(values).reshape(-1)
+    pt = np.array([c for p_ in point for c in p_], dtype=np.uint64) if point else np.zeros(1, dtype=np.uint64)
+    out = (ctypes.c_uint64 * 2)()
+    lib().or_mle(_ptr(v), int(is_ext), len(point), _ptr(pt), out)
+    return (int(out[0]), int(out[1]))
 
 
 def threads_available() -> int:

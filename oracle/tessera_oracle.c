@@ -1071,3 +1071,32 @@ void or_splitmix_fill(uint64_t seed, uint64_t *out, size_t n) {
         out[i] = canon(z ^ (z >> 31));
     }
 }
+
+/* ---- multilinear extension at a point (verifier side) ---------------------------------- */
+/* Σ_x values[x]·eq(point, x) over x < 2^log_n, x_1 the index's lowest bit: the eq table is built
+ * one coordinate at a time (eq over the first t coordinates doubled by (1 − r_t, r_t)), then one
+ * dot product — not the prover's variable-by-variable binding. values: prime-field words
+ * (is_ext = 0) or interleaved Fp2 pairs (is_ext = 1); point: log_n Fp2 pairs. */
+void or_mle(const uint64_t *values, int is_ext, uint32_t log_n, const uint64_t *point, uint64_t out[2]) {
+    const size_t n = (size_t)1 << log_n;
+    fp2 *eqt = (fp2 *)malloc(n * sizeof(fp2));
+    eqt[0] = E_ONE;
+    for (uint32_t t = 0; t < log_n; t++) {
+        const fp2 r = {point[2 * t], point[2 * t + 1]};
+        const fp2 one_minus = e_sub(E_ONE, r);
+        const size_t half = (size_t)1 << t;
+        for (size_t x = 0; x < half; x++) {
+            const fp2 e = eqt[x];
+            eqt[x + half] = e_mul(e, r);
+            eqt[x] = e_mul(e, one_minus);
+        }
+    }
+    fp2 acc = E_ZERO;
+    for (size_t x = 0; x < n; x++) {
+        const fp2 v = is_ext ? (fp2){values[2 * x], values[2 * x + 1]} : e_lift(values[x]);
+        acc = e_add(acc, e_mul(v, eqt[x]));
+    }
+    free(eqt);
+    out[0] = acc.c0;
+    out[1] = acc.c1;
+}

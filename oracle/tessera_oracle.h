@@ -117,6 +117,9 @@ void or_level_sums(int shape, const uint64_t lambda[2], const uint64_t *const *t
                    const uint64_t *low, const uint64_t *high, uint32_t low_bits, uint64_t out[6]);
 void or_level_bind(uint64_t *const *tables, int ntables, size_t len, const uint64_t r[2]);
 
+/* ---- multilinear extension Σ_x values[x]·eq(point, x) (eq table, then one dot product) ---- */
+void or_mle(const uint64_t *values, int is_ext, uint32_t log_n, const uint64_t *point, uint64_t out[2]);
+
 /* ---- synthetic inputs (tessera-bench/benches/primitives.rs:52-69) --------------------- */
 void or_splitmix_fill(uint64_t seed, uint64_t *out, size_t n); /* from_u64_reduced of each */
 

@@ -6,7 +6,9 @@ Run once, in a checkout that has the reference beside it:
     python3 tests/golden/make_fixtures.py /path/to/tessera
 
 It copies the reference's golden JSON for the hot path (spec/vectors/{blake3, encoding, hash,
-transcript, pcs-streaming, sumcheck}) into gzip files here, trimmed to what the tests read. For
+transcript, pcs-streaming, sumcheck, pcs}) into gzip files here, trimmed to what the tests read.
+The advice openings (spec/vectors/pcs/opening.json: honest openings with their witness, combined
+rows, drawn columns and multiproofs, and the rejections a verifier must return) are copied whole. For
 sumcheck stages whose tables the JSON does not record (more than 5 variables), it runs the
 reference's own stdlib-Python oracle (spec/vectors/sumcheck/generate.py) and records where each
 stage's tables start in its SplitMix64 stream, so the tests regenerate the tables exactly; the
@@ -112,6 +114,8 @@ def main() -> None:
     write("sumcheck.json.gz", {"seed": hex(seed), "sessions": sessions})
     # tree levels: product trees, product forests and LogUp leaf stages, with every level record
     write("trees.json.gz", {k: sc[k] for k in ("tree_batches", "forest_batches", "logup_batches")})
+    op = load(vec / "pcs" / "opening.json")
+    write("opening.json.gz", {k: op[k] for k in ("seed", "openings", "rejections")})
 
 
 if __name__ == "__main__":
