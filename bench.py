@@ -115,24 +115,71 @@ def dist_env():
 
 # ---- CPU port (the reference arm and the cpu_baseline leg) ---------------------------------------
 
-def cpu_sample(threads: int, polys: int, sc_vars: int) -> tuple[float, int, str]:
-    """Times the oracle (the plain-C port of the reference's algorithms) on a bounded sample of
-    the workload: `polys` rows of 2^20 committed at rate 1/2 with B = 32 (all 2^21 columns
-    chained and merkled), then the degree-3 sumcheck over three tables of 2^sc_vars."""
-    from oracle import oracle as O
+class CpuStep:
+    """The CPU port's time for one full step of the workload, composed from timed components.
 
-    rows = O.splitmix(SEED, polys << LOG_K)
-    f, g, h = (O.splitmix(SEED + 1 + i, 1 << sc_vars) for i in range(3))
-    ctx = bench_context().tce()
-    t0 = time.perf_counter()
-    O.commit_unmasked(rows, LOG_K, LOG_R, ROW_BLOCK, bytes([0x65]) * 32, threads=threads, keep_codewords=False)
-    t1 = time.perf_counter()
-    O.prove_batch(O.OracleTranscript(ctx), "stage/0", SC_DEGREE, [[(f, False, False), (g, False, False), (h, False, False)]])
-    t2 = time.perf_counter()
-    units = (polys << LOG_K) + (SC_DEGREE << sc_vars)
-    sample = (f"{polys} of 256 polynomials of 2^20 committed (all 2^21 columns chained and merkled) in {t1 - t0:.2f} s, "
-              f"sumcheck over 3 x 2^{sc_vars} in {t2 - t1:.2f} s, {threads} threads for the commitment")
-    return t2 - t0, units, sample
+    A full step at 1 thread takes about a minute, so each run times bounded samples of every
+    component and scales each by the units it processed: `polys` of the 256 rows encoded (k = 2^20,
+    rate 1/2), the 2^21 column chains' init and one 32-row absorb block over 2^21 >> col_shift
+    columns, the Merkle tree over as many leaves, and the whole degree-3 sumcheck over 3 x 2^22.
+    step = 256/polys · encode + 2^col_shift · (init + 8 · block + merkle) + sumcheck, each a
+    linear cost in its units (rows, columns, blocks, nodes)."""
+
+    def __init__(self, threads: int, polys: int, col_shift: int):
+        from oracle import oracle as O
+
+        self.O, self.threads, self.polys, self.col_shift = O, threads, polys, col_shift
+        n = 1 << (LOG_K + LOG_R)
+        self.cols = n >> col_shift
+        self.rows = O.splitmix(SEED, polys << LOG_K)
+        self.block = O.splitmix(SEED + 7, ROW_BLOCK * self.cols)  # symbols of one absorb block
+        self.leaves = np.frombuffer(O.splitmix(SEED + 8, 4 * self.cols).tobytes(), dtype=np.uint8).reshape(-1, 32)
+        self.tabs = [O.splitmix(SEED + 1 + i, 1 << SC_VARS) for i in range(3)]
+        self.ctx = bench_context().tce()
+
+    def run(self) -> dict:
+        O, T = self.O, self.threads
+        cid = bytes([0x65]) * 32
+        t0 = time.perf_counter()
+        O.encode_rows(self.rows, LOG_K, LOG_R, threads=T)
+        t1 = time.perf_counter()
+        O.column_chains(cid, self.block[:0], self.cols, ROW_BLOCK, threads=T)  # init only
+        t2 = time.perf_counter()
+        O.column_chains(cid, self.block, self.cols, ROW_BLOCK, threads=T)  # init + one block
+        t3 = time.perf_counter()
+        O.merkle_tree(self.leaves, threads=T)
+        t4 = time.perf_counter()
+        O.prove_batch(O.OracleTranscript(self.ctx), "stage/0", SC_DEGREE, [[(x, False, False) for x in self.tabs]])
+        t5 = time.perf_counter()
+        scale = 1 << self.col_shift
+        blocks = NPOLYS // ROW_BLOCK
+        parts = {"encode_s": (t1 - t0) * NPOLYS / self.polys, "chain_init_s": (t2 - t1) * scale,
+                 "chain_blocks_s": max(0.0, (t3 - t2) - (t2 - t1)) * scale * blocks, "merkle_s": (t4 - t3) * scale,
+                 "sumcheck_s": t5 - t4}
+        parts["step_s"] = sum(parts.values())
+        parts["sampled_s"] = t5 - t0
+        return parts
+
+    def sample(self) -> str:
+        return (f"composed step: {self.polys} of 256 rows encoded, chains (init + one 32-row block) and the Merkle "
+                f"tree over 2^{LOG_K + LOG_R - self.col_shift} of 2^{LOG_K + LOG_R} columns, each scaled to the full "
+                f"step, plus the whole sumcheck over 3 x 2^{SC_VARS}; {self.threads} thread(s)")
+
+
+def rfc0020(step: CpuStep, warmup: int, runs: int) -> dict:
+    """Warm-up runs, then measured runs: median, min, max and CV of the composed step time (the
+    reference's benchmarking protocol, docs/perf/README.md:25-27, flags CV above 3 %)."""
+    for _ in range(warmup):
+        step.run()
+    rs = [step.run() for _ in range(runs)]
+    ts = [r["step_s"] for r in rs]
+    med = statistics.median(ts)
+    cv = statistics.pstdev(ts) / statistics.mean(ts) if len(ts) > 1 else 0.0
+    mid = rs[ts.index(sorted(ts)[len(ts) // 2])]
+    return {"step_s_median": med, "step_s_min": min(ts), "step_s_max": max(ts), "cv": cv, "noisy": cv > 0.03,
+            "warmup": warmup, "runs": runs, "threads": step.threads, "value": UNITS / med,
+            "components_s": {k: v for k, v in mid.items() if k not in ("step_s", "sampled_s")},
+            "sampled_s_per_run": statistics.mean(r["sampled_s"] for r in rs), "sample": step.sample()}
 
 
 def bench_context():
@@ -142,6 +189,10 @@ def bench_context():
 
 
 def run_reference(args) -> None:
+    """The reference arm: the CPU port of the reference's algorithms (the oracle) on this host's
+    cores, one full step of the workload composed from timed components (CpuStep) per run, at
+    all host threads (the value) and at one thread (the reference's default), each with the
+    warm-up and measured runs of the reference's benchmarking protocol."""
     world, rank, _ = dist_env()
     if rank != 0:
         return
@@ -149,21 +200,20 @@ def run_reference(args) -> None:
 
     O.build()
     threads = O.threads_available()
-    times, units, sample = [], 0, ""
-    for i in range(args.warmup + args.steps):
-        dt, units, sample = cpu_sample(threads, args.ref_polys, SC_VARS)
-        if i >= args.warmup:
-            times.append(dt)
-    ms = 1e3 * statistics.mean(times)
-    value = units / (ms / 1e3)
+    allc = rfc0020(CpuStep(threads, args.ref_polys, 0), max(3, args.warmup), args.steps)
+    one = rfc0020(CpuStep(1, 2, 4), 1, 3)
+    value = allc["value"]
     line = {
         "metric": "committed+sumchecked field elems/s", "value": value, "unit": "elems/s", "n_gpus": args.gpus,
-        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic", "impl": "reference",
-        "config": CONFIG,
-        "cpu_baseline": {"value": value, "unit": "elems/s", "cores": threads, "kind": "port", "sample": sample},
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": 1e3 * allc["step_s_median"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)",
+        "data": "synthetic", "impl": "reference", "config": CONFIG,
+        "composed": "each step's time is composed from timed samples of every component, scaled to the full "
+                    "256 x 2^20 commitment and 3 x 2^22 sumcheck (a full step at one thread takes about a minute)",
+        "cpu_baseline": {"value": value, "unit": "elems/s", "cores": threads, "kind": "port", "sample": allc["sample"],
+                         "all_cores": allc, "one_thread": one},
         "e2e": {"value": value, "unit": "elems/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-        "latency_ms": {"p50": 1e3 * statistics.median(times), "p99": 1e3 * max(times)},
+        "latency_ms": {"p50": 1e3 * allc["step_s_median"], "p99": 1e3 * allc["step_s_max"]},
     }
     print(json.dumps(line), flush=True)
 
@@ -370,8 +420,10 @@ def run_gpu(args) -> None:
 
         O.build()
         threads = O.threads_available()
-        dt, units, sample = cpu_sample(threads, args.cpu_polys, SC_VARS)
-        line["cpu_baseline"] = {"value": units / dt, "unit": "elems/s", "cores": threads, "kind": "port", "sample": sample}
+        allc = rfc0020(CpuStep(threads, args.cpu_polys, 0), 1, 5)
+        one = rfc0020(CpuStep(1, 2, 4), 1, 3)
+        line["cpu_baseline"] = {"value": allc["value"], "unit": "elems/s", "cores": threads, "kind": "port",
+                                "sample": allc["sample"], "all_cores": allc, "one_thread": one}
     print(json.dumps(line), flush=True)
 
 
@@ -786,8 +838,8 @@ def main():
     ap.add_argument("--rate", type=float, default=20.0, help="serve: mean Poisson arrivals per second")
     ap.add_argument("--slots", type=int, default=8, help="serve: requests in flight at most")
     ap.add_argument("--serve-budget-gib", type=int, default=64, help="serve: HBM budget for admitted requests")
-    ap.add_argument("--cpu-polys", type=int, default=32, help="rows in the CPU baseline's bounded sample")
-    ap.add_argument("--ref-polys", type=int, default=32, help="rows per step in the reference arm's sample")
+    ap.add_argument("--cpu-polys", type=int, default=32, help="rows encoded per run in the CPU baseline's sample")
+    ap.add_argument("--ref-polys", type=int, default=32, help="rows encoded per run in the reference arm's sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--lde-group-mib", type=int, default=0, help="encoder scratch per group of rows (0: the library default)")
     ap.add_argument("--polys", type=int, default=NPOLYS,

@@ -134,6 +134,21 @@ int tg_encode_rows_noalloc_dev(tg_device *dev, uint32_t log_k, uint32_t log_inv_
                                const uint64_t *rows, size_t nrows, const uint64_t *masks, uint64_t *codewords,
                                void *stream);
 
+/* ---- Standalone transforms: NttPlan::{ntt, intt, coset_ntt, coset_intt}
+ * (crates/tessera-pcs/src/ntt.rs:461-516), over nrows rows of n = 2^log_n values each, in place,
+ * natural order on both sides: ntt gives values[j] = f(ω_n^j) from the coefficients, coset_ntt
+ * values[j] = f(shift·ω_n^j), intt and coset_intt their inverses. log_n <= 22; a zero or
+ * non-canonical shift is refused (PcsError::ZeroShift). The _dev forms work on device memory
+ * and are enqueued on `stream` (NULL: the device's stream); the others take host memory. */
+int tg_ntt_dev(tg_device *dev, uint32_t log_n, uint64_t *values, size_t nrows, void *stream);
+int tg_intt_dev(tg_device *dev, uint32_t log_n, uint64_t *values, size_t nrows, void *stream);
+int tg_coset_ntt_dev(tg_device *dev, uint32_t log_n, uint64_t shift, uint64_t *values, size_t nrows, void *stream);
+int tg_coset_intt_dev(tg_device *dev, uint32_t log_n, uint64_t shift, uint64_t *values, size_t nrows, void *stream);
+int tg_ntt(tg_device *dev, uint32_t log_n, uint64_t *values, size_t nrows);
+int tg_intt(tg_device *dev, uint32_t log_n, uint64_t *values, size_t nrows);
+int tg_coset_ntt(tg_device *dev, uint32_t log_n, uint64_t shift, uint64_t *values, size_t nrows);
+int tg_coset_intt(tg_device *dev, uint32_t log_n, uint64_t shift, uint64_t *values, size_t nrows);
+
 /* ---- Column chains and Merkle trees (crates/tessera-hash/src/columns.rs:72-104,
  * crates/tessera-hash/src/merkle.rs:93-113). chains: ncols x 32 bytes. */
 int tg_column_init_dev(tg_device *dev, const uint8_t commitment_id[32], uint64_t ncols, uint8_t *chains,

@@ -120,6 +120,14 @@ SIGNATURES = {
     "tg_encode_rows_dev": [V, U32, U32, U32, V, SZ, V, V, V],
     "tg_encode_rows": [V, U32, U32, U32, V, SZ, V, V],
     "tg_encode_rows_noalloc_dev": [V, U32, U32, U32, V, SZ, V, V, V],
+    "tg_ntt_dev": [V, U32, V, SZ, V],
+    "tg_intt_dev": [V, U32, V, SZ, V],
+    "tg_coset_ntt_dev": [V, U32, U64, V, SZ, V],
+    "tg_coset_intt_dev": [V, U32, U64, V, SZ, V],
+    "tg_ntt": [V, U32, V, SZ],
+    "tg_intt": [V, U32, V, SZ],
+    "tg_coset_ntt": [V, U32, U64, V, SZ],
+    "tg_coset_intt": [V, U32, U64, V, SZ],
     "tg_column_init_dev": [V, V, U64, V, V],
     "tg_column_absorb_dev": [V, V, U64, V, SZ, U32, V],
     "tg_merkle_tree_dev": [V, V, SZ, V, V],

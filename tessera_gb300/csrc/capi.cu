@@ -442,6 +442,59 @@ int tg_encode_rows(tg_device* dev, uint32_t log_k, uint32_t log_inv_rate, uint32
     return TG_OK;
 }
 
+static int ntt_dev(tg_device* dev, int kind, uint32_t log_n, uint64_t shift, uint64_t* values, size_t nrows, void* stream) {
+    Device* d = reinterpret_cast<Device*>(dev);
+    if (!d || (nrows && !values)) return fail(TG_ERR_INVALID, "transform: null argument");
+    std::lock_guard<std::mutex> lock(d->mu);
+    return ntt_rows(d, kind, log_n, shift, values, nrows, pick_stream(d, stream));
+}
+
+static int ntt_host(tg_device* dev, int kind, uint32_t log_n, uint64_t shift, uint64_t* values, size_t nrows) {
+    Device* d = reinterpret_cast<Device*>(dev);
+    if (!d || (nrows && !values)) return fail(TG_ERR_INVALID, "transform: null argument");
+    if (log_n > 22) return fail(TG_ERR_INVALID, "transforms of 2^%u points: the device transforms go up to 2^22", log_n);
+    if (nrows == 0) return TG_OK;
+    const size_t bytes = (nrows << log_n) * 8;
+    DevBuf v;
+    int rc = v.ensure(bytes);
+    if (rc) return rc;
+    cudaStream_t s = d->stream;
+    TG_CUDA(cudaMemcpyAsync(v.ptr, values, bytes, cudaMemcpyHostToDevice, s));
+    {
+        std::lock_guard<std::mutex> lock(d->mu);
+        rc = ntt_rows(d, kind, log_n, shift, (uint64_t*)v.ptr, nrows, s);
+    }
+    if (rc) return rc;
+    TG_CUDA(cudaMemcpyAsync(values, v.ptr, bytes, cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    return TG_OK;
+}
+
+int tg_ntt_dev(tg_device* dev, uint32_t log_n, uint64_t* values, size_t nrows, void* stream) {
+    return ntt_dev(dev, NTT_FORWARD, log_n, 1, values, nrows, stream);
+}
+int tg_intt_dev(tg_device* dev, uint32_t log_n, uint64_t* values, size_t nrows, void* stream) {
+    return ntt_dev(dev, NTT_INVERSE, log_n, 1, values, nrows, stream);
+}
+int tg_coset_ntt_dev(tg_device* dev, uint32_t log_n, uint64_t shift, uint64_t* values, size_t nrows, void* stream) {
+    return ntt_dev(dev, NTT_COSET_FORWARD, log_n, shift, values, nrows, stream);
+}
+int tg_coset_intt_dev(tg_device* dev, uint32_t log_n, uint64_t shift, uint64_t* values, size_t nrows, void* stream) {
+    return ntt_dev(dev, NTT_COSET_INVERSE, log_n, shift, values, nrows, stream);
+}
+int tg_ntt(tg_device* dev, uint32_t log_n, uint64_t* values, size_t nrows) {
+    return ntt_host(dev, NTT_FORWARD, log_n, 1, values, nrows);
+}
+int tg_intt(tg_device* dev, uint32_t log_n, uint64_t* values, size_t nrows) {
+    return ntt_host(dev, NTT_INVERSE, log_n, 1, values, nrows);
+}
+int tg_coset_ntt(tg_device* dev, uint32_t log_n, uint64_t shift, uint64_t* values, size_t nrows) {
+    return ntt_host(dev, NTT_COSET_FORWARD, log_n, shift, values, nrows);
+}
+int tg_coset_intt(tg_device* dev, uint32_t log_n, uint64_t shift, uint64_t* values, size_t nrows) {
+    return ntt_host(dev, NTT_COSET_INVERSE, log_n, shift, values, nrows);
+}
+
 int tg_column_init_dev(tg_device* dev, const uint8_t commitment_id[32], uint64_t ncols, uint8_t* chains, void* stream) {
     Device* d = reinterpret_cast<Device*>(dev);
     if (!d || !commitment_id || (ncols && !chains)) return fail(TG_ERR_INVALID, "tg_column_init_dev: null argument");

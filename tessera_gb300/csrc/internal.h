@@ -138,6 +138,12 @@ int lde_encode_into(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P, const uin
                     const uint64_t* masks, uint64_t* codewords, cudaStream_t s, uint64_t* pw, uint64_t* pow7k,
                     bool build_tables, uint64_t* y, uint64_t* z, size_t group);
 
+// Standalone transforms over nrows rows of n = 2^lgn values in place, natural order on both
+// sides (NttPlan::{ntt, intt, coset_ntt, coset_intt}, crates/tessera-pcs/src/ntt.rs:461-516);
+// shift is used by the coset kinds only. lgn <= 22.
+enum { NTT_FORWARD = 0, NTT_INVERSE = 1, NTT_COSET_FORWARD = 2, NTT_COSET_INVERSE = 3 };
+int ntt_rows(Device* d, int kind, uint32_t lgn, uint64_t shift, uint64_t* values, size_t nrows, cudaStream_t s);
+
 // ---- hashing (hash.cu) ----------------------------------------------------------------------
 // Context keys of the domains the hot path uses, derived on the host.
 void context_key(const char* name, uint32_t key[8]);

@@ -353,6 +353,9 @@ static int fast_pass(int which, int lg, dim3 grid, const fast::Args& a, cudaStre
 
 static bool fast_shape(uint32_t lgk) { return lgk >= 13 && lgk <= 22; }
 
+// RB, the second radix of the register-resident transform of length 2^lg (fast_pass's cases).
+static int fast_rb(int lg) { return lg <= 7 ? 8 : lg <= 9 ? 16 : 32; }
+
 // Words of one CTA's tile for a column length 2^lg: 8,192 (32 elements per thread) up to 2^10,
 // 16,384 for columns of 2^11 (64 per thread).
 static uint64_t fast_tile(int lg) { return lg <= 10 ? 8192 : 16384; }
@@ -376,9 +379,7 @@ static int fast_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const
     const uint64_t pow7_k = pow(7, k);
     const uint64_t w_r = root_of_unity(lgr), w_n = root_of_unity(lgn);
     // pass M's chain step s_e^{K2·RB}, RB the second radix of the length-K1 transform
-    const int lg1 = a.lgk1;
-    const int rb = lg1 == 6 ? 8 : lg1 == 7 ? 8 : lg1 == 8 ? 16 : lg1 == 9 ? 16 : 32;
-    const uint64_t m = (uint64_t)rb << a.lgk2;
+    const uint64_t m = (uint64_t)fast_rb(a.lgk1) << a.lgk2;
     uint64_t we = 1;
     for (int e = 0; e < (1 << lgr); e++) {
         a.mk[e] = mul(k % P, sub(mul(pow7_k, we), 1));
@@ -550,6 +551,145 @@ int lde_encode_into(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const ui
         {
             Launch L(d, s, "lde_pass_c", 1, g);
             lde_pass_c<<<dim3((unsigned)(K1 >> lgw_c), g), 512, smem_c, s>>>(a);
+        }
+    }
+    TG_CUDA(cudaGetLastError());
+    return TG_OK;
+}
+
+}  // namespace tg
+
+namespace tg {
+
+// ---- standalone transforms: NttPlan::{ntt, intt, coset_ntt, coset_intt} ----------------------
+//
+// The reference's plan transforms one row in place, natural order on both sides
+// (crates/tessera-pcs/src/ntt.rs:461-516). Here many rows go at once. Rows of n ≤ 2^12 take one
+// CTA each in shared memory; rows of 2^13..2^22 run through the encoder's register-resident
+// passes with a one-coset (rate 1) setting: the forward transform is passes M2 and C (the
+// coefficients laid out as the encoder's C_0, natural order), the inverse passes A and M1 with
+// M1's per-element scale taken from a table of shift^{−i}/n instead of the coset powers.
+
+// values[i] *= scale[i mod n] over g rows of n = 2^lgn.
+__global__ void ntt_scale(uint64_t* values, uint32_t lgn, size_t total, const uint64_t* scale) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t mask = ((size_t)1 << lgn) - 1;
+    for (size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride)
+        values[i] = mul(values[i], scale[i & mask]);
+}
+
+// One row per CTA: forward — x_i·scale[i] (when scale is set), DIF with ω_n, written back in
+// natural order; inverse — DIF with ω_n^{−1}, each output c_j times scale[j] (shift^{−j}/n).
+__global__ void __launch_bounds__(512) ntt_small(uint64_t* values, int lgn, const uint64_t* pw, const uint64_t* scale,
+                                                  int inverse) {
+    extern __shared__ uint64_t sm[];
+    const int n = 1 << lgn;
+    uint64_t* buf = sm;
+    uint64_t* tw = sm + n;
+    uint64_t* row = values + ((size_t)blockIdx.x << lgn);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) buf[i] = (!inverse && scale) ? mul(row[i], scale[i]) : row[i];
+    load_twiddles(tw, pw, lgn, lgn, inverse != 0);
+    __syncthreads();
+    dif_smem<false>(buf, lgn, 0, 0, 1, tw);
+    for (int p = threadIdx.x; p < n; p += blockDim.x) {
+        const uint32_t j = brev(p, lgn);
+        row[j] = inverse ? mul(buf[p], scale[j]) : buf[p];
+    }
+}
+
+int ntt_rows(Device* d, int kind, uint32_t lgn, uint64_t shift, uint64_t* values, size_t nrows, cudaStream_t s) {
+    const bool inverse = kind == NTT_INVERSE || kind == NTT_COSET_INVERSE;
+    const bool coset = kind == NTT_COSET_FORWARD || kind == NTT_COSET_INVERSE;
+    if (kind < NTT_FORWARD || kind > NTT_COSET_INVERSE) return fail(TG_ERR_INVALID, "unknown transform kind %d", kind);
+    if (lgn > 22) return fail(TG_ERR_INVALID, "transforms of 2^%u points: the device transforms go up to 2^22", lgn);
+    if (coset && (shift == 0 || shift >= P)) return fail(TG_ERR_INVALID, "coset shift %llu is zero or not canonical",
+                                                          (unsigned long long)shift);
+    if (nrows == 0 || lgn == 0) return TG_OK;  // a transform of one point is the identity
+    const size_t n = (size_t)1 << lgn;
+    const Tables* t;
+    int rc = d->get_tables(lgn, lgn, &t);
+    if (rc) return rc;
+    // the scale table: forward shift^i (coset only); inverse shift^{−i}/n (shift 1 for the plain inverse)
+    const bool scaled = inverse || coset;
+    uint64_t* scale = nullptr;
+    if (scaled) {
+        rc = d->scratch_z.ensure(n * 8);
+        if (rc) return rc;
+        scale = (uint64_t*)d->scratch_z.ptr;
+        const uint64_t base = inverse ? (coset ? inv(shift) : 1) : shift;
+        const uint64_t first = inverse ? inv(n % P) : 1;
+        const uint32_t cl = 6;
+        const size_t threads = (n + (1u << cl) - 1) >> cl;
+        Launch L(d, s, "ntt_tables", 1, n);
+        fill_powers<<<(unsigned)((threads + 255) / 256), 256, 0, s>>>(scale, n, base, first, cl);
+    }
+    if (lgn <= 12) {
+        const size_t smem = (n + n / 2) * 8;
+        const int threads = (int)std::min<size_t>(512, std::max<size_t>(32, n / 2));
+        for (size_t r0 = 0; r0 < nrows; r0 += 65535) {
+            const size_t g = std::min<size_t>(65535, nrows - r0);
+            Launch L(d, s, "ntt_small", 1, g);
+            ntt_small<<<(unsigned)g, threads, smem, s>>>(values + (r0 << lgn), (int)lgn, t->pw, scale, inverse);
+        }
+        TG_CUDA(cudaGetLastError());
+        return TG_OK;
+    }
+    fast::Args a = {};
+    a.pw = t->pw;
+    a.pow7k = scale;
+    a.lgk = (int)lgn;
+    a.lgr = 0;
+    a.P = 0;
+    a.lgk1 = (int)(lgn + 1) / 2;
+    a.lgk2 = (int)lgn / 2;
+    if (inverse) {
+        // pass M1's running scale steps by base^m along a thread's elements, m = RB·K2
+        const uint64_t base = coset ? inv(shift) : 1;
+        a.sstep[0] = pow(base, (uint64_t)fast_rb(a.lgk1) << a.lgk2);
+    }
+    size_t group = std::max<size_t>(1, d->cfg.lde_group_bytes / (n * 8));
+    group = std::min<size_t>(group, std::min<size_t>(nrows, 65535));
+    rc = d->scratch_y.ensure(group * n * 8);
+    if (rc) return rc;
+    uint64_t* tmp = (uint64_t*)d->scratch_y.ptr;
+    const size_t tiles_k2 = n / fast_tile(a.lgk2), tiles_k1 = n / fast_tile(a.lgk1);
+    for (size_t r0 = 0; r0 < nrows; r0 += group) {
+        const unsigned g = (unsigned)std::min(group, nrows - r0);
+        uint64_t* rows = values + (r0 << lgn);
+        if (inverse) {
+            a.rows = rows;
+            a.y = tmp;
+            a.z = rows;  // the coefficients land in place
+            {
+                Launch L(d, s, "ntt_pass_a", 1, g);
+                rc = fast_pass(0, a.lgk2, dim3((unsigned)tiles_k2, g), a, s);
+            }
+            if (rc) return rc;
+            {
+                Launch L(d, s, "ntt_pass_m1", 1, g);
+                rc = fast_pass(1, a.lgk1, dim3((unsigned)tiles_k1, g), a, s);
+            }
+            if (rc) return rc;
+        } else {
+            if (coset) {
+                const size_t total = (size_t)g << lgn;
+                Launch L(d, s, "ntt_scale", 1, g);
+                ntt_scale<<<(unsigned)std::min<size_t>((total + 255) / 256, (size_t)d->sm_count * 16), 256, 0, s>>>(
+                    rows, lgn, total, scale);
+            }
+            a.z = rows;  // pass M2 works in place
+            a.out = tmp;
+            {
+                Launch L(d, s, "ntt_pass_m2", 1, g);
+                rc = fast_pass(2, a.lgk1, dim3((unsigned)tiles_k1, g), a, s);
+            }
+            if (rc) return rc;
+            {
+                Launch L(d, s, "ntt_pass_c", 1, g);
+                rc = fast_pass(3, a.lgk2, dim3((unsigned)tiles_k2, g), a, s);
+            }
+            if (rc) return rc;
+            TG_CUDA(cudaMemcpyAsync(rows, tmp, ((size_t)g << lgn) * 8, cudaMemcpyDeviceToDevice, s));
         }
     }
     TG_CUDA(cudaGetLastError());

@@ -184,7 +184,7 @@ class MerkleTree:
             raise ValueError(f"a Merkle tree needs a power-of-two number of leaves, not {n}")
         d = resolve(device)
         dev = f"cuda:{d.ordinal}"
-        src = torch.from_numpy(lv.reshape(-1)).to(dev)
+        src = torch.from_numpy(np.array(lv.reshape(-1), copy=True)).to(dev)
         nodes = torch.empty((2 * n - 1) * 32, dtype=torch.uint8, device=dev)
         N.call("tg_merkle_tree_dev", d.handle, ctypes.c_void_p(src.data_ptr()), n, ctypes.c_void_p(nodes.data_ptr()),
                torch_stream())

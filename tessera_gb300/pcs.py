@@ -1,7 +1,7 @@
 """Commitments on the GPU: the reference's tessera-pcs surface for the hot path
 (crates/tessera-pcs/src/lib.rs:352-375).
 
-`RowEncoder` (encoding.rs:126-313), `CommitmentParams` (commitment.rs:79-105),
+`NttPlan` (ntt.rs:461-516), `RowEncoder` (encoding.rs:126-313), `CommitmentParams` (commitment.rs:79-105),
 `ReferenceCommitment.commit_unmasked` (commitment.rs:343-458), the `BlockSink` that
 `StreamingCommitter::with_sink` drives (streaming.rs:24-37, the reference's AdviceSink),
 `merge_segments` (streaming.rs:382-404), and `WeightEncoding`/`MatrixSink`
@@ -16,9 +16,10 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _native as N
-from .device import Device, digests, host_u64, ptr, resolve
+from .device import Device, digests, host_u64, is_device_tensor, ptr, resolve, torch_stream
 
 COSET_SHIFT = 7
+P_FIELD = 0xFFFFFFFF00000001
 Digest = bytes
 
 
@@ -26,6 +27,52 @@ def _log2_exact(n: int, what: str) -> int:
     if n < 1 or n & (n - 1):
         raise ValueError(f"{what} {n} is not a power of two")
     return n.bit_length() - 1
+
+
+class NttPlan:
+    """Transforms of size n = 2^log_size, natural order on both sides (the reference's NttPlan,
+    crates/tessera-pcs/src/ntt.rs:461-516): ntt gives f(ω_n^j) from the coefficients, coset_ntt
+    f(shift·ω_n^j), intt and coset_intt their inverses. Each takes one row of n values or many
+    (an (m, n) array, or a flat array of whole rows): host arrays come back as new arrays, device
+    tensors are transformed in place on torch's current stream."""
+
+    def __init__(self, log_size: int, device: Device | None = None):
+        if log_size > 22:
+            raise ValueError(f"transforms of 2^{log_size} points: the device transforms go up to 2^22")
+        self.log_size = log_size
+        self.device = resolve(device)
+
+    def size(self) -> int:
+        return 1 << self.log_size
+
+    def _run(self, name: str, values, shift=None):
+        n = self.size()
+        extra = [] if shift is None else [int(shift)]
+        if shift is not None and (int(shift) % P_FIELD) == 0:
+            raise ValueError("a coset shift of zero")
+        if is_device_tensor(values):
+            if values.numel() % n:
+                raise ValueError(f"{values.numel()} values are not whole rows of {n}")
+            N.call(f"tg_{name}_dev", self.device.handle, self.log_size, *extra, ctypes.c_void_p(values.data_ptr()),
+                   values.numel() // n, torch_stream())
+            return values
+        v = np.array(host_u64(values), dtype=np.uint64, copy=True)
+        if v.size % n:
+            raise ValueError(f"{v.size} values are not whole rows of {n}")
+        N.call(f"tg_{name}", self.device.handle, self.log_size, *extra, ptr(v), v.size // n)
+        return v
+
+    def ntt(self, values):
+        return self._run("ntt", values)
+
+    def intt(self, values):
+        return self._run("intt", values)
+
+    def coset_ntt(self, values, shift: int):
+        return self._run("coset_ntt", values, shift)
+
+    def coset_intt(self, values, shift: int):
+        return self._run("coset_intt", values, shift)
 
 
 class RowEncoder:
