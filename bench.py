@@ -686,11 +686,17 @@ def run_logup(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+CC_ID = bytes([0x5A]) * 32  # the commitment id of the reference benchmark's c_c run
+
+
 def run_cc(args) -> None:
-    """The reference benchmark's c_c measurement shape: rows of k = 2^cc_log_k values with P mask
-    coefficients, generated on the device 32 rows at a time, encoded at rate 1/2 and absorbed into
-    the 2k column chains (B = 32); the cost per committed element is (generate + encode + hash −
-    generate) ÷ rows·k, as the reference reports it."""
+    """The reference benchmark's c_c measurement (crates/tessera-bench/examples/gpu_unit_costs.rs
+    `cc`): rows of k = 2^cc_log_k values with P mask coefficients, generated on the device 32 rows
+    at a time by the reference's counter generator (rows from counter 32·k·block, masks from
+    2^62 + 32·P·block), encoded at rate 1/2 and absorbed into the 2k column chains (B = 32); the
+    cost per committed element is (generate + encode + hash − generate) ÷ rows·k, medians over the
+    timed runs, as the reference reports it. --impl refgpu runs the reference's own kernels the
+    same way (oracle/refgpu.cpp)."""
     import ctypes
 
     import torch
@@ -709,50 +715,98 @@ def run_cc(args) -> None:
     masks = torch.empty(max(B * P_, 1), dtype=torch.int64, device=cuda)
     cw = torch.empty(B * n, dtype=torch.int64, device=cuda)
     chains = torch.empty(n * 32, dtype=torch.uint8, device=cuda)
-    cid = (ctypes.c_uint8 * 32)(*([0x65] * 32))
+    cid = (ctypes.c_uint8 * 32)(*CC_ID)
     torch.cuda.synchronize()
     v = ctypes.c_void_p
     stream = torch.cuda.ExternalStream(dev.stream_ptr(), device=cuda)
 
     def generate(b):
-        N.call("tg_fill_splitmix", dev.handle, v(rows.data_ptr()), B * k, SEED_CC + b, None)
+        N.call("tg_fill_counter", dev.handle, v(rows.data_ptr()), B * k, b * B * k, None)
         if P_:
-            N.call("tg_fill_splitmix", dev.handle, v(masks.data_ptr()), B * P_, SEED_CC ^ (0x6D61736B << 16) ^ b, None)
+            N.call("tg_fill_counter", dev.handle, v(masks.data_ptr()), B * P_, (1 << 62) + b * B * P_, None)
 
-    def run(encode):
+    def run(mode):
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        if encode:
+        if mode == 2:
             N.call("tg_column_init_dev", dev.handle, cid, n, v(chains.data_ptr()), None)
         for b in range(blocks):
             generate(b)
-            if encode:
+            if mode >= 1:
                 N.call("tg_encode_rows_dev", dev.handle, lgk, lgr, P_, v(rows.data_ptr()), B,
                        v(masks.data_ptr()) if P_ else None, v(cw.data_ptr()), None)
+            if mode == 2:
                 N.call("tg_column_absorb_dev", dev.handle, v(chains.data_ptr()), n, v(cw.data_ptr()), B, B, None)
         e1.record(stream)
         e1.synchronize()
         return e0.elapsed_time(e1) / 1e3
 
-    for _ in range(args.warmup):
-        run(True)
-    full = [run(True) for _ in range(args.steps)]
-    gen = [run(False) for _ in range(args.steps)]
+    def block0_chains():
+        N.call("tg_column_init_dev", dev.handle, cid, n, v(chains.data_ptr()), None)
+        generate(0)
+        N.call("tg_encode_rows_dev", dev.handle, lgk, lgr, P_, v(rows.data_ptr()), B,
+               v(masks.data_ptr()) if P_ else None, v(cw.data_ptr()), None)
+        N.call("tg_column_absorb_dev", dev.handle, v(chains.data_ptr()), n, v(cw.data_ptr()), B, B, None)
+        dev.sync()
+        return chains.cpu().numpy().tobytes()
+
     elems = blocks * B * k
-    ps_full, ps_gen = statistics.median(full) / elems * 1e12, statistics.median(gen) / elems * 1e12
-    dev.close()
+    impl = args.impl
+    if impl == "refgpu":
+        # the reference's kernels in their own module and stream; the library's chains of block 0
+        # are computed first, on the same counter-generated inputs, to compare with theirs
+        ours = block0_chains()
+        del rows, masks, cw, chains
+        torch.cuda.synchronize()
+        dev.close()
+        fatbin = ROOT / "oracle" / "_ref" / "commit.fatbin"
+        lib_path = ROOT / "oracle" / "_build" / "librefgpu.so"
+        if not fatbin.exists() or not lib_path.exists():
+            if rank == 0:
+                print(json.dumps({"impl": "refgpu", "unavailable": "the reference kernels were not compiled here "
+                                  "(oracle/_ref/commit.fatbin needs the reference checkout; make -C oracle ref refgpu)"}))
+            return
+        from oracle import oracle as O
+
+        lib = ctypes.CDLL(str(lib_path))
+        lib.refgpu_last_error.restype = ctypes.c_char_p
+        out = (ctypes.c_double * 3)()
+        theirs = ctypes.create_string_buffer(n * 32)
+        rc = lib.refgpu_cc(str(fatbin).encode(), ctypes.c_uint32(lgk), ctypes.c_uint32(args.cc_rows),
+                           ctypes.c_uint32(P_), ctypes.c_int(args.warmup), ctypes.c_int(args.steps),
+                           ctypes.c_int(O.threads_available()), out, theirs)
+        if rc != 0:
+            raise RuntimeError("reference kernels: " + lib.refgpu_last_error().decode())
+        full, gen, enc = out[0], out[1], out[2]
+        same = theirs.raw == ours
+    else:
+        for _ in range(args.warmup):
+            run(2)
+        full = statistics.median([run(2) for _ in range(args.steps)])
+        gen = statistics.median([run(0) for _ in range(args.steps)])
+        enc = statistics.median([run(1) for _ in range(args.steps)])
+        same = None
+        del rows, masks, cw, chains
+        dev.close()
     if rank != 0:
         return
+    ps = lambda t: t / elems * 1e12  # noqa: E731
     line = {
         "metric": "c_c: ps per committed element (encode at rate 1/2 with masks + BLAKE3 column chains)",
-        "value": ps_full - ps_gen, "unit": "ps/element", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "value": ps(full) - ps(gen), "unit": "ps/element", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)",
-        "data": "synthetic (SplitMix64 rows and masks generated on the device, 32 rows at a time)",
+        "impl": impl,
+        "data": "synthetic (the reference benchmark's counter generator on the device, 32 rows and their masks at a time)",
         "config": {"workload": f"{blocks * B} rows of k = 2^{lgk}, P = {P_} masks, rate 1/2, B = {B}",
                    "timing": "CUDA events over all blocks, median over steps"},
-        "generate_encode_hash_ps": ps_full, "generate_ps": ps_gen,
-        "reference_h100_ps": 134.8,
+        "generate_encode_hash_ps": ps(full), "generate_ps": ps(gen), "encode_ps": ps(enc) - ps(gen),
+        "hash_ps": ps(full) - ps(enc), "reference_h100_ps": 134.8,
     }
+    if impl == "refgpu":
+        line["kernels"] = ("the reference's crates/tessera-gpu/kernels/commit.cu (fill_counter, ntt_pass, encode_low, "
+                           "column_init, column_step) compiled for sm_103 with its own flags, launched with the geometry "
+                           "of crates/tessera-gpu/src/commit.rs; block 0 checked against the CPU oracle")
+        line["block0_chains_equal_library"] = same
     print(json.dumps(line), flush=True)
 
 
@@ -812,9 +866,6 @@ def run_forest(args) -> None:
     print(json.dumps(line), flush=True)
 
 
-SEED_CC = 0x00650007
-
-
 SEED_SERVE = 0x00650005
 
 
@@ -823,7 +874,9 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--impl", choices=["gb300", "reference", "refgpu"], default="gb300",
+                    help="reference: the CPU port of the reference's algorithms; refgpu: the reference's own CUDA "
+                         "kernels on this GPU (--workload cc)")
     ap.add_argument("--workload", choices=["large", "batched", "serve", "logup", "cc", "forest"], default="large",
                     help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain; "
                          "serve: the proof server against one-at-a-time proofs")
@@ -851,7 +904,9 @@ def main():
         UNITS = COMMITTED + SUMCHECKED
         CONFIG["polys"] = args.polys
         CONFIG["workload"] = CONFIG["workload"].replace("commit 256", f"commit {args.polys}")
-    if args.impl == "reference":
+    if args.impl == "refgpu" and args.workload != "cc":
+        print(json.dumps({"impl": "refgpu", "unavailable": "the reference's own kernels are driven for --workload cc only"}))
+    elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":
         run_batched(args)

@@ -27,6 +27,12 @@ def build() -> Path:
     return LIB_PATH
 
 
+def build_baseline() -> None:
+    """The GPU baseline: the reference's own kernels compiled from its checkout (when present)
+    into oracle/_ref/, and the harness that drives them, oracle/_build/librefgpu.so."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "ref", "refgpu"], check=True)
+
+
 def lib():
     global _lib
     if _lib is None:
