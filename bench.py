@@ -228,6 +228,30 @@ def measured_peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
+def bind_gpu_local_cpus(ordinal: int) -> dict | None:
+    """Restricts this process to the CPUs local to the GPU (its PCI device's local_cpulist), so
+    that host buffers allocated and touched next land on the GPU's NUMA node; returns what was
+    found, or None where the topology is not visible."""
+    try:
+        import torch
+
+        p = torch.cuda.get_device_properties(ordinal)
+        dev = Path(f"/sys/bus/pci/devices/{p.pci_domain_id:04x}:{p.pci_bus_id:02x}:{p.pci_device_id:02x}.0")
+        node = int((dev / "numa_node").read_text().strip())
+        cpus = set()
+        for part in (dev / "local_cpulist").read_text().strip().split(","):
+            if part:
+                a, _, b = part.partition("-")
+                cpus.update(range(int(a), int(b or a) + 1))
+        cpus &= os.sched_getaffinity(0)
+        if not cpus:
+            return None
+        os.sched_setaffinity(0, cpus)
+        return {"numa_node": node, "local_cpus": len(cpus)}
+    except Exception:  # noqa: BLE001 - no sysfs, no affinity API, or a device without topology
+        return None
+
+
 def traffic_table() -> dict:
     p = ROOT / "profiles" / "traffic.json"
     return json.loads(p.read_text()) if p.exists() else {}
@@ -253,9 +277,14 @@ def run_gpu(args) -> None:
     cuda = f"cuda:{local}"
     stream = torch.cuda.ExternalStream(dev.stream_ptr(), device=cuda)
 
-    # inputs: host (pinned, for e2e) and resident device copies
+    # inputs: host (pinned, for e2e) and resident device copies; the pinned pages are first
+    # touched from the GPU's own NUMA node, where its host link is shortest
+    saved = os.sched_getaffinity(0) if hasattr(os, "sched_getaffinity") else None
+    host_numa = bind_gpu_local_cpus(local)
     rows_h = torch.from_numpy(splitmix_words(SEED, COMMITTED).view(np.int64)).pin_memory()
     tabs_h = [torch.from_numpy(splitmix_words(SEED + 1 + i, 1 << SC_VARS).view(np.int64)).pin_memory() for i in range(3)]
+    if saved is not None and host_numa:
+        os.sched_setaffinity(0, saved)
     rows_d = rows_h.to(cuda)
     tabs_d = [t.to(cuda) for t in tabs_h]
     n = 1 << (LOG_K + LOG_R)
@@ -410,6 +439,7 @@ def run_gpu(args) -> None:
         "latency_ms": {"p50": statistics.median(step_ms), "p99": max(step_ms) if len(step_ms) < 100 else
                        sorted(step_ms)[int(0.99 * len(step_ms))]},
         "gpu_launches": launches,
+        "host_buffers": host_numa or "NUMA placement not visible; pinned with default first-touch",
         "roofline": roofline,
         "int_rate": int_rate,
         "kernels": kernels,
@@ -545,7 +575,7 @@ def run_serve(args) -> None:
     torch.cuda.set_device(local)
     dev = Device(local)
     rs = random.Random(SEED_SERVE)
-    reqs, arrivals, units = [], [], 0
+    reqs, arrivals, units, sizes = [], [], 0, []
     t = 0.0
     keep = []
     for i in range(args.requests):
@@ -559,8 +589,10 @@ def run_serve(args) -> None:
                              i.to_bytes(16, "little"))
         cid = bytes(rs.randrange(256) for _ in range(32))
         reqs.append(ProofRequest(CommitmentParams(log_k, log_r, 0, ROW_BLOCK, cid), rows.numpy().view(np.uint64),
-                                 degree, [x.numpy().view(np.uint64) for x in tabs], Transcript(ctx), "stage/0"))
+                                 degree, [x.numpy().view(np.uint64) for x in tabs], Transcript(ctx), "stage/0",
+                                 args.queries))
         units += (polys << log_k) + (degree << vars_)
+        sizes.append((polys << log_k) + (degree << vars_))
         t += rs.expovariate(args.rate)
         arrivals.append(t)
 
@@ -603,10 +635,17 @@ def run_serve(args) -> None:
     for mode, offered in (("poisson", arrivals), ("saturated", [0.0] * len(reqs))):
         pw, pl = plain(offered)
         sw, sl, st = served(offered)
-        q = lambda xs, f: sorted(xs)[min(len(xs) - 1, int(f * len(xs)))] * 1e3
+        q = lambda xs, f: sorted(xs)[min(len(xs) - 1, int(f * len(xs)))] * 1e3  # noqa: E731
+
+        def tail(xs):  # the slowest requests: (latency ms, request index, committed + sumchecked elements)
+            worst = sorted(range(len(xs)), key=lambda i: -xs[i])[:4]
+            return [(round(xs[i] * 1e3, 3), i, sizes[i]) for i in worst]
+
         out[mode] = {
-            "plain": {"proofs_per_s": len(reqs) / pw, "elems_per_s": units / pw, "latency_ms": {"p50": q(pl, 0.5), "p99": q(pl, 0.99)}},
-            "served": {"proofs_per_s": len(reqs) / sw, "elems_per_s": units / sw, "latency_ms": {"p50": q(sl, 0.5), "p99": q(sl, 0.99)},
+            "plain": {"proofs_per_s": len(reqs) / pw, "elems_per_s": units / pw,
+                      "latency_ms": {"p50": q(pl, 0.5), "p99": q(pl, 0.99)}, "slowest": tail(pl)},
+            "served": {"proofs_per_s": len(reqs) / sw, "elems_per_s": units / sw,
+                       "latency_ms": {"p50": q(sl, 0.5), "p99": q(sl, 0.99)}, "slowest": tail(sl),
                        "peak_inflight": st["peak_inflight"], "peak_gib": st["peak_bytes"] / 2**30},
         }
     del keep
@@ -619,8 +658,10 @@ def run_serve(args) -> None:
         "value": sat["served"]["proofs_per_s"], "unit": "proofs/s", "n_gpus": world, "steps": 1, "warmup": 1,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic",
         "config": {"workload": f"serve: {len(reqs)} proof requests (commit 8/32/128 x 2^10..2^16 at rate 1/2 or 1/4, "
-                               f"B = 32, then a degree-2/3 sumcheck over 2^10..2^18 bound to the root), Poisson "
+                               f"B = 32, then a degree-2/3 sumcheck over 2^10..2^18 bound to the root, then "
+                               f"{args.queries} column queries answered from the resident commitment), Poisson "
                                f"{args.rate} req/s, then all at once", "seed": SEED_SERVE, "slots": args.slots,
+                   "queries": args.queries,
                    "hbm_budget_gib": args.serve_budget_gib, "elems": units,
                    "timing": "host wall clock; latency = arrival to result on the host"},
         **out,
@@ -890,6 +931,8 @@ def main():
     ap.add_argument("--rows-log", type=int, default=24, help="logup: log2 of the table rows")
     ap.add_argument("--rate", type=float, default=20.0, help="serve: mean Poisson arrivals per second")
     ap.add_argument("--slots", type=int, default=8, help="serve: requests in flight at most")
+    ap.add_argument("--queries", type=int, default=32,
+                    help="serve: column queries each request answers from its resident commitment after the proof")
     ap.add_argument("--serve-budget-gib", type=int, default=64, help="serve: HBM budget for admitted requests")
     ap.add_argument("--cpu-polys", type=int, default=32, help="rows encoded per run in the CPU baseline's sample")
     ap.add_argument("--ref-polys", type=int, default=32, help="rows encoded per run in the reference arm's sample")

@@ -406,8 +406,19 @@ int tg_logup_leaves(tg_device *dev, uint64_t key_seed, uint64_t value_seed, int 
  * admitted first come first served while a stream slot is free and their device footprint fits
  * the HBM budget (a request larger than the budget runs alone); admitted requests run on their own
  * streams with stream-ordered device memory, so their work overlaps on the GPU, and a scheduler
- * thread advances each one. Results are byte-identical to proving the request alone. Host rows and
- * tables must stay valid until the request completes (pinned memory lets their copies overlap). */
+ * thread advances each one, woken by the streams' completions; when requests overlap, the oldest
+ * in flight runs on high-priority streams. Results are byte-identical to proving the request
+ * alone. Host rows and tables must stay valid until the request completes (pinned memory lets
+ * their copies overlap).
+ * With queries > 0 the proof ends with an opening round on the still-resident commitment: after
+ * the sumcheck, `queries` column indices are drawn from the transcript under "<prefix>/queries"
+ * (Transcript::challenge_indices over log2 n bits, crates/tessera-hash/src/transcript.rs), and the
+ * answer is read from the codewords and Merkle nodes the commitment left on the device: each
+ * distinct queried column's symbols (one per row, in row order, the columns in increasing index
+ * order) and the canonical multiproof of those indices (the siblings the verifier cannot compute,
+ * level by level from the leaves up, left to right within a level; the verifier's
+ * verify_multiproof, verifier/crates/tv-hash/src/merkle.rs:137). A request's answer must fit
+ * 1 MiB of staging: queries · (8·npolys + 32·log2 n) bytes, about. */
 typedef struct {
     uint32_t log_k, log_inv_rate, row_block;
     uint8_t commitment_id[32];
@@ -417,6 +428,7 @@ typedef struct {
     const uint64_t *const *tables; /* host */
     tg_transcript transcript;      /* the proof's transcript at its start */
     const char *prefix;
+    uint32_t queries;              /* column queries answered after the proof (0: none) */
 } tg_proof_request;
 typedef struct {
     int status;                    /* TG_OK once done */
@@ -427,6 +439,11 @@ typedef struct {
     uint64_t *final_evals;         /* ntables Fp2 */
     tg_transcript transcript;      /* at the end of the proof */
     double queued_ms, latency_ms;  /* submission to admission, submission to completion */
+    /* the opening round (caller buffers, used when queries > 0): */
+    uint64_t *query_indices;       /* queries indices, in draw order */
+    uint64_t *columns;             /* n_distinct x npolys symbols (room for queries x npolys) */
+    uint8_t *siblings;             /* n_siblings digests (room for queries x log2 n) */
+    uint32_t n_distinct, n_siblings;
 } tg_proof_result;
 typedef struct {
     uint64_t submitted, completed, peak_inflight;

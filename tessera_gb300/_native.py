@@ -56,13 +56,16 @@ class ProofRequestC(ctypes.Structure):
     _fields_ = [("log_k", ctypes.c_uint32), ("log_inv_rate", ctypes.c_uint32), ("row_block", ctypes.c_uint32),
                 ("commitment_id", ctypes.c_uint8 * 32), ("rows", ctypes.c_void_p), ("npolys", ctypes.c_size_t),
                 ("degree", ctypes.c_int), ("ntables", ctypes.c_int), ("vars", ctypes.c_int),
-                ("tables", ctypes.POINTER(ctypes.c_void_p)), ("transcript", TranscriptState), ("prefix", ctypes.c_char_p)]
+                ("tables", ctypes.POINTER(ctypes.c_void_p)), ("transcript", TranscriptState), ("prefix", ctypes.c_char_p),
+                ("queries", ctypes.c_uint32)]
 
 
 class ProofResultC(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int), ("root", ctypes.c_uint8 * 32), ("gamma", ctypes.c_uint64 * 2),
                 ("rounds", ctypes.c_void_p), ("challenges", ctypes.c_void_p), ("final_evals", ctypes.c_void_p),
-                ("transcript", TranscriptState), ("queued_ms", ctypes.c_double), ("latency_ms", ctypes.c_double)]
+                ("transcript", TranscriptState), ("queued_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
+                ("query_indices", ctypes.c_void_p), ("columns", ctypes.c_void_p), ("siblings", ctypes.c_void_p),
+                ("n_distinct", ctypes.c_uint32), ("n_siblings", ctypes.c_uint32)]
 
 
 class ServerStatsC(ctypes.Structure):

@@ -155,6 +155,14 @@ int column_absorb(Device* d, uint8_t* chains, uint64_t ncols, const uint64_t* ro
 int merkle_tree(Device* d, const uint8_t* leaves, size_t n, uint8_t* nodes, cudaStream_t s);
 int column_merge(Device* d, const uint8_t* segs, size_t nseg, uint64_t n, uint8_t* leaves, cudaStream_t s);
 
+// ---- openings (opening.cu) -------------------------------------------------------------------
+// The answer to column queries on resident codewords (rows x n) and Merkle nodes (2n − 1
+// digests, leaves first): cols[q·rows + r] = cw[r·n + idx[q]] for the m indices, and sib[t] the
+// digest of node node[t], for ns nodes. All pointers on the device; enqueued on s.
+int gather_answer(Device* d, const uint64_t* cw, uint64_t n, uint32_t rows, const uint64_t* idx, uint32_t m,
+                  uint64_t* cols, const uint8_t* nodes, const uint64_t* node, uint32_t ns, uint8_t* sib,
+                  cudaStream_t s);
+
 // A bump allocator over one device buffer, 256-byte aligned pieces.
 struct Arena {
     size_t used = 0;

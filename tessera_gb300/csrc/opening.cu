@@ -67,6 +67,37 @@ __global__ void combine_rows_kernel(const uint64_t* values, uint32_t rows, uint6
     }
 }
 
+// An answer to column queries on resident data: cols[q·rows + r] = cw[r·n + idx[q]] (each queried
+// column's symbols of every row, in row order) and sib[t] = nodes[node[t]] (32-byte digests).
+__global__ void gather_answer_kernel(const uint64_t* cw, uint64_t n, uint32_t rows, const uint64_t* idx, uint32_t m,
+                                     uint64_t* cols, const uint64_t* nodes, const uint64_t* node, uint32_t ns,
+                                     uint64_t* sib) {
+    const uint64_t ncols = (uint64_t)rows * m, total = ncols + 4ull * ns;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride) {
+        if (i < ncols) {
+            const uint64_t q = i / rows, r = i % rows;
+            cols[i] = cw[r * n + idx[q]];
+        } else {
+            const uint64_t j = i - ncols;
+            sib[j] = nodes[4 * node[j >> 2] + (j & 3)];
+        }
+    }
+}
+
+int gather_answer(Device* d, const uint64_t* cw, uint64_t n, uint32_t rows, const uint64_t* idx, uint32_t m,
+                  uint64_t* cols, const uint8_t* nodes, const uint64_t* node, uint32_t ns, uint8_t* sib,
+                  cudaStream_t s) {
+    const uint64_t total = (uint64_t)rows * m + 4ull * ns;
+    if (total == 0) return TG_OK;
+    const uint64_t blocks = std::min<uint64_t>((total + 255) / 256, (uint64_t)d->sm_count * 8);
+    Launch L(d, s, "gather_answer", 1, total);
+    gather_answer_kernel<<<(unsigned)blocks, 256, 0, s>>>(cw, n, rows, idx, m, cols, (const uint64_t*)nodes, node, ns,
+                                                          (uint64_t*)sib);
+    TG_CUDA(cudaGetLastError());
+    return TG_OK;
+}
+
 static void zero(DevBuf& b, cudaStream_t s) {
     if (b.ptr) cudaMemsetAsync(b.ptr, 0, b.bytes, s);
 }

@@ -8,8 +8,16 @@
 //   1. commit: rows host → device, encode, column chains, Merkle tree, root → pinned host memory
 //   2. the host absorbs the root into the request's transcript (the sumcheck's challenges depend
 //      on the commitment), draws γ, and enqueues the sumcheck with its transcript on the device
-//   3. the host finishes the proof (transcript, round messages, evaluations), frees the request's
-//      device memory on its stream and hands the result to the waiting caller
+//   3. with queries: the host finishes the sumcheck's transcript, draws the query indices from it,
+//      and the device gathers the answer (the queried columns of the resident codewords and the
+//      canonical multiproof from the resident Merkle nodes) into pinned host memory
+//   4. the host finishes the proof (transcript, round messages, evaluations, answer), frees the
+//      request's device memory and hands the result to the waiting caller
+//
+// A stage's work ends with a host function on its stream that wakes the scheduler, so no thread
+// polls while the GPU works. Each slot has a high- and a low-priority stream: the oldest request
+// in flight enqueues its next stage on the high one, the others on the low one, so overlapping
+// requests are served first come first served and the newer fill the gaps.
 //
 // A request's proof is a unit of the reference's prover shape: a resident unmasked commitment
 // (crates/tessera-pcs/src/commitment.rs:343-458) whose root is absorbed under "<prefix>/root",
@@ -44,9 +52,12 @@ struct ServeReq {
     tg_proof_result* out = nullptr;
     // sizes and the request's device block: rows | codewords | nodes | encoder y | encoder z | sumcheck arena
     uint64_t k = 0, n = 0;
-    size_t group = 0, off_cw = 0, off_nodes = 0, off_y = 0, off_z = 0, off_sc = 0, footprint = 0;
+    size_t group = 0, off_cw = 0, off_nodes = 0, off_y = 0, off_z = 0, off_sc = 0, off_q = 0, footprint = 0;
     uint8_t* dmem = nullptr;
+    cudaStream_t s = nullptr;  // the stream of the request's current stage
     int slot = -1, stage = 0, status = TG_OK;
+    // the opening round: distinct indices and sibling nodes, uploaded from the slot's staging
+    std::vector<uint64_t> distinct, sib_nodes;
     Clock::time_point t_submit, t_admit;
     // the sumcheck
     tg_transcript transcript;
@@ -73,17 +84,55 @@ struct tg_server {
     std::deque<tg::ServeReq*> queue;
     std::vector<tg::ServeReq*> active;
     std::map<uint64_t, tg::ServeReq*> finished;  // done, not yet collected
-    std::vector<cudaStream_t> streams;
+    std::vector<cudaStream_t> streams, streams_hi;  // per slot: low and high priority
     std::vector<cudaEvent_t> events;
     std::vector<int> slot_busy;
     uint8_t* pinned = nullptr;  // kSlotPinned bytes per slot
     size_t in_use = 0;
+    uint64_t completions = 0;  // stage ends signalled by the streams' host functions
     tg_server_stats stats;
 };
 
 namespace tg {
 
-constexpr size_t kSlotPinned = 64 << 10;
+constexpr size_t kSlotPinned = 1 << 20;
+constexpr size_t kSumcheckPinned = 64 << 10;  // the sumcheck's outputs, after the 32-byte root
+
+// A request's answer and its uploaded index lists: at most queries · (8·npolys + 40·log2 n + 8)
+// bytes (distinct indices ≤ queries, multiproof siblings ≤ queries·log2 n).
+static size_t answer_bytes(uint32_t queries, size_t npolys, uint32_t log_n) {
+    return (size_t)queries * (8 * npolys + 40ull * log_n + 8);
+}
+
+// Runs on a CUDA host thread after a stage's work: wakes the scheduler (no CUDA calls here).
+static void CUDART_CB stage_done(void* arg) {
+    tg_server* sv = static_cast<tg_server*>(arg);
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        sv->completions++;
+    }
+    sv->wake.notify_all();
+}
+
+// Records the slot's event and the wake-up after the work just enqueued on the stage's stream.
+static int end_stage(tg_server* sv, ServeReq* r) {
+    TG_CUDA(cudaEventRecord(sv->events[r->slot], r->s));
+    TG_CUDA(cudaLaunchHostFunc(r->s, stage_done, sv));
+    return TG_OK;
+}
+
+// The stream for a request's next stage: the slot's high-priority one for the oldest request in
+// flight (the lowest ticket among the active), else its low one. The previous stage has ended.
+static cudaStream_t stage_stream(tg_server* sv, ServeReq* r) {
+    bool oldest = true;
+    {
+        std::lock_guard<std::mutex> lock(sv->mu);
+        for (ServeReq* o : sv->active)
+            if (o->ticket < r->ticket) oldest = false;
+    }
+    r->s = oldest ? sv->streams_hi[r->slot] : sv->streams[r->slot];
+    return r->s;
+}
 constexpr size_t kServeGroupBytes = 256ull << 20;  // encoder scratch per request
 
 // The request's sumcheck job over its (host) tables, on its own transcript copy.
@@ -108,10 +157,10 @@ static void build_job(ServeReq* r) {
     r->job.final_evals = r->out->final_evals;
 }
 
-// Stage 1: rows in, encode, chains, tree, root out; on the slot's stream.
+// Stage 1: rows in, encode, chains, tree, root out.
 static int start_commit(tg_server* sv, ServeReq* r) {
     Device* d = sv->d;
-    cudaStream_t s = sv->streams[r->slot];
+    cudaStream_t s = stage_stream(sv, r);
     TG_CUDA(cudaMallocAsync((void**)&r->dmem, r->footprint, s));
     uint64_t* rows = (uint64_t*)r->dmem;
     uint64_t* cw = (uint64_t*)(r->dmem + r->off_cw);
@@ -127,14 +176,13 @@ static int start_commit(tg_server* sv, ServeReq* r) {
     if (!rc) rc = merkle_tree(d, nodes, r->n, nodes, s);
     if (rc) return rc;
     TG_CUDA(cudaMemcpyAsync(sv->pinned + kSlotPinned * r->slot, nodes + 32 * (2 * r->n - 2), 32, cudaMemcpyDeviceToHost, s));
-    TG_CUDA(cudaEventRecord(sv->events[r->slot], s));
-    return TG_OK;
+    return end_stage(sv, r);
 }
 
 // Stage 2: the root into the transcript, γ, and the sumcheck on the device.
 static int start_sumcheck(tg_server* sv, ServeReq* r) {
     Device* d = sv->d;
-    cudaStream_t s = sv->streams[r->slot];
+    cudaStream_t s = stage_stream(sv, r);
     uint8_t* pin = sv->pinned + kSlotPinned * r->slot;
     memcpy(r->out->root, pin, 32);
     int rc = tg_transcript_absorb(&r->transcript, (r->prefix + "/root").c_str(), r->out->root, 32);
@@ -142,20 +190,82 @@ static int start_sumcheck(tg_server* sv, ServeReq* r) {
     build_job(r);
     r->run = sc_prepare(d, &r->job, 1, 0, &rc);
     if (!r->run) return rc;
-    if (sc_host_bytes(r->run) + 32 > kSlotPinned) return fail(TG_ERR_INVALID, "sumcheck outputs exceed the slot's staging");
+    if (sc_host_bytes(r->run) + 32 > kSumcheckPinned) return fail(TG_ERR_INVALID, "sumcheck outputs exceed the slot's staging");
     {
         std::lock_guard<std::mutex> lock(d->mu);
         rc = sc_enqueue(d, r->run, s, r->dmem + r->off_sc, pin + 32);
     }
     if (rc) return rc;
-    TG_CUDA(cudaEventRecord(sv->events[r->slot], s));
-    return TG_OK;
+    return end_stage(sv, r);
+}
+
+// Stage 3: the sumcheck's transcript finished on the host, the query indices drawn from it, and
+// the answer gathered from the resident codewords and Merkle nodes into the slot's staging.
+static int start_opening(tg_server* sv, ServeReq* r) {
+    Device* d = sv->d;
+    cudaStream_t s = stage_stream(sv, r);
+    int rc = sc_finish(r->run);
+    sc_free(r->run);
+    r->run = nullptr;
+    if (rc) return rc;
+    const uint32_t lgn = r->req.log_k + r->req.log_inv_rate, tau = r->req.queries;
+    rc = tg_transcript_challenge_indices(&r->transcript, (r->prefix + "/queries").c_str(), lgn, tau,
+                                         r->out->query_indices);
+    if (rc) return rc;
+    r->distinct.assign(r->out->query_indices, r->out->query_indices + tau);
+    std::sort(r->distinct.begin(), r->distinct.end());
+    r->distinct.erase(std::unique(r->distinct.begin(), r->distinct.end()), r->distinct.end());
+    // the canonical multiproof: per level from the leaves up, the sibling of every opened node
+    // whose sibling is not opened, left to right; a level's nodes follow the level below's
+    r->sib_nodes.clear();
+    std::vector<uint64_t> cur = r->distinct, up;
+    uint64_t base = 0, width = r->n;
+    while (width > 1) {
+        for (size_t i = 0; i < cur.size(); i++) {
+            const uint64_t x = cur[i];
+            const bool paired = (x & 1) ? (i > 0 && cur[i - 1] == (x ^ 1)) : (i + 1 < cur.size() && cur[i + 1] == (x ^ 1));
+            if (!paired) r->sib_nodes.push_back(base + (x ^ 1));
+        }
+        up.clear();
+        for (uint64_t x : cur)
+            if (up.empty() || up.back() != (x >> 1)) up.push_back(x >> 1);
+        cur.swap(up);
+        base += width;
+        width >>= 1;
+    }
+    const uint32_t m = (uint32_t)r->distinct.size(), ns = (uint32_t)r->sib_nodes.size();
+    const size_t npolys = r->req.npolys;
+    uint8_t* stage = sv->pinned + kSlotPinned * r->slot + kSumcheckPinned;
+    uint64_t* lists = (uint64_t*)(r->dmem + r->off_q);
+    memcpy(stage, r->distinct.data(), 8 * (size_t)m);
+    memcpy(stage + 8 * (size_t)m, r->sib_nodes.data(), 8 * (size_t)ns);
+    TG_CUDA(cudaMemcpyAsync(lists, stage, 8 * ((size_t)m + ns), cudaMemcpyHostToDevice, s));
+    uint64_t* cols = lists + m + ns;
+    uint8_t* sib = (uint8_t*)(cols + (size_t)m * npolys);
+    {
+        std::lock_guard<std::mutex> lock(d->mu);
+        rc = gather_answer(d, (const uint64_t*)(r->dmem + r->off_cw), r->n, (uint32_t)npolys, lists, m, cols,
+                           r->dmem + r->off_nodes, lists + m, ns, sib, s);
+    }
+    if (rc) return rc;
+    // the answer lands after the index lists in the staging, which the copy above has read by then
+    uint8_t* back = stage + 8 * ((size_t)m + ns);
+    TG_CUDA(cudaMemcpyAsync(back, cols, 8 * (size_t)m * npolys + 32 * (size_t)ns, cudaMemcpyDeviceToHost, s));
+    return end_stage(sv, r);
 }
 
 // Stage 3: the proof's outputs, memory back to the pool, the slot freed.
 static void finish(tg_server* sv, ServeReq* r, int status) {
-    cudaStream_t s = sv->streams[r->slot];
+    cudaStream_t s = r->s ? r->s : sv->streams[r->slot];
     if (!status && r->run) status = sc_finish(r->run);
+    if (!status && r->req.queries) {
+        const size_t m = r->distinct.size(), ns = r->sib_nodes.size(), npolys = r->req.npolys;
+        const uint8_t* back = sv->pinned + kSlotPinned * r->slot + kSumcheckPinned + 8 * (m + ns);
+        memcpy(r->out->columns, back, 8 * m * npolys);
+        memcpy(r->out->siblings, back + 8 * m * npolys, 32 * ns);
+        r->out->n_distinct = (uint32_t)m;
+        r->out->n_siblings = (uint32_t)ns;
+    }
     if (r->run) {
         sc_free(r->run);
         r->run = nullptr;
@@ -188,8 +298,10 @@ static void scheduler(tg_server* sv) {
     for (;;) {
         bool progressed = false;
         std::vector<ServeReq*> admitted;
+        uint64_t seen;
         {
             std::unique_lock<std::mutex> lock(sv->mu);
+            seen = sv->completions;
             if (sv->stop && sv->queue.empty() && sv->active.empty()) return;
             // admission, first come first served: a free slot and room in the budget (a request
             // larger than the whole budget runs alone)
@@ -238,13 +350,21 @@ static void scheduler(tg_server* sv) {
                 r->stage = 2;
                 const int rc = start_sumcheck(sv, r);
                 if (rc) finish(sv, r, rc);
+            } else if (r->stage == 2 && r->req.queries) {
+                r->stage = 3;
+                const int rc = start_opening(sv, r);
+                if (rc) finish(sv, r, rc);
             } else {
                 finish(sv, r, TG_OK);
             }
         }
         if (!progressed) {
+            // sleep until a stream signals the end of a stage or a request arrives (the bound is a
+            // safety net only: every stage ends with a wake-up)
             std::unique_lock<std::mutex> lock(sv->mu);
-            sv->wake.wait_for(lock, std::chrono::microseconds(50));
+            sv->wake.wait_for(lock, std::chrono::milliseconds(20), [&] {
+                return sv->completions != seen || !sv->queue.empty() || sv->stop;
+            });
         }
     }
 }
@@ -261,6 +381,10 @@ static int check_request(const tg_proof_request& q) {
     for (int k = 0; k < q.ntables; k++)
         if (!q.tables[k]) return fail(TG_ERR_INVALID, "table %d: null values", k);
     if (!q.prefix || strlen(q.prefix) > 150) return fail(TG_ERR_INVALID, "a prefix of at most 150 characters");
+    if (q.queries && q.npolys == 0) return fail(TG_ERR_INVALID, "queries on a commitment of no rows");
+    if (q.queries && answer_bytes(q.queries, q.npolys, q.log_k + q.log_inv_rate) > kSlotPinned - kSumcheckPinned)
+        return fail(TG_ERR_INVALID, "an answer to %u queries over %zu rows exceeds the 1 MiB staging", q.queries,
+                    q.npolys);
     return TG_OK;
 }
 
@@ -286,16 +410,21 @@ extern "C" int tg_server_open(tg_device* dev, size_t hbm_budget_bytes, int max_i
     sv->max_inflight = max_inflight;
     memset(&sv->stats, 0, sizeof sv->stats);
     sv->streams.assign(max_inflight, nullptr);
+    sv->streams_hi.assign(max_inflight, nullptr);
     sv->events.assign(max_inflight, nullptr);
     sv->slot_busy.assign(max_inflight, 0);
-    cudaError_t e = cudaHostAlloc((void**)&sv->pinned, kSlotPinned * max_inflight, cudaHostAllocDefault);
+    int least = 0, greatest = 0;
+    cudaError_t e = cudaDeviceGetStreamPriorityRange(&least, &greatest);
+    if (e == cudaSuccess) e = cudaHostAlloc((void**)&sv->pinned, kSlotPinned * max_inflight, cudaHostAllocDefault);
     for (int i = 0; e == cudaSuccess && i < max_inflight; i++) {
-        e = cudaStreamCreateWithFlags(&sv->streams[i], cudaStreamNonBlocking);
+        e = cudaStreamCreateWithPriority(&sv->streams[i], cudaStreamNonBlocking, least);
+        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&sv->streams_hi[i], cudaStreamNonBlocking, greatest);
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sv->events[i], cudaEventDisableTiming);
     }
     if (e != cudaSuccess) {
         for (int i = 0; i < max_inflight; i++) {
             if (sv->streams[i]) cudaStreamDestroy(sv->streams[i]);
+            if (sv->streams_hi[i]) cudaStreamDestroy(sv->streams_hi[i]);
             if (sv->events[i]) cudaEventDestroy(sv->events[i]);
         }
         if (sv->pinned) cudaFreeHost(sv->pinned);
@@ -311,6 +440,8 @@ extern "C" int tg_server_submit(tg_server* sv, const tg_proof_request* req, tg_p
     if (!sv || !req || !out || !ticket) return fail(TG_ERR_INVALID, "tg_server_submit: null argument");
     int rc = check_request(*req);
     if (rc) return rc;
+    if (req->queries && (!out->query_indices || !out->columns || !out->siblings))
+        return fail(TG_ERR_INVALID, "an opening round needs the result's index, column and sibling buffers");
     ServeReq* r = new ServeReq();
     r->req = *req;
     r->table_ptrs.assign(req->tables, req->tables + req->ntables);
@@ -345,6 +476,8 @@ extern "C" int tg_server_submit(tg_server* sv, const tg_proof_request* req, tg_p
         off += align256(r->group * r->n * 8);
         r->off_sc = off;
         off += align256(sc_bytes);
+        r->off_q = off;
+        off += align256(answer_bytes(req->queries, req->npolys, req->log_k + req->log_inv_rate));
         r->footprint = off;
     }
     {
@@ -404,7 +537,9 @@ extern "C" int tg_server_close(tg_server* sv) {
     for (auto& kv : sv->finished) delete kv.second;
     for (int i = 0; i < sv->max_inflight; i++) {
         cudaStreamSynchronize(sv->streams[i]);
+        cudaStreamSynchronize(sv->streams_hi[i]);
         cudaStreamDestroy(sv->streams[i]);
+        cudaStreamDestroy(sv->streams_hi[i]);
         cudaEventDestroy(sv->events[i]);
     }
     cudaFreeHost(sv->pinned);

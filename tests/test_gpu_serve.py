@@ -133,3 +133,51 @@ def test_submit_refusals(dev):
             with pytest.raises(N.TesseraError):
                 srv.submit(bad)
         assert srv.wait(srv.submit(good)).root
+
+
+def test_served_opening_rounds_equal_plain_and_verify(dev):
+    """Requests with an opening round: the query indices, the queried columns read from the
+    device-resident codewords and the multiproof read from the resident Merkle nodes equal the
+    plain path's (which answers from tg_commit_unmasked_dev's buffers), in a mix with requests
+    that have no opening round and alone; the restated verifier accepts every answer (leaves
+    recomputed from the columns' chains, the root from the multiproof) and rejects a changed
+    symbol."""
+    from oracle import verifier as V
+    from tessera_gb300.serve import ProofServer, prove_plain
+
+    reqs = requests(20, seed=17)
+    for i, r in enumerate(reqs):
+        r.queries = [0, 1, 7, 32][i % 4]
+    plain = [prove_plain(r, dev) for r in reqs]
+    with ProofServer(dev, slots=6) as srv:
+        served = [srv.wait(t) for t in [srv.submit(r) for r in reqs]]
+    with ProofServer(dev, slots=1) as srv:
+        alone = [srv.wait(srv.submit(r)) for r in reqs]
+    for i, (r, a, b, c) in enumerate(zip(reqs, served, plain, alone)):
+        assert a.same_proof(b) and c.same_proof(b), i
+        if not r.queries:
+            assert a.query_indices is None
+            continue
+        p = r.params
+        n = 1 << (p.log2_k + p.log2_inv_rate)
+        distinct = sorted(set(a.query_indices))
+        assert len(a.query_indices) == r.queries and a.columns.shape == (len(distinct), len(r.rows) >> p.log2_k)
+        leaves = [(j, V.column_digest(p.commitment_id, j, list(a.columns[q]), p.row_block))
+                  for q, j in enumerate(distinct)]
+        V.verify_multiproof(a.root, n, leaves, a.siblings)
+        bad = [list(col) for col in a.columns]
+        bad[-1][0] = (int(bad[-1][0]) + 1) % O.P
+        with pytest.raises(V.Reject):
+            V.verify_multiproof(a.root, n, [(j, V.column_digest(p.commitment_id, j, bad[q], p.row_block))
+                                            for q, j in enumerate(distinct)], a.siblings)
+
+
+def test_opening_round_refusals(dev):
+    from tessera_gb300 import _native as N
+    from tessera_gb300.serve import ProofServer
+
+    big = requests(1, seed=19)[0]
+    big.queries = 1 << 20  # far beyond the answer's staging
+    with ProofServer(dev, slots=2) as srv:
+        with pytest.raises(N.TesseraError):
+            srv.submit(big)
