@@ -625,6 +625,7 @@ def run_serve(args) -> None:
             res = [srv.wait(tk) for tk in tickets]
             wall = time.perf_counter() - start
             st = srv.stats()
+        st["stages"] = [(round(x.queued_ms, 3),) + tuple(round(v, 3) for v in x.stage_ms) for x in res]
         return wall, [x.latency_ms / 1e3 for x in res], st
 
     # warm-up: shapes' tables, pools, pinned paths
@@ -646,6 +647,7 @@ def run_serve(args) -> None:
                       "latency_ms": {"p50": q(pl, 0.5), "p99": q(pl, 0.99)}, "slowest": tail(pl)},
             "served": {"proofs_per_s": len(reqs) / sw, "elems_per_s": units / sw,
                        "latency_ms": {"p50": q(sl, 0.5), "p99": q(sl, 0.99)}, "slowest": tail(sl),
+                       "slowest_stages_ms": [st["stages"][i] for _, i, _ in tail(sl)],
                        "peak_inflight": st["peak_inflight"], "peak_gib": st["peak_bytes"] / 2**30},
         }
     del keep

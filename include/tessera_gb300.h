@@ -444,6 +444,8 @@ typedef struct {
     uint64_t *columns;             /* n_distinct x npolys symbols (room for queries x npolys) */
     uint8_t *siblings;             /* n_siblings digests (room for queries x log2 n) */
     uint32_t n_distinct, n_siblings;
+    /* when the scheduler saw each stage end (commit, sumcheck, opening), ms after submission */
+    double stage_ms[3];
 } tg_proof_result;
 typedef struct {
     uint64_t submitted, completed, peak_inflight;

@@ -65,7 +65,7 @@ class ProofResultC(ctypes.Structure):
                 ("rounds", ctypes.c_void_p), ("challenges", ctypes.c_void_p), ("final_evals", ctypes.c_void_p),
                 ("transcript", TranscriptState), ("queued_ms", ctypes.c_double), ("latency_ms", ctypes.c_double),
                 ("query_indices", ctypes.c_void_p), ("columns", ctypes.c_void_p), ("siblings", ctypes.c_void_p),
-                ("n_distinct", ctypes.c_uint32), ("n_siblings", ctypes.c_uint32)]
+                ("n_distinct", ctypes.c_uint32), ("n_siblings", ctypes.c_uint32), ("stage_ms", ctypes.c_double * 3)]
 
 
 class ServerStatsC(ctypes.Structure):

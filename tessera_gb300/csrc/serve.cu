@@ -346,6 +346,9 @@ static void scheduler(tg_server* sv) {
                 finish(sv, r, cuda_fail(e, "request stream"));
                 continue;
             }
+            if (r->stage >= 1 && r->stage <= 3)
+                r->out->stage_ms[r->stage - 1] =
+                    std::chrono::duration<double, std::milli>(Clock::now() - r->t_submit).count();
             if (r->stage == 1) {
                 r->stage = 2;
                 const int rc = start_sumcheck(sv, r);

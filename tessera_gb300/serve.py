@@ -44,6 +44,7 @@ class ProofResult:
     counter: int
     queued_ms: float = 0.0
     latency_ms: float = 0.0
+    stage_ms: tuple = ()        # when each stage (commit, sumcheck, opening) was seen to end, ms after submission
     query_indices: list = None  # the opening round: indices in draw order,
     columns: np.ndarray = None  # each distinct queried column's symbols (distinct x npolys, increasing index),
     siblings: list = None       # and the canonical multiproof of those indices
@@ -125,7 +126,7 @@ class ProofServer:
         res = ProofResult(bytes(out.root), (int(out.gamma[0]), int(out.gamma[1])),
                           [_pairs(rounds[j * degree * 2:(j + 1) * degree * 2], degree) for j in range(vars_)],
                           _pairs(chal, vars_), _pairs(evals, len(tabs)), bytes(out.transcript.state),
-                          int(out.transcript.counter), out.queued_ms, out.latency_ms)
+                          int(out.transcript.counter), out.queued_ms, out.latency_ms, tuple(out.stage_ms))
         if tau:
             m, ns = out.n_distinct, out.n_siblings
             res.query_indices = [int(x) for x in qidx[:tau]]
