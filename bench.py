@@ -360,6 +360,21 @@ def run_gpu(args) -> None:
     ms_per_step = total_ms / args.steps
     value = UNITS * world / (total_ms / 1e3 / args.steps)
 
+    # the host link's rate from pinned memory (the best of three 512 MiB copies), which bounds the
+    # end-to-end step from below: it moves h2d bytes per step
+    link = rows_h[: 64 << 20]
+    link_d = torch.empty_like(link, device=cuda)
+    link_gbs = 0.0
+    for _ in range(3):
+        l0, l1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        l0.record(stream)
+        with torch.cuda.stream(stream):
+            link_d.copy_(link, non_blocking=True)
+        l1.record(stream)
+        l1.synchronize()
+        link_gbs = max(link_gbs, link.numel() * 8 / (l0.elapsed_time(l1) / 1e3) / 1e9)
+    del link_d
+
     # end to end through the host-memory path
     for _ in range(max(1, args.warmup // 2)):
         step_e2e()
@@ -435,7 +450,10 @@ def run_gpu(args) -> None:
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic", "config": CONFIG,
         "e2e": {"value": UNITS * world / (e2e_ms / 1e3), "unit": "elems/s", "ms_per_step": e2e_ms,
-                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "host_link_gbs": link_gbs, "host_link_floor_ms": h2d / (link_gbs * 1e9) * 1e3 if link_gbs else None,
+                "note": "the step's copies cross the host link at host_link_gbs (measured here, pinned memory); "
+                        "e2e is at least max(ms_per_step, host_link_floor_ms)"},
         "latency_ms": {"p50": statistics.median(step_ms), "p99": max(step_ms) if len(step_ms) < 100 else
                        sorted(step_ms)[int(0.99 * len(step_ms))]},
         "gpu_launches": launches,
