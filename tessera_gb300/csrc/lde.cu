@@ -356,9 +356,8 @@ static bool fast_shape(uint32_t lgk) { return lgk >= 13 && lgk <= 22; }
 // RB, the second radix of the register-resident transform of length 2^lg (fast_pass's cases).
 static int fast_rb(int lg) { return lg <= 7 ? 8 : lg <= 9 ? 16 : 32; }
 
-// Words of one CTA's tile for a column length 2^lg: 8,192 (32 elements per thread) up to 2^10,
-// 16,384 for columns of 2^11 (64 per thread).
-static uint64_t fast_tile(int lg) { return lg <= 10 ? 8192 : 16384; }
+// Words of one CTA's tile: 8,192 for every column length (32 elements per thread).
+static uint64_t fast_tile(int) { return 8192; }
 
 // Encodes rows in groups through the three register-resident passes; y/z hold `group` rows.
 static int fast_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_t* rows, size_t npolys,

@@ -24,6 +24,12 @@
 // product. All arithmetic is lazy (tg::lz): values stay any 64-bit word until the codeword is
 // written, and every carry is folded with the carry flag.
 //
+// Columns of 2,048 (k = 2^21..2^22) keep 32 elements per thread too: round 2's length-64
+// sub-transforms are split across two threads. Each loads the 64 values of its sub-transform, does
+// the first radix-2 stage on load and keeps one half — the even outputs (sums) or the odd ones
+// (differences times ω_64^t, a shift) —, then runs the length-32 transform on it; the two halves
+// sit in different warps, so the choice never diverges within a warp.
+//
 // A CTA holds an 8,192-element tile (W = 8192/L columns, 64 KiB of shared memory) with 256
 // threads, so that two CTAs share an SM and one's loads overlap the other's arithmetic. Each
 // round maps threads to columns so that its global accesses are coalesced: when the column's
@@ -110,29 +116,8 @@ __device__ __forceinline__ void swap_halves(uint64_t (&x)[N]) {
 template <int R, bool INV, int BASE, int N>
 __device__ __forceinline__ void dft_dif(uint64_t (&x)[N]);
 
-// Length 64 as its first stage and then the two independent length-32 halves (a DIF's later
-// stages never cross the halves, and their twiddles ω_64^{2m} are ω_32^m), the halves run by one
-// copy of the length-32 code in a rolled loop that swaps them: half the instruction footprint of
-// the unrolled transform, which otherwise misses the instruction cache.
-template <bool INV, int BASE, int N>
-__device__ __forceinline__ void dft_dif64(uint64_t (&x)[N]) {
-    static_for<32>([&](auto b_) {
-        constexpr int b = decltype(b_)::value;
-        bf_gs<tw_exp(64, b, INV)>(x[BASE + b], x[BASE + b + 32]);
-    });
-#pragma unroll 1
-    for (int h = 0; h < 2; h++) {
-        dft_dif<32, INV, BASE>(x);
-        swap_halves<32, BASE>(x);
-    }
-}
-
 template <int R, bool INV, int BASE, int N>
 __device__ __forceinline__ void dft_dif(uint64_t (&x)[N]) {
-    if constexpr (R == 64) {
-        dft_dif64<INV, BASE>(x);
-        return;
-    }
     static_for<ilog2(R)>([&](auto s_) {
         constexpr int s = decltype(s_)::value;
         constexpr int h = R >> (s + 1);
@@ -194,27 +179,43 @@ __device__ __forceinline__ uint64_t rootp(const uint64_t* pw, int lgn, int lg, u
 template <int RA, int RB>
 struct Shape {
     static constexpr int L = RA * RB;
-    static constexpr int E = L > 1024 ? 64 : 32;  // elements per thread: 64 for columns of 2048
+    static constexpr int E = 32;                  // elements per thread
     static constexpr int T = L / E;               // threads per column
     static constexpr int W = THREADS / T;         // columns per CTA
-    static constexpr int TILE_WORDS = W * L;      // 8,192 (32 KiB... 64 KiB) or 16,384 for E = 64
-    static constexpr int MINB = E == 64 ? 1 : 2;  // CTAs per SM the registers allow
+    static constexpr int TILE_WORDS = W * L;      // 8,192
+    static constexpr int MINB = 2;                // CTAs per SM the registers allow
     static constexpr int NA = RA / T;             // round-1 sub-transforms per thread (length RB)
-    static constexpr int NB = RB / T;             // round-2 sub-transforms per thread (length RA)
-    static_assert(L >= 32 && L <= 2048 && NA >= 1 && NB >= 1 && NA * RB == E && NB * RA == E, "column length");
-    static_assert(W >= 8, "at least 8 columns per tile");
+    // Round 2: RB sub-transforms of length RA over T threads, NB each; with RB < T (columns of
+    // 2,048) each is split over two threads, thread q taking kb = q mod RB and half h = q / RB.
+    static constexpr bool SPLIT = RB < T;
+    static constexpr int NB = SPLIT ? 1 : RB / T;
+    static constexpr int KA_N = SPLIT ? RA / 2 : RA;  // round-2 outputs a thread holds per sub-transform
+    static constexpr int KA_STEP = SPLIT ? 2 : 1;     // they are ka = h + KA_STEP·j, j < KA_N
+    static_assert(L >= 32 && L <= 2048 && NA >= 1 && NA * RB == E && NB * KA_N == E, "column length");
+    static_assert(!SPLIT || (RA == 64 && RB == 32), "split only for columns of 2,048");
+    static_assert(W >= 4, "at least 4 columns per tile");
     // Exchange slots. With W ≥ 16 columns a row of the tile spans every bank and the column is
     // XORed with ta: a warp along a column (fixed c, 32 ta) and a warp across columns both hit
     // 16 distinct 8-byte bank pairs. With W = 8 a row is half the banks: kb-planes are padded by
     // 8 words so that rows of odd ta + kb take the other half, and the column is XORed with ta/2.
-    static constexpr int PAD = W >= 16 ? 0 : 8;
+    // With W = 4 (split) a row is a quarter: planes are padded by 4 words, so that four
+    // consecutive kb (a half-warp of round 2) take four quarters, and the column is XORed with
+    // ta/4, so that sixteen consecutive ta of one column (a half-warp of a q-fast round 1) do.
+    static constexpr int PAD = W >= 16 ? 0 : W == 8 ? 8 : 4;
     static constexpr int WORDS = RB * (RA * W + PAD);
     __device__ static __forceinline__ int slot(int c, int ta, int kb) {
         if constexpr (W >= 16)
             return (kb * RA + ta) * W + (c ^ (ta & 15));
-        else
+        else if constexpr (W == 8)
             return kb * (RA * W + PAD) + ta * W + (c ^ ((ta >> 1) & 7));
+        else
+            return kb * (RA * W + PAD) + ta * W + (c ^ ((ta >> 2) & 3));
     }
+    // Round 2's ownership for thread q (c-fast): sub-transform i's kb, and the half h.
+    __device__ static __forceinline__ int kb_of(int q, int i) { return SPLIT ? (q & (RB - 1)) : q + T * i; }
+    __device__ static __forceinline__ int h_of(int q) { return SPLIT ? q / RB : 0; }
+    // The register of output ka = h + KA_STEP·j of sub-transform i (bit-reversed order).
+    static constexpr int reg_of(int i, int j) { return SPLIT ? brev_c(j, ilog2(RA / 2)) : i * RA + brev_c(j, ilog2(RA)); }
 };
 
 // tw[kb·RA + ta] = ω_L^{±ta·kb}.
@@ -350,10 +351,33 @@ __device__ __forceinline__ void round1_store(uint64_t (&v)[N], uint64_t* sm, con
 }
 
 // Round 2 (c-fast): v[i·RA + ta] = Y[ta][kb_i], kb_i = q + T·i, then DIF of length RA:
-// v[i·RA + p] holds output kb_i + RB·rev(p).
+// v[i·RA + p] holds output kb_i + RB·rev(p). Split: thread (kb, h) keeps the first stage's half h
+// of Y[·][kb] and runs DIF of length RA/2 on it: v[p] holds output kb + RB·(2·rev(p) + h).
 template <int RA, int RB, bool INV, int N>
 __device__ __forceinline__ void round2(uint64_t (&v)[N], const uint64_t* sm, int c, int q) {
     using S = Shape<RA, RB>;
+    if constexpr (S::SPLIT) {
+        constexpr int H = RA / 2;
+        const int kb = S::kb_of(q, 0);
+        if (S::h_of(q) == 0) {  // warp-uniform: h = q / RB and a warp spans 8 consecutive q
+            static_for<H>([&](auto t_) {
+                constexpr int t = decltype(t_)::value;
+                v[t] = lz::add(sm[S::slot(c, t, kb)], sm[S::slot(c, t + H, kb)]);
+            });
+        } else {
+            static_for<H>([&](auto t_) {
+                constexpr int t = decltype(t_)::value;
+                constexpr int E2 = tw_exp(RA, t, INV);
+                const uint64_t a = sm[S::slot(c, t, kb)], b = sm[S::slot(c, t + H, kb)];
+                if constexpr (E2 >= 96)
+                    v[t] = lz::mulp2<E2 - 96>(lz::sub(b, a));
+                else
+                    v[t] = lz::mulp2<E2>(lz::sub(a, b));
+            });
+        }
+        dft_dif<H, INV, 0>(v);
+        return;
+    }
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
         const int kb = q + S::T * i;
@@ -378,12 +402,13 @@ __global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_a(Args a) {
     const int K1 = 1 << a.lgk1;
     const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast throughout
     const uint32_t t1 = t1_0 + c;
+    const int h = S::h_of(q);
     // the outer twiddles, fetched before the tile so that their latency hides behind it
-    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * t1, true);
+    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * S::KA_STEP * t1, true);
     uint64_t t0[S::NB];
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
-        t0[i] = rootp(a.pw, lgn, a.lgk, (uint64_t)(q + S::T * i) * t1, true);
+        t0[i] = rootp(a.pw, lgn, a.lgk, (uint64_t)(S::kb_of(q, i) + RB * h) * t1, true);
     });
     uint64_t v[S::E];
     load_staged<RA, RB, true>(v, sm, a.rows + (row << a.lgk) + t1_0, K1, c, q);  // its syncs cover the twiddles
@@ -393,13 +418,14 @@ __global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_a(Args a) {
     uint64_t* y = a.y + (row << a.lgk) + t1;
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
-        const int kb = q + S::T * i;
-        // output j2 = kb + RB·ka at v[i·RA + rev(ka)]; × ω_k^{−j2·t1}; Y[j2][t1]
+        const int kb = S::kb_of(q, i);
+        // output j2 = kb + RB·ka, ka = h + KA_STEP·j, at v[reg_of(i, j)]; × ω_k^{−j2·t1}; Y[j2][t1]
         uint64_t t = t0[i];
-        static_for<RA>([&](auto ka_) {
-            constexpr int ka = decltype(ka_)::value;
-            st_keep(y + (size_t)(kb + RB * ka) * K1, lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t));
-            if constexpr (ka + 1 < RA) t = lz::mul(t, step);
+        static_for<S::KA_N>([&](auto j_) {
+            constexpr int j = decltype(j_)::value;
+            const int ka = h + S::KA_STEP * j;
+            st_keep(y + (size_t)(kb + RB * ka) * K1, lz::mul(v[S::reg_of(i, j)], t));
+            if constexpr (j + 1 < S::KA_N) t = lz::mul(t, step);
         });
     });
 }
@@ -417,12 +443,13 @@ __global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_m1(Args a) 
     const int K2 = 1 << a.lgk2;
     const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast (round 2 and the stores)
     const uint32_t j2 = j2_0 + c;
+    const int h = S::h_of(q);
     // the scales' starting points, fetched before the tile so that their latency hides behind it:
-    // 7^idx0 / k and ω_n^idx0 (coset 1), idx0 = j2 + K2·kb
+    // 7^idx0 / k and ω_n^idx0 (coset 1), idx0 = j2 + K2·(kb + RB·h)
     uint64_t p7[S::NB], w1[S::NB];
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
-        const uint32_t idx0 = j2 + (uint32_t)K2 * (q + S::T * i);
+        const uint32_t idx0 = j2 + (uint32_t)K2 * (S::kb_of(q, i) + RB * h);
         p7[i] = a.pow7k[idx0];
         w1[i] = a.pw[idx0];
     });
@@ -434,25 +461,27 @@ __global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_m1(Args a) 
     }
     __syncthreads();
     round2<RA, RB, true>(v, sm, c, q);
-    // v[i·RA + rev(ka)] = k·a_idx, idx = j2 + K2·(kb + RB·ka); C_e[j1][j2] = that × s_e^idx / k
-    // (mask terms are added afterwards by mask_fixup)
+    // v[reg_of(i, j)] = k·a_idx, idx = j2 + K2·(kb + RB·ka), ka = h + KA_STEP·j;
+    // C_e[j1][j2] = that × s_e^idx / k (mask terms are added afterwards by mask_fixup)
     uint64_t* z = a.z + (row << lgn) + j2;
     for (int e = 0; e < (1 << a.lgr); e++) {
         uint64_t* ce = z + ((size_t)e << a.lgk);
+        // the scale's step along j: s_e^{K2·RB·KA_STEP}
+        const uint64_t step = S::KA_STEP == 2 ? lz::mul(a.sstep[e], a.sstep[e]) : a.sstep[e];
         static_for<S::NB>([&](auto i_) {
             constexpr int i = decltype(i_)::value;
-            const int kb = q + S::T * i;
-            const uint32_t idx0 = j2 + (uint32_t)K2 * kb;
+            const int kb = S::kb_of(q, i);
+            const uint32_t idx0 = j2 + (uint32_t)K2 * (kb + RB * h);
             uint64_t t = p7[i];  // s_e^idx0 / k
             if (e == 1)
                 t = lz::mul(t, w1[i]);
             else if (e > 1)
                 t = lz::mul(t, a.pw[((uint64_t)e * idx0) & ((1ull << lgn) - 1)]);
-            const uint64_t step = a.sstep[e];
-            static_for<RA>([&](auto ka_) {
-                constexpr int ka = decltype(ka_)::value;
-                st_keep(ce + (size_t)(kb + RB * ka) * K2, lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t));
-                if constexpr (ka + 1 < RA) t = lz::mul(t, step);
+            static_for<S::KA_N>([&](auto j_) {
+                constexpr int j = decltype(j_)::value;
+                const int ka = h + S::KA_STEP * j;
+                st_keep(ce + (size_t)(kb + RB * ka) * K2, lz::mul(v[S::reg_of(i, j)], t));
+                if constexpr (j + 1 < S::KA_N) t = lz::mul(t, step);
             });
         });
     }
@@ -492,12 +521,13 @@ __global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_m2(Args a) 
     const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast throughout
     uint64_t* z = a.z + (row << lgn) + ((size_t)e << a.lgk) + j2_0;
     const uint32_t j2 = j2_0 + c;
+    const int h = S::h_of(q);
     // the outer twiddles, fetched before the tile so that their latency hides behind it
-    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * j2, false);
+    const uint64_t step = rootp(a.pw, lgn, a.lgk, (uint64_t)RB * S::KA_STEP * j2, false);
     uint64_t t0[S::NB];
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
-        t0[i] = rootp(a.pw, lgn, a.lgk, (uint64_t)(q + S::T * i) * j2, false);
+        t0[i] = rootp(a.pw, lgn, a.lgk, (uint64_t)(S::kb_of(q, i) + RB * h) * j2, false);
     });
     uint64_t v[S::E];
     load_staged<RA, RB, false>(v, sm, z, K2, c, q);  // every load of this tile is done before any store below
@@ -506,13 +536,14 @@ __global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_m2(Args a) 
     round2<RA, RB, false>(v, sm, c, q);
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
-        const int kb = q + S::T * i;
-        // output v2 = kb + RB·ka; × ω_k^{v2·j2}; Z_e[v2][j2]
+        const int kb = S::kb_of(q, i);
+        // output v2 = kb + RB·ka, ka = h + KA_STEP·j; × ω_k^{v2·j2}; Z_e[v2][j2]
         uint64_t t = t0[i];
-        static_for<RA>([&](auto ka_) {
-            constexpr int ka = decltype(ka_)::value;
-            st_keep(z + c + (size_t)(kb + RB * ka) * K2, lz::mul(v[i * RA + brev_c(ka, ilog2(RA))], t));
-            if constexpr (ka + 1 < RA) t = lz::mul(t, step);
+        static_for<S::KA_N>([&](auto j_) {
+            constexpr int j = decltype(j_)::value;
+            const int ka = h + S::KA_STEP * j;
+            st_keep(z + c + (size_t)(kb + RB * ka) * K2, lz::mul(v[S::reg_of(i, j)], t));
+            if constexpr (j + 1 < S::KA_N) t = lz::mul(t, step);
         });
     });
 }
@@ -543,13 +574,15 @@ __global__ void __launch_bounds__(THREADS, Shape<RA, RB>::MINB) pass_c(Args a) {
     const int c = threadIdx.x % S::W, q = threadIdx.x / S::W;  // c-fast
     round2<RA, RB, false>(v, sm, c, q);
     uint64_t* out = a.out + (row << lgn) + col0 + c;
+    const int h = S::h_of(q);
     static_for<S::NB>([&](auto i_) {
         constexpr int i = decltype(i_)::value;
-        const int kb = q + S::T * i;
-        static_for<RA>([&](auto ka_) {
-            constexpr int ka = decltype(ka_)::value;
-            // symbol (v2 + K1·v1)·2^r + e with v1 = kb + RB·ka
-            st_stream(out + (((size_t)(kb + RB * ka) * K1) << a.lgr), lz::canon(v[i * RA + brev_c(ka, ilog2(RA))]));
+        const int kb = S::kb_of(q, i);
+        static_for<S::KA_N>([&](auto j_) {
+            constexpr int j = decltype(j_)::value;
+            // symbol (v2 + K1·v1)·2^r + e with v1 = kb + RB·ka, ka = h + KA_STEP·j
+            const int ka = h + S::KA_STEP * j;
+            st_stream(out + (((size_t)(kb + RB * ka) * K1) << a.lgr), lz::canon(v[S::reg_of(i, j)]));
         });
     });
 }
