@@ -891,6 +891,55 @@ def run_forest(args) -> None:
     s_, h_ = args.forest_trees_log, args.forest_leaves_log
     leaves = fill_counter(torch.empty(1 << (s_ + h_), dtype=torch.int64, device=f"cuda:{local}"), 1 << 61, dev)
     torch.cuda.synchronize()
+    if args.impl == "refgpu":
+        # the reference's own forest prover (oracle/refgpu.cpp over crates/tessera-gpu/kernels/trees.cu),
+        # on its benchmark's transcript; the library proves the same forest on the same transcript
+        # first, and the two final transcript states must agree (every message was absorbed)
+        import ctypes
+
+        bench_ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "bench/1", bytes([0x65]) * 32,
+                                   bytes([0x13]) * 16)
+        t = Transcript(bench_ctx)
+        with LeafStage([Forest(s_, leaves, True)], dev) as st:
+            st.prove(t)
+        ours = (t.state, t.counter)
+        del leaves
+        torch.cuda.synchronize()
+        dev.trim()
+        dev.close()
+        trees_fb, commit_fb = ROOT / "oracle" / "_ref" / "trees.fatbin", ROOT / "oracle" / "_ref" / "commit.fatbin"
+        lib_path = ROOT / "oracle" / "_build" / "librefgpu.so"
+        if not (trees_fb.exists() and commit_fb.exists() and lib_path.exists()):
+            if rank == 0:
+                print(json.dumps({"impl": "refgpu", "unavailable": "the reference kernels were not compiled here "
+                                  "(oracle/_ref/{trees,commit}.fatbin need the reference checkout)"}))
+            return
+        lib = ctypes.CDLL(str(lib_path))
+        lib.refgpu_last_error.restype = ctypes.c_char_p
+        out = (ctypes.c_double * 1)()
+        state = ctypes.create_string_buffer(32)
+        counter = ctypes.c_uint64()
+        rc = lib.refgpu_pi(str(trees_fb).encode(), str(commit_fb).encode(), ctypes.c_uint32(s_), ctypes.c_uint32(h_),
+                           ctypes.c_int(args.warmup), ctypes.c_int(args.steps), out, state, ctypes.byref(counter))
+        if rc != 0:
+            raise RuntimeError("reference kernels: " + lib.refgpu_last_error().decode())
+        if rank != 0:
+            return
+        print(json.dumps({
+            "metric": "c_pi: ps per product-forest leaf (level build + level sumchecks on a transcript)",
+            "value": out[0] / (1 << (s_ + h_)) * 1e12, "unit": "ps/leaf", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u64 (Goldilocks; Fp2 after the first bind)", "impl": "refgpu",
+            "data": "synthetic (counter-generated prime-field leaves on the device, as the reference benchmark)",
+            "config": {"workload": f"one forest of 2^{s_} trees of 2^{h_} leaves",
+                       "timing": "host wall clock per proof (leaves already on the device), median over steps"},
+            "proof_ms": out[0] * 1e3,
+            "kernels": "the reference's crates/tessera-gpu/kernels/trees.cu (tree_level, eq_table, level_sums_base, "
+                       "bind_sums_base, bind_sums_ext, reduce_sums, bind_base, bind_ext) compiled for sm_103 with its "
+                       "own flags, driven as crates/tessera-gpu/src/trees.rs prove_forest_in does",
+            "final_transcript_equal_library": (state.raw, counter.value) == ours,
+        }), flush=True)
+        return
 
     def one():
         start = time.perf_counter()
@@ -937,7 +986,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference", "refgpu"], default="gb300",
                     help="reference: the CPU port of the reference's algorithms; refgpu: the reference's own CUDA "
-                         "kernels on this GPU (--workload cc)")
+                         "kernels on this GPU (--workload cc, forest)")
     ap.add_argument("--workload", choices=["large", "batched", "serve", "logup", "cc", "forest"], default="large",
                     help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain; "
                          "serve: the proof server against one-at-a-time proofs")
@@ -967,8 +1016,8 @@ def main():
         UNITS = COMMITTED + SUMCHECKED
         CONFIG["polys"] = args.polys
         CONFIG["workload"] = CONFIG["workload"].replace("commit 256", f"commit {args.polys}")
-    if args.impl == "refgpu" and args.workload != "cc":
-        print(json.dumps({"impl": "refgpu", "unavailable": "the reference's own kernels are driven for --workload cc only"}))
+    if args.impl == "refgpu" and args.workload not in ("cc", "forest"):
+        print(json.dumps({"impl": "refgpu", "unavailable": "the reference's own kernels are driven for --workload cc and forest"}))
     elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":

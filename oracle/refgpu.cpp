@@ -16,12 +16,25 @@
 //   timed runs after the warm-ups (gpu_unit_costs.rs:93-170). Before timing, block 0's chains
 //   are checked against the CPU oracle's encoding and chains, as the reference's benchmark
 //   checks them against its CPU crates.
+//
+//   refgpu_pi: the product-forest leaf cost c_π with the reference's crates/tessera-gpu/kernels/
+//   trees.cu (oracle/_ref/trees.fatbin): a forest of 2^s trees of 2^h prime-field leaves from the
+//   counter generator at 2^61, proved level by level as Device::prove_forest_in does
+//   (crates/tessera-gpu/src/trees.rs:176-318): the levels built bottom up (tree_level), then per
+//   level the root challenges, γ, each round's split eq tables (eq_table), fused bind-and-sums
+//   (level_sums_base, bind_sums_base, bind_sums_ext) and their block reduction (reduce_sums) read
+//   back, the round message p(0), p(2), p(3) formed on the host, the last binding (bind_base,
+//   bind_ext), the evaluations and ρ; the transcript is the CPU oracle's (the reference runs its
+//   own on the host too). Timed on the host clock per proof with the workspace reused, as
+//   gpu_unit_costs.rs `pi` (:175-205) times it; the final transcript state is returned so that the
+//   caller can check that the library proves the same forest to the same bytes.
 #include <cuda.h>
 #include <stdint.h>
 #include <stdio.h>
 #include <string.h>
 
 #include <algorithm>
+#include <chrono>
 #include <string>
 #include <vector>
 
@@ -266,6 +279,249 @@ struct Bench {
     }
 };
 
+// ---- c_π ----------------------------------------------------------------------------------
+
+struct F2 {
+    uint64_t a, b;
+};
+uint64_t addm(uint64_t x, uint64_t y) { return (uint64_t)(((unsigned __int128)x + y) % P); }
+uint64_t subm(uint64_t x, uint64_t y) { return x >= y ? x - y : (uint64_t)((unsigned __int128)x + P - y); }
+F2 f2add(F2 x, F2 y) { return {addm(x.a, y.a), addm(x.b, y.b)}; }
+F2 f2sub(F2 x, F2 y) { return {subm(x.a, y.a), subm(x.b, y.b)}; }
+F2 f2mul(F2 x, F2 y) {
+    return {addm(mulm(x.a, y.a), mulm(7, mulm(x.b, y.b))), addm(mulm(x.a, y.b), mulm(x.b, y.a))};
+}
+const F2 F2_ONE = {1, 0};
+
+constexpr uint32_t SUM_THREADS = 256;  // trees.rs SUM_THREADS
+constexpr uint64_t SUM_BLOCKS = 2048;  // trees.rs SUM_BLOCKS
+
+struct Forest {
+    CUcontext ctx = nullptr;
+    CUmodule mod = nullptr, cmod = nullptr;
+    CUstream s = nullptr;
+    CUdevice dev = 0;
+    CUfunction fill_counter, tree_level, level_sums_base, bind_sums_base, bind_sums_ext, eq_table, reduce_sums,
+        bind_base, bind_ext;
+    uint32_t height = 0, vars = 0;
+    uint64_t leaves_n = 0;
+    CUdeviceptr leaves = 0, cur0 = 0, cur1 = 0, sp0 = 0, sp1 = 0, partials = 0, sums = 0, eq_lo = 0, eq_hi = 0,
+                points = 0;
+    std::vector<CUdeviceptr> levels;  // level t at index t − 1, 1 <= t < h
+
+    bool open(const char* trees_fatbin, const char* commit_fatbin, uint32_t s_log, uint32_t h) {
+        height = h;
+        vars = s_log + h;
+        leaves_n = 1ull << vars;
+        CK(cuInit(0));
+        CK(cuDeviceGet(&dev, 0));
+        CK(cuDevicePrimaryCtxRetain(&ctx, dev));
+        CK(cuCtxSetCurrent(ctx));
+        CK(cuModuleLoad(&mod, trees_fatbin));
+        CK(cuModuleLoad(&cmod, commit_fatbin));
+        CK(cuModuleGetFunction(&fill_counter, cmod, "fill_counter"));
+        CK(cuModuleGetFunction(&tree_level, mod, "tree_level"));
+        CK(cuModuleGetFunction(&level_sums_base, mod, "level_sums_base"));
+        CK(cuModuleGetFunction(&bind_sums_base, mod, "bind_sums_base"));
+        CK(cuModuleGetFunction(&bind_sums_ext, mod, "bind_sums_ext"));
+        CK(cuModuleGetFunction(&eq_table, mod, "eq_table"));
+        CK(cuModuleGetFunction(&reduce_sums, mod, "reduce_sums"));
+        CK(cuModuleGetFunction(&bind_base, mod, "bind_base"));
+        CK(cuModuleGetFunction(&bind_ext, mod, "bind_ext"));
+        CK(cuStreamCreate(&s, CU_STREAM_NON_BLOCKING));
+        // the workspace of Device::forest_workspace (trees.rs:128-160)
+        CK(cuMemAlloc(&leaves, leaves_n * 8));
+        for (uint32_t t = 1; t < h; t++) {
+            CUdeviceptr p;
+            CK(cuMemAlloc(&p, (leaves_n >> (h - t)) * 8));
+            levels.push_back(p);
+        }
+        const uint64_t width = std::max<uint64_t>(leaves_n / 2, 2);
+        for (CUdeviceptr* p : {&cur0, &cur1, &sp0, &sp1}) CK(cuMemAlloc(p, width * 8));
+        CK(cuMemAlloc(&partials, 6 * SUM_BLOCKS * 8));
+        CK(cuMemAlloc(&sums, 6 * SUM_THREADS * 8));
+        const uint32_t half = vars >= 2 ? (vars - 2 + 1) / 2 : 0;
+        const uint64_t eq_len = 2ull << half;
+        CK(cuMemAlloc(&eq_lo, eq_len * 8));
+        CK(cuMemAlloc(&eq_hi, eq_len * 8));
+        CK(cuMemAlloc(&points, 2 * 8 * (vars + 1)));
+        // the leaves: Device::fill_counter(leaves, 1 << 61) (gpu_unit_costs.rs:180)
+        uint64_t len = leaves_n, base = 1ull << 61;
+        void* args[] = {&leaves, &len, &base};
+        CK(cuLaunchKernel(fill_counter, (uint32_t)((len + 1023) / 1024), 1, 1, 1024, 1, 1, 0, s, args, nullptr));
+        CK(cuStreamSynchronize(s));
+        return true;
+    }
+
+    bool launch1024(CUfunction f, uint64_t items, void** args) {
+        CK(cuLaunchKernel(f, (uint32_t)std::max<uint64_t>(1, (items + 1023) / 1024), 1, 1, 1024, 1, 1, 0, s, args,
+                          nullptr));
+        return true;
+    }
+
+    bool eq(uint32_t first, uint32_t m, CUdeviceptr out) {
+        void* args[] = {&points, &first, &m, &out};
+        return launch1024(eq_table, 1ull << m, args);
+    }
+
+    // One round's three sums (trees.rs:342-452): the fused kernel, the reduction, the read-back.
+    bool round_sums(int kind, CUdeviceptr v, CUdeviceptr e, CUdeviceptr o, F2 c, CUdeviceptr eo, CUdeviceptr oo,
+                    uint64_t pairs, uint32_t lo_bits, F2 out[3]) {
+        uint32_t blocks = (uint32_t)std::min<uint64_t>(std::max<uint64_t>((pairs + SUM_THREADS - 1) / SUM_THREADS, 1),
+                                                       SUM_BLOCKS);
+        uint64_t c0 = c.a, c1 = c.b;
+        if (kind == 0) {
+            void* args[] = {&v, &pairs, &eq_lo, &lo_bits, &eq_hi, &partials};
+            CK(cuLaunchKernel(level_sums_base, blocks, 1, 1, SUM_THREADS, 1, 1, 0, s, args, nullptr));
+        } else if (kind == 1) {
+            void* args[] = {&v, &pairs, &c0, &c1, &eo, &oo, &eq_lo, &lo_bits, &eq_hi, &partials};
+            CK(cuLaunchKernel(bind_sums_base, blocks, 1, 1, SUM_THREADS, 1, 1, 0, s, args, nullptr));
+        } else {
+            void* args[] = {&e, &o, &pairs, &c0, &c1, &eo, &oo, &eq_lo, &lo_bits, &eq_hi, &partials};
+            CK(cuLaunchKernel(bind_sums_ext, blocks, 1, 1, SUM_THREADS, 1, 1, 0, s, args, nullptr));
+        }
+        void* rargs[] = {&partials, &blocks, &sums};
+        CK(cuLaunchKernel(reduce_sums, 1, 1, 1, SUM_THREADS, 1, 1, 0, s, rargs, nullptr));
+        uint64_t w[6];
+        CK(cuMemcpyDtoHAsync(w, sums, 48, s));
+        CK(cuStreamSynchronize(s));
+        for (int k = 0; k < 3; k++) out[k] = {w[2 * k], w[2 * k + 1]};
+        return true;
+    }
+
+    // Device::prove_forest_in (trees.rs:176-318) on transcript t.
+    bool prove(or_transcript* t) {
+        for (uint32_t lvl = height - 1; lvl >= 1; lvl--) {  // level lvl from level lvl + 1
+            CUdeviceptr child = lvl + 1 < height ? levels[lvl] : leaves, parent = levels[lvl - 1];
+            uint64_t n = leaves_n >> (height - lvl);
+            void* args[] = {&child, &parent, &n};
+            if (!launch1024(tree_level, n, args)) return false;
+        }
+        char label[96];
+        std::vector<F2> point;
+        for (uint32_t c = 0; c < vars - height; c++) {
+            snprintf(label, sizeof label, "tree/0/root/%u", c);
+            uint64_t r[2];
+            or_transcript_challenge_fp2(t, label, r);
+            point.push_back({r[0], r[1]});
+        }
+        for (uint32_t level = 0; level < height; level++) {
+            uint64_t g[2];
+            snprintf(label, sizeof label, "tree/%u/gamma", level);
+            or_transcript_challenge_fp2(t, label, g);
+            const CUdeviceptr table = level < levels.size() ? levels[level] : leaves;
+            const uint32_t n = (uint32_t)point.size();
+            std::vector<F2> chal;
+            F2 u, w;
+            if (n == 0) {
+                uint64_t v[2];
+                CK(cuMemcpyDtoHAsync(v, table, 16, s));
+                CK(cuStreamSynchronize(s));
+                u = {v[0], 0};
+                w = {v[1], 0};
+            } else {
+                std::vector<uint64_t> pw;
+                for (const F2& x : point) {
+                    pw.push_back(x.a);
+                    pw.push_back(x.b);
+                }
+                CK(cuMemcpyHtoDAsync(points, pw.data(), pw.size() * 8, s));
+                F2 scale = F2_ONE;
+                for (uint32_t j = 0; j < n; j++) {
+                    const uint64_t pairs = 1ull << (n - 1 - j);
+                    const uint32_t rest = n - 1 - j, lo_bits = (rest + 1) / 2;
+                    if (!eq(j + 1, lo_bits, eq_lo) || !eq(j + 1 + lo_bits, rest - lo_bits, eq_hi)) return false;
+                    F2 sm[3];
+                    bool ok_;
+                    if (j == 0) {
+                        ok_ = round_sums(0, table, 0, 0, F2{0, 0}, 0, 0, pairs, lo_bits, sm);
+                    } else if (j == 1) {
+                        ok_ = round_sums(1, table, 0, 0, chal.back(), cur0, cur1, pairs, lo_bits, sm);
+                    } else {
+                        ok_ = round_sums(2, 0, cur0, cur1, chal.back(), sp0, sp1, pairs, lo_bits, sm);
+                        std::swap(cur0, sp0);
+                        std::swap(cur1, sp1);
+                    }
+                    if (!ok_) return false;
+                    const F2 r = point[j];
+                    auto eq_at = [&](F2 c) { return f2add(f2mul(f2sub(F2_ONE, r), f2sub(F2_ONE, c)), f2mul(r, c)); };
+                    const F2 two = {2, 0}, three = {3, 0};
+                    const F2 s3 = f2add(f2sub(sm[0], f2mul(three, sm[1])), f2mul(three, sm[2]));
+                    uint64_t msg[6];
+                    const F2 m0 = f2mul(f2mul(scale, eq_at(F2{0, 0})), sm[0]);
+                    const F2 m2 = f2mul(f2mul(scale, eq_at(two)), sm[2]);
+                    const F2 m3 = f2mul(f2mul(scale, eq_at(three)), s3);
+                    msg[0] = m0.a, msg[1] = m0.b, msg[2] = m2.a, msg[3] = m2.b, msg[4] = m3.a, msg[5] = m3.b;
+                    snprintf(label, sizeof label, "tree/%u/round/%u", level, j);
+                    or_transcript_absorb_fp2s(t, label, msg, 3);
+                    uint64_t c[2];
+                    snprintf(label, sizeof label, "tree/%u/r/%u", level, j);
+                    or_transcript_challenge_fp2(t, label, c);
+                    scale = f2mul(scale, eq_at(F2{c[0], c[1]}));
+                    chal.push_back({c[0], c[1]});
+                }
+                // the last round's binding, to one entry per table
+                uint64_t c0 = chal.back().a, c1 = chal.back().b, one = 1;
+                if (n == 1) {
+                    CUdeviceptr tb = table;
+                    void* args[] = {&tb, &one, &c0, &c1, &cur0, &cur1};
+                    if (!launch1024(bind_base, 1, args)) return false;
+                } else {
+                    void* args[] = {&cur0, &cur1, &one, &c0, &c1, &sp0, &sp1};
+                    if (!launch1024(bind_ext, 1, args)) return false;
+                    std::swap(cur0, sp0);
+                    std::swap(cur1, sp1);
+                }
+                uint64_t e[2], o[2];
+                CK(cuMemcpyDtoHAsync(e, cur0, 16, s));
+                CK(cuMemcpyDtoHAsync(o, cur1, 16, s));
+                CK(cuStreamSynchronize(s));
+                u = {e[0], e[1]};
+                w = {o[0], o[1]};
+            }
+            uint64_t ev[4] = {u.a, u.b, w.a, w.b};
+            snprintf(label, sizeof label, "tree/%u/evals", level);
+            or_transcript_absorb_fp2s(t, label, ev, 2);
+            uint64_t rho[2];
+            snprintf(label, sizeof label, "tree/%u/line", level);
+            or_transcript_challenge_fp2(t, label, rho);
+            point.clear();
+            point.push_back({rho[0], rho[1]});
+            point.insert(point.end(), chal.begin(), chal.end());
+        }
+        return true;
+    }
+
+    void close() {
+        for (CUdeviceptr p : levels) cuMemFree(p);
+        for (CUdeviceptr p : {leaves, cur0, cur1, sp0, sp1, partials, sums, eq_lo, eq_hi, points})
+            if (p) cuMemFree(p);
+        if (s) cuStreamDestroy(s);
+        if (mod) cuModuleUnload(mod);
+        if (cmod) cuModuleUnload(cmod);
+        if (ctx) cuDevicePrimaryCtxRelease(dev);
+    }
+};
+
+// The transcript of the reference benchmark's proofs (gpu_unit_costs.rs transcript()): protocol
+// "tessera-protocol/1", non-interactive, params "bench/1", statement [0x65; 32], session [0x13; 16].
+void bench_transcript(or_transcript* t) {
+    std::vector<uint8_t> tce;
+    auto le = [&](uint64_t v, int bytes) {
+        for (int i = 0; i < bytes; i++) tce.push_back((uint8_t)(v >> (8 * i)));
+    };
+    const char* proto = "tessera-protocol/1";
+    const char* params = "bench/1";
+    le(strlen(proto), 8);
+    tce.insert(tce.end(), proto, proto + strlen(proto));
+    le(1, 2);
+    le(strlen(params), 8);
+    tce.insert(tce.end(), params, params + strlen(params));
+    tce.insert(tce.end(), 32, 0x65);
+    tce.insert(tce.end(), 16, 0x13);
+    or_transcript_init(t, tce.data(), tce.size());
+}
+
 double median(std::vector<double> v) {
     std::sort(v.begin(), v.end());
     return v.size() % 2 ? v[v.size() / 2] : 0.5 * (v[v.size() / 2 - 1] + v[v.size() / 2]);
@@ -312,6 +568,36 @@ int refgpu_cc(const char* fatbin, uint32_t log_k, uint32_t rows, uint32_t mask_c
     out[0] = median(full);
     out[1] = median(gen);
     out[2] = median(enc);
+    return 0;
+}
+
+// c_π: out[0] the median seconds of one forest proof (after `warmup` proofs, over `runs`);
+// state (32 bytes) and *counter: the transcript after the first proof. Returns 0 or −1.
+int refgpu_pi(const char* trees_fatbin, const char* commit_fatbin, uint32_t s_log, uint32_t h, int warmup, int runs,
+              double* out, uint8_t* state, uint64_t* counter) {
+    if (h < 1 || s_log + h > 34 || runs < 1) {
+        g_err = "a forest of 2^s trees of height 1..34 - s";
+        return -1;
+    }
+    Forest f;
+    bool good = f.open(trees_fatbin, commit_fatbin, s_log, h);
+    std::vector<double> ts;
+    for (int i = 0; good && i < warmup + runs; i++) {
+        or_transcript t;
+        bench_transcript(&t);
+        const auto t0 = std::chrono::steady_clock::now();
+        good = f.prove(&t);
+        if (good) good = ok(cuStreamSynchronize(f.s), "cuStreamSynchronize");
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (good && i == 0) {
+            memcpy(state, t.state, 32);
+            *counter = t.counter;
+        }
+        if (good && i >= warmup) ts.push_back(dt);
+    }
+    f.close();
+    if (!good) return -1;
+    out[0] = median(ts);
     return 0;
 }
 
