@@ -689,42 +689,113 @@ def run_serve(args) -> None:
     print(json.dumps(line), flush=True)
 
 
+# The reference benchmark's c_ℓ inputs (crates/tessera-bench/examples/gpu_unit_costs.rs `l`): fixed
+# α and β, and the counter generator's seeds of the lookup tree's keys and values and of the table
+# tree's keys, values and multiplicities.
+LOGUP_ALPHA = (0x123456789ABCDEF0, 0x0FEDCBA987654321)
+LOGUP_BETA = (0x1111222233334444, 0x5555666677778888)
+LOGUP_LOOKUP = (1 << 56, 1 << 57, None)
+LOGUP_TABLE = (1 << 58, 1 << 59, 1 << 60)
+
+
+def bench_transcript_context():
+    """The reference benchmark's transcript context for its tree proofs (gpu_unit_costs.rs
+    transcript()): params "bench/1", statement [0x65; 32], session [0x13; 16]."""
+    from tessera_gb300.hash import Mode, SessionContext
+
+    return SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "bench/1", bytes([0x65]) * 32, bytes([0x13]) * 16)
+
+
 def run_logup(args) -> None:
-    """LogUp fraction trees, the reference benchmark's c_ℓ measurement shape: a lookup tree of 2^A
+    """LogUp fraction trees, the reference benchmark's c_ℓ measurement: a lookup tree of 2^A
     generated leaves (1, α − (k + β·v)) and a table tree of 2^T leaves (−m, α − (k + β·v)), each
-    built on the device and proven level by level as its own leaf stage on a transcript; the time
-    per lookup is the two trees' time over 2^A."""
+    built on the device and proven level by level as its own leaf stage on a fresh transcript,
+    with the reference benchmark's seeds, α, β and transcript; the time per lookup is the two
+    trees' time over 2^A. --impl refgpu runs the reference's own kernels the same way
+    (oracle/refgpu.cpp) after checking that both prove each tree to the same transcript."""
+    import ctypes
+
     import torch
 
     from tessera_gb300.device import Device
-    from tessera_gb300.hash import Mode, SessionContext, Transcript
+    from tessera_gb300.hash import Transcript
     from tessera_gb300.trees import LeafStage, generated_fraction
 
     world, rank, local = dist_env()
     torch.cuda.set_device(local)
     dev = Device(local)
-    ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([0x65]) * 32, bytes([0x65]) * 16)
+    ctx = bench_transcript_context()
 
-    def one(height, mult_seed):
+    def one(height, seeds, keep=None):
         start = time.perf_counter()
         t = Transcript(ctx)
-        alpha, beta = t.challenge_fp2("logup/alpha"), t.challenge_fp2("logup/beta")
-        tree = generated_fraction(height, 0x6B6579, 0x76616C, mult_seed, alpha, beta, dev, deferred=True)
+        tree = generated_fraction(height, seeds[0], seeds[1], seeds[2], LOGUP_ALPHA, LOGUP_BETA, dev, deferred=True)
         with LeafStage([tree], dev) as st:
             st.prove(t)
         torch.cuda.synchronize()
+        if keep is not None:
+            keep.append((t.state, t.counter))
         return time.perf_counter() - start
 
+    if args.impl == "refgpu":
+        ours = []
+        one(args.lookups_log, LOGUP_LOOKUP, ours)
+        one(args.rows_log, LOGUP_TABLE, ours)
+        torch.cuda.synchronize()
+        dev.trim()
+        dev.close()
+        trees_fb = ROOT / "oracle" / "_ref" / "trees.fatbin"
+        lib_path = ROOT / "oracle" / "_build" / "librefgpu.so"
+        if not (trees_fb.exists() and lib_path.exists()):
+            if rank == 0:
+                print(json.dumps({"impl": "refgpu", "unavailable": "the reference kernels were not compiled here "
+                                  "(oracle/_ref/trees.fatbin needs the reference checkout)"}))
+            return
+        lib = ctypes.CDLL(str(lib_path))
+        lib.refgpu_last_error.restype = ctypes.c_char_p
+        med, same = {}, []
+        for name, height, seeds, theirs_ours in (("lookup", args.lookups_log, LOGUP_LOOKUP, ours[0]),
+                                                 ("table", args.rows_log, LOGUP_TABLE, ours[1])):
+            words = (ctypes.c_uint64 * 7)(seeds[0], seeds[1], seeds[2] or 0, *LOGUP_ALPHA, *LOGUP_BETA)
+            out = (ctypes.c_double * 1)()
+            state = ctypes.create_string_buffer(32)
+            counter = ctypes.c_uint64()
+            rc = lib.refgpu_fraction(str(trees_fb).encode(), ctypes.c_uint32(height), words,
+                                     ctypes.c_uint32(int(seeds[2] is None)), ctypes.c_int(args.warmup),
+                                     ctypes.c_int(args.steps), out, state, ctypes.byref(counter))
+            if rc != 0:
+                raise RuntimeError("reference kernels: " + lib.refgpu_last_error().decode())
+            med[name] = out[0]
+            same.append((state.raw, counter.value) == theirs_ours)
+        if rank != 0:
+            return
+        print(json.dumps({
+            "metric": "LogUp ps per lookup (fraction-tree build + level sumchecks, lookup and table trees)",
+            "value": (med["lookup"] + med["table"]) / (1 << args.lookups_log) * 1e12, "unit": "ps/lookup",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u64 (Goldilocks Fp2)", "impl": "refgpu",
+            "data": "synthetic (the reference benchmark's counter-generated keys, values and multiplicities)",
+            "config": {"workload": f"2^{args.lookups_log} lookups into 2^{args.rows_log} rows, each tree its own proof",
+                       "timing": "host wall clock per tree, median over steps, leaves generated on the device inside"},
+            "lookup_tree_ms": med["lookup"] * 1e3, "table_tree_ms": med["table"] * 1e3,
+            "kernels": "the reference's crates/tessera-gpu/kernels/trees.cu (frac_level_leaves, frac_level, "
+                       "frac_sums_*, frac_bind_sums_*, frac_first_*, frac_last_*, eq_table, reduce_sums) compiled "
+                       "for sm_103 with its own flags, driven as crates/tessera-gpu/src/fraction.rs "
+                       "prove_fraction_tree_in does",
+            "final_transcripts_equal_library": same,
+        }), flush=True)
+        return
+
     for _ in range(args.warmup):
-        one(args.lookups_log, None)
-        one(args.rows_log, 0x6D756C)
+        one(args.lookups_log, LOGUP_LOOKUP)
+        one(args.rows_log, LOGUP_TABLE)
     times = {"lookup": [], "table": []}
     for _ in range(args.steps):  # timed without per-launch events
-        times["lookup"].append(one(args.lookups_log, None))
-        times["table"].append(one(args.rows_log, 0x6D756C))
+        times["lookup"].append(one(args.lookups_log, LOGUP_LOOKUP))
+        times["table"].append(one(args.rows_log, LOGUP_TABLE))
     dev.profile(True)  # one more step, profiled, for the kernel breakdown
-    one(args.lookups_log, None)
-    one(args.rows_log, 0x6D756C)
+    one(args.lookups_log, LOGUP_LOOKUP)
+    one(args.rows_log, LOGUP_TABLE)
     dev.profile(False)
     prof = dev.profile_read()
     kernels = {k: {"ms_per_step": v[0], "launches_per_step": v[1]} for k, v in prof.items()}
@@ -737,8 +808,8 @@ def run_logup(args) -> None:
         "metric": "LogUp ps per lookup (fraction-tree build + level sumchecks, lookup and table trees)",
         "value": ps, "unit": "ps/lookup", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks Fp2)",
-        "data": "synthetic (counter-generated keys, values and multiplicities)",
-        "config": {"workload": f"2^{args.lookups_log} lookups into 2^{args.rows_log} rows, each tree its own leaf stage",
+        "data": "synthetic (the reference benchmark's counter-generated keys, values and multiplicities)",
+        "config": {"workload": f"2^{args.lookups_log} lookups into 2^{args.rows_log} rows, each tree its own proof",
                    "timing": "host wall clock per tree, median over steps, leaves generated on the device inside; "
                              "kernels from one more profiled step"},
         "lookup_tree_ms": med["lookup"] * 1e3, "table_tree_ms": med["table"] * 1e3,
@@ -986,7 +1057,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference", "refgpu"], default="gb300",
                     help="reference: the CPU port of the reference's algorithms; refgpu: the reference's own CUDA "
-                         "kernels on this GPU (--workload cc, forest)")
+                         "kernels on this GPU (--workload cc, forest, logup)")
     ap.add_argument("--workload", choices=["large", "batched", "serve", "logup", "cc", "forest"], default="large",
                     help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain; "
                          "serve: the proof server against one-at-a-time proofs")
@@ -1016,8 +1087,8 @@ def main():
         UNITS = COMMITTED + SUMCHECKED
         CONFIG["polys"] = args.polys
         CONFIG["workload"] = CONFIG["workload"].replace("commit 256", f"commit {args.polys}")
-    if args.impl == "refgpu" and args.workload not in ("cc", "forest"):
-        print(json.dumps({"impl": "refgpu", "unavailable": "the reference's own kernels are driven for --workload cc and forest"}))
+    if args.impl == "refgpu" and args.workload not in ("cc", "forest", "logup"):
+        print(json.dumps({"impl": "refgpu", "unavailable": "the reference's own kernels are driven for --workload cc, forest and logup"}))
     elif args.impl == "reference":
         run_reference(args)
     elif args.workload == "batched":

@@ -28,6 +28,14 @@
 //   own on the host too). Timed on the host clock per proof with the workspace reused, as
 //   gpu_unit_costs.rs `pi` (:175-205) times it; the final transcript state is returned so that the
 //   caller can check that the library proves the same forest to the same bytes.
+//
+//   refgpu_fraction: one LogUp fraction tree of c_ℓ, as Device::prove_fraction_tree_in does
+//   (crates/tessera-gpu/src/fraction.rs:208-634): leaves generated in the kernels from the counter
+//   generator (LEAF_ARGS: key, value and multiplicity seeds, α, β, unit), levels h − 1 .. 1 built
+//   (frac_level_leaves, frac_level), then per level γ, λ, the rounds (frac_sums_*, frac_bind_sums_*,
+//   reduce_sums), the last binding (frac_last_*) or the one-entry level (frac_first_*), the four
+//   evaluations and ρ. c_ℓ is the lookup tree's proof plus the table tree's, per lookup
+//   (gpu_unit_costs.rs `l`, :212-296).
 #include <cuda.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -503,6 +511,216 @@ struct Forest {
     }
 };
 
+// ---- c_ℓ: one fraction tree -----------------------------------------------------------------
+
+struct Fraction {
+    CUcontext ctx = nullptr;
+    CUmodule mod = nullptr;
+    CUstream s = nullptr;
+    CUdevice dev = 0;
+    CUfunction level_leaves, level, first_stored, first_leaves, sums_stored, sums_leaves, bind_sums_stored,
+        bind_sums_leaves, bind_sums_bound, last_stored, last_leaves, last_bound, eq_table, reduce_sums;
+    uint32_t height = 0, unit = 0;
+    uint64_t leaf[7];  // key seed, value seed, multiplicity seed, α (two words), β (two words)
+    std::vector<CUdeviceptr> num, den;  // level t at index t − 1, 1 <= t < h: 2^t Fp2 entries
+    CUdeviceptr cur[4] = {0, 0, 0, 0}, spare[4] = {0, 0, 0, 0}, partials = 0, sums = 0, eq_lo = 0, eq_hi = 0,
+                finals = 0, points = 0;
+
+    bool open(const char* trees_fatbin, uint32_t h, const uint64_t seeds_ab[7], uint32_t unit_) {
+        height = h;
+        unit = unit_;
+        memcpy(leaf, seeds_ab, sizeof leaf);
+        CK(cuInit(0));
+        CK(cuDeviceGet(&dev, 0));
+        CK(cuDevicePrimaryCtxRetain(&ctx, dev));
+        CK(cuCtxSetCurrent(ctx));
+        CK(cuModuleLoad(&mod, trees_fatbin));
+        const char* names[] = {"frac_level_leaves", "frac_level", "frac_first_stored", "frac_first_leaves",
+                               "frac_sums_stored", "frac_sums_leaves", "frac_bind_sums_stored",
+                               "frac_bind_sums_leaves", "frac_bind_sums_bound", "frac_last_stored",
+                               "frac_last_leaves", "frac_last_bound", "eq_table", "reduce_sums"};
+        CUfunction* fns[] = {&level_leaves, &level, &first_stored, &first_leaves, &sums_stored, &sums_leaves,
+                             &bind_sums_stored, &bind_sums_leaves, &bind_sums_bound, &last_stored, &last_leaves,
+                             &last_bound, &eq_table, &reduce_sums};
+        for (int i = 0; i < 14; i++) CK(cuModuleGetFunction(fns[i], mod, names[i]));
+        CK(cuStreamCreate(&s, CU_STREAM_NON_BLOCKING));
+        // the workspace of Device::fraction_workspace (fraction.rs:160-206)
+        const uint64_t d_len = 2 * std::max<uint64_t>(1ull << (h >= 2 ? h - 2 : 0), 2);
+        const uint64_t n_len = unit ? 2 * std::max<uint64_t>(1ull << (h >= 3 ? h - 3 : 0), 2) : d_len;
+        const uint32_t half = h >= 2 ? (h - 2 + 1) / 2 : 0;
+        const uint64_t eq_len = 2ull << half;
+        for (uint32_t t = 1; t < h; t++) {
+            CUdeviceptr a, b;
+            CK(cuMemAlloc(&a, (2ull << t) * 8));
+            CK(cuMemAlloc(&b, (2ull << t) * 8));
+            num.push_back(a);
+            den.push_back(b);
+        }
+        const uint64_t lens[4] = {n_len, n_len, d_len, d_len};
+        for (int i = 0; i < 4; i++) {
+            CK(cuMemAlloc(&cur[i], lens[i] * 8));
+            CK(cuMemAlloc(&spare[i], lens[i] * 8));
+        }
+        CK(cuMemAlloc(&partials, 6 * SUM_BLOCKS * 8));
+        CK(cuMemAlloc(&sums, 6 * SUM_THREADS * 8));
+        CK(cuMemAlloc(&eq_lo, eq_len * 8));
+        CK(cuMemAlloc(&eq_hi, eq_len * 8));
+        CK(cuMemAlloc(&finals, 64));
+        CK(cuMemAlloc(&points, 2 * 8 * (h + 1)));
+        return true;
+    }
+
+    // Pushes LEAF_ARGS (seven words and unit) then `rest` into one argument list.
+    std::vector<void*> with_leaf(std::initializer_list<void*> rest) {
+        std::vector<void*> a;
+        for (int i = 0; i < 7; i++) a.push_back(&leaf[i]);
+        a.push_back(&unit);
+        a.insert(a.end(), rest.begin(), rest.end());
+        return a;
+    }
+
+    bool launch(CUfunction f, uint32_t blocks, uint32_t threads, std::vector<void*> args) {
+        CK(cuLaunchKernel(f, blocks, 1, 1, threads, 1, 1, 0, s, args.data(), nullptr));
+        return true;
+    }
+
+    bool prove(or_transcript* t) {
+        // levels h − 1 down to 1 (fraction.rs:327-375)
+        for (uint32_t lv = height - 1; lv >= 1; lv--) {
+            uint64_t parents = 1ull << lv;
+            const uint32_t blocks = (uint32_t)((parents + 1023) / 1024);
+            CUdeviceptr no = num[lv - 1], dout = den[lv - 1];
+            if (lv + 1 < height) {
+                CUdeviceptr ni = num[lv], di = den[lv];
+                if (!launch(level, blocks, 1024, {&ni, &di, &no, &dout, &parents})) return false;
+            } else if (!launch(level_leaves, blocks, 1024, with_leaf({&no, &dout, &parents}))) {
+                return false;
+            }
+        }
+        char label[96];
+        std::vector<F2> point;
+        for (uint32_t lvl = 0; lvl < height; lvl++) {
+            uint64_t g[2], lam[2];
+            snprintf(label, sizeof label, "tree/%u/gamma", lvl);
+            or_transcript_challenge_fp2(t, label, g);
+            snprintf(label, sizeof label, "tree/%u/lambda", lvl);
+            or_transcript_challenge_fp2(t, label, lam);
+            const bool stored = lvl + 1 < height;
+            CUdeviceptr nt = stored ? num[lvl] : 0, dt = stored ? den[lvl] : 0;
+            uint32_t level_unit = (!stored && unit == 1) ? 1 : 0;
+            const uint32_t n = (uint32_t)point.size();
+            std::vector<F2> chal;
+            if (n == 0) {
+                if (stored) {
+                    if (!launch(first_stored, 1, 1, {&nt, &dt, &finals})) return false;
+                } else if (!launch(first_leaves, 1, 1, with_leaf({&finals}))) {
+                    return false;
+                }
+            } else {
+                std::vector<uint64_t> pw;
+                for (const F2& x : point) {
+                    pw.push_back(x.a);
+                    pw.push_back(x.b);
+                }
+                CK(cuMemcpyHtoDAsync(points, pw.data(), pw.size() * 8, s));
+                F2 scale = F2_ONE;
+                for (uint32_t j = 0; j < n; j++) {
+                    uint64_t pairs = 1ull << (n - 1 - j);
+                    uint32_t rest = n - 1 - j, lo_bits = (rest + 1) / 2, hi_bits = rest - lo_bits;
+                    uint32_t first = j + 1, first_hi = j + 1 + lo_bits;
+                    if (!launch(eq_table, (uint32_t)std::max<uint64_t>(1, ((1ull << lo_bits) + 1023) / 1024), 1024,
+                                {&points, &first, &lo_bits, &eq_lo}) ||
+                        !launch(eq_table, (uint32_t)std::max<uint64_t>(1, ((1ull << hi_bits) + 1023) / 1024), 1024,
+                                {&points, &first_hi, &hi_bits, &eq_hi}))
+                        return false;
+                    uint32_t blocks = (uint32_t)std::min<uint64_t>(
+                        std::max<uint64_t>((pairs + SUM_THREADS - 1) / SUM_THREADS, 1), SUM_BLOCKS);
+                    uint64_t l0 = lam[0], l1 = lam[1];
+                    uint64_t c0 = chal.empty() ? 0 : chal.back().a, c1 = chal.empty() ? 0 : chal.back().b;
+                    bool good;
+                    if (j == 0 && stored) {
+                        good = launch(sums_stored, blocks, SUM_THREADS,
+                                      {&nt, &dt, &pairs, &l0, &l1, &eq_lo, &lo_bits, &eq_hi, &partials});
+                    } else if (j == 0) {
+                        good = launch(sums_leaves, blocks, SUM_THREADS,
+                                      with_leaf({&pairs, &l0, &l1, &eq_lo, &lo_bits, &eq_hi, &partials}));
+                    } else if (j == 1 && stored) {
+                        good = launch(bind_sums_stored, blocks, SUM_THREADS,
+                                      {&nt, &dt, &c0, &c1, &cur[0], &cur[1], &cur[2], &cur[3], &pairs, &l0, &l1,
+                                       &eq_lo, &lo_bits, &eq_hi, &partials});
+                    } else if (j == 1) {
+                        good = launch(bind_sums_leaves, blocks, SUM_THREADS,
+                                      with_leaf({&c0, &c1, &cur[0], &cur[1], &cur[2], &cur[3], &pairs, &l0, &l1,
+                                                 &eq_lo, &lo_bits, &eq_hi, &partials}));
+                    } else {
+                        good = launch(bind_sums_bound, blocks, SUM_THREADS,
+                                      {&cur[0], &cur[1], &cur[2], &cur[3], &level_unit, &c0, &c1, &spare[0],
+                                       &spare[1], &spare[2], &spare[3], &pairs, &l0, &l1, &eq_lo, &lo_bits, &eq_hi,
+                                       &partials});
+                        for (int i = 0; i < 4; i++) std::swap(cur[i], spare[i]);
+                    }
+                    if (!good) return false;
+                    if (!launch(reduce_sums, 1, SUM_THREADS, {&partials, &blocks, &sums})) return false;
+                    uint64_t w[6];
+                    CK(cuMemcpyDtoHAsync(w, sums, 48, s));
+                    CK(cuStreamSynchronize(s));
+                    const F2 sm[3] = {{w[0], w[1]}, {w[2], w[3]}, {w[4], w[5]}};
+                    const F2 r = point[j];
+                    auto eq_at = [&](F2 c) { return f2add(f2mul(f2sub(F2_ONE, r), f2sub(F2_ONE, c)), f2mul(r, c)); };
+                    const F2 two = {2, 0}, three = {3, 0};
+                    const F2 s3 = f2add(f2sub(sm[0], f2mul(three, sm[1])), f2mul(three, sm[2]));
+                    const F2 m0 = f2mul(f2mul(scale, eq_at(F2{0, 0})), sm[0]);
+                    const F2 m2 = f2mul(f2mul(scale, eq_at(two)), sm[2]);
+                    const F2 m3 = f2mul(f2mul(scale, eq_at(three)), s3);
+                    uint64_t msg[6] = {m0.a, m0.b, m2.a, m2.b, m3.a, m3.b};
+                    snprintf(label, sizeof label, "tree/%u/round/%u", lvl, j);
+                    or_transcript_absorb_fp2s(t, label, msg, 3);
+                    uint64_t c[2];
+                    snprintf(label, sizeof label, "tree/%u/r/%u", lvl, j);
+                    or_transcript_challenge_fp2(t, label, c);
+                    scale = f2mul(scale, eq_at(F2{c[0], c[1]}));
+                    chal.push_back({c[0], c[1]});
+                }
+                uint64_t c0 = chal.back().a, c1 = chal.back().b;
+                bool good;
+                if (n == 1 && stored)
+                    good = launch(last_stored, 1, 1, {&nt, &dt, &c0, &c1, &finals});
+                else if (n == 1)
+                    good = launch(last_leaves, 1, 1, with_leaf({&c0, &c1, &finals}));
+                else
+                    good = launch(last_bound, 1, 1, {&cur[0], &cur[1], &cur[2], &cur[3], &level_unit, &c0, &c1, &finals});
+                if (!good) return false;
+            }
+            uint64_t f[8];
+            CK(cuMemcpyDtoHAsync(f, finals, 64, s));
+            CK(cuStreamSynchronize(s));
+            snprintf(label, sizeof label, "tree/%u/evals", lvl);
+            or_transcript_absorb_fp2s(t, label, f, 4);
+            uint64_t rho[2];
+            snprintf(label, sizeof label, "tree/%u/line", lvl);
+            or_transcript_challenge_fp2(t, label, rho);
+            point.clear();
+            point.push_back({rho[0], rho[1]});
+            point.insert(point.end(), chal.begin(), chal.end());
+        }
+        return true;
+    }
+
+    void close() {
+        for (CUdeviceptr p : num) cuMemFree(p);
+        for (CUdeviceptr p : den) cuMemFree(p);
+        for (int i = 0; i < 4; i++) {
+            if (cur[i]) cuMemFree(cur[i]);
+            if (spare[i]) cuMemFree(spare[i]);
+        }
+        for (CUdeviceptr p : {partials, sums, eq_lo, eq_hi, finals, points})
+            if (p) cuMemFree(p);
+        if (s) cuStreamDestroy(s);
+        if (mod) cuModuleUnload(mod);
+        if (ctx) cuDevicePrimaryCtxRelease(dev);
+    }
+};
+
 // The transcript of the reference benchmark's proofs (gpu_unit_costs.rs transcript()): protocol
 // "tessera-protocol/1", non-interactive, params "bench/1", statement [0x65; 32], session [0x13; 16].
 void bench_transcript(or_transcript* t) {
@@ -581,6 +799,38 @@ int refgpu_pi(const char* trees_fatbin, const char* commit_fatbin, uint32_t s_lo
     }
     Forest f;
     bool good = f.open(trees_fatbin, commit_fatbin, s_log, h);
+    std::vector<double> ts;
+    for (int i = 0; good && i < warmup + runs; i++) {
+        or_transcript t;
+        bench_transcript(&t);
+        const auto t0 = std::chrono::steady_clock::now();
+        good = f.prove(&t);
+        if (good) good = ok(cuStreamSynchronize(f.s), "cuStreamSynchronize");
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (good && i == 0) {
+            memcpy(state, t.state, 32);
+            *counter = t.counter;
+        }
+        if (good && i >= warmup) ts.push_back(dt);
+    }
+    f.close();
+    if (!good) return -1;
+    out[0] = median(ts);
+    return 0;
+}
+
+// One fraction tree of height h: leaf j is (1, α − (k_j + β·v_j)) with unit, else (−m_j, α −
+// (k_j + β·v_j)), k_j = counter(key_seed + j), v_j = counter(value_seed + j), m_j =
+// counter(mult_seed + j) mod 2^16 (fraction.rs:61-105); seeds_ab = {key, value, mult, α0, α1, β0, β1}.
+// out[0]: the median seconds of one proof; state and *counter: the transcript after the first.
+int refgpu_fraction(const char* trees_fatbin, uint32_t h, const uint64_t seeds_ab[7], uint32_t unit, int warmup,
+                    int runs, double* out, uint8_t* state, uint64_t* counter) {
+    if (h < 1 || h > 34 || runs < 1) {
+        g_err = "a fraction tree of height 1..34";
+        return -1;
+    }
+    Fraction f;
+    bool good = f.open(trees_fatbin, h, seeds_ab, unit);
     std::vector<double> ts;
     for (int i = 0; good && i < warmup + runs; i++) {
         or_transcript t;
