@@ -149,6 +149,17 @@ int tg_intt(tg_device *dev, uint32_t log_n, uint64_t *values, size_t nrows);
 int tg_coset_ntt(tg_device *dev, uint32_t log_n, uint64_t shift, uint64_t *values, size_t nrows);
 int tg_coset_intt(tg_device *dev, uint32_t log_n, uint64_t shift, uint64_t *values, size_t nrows);
 
+/* ---- The advice mask stream: ProverDomain::AdviceMasks (crates/tessera-hash/src/domain.rs:83-127)
+ * out[i] is the (first + i)-th word below p of BLAKE3's extended output of
+ * H("advice-masks", seed) in derive-key mode (eight little-endian words per 64-byte output block,
+ * words at or above p skipped), i < count: the masks a prover draws for its advice commitment,
+ * P per row, m_0 first, in row order. seed: at most 64 bytes (a proof seed is 32). The _dev form
+ * writes device memory on `stream` and returns once the values are written; the other host
+ * memory. The values are secret-class: the host form clears its device copy. */
+int tg_advice_masks_dev(tg_device *dev, const uint8_t *seed, size_t seed_len, uint64_t first, size_t count,
+                        uint64_t *out, void *stream);
+int tg_advice_masks(tg_device *dev, const uint8_t *seed, size_t seed_len, uint64_t first, size_t count, uint64_t *out);
+
 /* ---- Column chains and Merkle trees (crates/tessera-hash/src/columns.rs:72-104,
  * crates/tessera-hash/src/merkle.rs:93-113). chains: ncols x 32 bytes. */
 int tg_column_init_dev(tg_device *dev, const uint8_t commitment_id[32], uint64_t ncols, uint8_t *chains,

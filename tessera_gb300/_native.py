@@ -123,6 +123,8 @@ SIGNATURES = {
     "tg_encode_rows_dev": [V, U32, U32, U32, V, SZ, V, V, V],
     "tg_encode_rows": [V, U32, U32, U32, V, SZ, V, V],
     "tg_encode_rows_noalloc_dev": [V, U32, U32, U32, V, SZ, V, V, V],
+    "tg_advice_masks_dev": [V, V, SZ, U64, SZ, V, V],
+    "tg_advice_masks": [V, V, SZ, U64, SZ, V],
     "tg_ntt_dev": [V, U32, V, SZ, V],
     "tg_intt_dev": [V, U32, V, SZ, V],
     "tg_coset_ntt_dev": [V, U32, U64, V, SZ, V],

@@ -317,6 +317,7 @@ int tg_device_close(tg_device* dev) {
     d->scratch_y.release();
     d->scratch_z.release();
     d->scratch_misc.release();
+    d->scratch_aux.release();
     d->scratch_sc.release();
     d->err.release();
     cudaStreamDestroy(d->stream);
@@ -493,6 +494,33 @@ int tg_coset_ntt(tg_device* dev, uint32_t log_n, uint64_t shift, uint64_t* value
 }
 int tg_coset_intt(tg_device* dev, uint32_t log_n, uint64_t shift, uint64_t* values, size_t nrows) {
     return ntt_host(dev, NTT_COSET_INVERSE, log_n, shift, values, nrows);
+}
+
+int tg_advice_masks_dev(tg_device* dev, const uint8_t* seed, size_t seed_len, uint64_t first, size_t count,
+                        uint64_t* out, void* stream) {
+    Device* d = reinterpret_cast<Device*>(dev);
+    if (!d || (seed_len && !seed) || (count && !out)) return fail(TG_ERR_INVALID, "tg_advice_masks_dev: null argument");
+    std::lock_guard<std::mutex> lock(d->mu);
+    return advice_masks(d, seed, seed_len, first, count, out, pick_stream(d, stream));
+}
+
+int tg_advice_masks(tg_device* dev, const uint8_t* seed, size_t seed_len, uint64_t first, size_t count, uint64_t* out) {
+    Device* d = reinterpret_cast<Device*>(dev);
+    if (!d || (seed_len && !seed) || (count && !out)) return fail(TG_ERR_INVALID, "tg_advice_masks: null argument");
+    if (count == 0) return TG_OK;
+    DevBuf v;
+    int rc = v.ensure(count * 8);
+    if (rc) return rc;
+    cudaStream_t s = d->stream;
+    {
+        std::lock_guard<std::mutex> lock(d->mu);
+        rc = advice_masks(d, seed, seed_len, first, count, (uint64_t*)v.ptr, s);
+    }
+    if (rc) return rc;
+    TG_CUDA(cudaMemcpyAsync(out, v.ptr, count * 8, cudaMemcpyDeviceToHost, s));
+    clear(v, s);  // secret-class values are cleared before the memory is released
+    TG_CUDA(cudaStreamSynchronize(s));
+    return TG_OK;
 }
 
 int tg_column_init_dev(tg_device* dev, const uint8_t commitment_id[32], uint64_t ncols, uint8_t* chains, void* stream) {

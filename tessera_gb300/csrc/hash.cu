@@ -11,6 +11,7 @@
 // and its 8-word chaining value never leaves registers.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <string.h>
 
 #include "b3.cuh"
 #include "internal.h"
@@ -247,6 +248,155 @@ int column_merge(Device* d, const uint8_t* segs, size_t nseg, uint64_t n, uint8_
                                                                     (uint32_t*)leaves);
     TG_CUDA(cudaGetLastError());
     return TG_OK;
+}
+
+// ---- the advice mask stream (crates/tessera-hash/src/domain.rs:83-127, ProverDomain::AdviceMasks)
+//
+// The stream is BLAKE3's extended output of H("advice-masks", seed) in derive-key mode: output
+// block t (64 bytes, eight little-endian words) is the root compression of the seed's one block at
+// counter t. The masks are its words below p, in order (rejection sampling). Output blocks are
+// independent, so each thread makes one; the words kept are placed by a count, a scan of the
+// per-CTA counts, and a second pass that recomputes and scatters.
+
+constexpr int MASK_THREADS = 256;
+
+struct MaskSeed {
+    uint32_t key[8];
+    uint32_t m[16];
+    uint32_t len;
+};
+
+__device__ __forceinline__ void mask_block(const MaskSeed& ms, uint64_t t, uint64_t w[8]) {
+    uint32_t out[16];
+    b3::compress_full(ms.key, ms.m, t, ms.len,
+                      b3::DERIVE_KEY_MATERIAL | b3::CHUNK_START | b3::CHUNK_END | b3::ROOT, out);
+#pragma unroll
+    for (int i = 0; i < 8; i++) w[i] = (uint64_t)out[2 * i] | ((uint64_t)out[2 * i + 1] << 32);
+}
+
+// counts[b]: the words below p among CTA b's output blocks (one a thread).
+__global__ void __launch_bounds__(MASK_THREADS) mask_count_kernel(MaskSeed ms, uint64_t nblocks, uint32_t* counts) {
+    __shared__ uint32_t part[MASK_THREADS / 32];
+    const uint64_t t = (uint64_t)blockIdx.x * MASK_THREADS + threadIdx.x;
+    uint32_t c = 0;
+    if (t < nblocks) {
+        uint64_t w[8];
+        mask_block(ms, t, w);
+#pragma unroll
+        for (int i = 0; i < 8; i++) c += w[i] < P;
+    }
+    for (int o = 16; o; o >>= 1) c += __shfl_down_sync(0xFFFFFFFFu, c, o);
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = c;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t sum = 0;
+        for (int i = 0; i < MASK_THREADS / 32; i++) sum += part[i];
+        counts[blockIdx.x] = sum;
+    }
+}
+
+// offsets[b] = Σ_{b' < b} counts[b'], offsets[n] the total; one CTA, in chunks of its width.
+__global__ void __launch_bounds__(1024) mask_scan_kernel(const uint32_t* counts, uint32_t n, uint64_t* offsets) {
+    __shared__ uint64_t warp_sum[32];
+    __shared__ uint64_t carry;
+    if (threadIdx.x == 0) carry = 0;
+    __syncthreads();
+    for (uint32_t base = 0; base < n; base += 1024) {
+        const uint32_t i = base + threadIdx.x;
+        const uint64_t v = i < n ? counts[i] : 0;
+        uint64_t x = v;  // inclusive scan within the warp
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+            if ((threadIdx.x & 31) >= (unsigned)o) x += y;
+        }
+        if ((threadIdx.x & 31) == 31) warp_sum[threadIdx.x >> 5] = x;
+        __syncthreads();
+        if (threadIdx.x < 32) {
+            uint64_t ws = warp_sum[threadIdx.x];
+            for (int o = 1; o < 32; o <<= 1) {
+                const uint64_t y = __shfl_up_sync(0xFFFFFFFFu, ws, o);
+                if (threadIdx.x >= (unsigned)o) ws += y;
+            }
+            warp_sum[threadIdx.x] = ws;  // inclusive over warps
+        }
+        __syncthreads();
+        const uint64_t before = carry + ((threadIdx.x >> 5) ? warp_sum[(threadIdx.x >> 5) - 1] : 0) + x - v;
+        if (i < n) offsets[i] = before;
+        __syncthreads();
+        if (threadIdx.x == 0) carry += warp_sum[31];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) offsets[n] = carry;
+}
+
+// The kept words of CTA b's blocks, in order, from position offsets[b]; those at positions in
+// [first, first + count) land in out[position − first].
+__global__ void __launch_bounds__(MASK_THREADS) mask_scatter_kernel(MaskSeed ms, uint64_t nblocks,
+                                                                    const uint64_t* offsets, uint64_t first,
+                                                                    uint64_t count, uint64_t* out) {
+    __shared__ uint32_t part[MASK_THREADS / 32];
+    const uint64_t t = (uint64_t)blockIdx.x * MASK_THREADS + threadIdx.x;
+    uint64_t w[8];
+    uint32_t c = 0;
+    if (t < nblocks) {
+        mask_block(ms, t, w);
+#pragma unroll
+        for (int i = 0; i < 8; i++) c += w[i] < P;
+    }
+    // exclusive prefix of c over the CTA
+    uint32_t x = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, x, o);
+        if ((threadIdx.x & 31) >= (unsigned)o) x += y;
+    }
+    if ((threadIdx.x & 31) == 31) part[threadIdx.x >> 5] = x;
+    __syncthreads();
+    uint32_t warps_before = 0;
+    for (int i = 0; i < (int)(threadIdx.x >> 5); i++) warps_before += part[i];
+    if (t >= nblocks) return;
+    uint64_t pos = offsets[blockIdx.x] + warps_before + x - c;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        if (w[i] < P) {
+            if (pos >= first && pos - first < count) out[pos - first] = w[i];
+            pos++;
+        }
+    }
+}
+
+int advice_masks(Device* d, const uint8_t* seed, size_t seed_len, uint64_t first, uint64_t count, uint64_t* out,
+                 cudaStream_t s) {
+    if (seed_len > 64) return fail(TG_ERR_INVALID, "a seed of %zu bytes: at most one BLAKE3 block (64)", seed_len);
+    if (count == 0) return TG_OK;
+    MaskSeed ms;
+    context_key("advice-masks", ms.key);
+    uint8_t block[64] = {0};
+    memcpy(block, seed, seed_len);
+    for (int i = 0; i < 16; i++) ms.m[i] = b3::le32(block + 4 * i);
+    ms.len = (uint32_t)seed_len;
+    // words drawn: the values wanted and some slack for rejected words (each word is rejected with
+    // probability below 2^-32); drawn again with more if the slack ran out
+    for (uint64_t slack = 64;; slack *= 16) {
+        const uint64_t words = first + count + slack;
+        const uint64_t nblocks = (words + 7) / 8;
+        const uint64_t ctas = (nblocks + MASK_THREADS - 1) / MASK_THREADS;
+        if (ctas > 0xFFFFFFFFull) return fail(TG_ERR_INVALID, "%llu mask values", (unsigned long long)(first + count));
+        int rc = d->scratch_aux.ensure(ctas * 4 + (ctas + 1) * 8 + 8);
+        if (rc) return rc;
+        uint64_t* offsets = (uint64_t*)d->scratch_aux.ptr;
+        uint32_t* counts = (uint32_t*)(offsets + ctas + 1);
+        {
+            Launch L(d, s, "advice_masks", 3, words);
+            mask_count_kernel<<<(unsigned)ctas, MASK_THREADS, 0, s>>>(ms, nblocks, counts);
+            mask_scan_kernel<<<1, 1024, 0, s>>>(counts, (uint32_t)ctas, offsets);
+            mask_scatter_kernel<<<(unsigned)ctas, MASK_THREADS, 0, s>>>(ms, nblocks, offsets, first, count, out);
+        }
+        TG_CUDA(cudaGetLastError());
+        uint64_t total = 0;
+        TG_CUDA(cudaMemcpyAsync(&total, offsets + ctas, 8, cudaMemcpyDeviceToHost, s));
+        TG_CUDA(cudaStreamSynchronize(s));
+        if (total >= first + count) return TG_OK;
+    }
 }
 
 }  // namespace tg

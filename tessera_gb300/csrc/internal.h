@@ -75,6 +75,7 @@ struct Device {
     cudaEvent_t staged[2] = {nullptr, nullptr}, consumed[2] = {nullptr, nullptr};
     cudaEvent_t ramp[4] = {nullptr, nullptr, nullptr, nullptr};  // the first chunk's pieces landed
     DevBuf err;  // device error words for bounded waits
+    DevBuf scratch_aux;  // the advice mask stream's per-CTA counts and offsets
     // Pinned host memory that small results (a tree level's or a sumcheck batch's transcript
     // states, messages, challenges, evaluations) come back through in one copy and one wait, not a
     // synchronous copy each (readback_ensure grows it; used under mu).
@@ -154,6 +155,10 @@ int column_absorb(Device* d, uint8_t* chains, uint64_t ncols, const uint64_t* ro
                   uint32_t block, cudaStream_t s);
 int merkle_tree(Device* d, const uint8_t* leaves, size_t n, uint8_t* nodes, cudaStream_t s);
 int column_merge(Device* d, const uint8_t* segs, size_t nseg, uint64_t n, uint8_t* leaves, cudaStream_t s);
+// out[i] = the (first + i)-th word below p of the advice mask stream of `seed` (BLAKE3's extended
+// output of H("advice-masks", seed), rejection-sampled), i < count; waits for the stream.
+int advice_masks(Device* d, const uint8_t* seed, size_t seed_len, uint64_t first, uint64_t count, uint64_t* out,
+                 cudaStream_t s);
 
 // ---- openings (opening.cu) -------------------------------------------------------------------
 // The answer to column queries on resident codewords (rows x n) and Merkle nodes (2n − 1

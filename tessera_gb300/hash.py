@@ -199,3 +199,14 @@ class MerkleTree:
 
     def nodes(self) -> np.ndarray:
         return self._nodes
+
+
+def advice_masks(seed: bytes, count: int, first: int = 0, device: Device | None = None) -> np.ndarray:
+    """The advice mask stream of `seed` (ProverDomain::AdviceMasks, crates/tessera-hash/src/
+    domain.rs:83-127): values first .. first + count of the words below p of BLAKE3's extended
+    output of H("advice-masks", seed), computed on the GPU."""
+    d = resolve(device)
+    out = np.zeros(max(1, count), dtype=np.uint64)
+    buf = ctypes.create_string_buffer(bytes(seed), max(1, len(seed)))
+    N.call("tg_advice_masks", d.handle, buf, len(seed), first, count, out.ctypes.data)
+    return out[:count]

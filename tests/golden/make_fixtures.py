@@ -93,7 +93,7 @@ def main() -> None:
     write("blake3.json.gz", load(vec / "blake3" / "test_vectors.json"))
     write("encoding.json.gz", load(vec / "encoding" / "encoding.json"))
     h = load(vec / "hash" / "hash.json")
-    write("hash.json.gz", {k: h[k] for k in ("input_lengths", "domains", "merkle", "columns")})
+    write("hash.json.gz", {k: h[k] for k in ("input_lengths", "domains", "merkle", "columns", "prover_streams")})
     write("transcript.json.gz", load(vec / "transcript" / "transcript.json"))
     s = load(vec / "pcs-streaming" / "streaming.json")
     write("streaming.json.gz", {"cases": s["cases"]})

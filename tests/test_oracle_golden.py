@@ -11,6 +11,8 @@ import pytest
 from golden_data import blake3_input, context_tce, fp2s, load, num, stage_tables
 from oracle import oracle as O
 
+P = 0xFFFFFFFF00000001
+
 
 def test_blake3_official_vectors():
     v = load("blake3")
@@ -126,3 +128,21 @@ def test_sumcheck_stages():
             assert t.state.hex() == st["state"] and t.counter == st["counter"]
             stages += 1
     assert stages == 62
+
+
+def advice_stream(seed: bytes, words: int):
+    raw = O.blake3("derive", seed, 8 * words, key="tessera/v1/advice-masks")
+    return [int.from_bytes(raw[8 * i:8 * i + 8], "little") for i in range(words)]
+
+
+def test_advice_mask_stream():
+    """The advice mask stream (ProverDomain::AdviceMasks): the oracle's BLAKE3 extended output of
+    H("advice-masks", seed), its words below p in order, reproduces the vectors' masks and the
+    pinned seed whose word 6 is rejected."""
+    ps = load("hash")["prover_streams"]
+    words = advice_stream(bytes.fromhex(ps["proof_seed"]), 32)
+    assert [w for w in words if w < P][:24] == [num(x) for x in ps["advice_masks"]]
+    rj = ps["rejection"]
+    words = advice_stream(bytes.fromhex(rj["seed"]), 16)
+    assert words == [num(x) for x in rj["words"]] and words[rj["rejected_word_index"]] >= P
+    assert [w for w in words if w < P] == [num(x) for x in rj["values"]]
