@@ -204,16 +204,34 @@ typedef struct {
 int tg_commit_many(tg_device *dev, tg_commit_job *jobs, int njobs, int workers);
 
 /* A batch of commitments captured once into a CUDA graph and replayed. Creating the plan
- * builds the twiddle tables, allocates the encoder scratch the graph keeps, and (workers = 0)
- * autotunes the worker count over {1, 2, 4, 8} by timing a replay of each candidate on the batch;
- * every launch then re-reads the jobs' row buffers (same addresses, new contents) and writes
- * the codewords, nodes, and the njobs x 32 roots to host `roots`. */
+ * builds the twiddle tables, allocates the encoder scratch the graph keeps, and autotunes on the
+ * batch itself: (1) for each encoder shape (k, rate, rows) with 2^13 <= k <= 2^22, the split of
+ * the row transform k = K1 x K2 (K1 = 2^split_log) and the rows per group, by timing each
+ * candidate's encode of the first job of that shape (or read from the cache file named by the
+ * environment variable TESSERA_GB300_TUNE_CACHE, written after tuning, for a GPU of the same SM
+ * count); (2) with workers = 0, the worker count over {1, 2, 4, 8}, by timing a replay of each
+ * candidate graph. Every launch then re-reads the jobs' row buffers (same addresses, new
+ * contents) and writes the codewords, nodes, and the njobs x 32 roots to host `roots`. */
 typedef struct tg_commit_plan tg_commit_plan;
 int tg_commit_plan_create(tg_device *dev, const tg_commit_job *jobs, int njobs, int workers, tg_commit_plan **out);
 int tg_commit_plan_launch(tg_commit_plan *plan, uint8_t *roots);
 /* The chosen worker count, kernels per replay, and the autotuner's replay times (ms) at
  * 1, 2, 4 and 8 workers (0 where not tried). */
 int tg_commit_plan_info(const tg_commit_plan *plan, int *workers, uint64_t *kernels, double tuned_ms[4]);
+/* The encoder configuration the plan chose for one shape. */
+typedef struct {
+    uint32_t log_k, log_inv_rate;
+    uint64_t npolys;
+    int32_t split_log;   /* log2 K1, the length of passes M1/M2's columns */
+    int32_t candidates;  /* configurations timed (0: read from the cache) */
+    uint64_t group;      /* rows per group */
+    double ms_default;   /* one encode of the shape with the default split and group */
+    double ms_tuned;     /* ... with the chosen ones */
+    int32_t from_cache;
+    int32_t reserved;
+} tg_encode_tuning;
+/* Writes up to cap shapes to out; *count = the plan's number of tuned shapes. */
+int tg_commit_plan_tuning(const tg_commit_plan *plan, tg_encode_tuning *out, int cap, int *count);
 int tg_commit_plan_destroy(tg_commit_plan *plan);
 
 /* merge_segments on host buffers (crates/tessera-pcs/src/streaming.rs:382-404). */

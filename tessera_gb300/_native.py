@@ -52,6 +52,13 @@ class CommitJobC(ctypes.Structure):
                 ("codewords", ctypes.c_void_p), ("nodes", ctypes.c_void_p), ("root", ctypes.c_uint8 * 32)]
 
 
+class EncodeTuningC(ctypes.Structure):
+    _fields_ = [("log_k", ctypes.c_uint32), ("log_inv_rate", ctypes.c_uint32), ("npolys", ctypes.c_uint64),
+                ("split_log", ctypes.c_int32), ("candidates", ctypes.c_int32), ("group", ctypes.c_uint64),
+                ("ms_default", ctypes.c_double), ("ms_tuned", ctypes.c_double), ("from_cache", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
 class ProofRequestC(ctypes.Structure):
     _fields_ = [("log_k", ctypes.c_uint32), ("log_inv_rate", ctypes.c_uint32), ("row_block", ctypes.c_uint32),
                 ("commitment_id", ctypes.c_uint8 * 32), ("rows", ctypes.c_void_p), ("npolys", ctypes.c_size_t),
@@ -164,6 +171,7 @@ SIGNATURES = {
     "tg_commit_plan_create": [V, V, INT, INT, V],
     "tg_commit_plan_launch": [V, V],
     "tg_commit_plan_info": [V, V, V, V],
+    "tg_commit_plan_tuning": [V, V, INT, V],
     "tg_commit_plan_destroy": [V],
     "tg_column_sink_open": [V, U32, U32, U32, U32, V, SZ, V],
     "tg_column_sink_select": [V, V, SZ, V, V],

@@ -9,10 +9,19 @@
 //
 // A plan captures the whole batch (fork from the device stream, the workers' encoders, chains,
 // trees and root copies, join) into one CUDA graph and replays it: one graph launch instead of
-// dozens of kernel launches per commitment. Creating a plan autotunes W over {1, 2, 4, 8} by
-// timing a replay of each candidate graph on the batch itself, and keeps the fastest.
+// dozens of kernel launches per commitment. Creating a plan autotunes in two steps, on the batch
+// itself:
+//   1. per encoder shape (k, rate, rows) of the register-resident encoder: the split of the row
+//      transform k = K1·K2 (which sets the tile shapes of the four passes: 2^13 / L columns of
+//      length L = K1 or K2 per CTA) and the rows per group (the default, or few enough rows that
+//      a group's scratch stays in L2 between passes), each candidate timed on the first job of
+//      that shape; results can be kept in a cache file (TESSERA_GB300_TUNE_CACHE) and read back
+//      by later plans on a GPU with the same SM count;
+//   2. the worker count W over {1, 2, 4, 8}, by timing a replay of each candidate graph.
 #include <cuda_runtime.h>
 #include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <algorithm>
@@ -24,6 +33,7 @@
 struct tg_commit_plan {
     tg::Device* d = nullptr;
     std::vector<tg_commit_job> jobs;
+    std::vector<tg_encode_tuning> shapes;  // the encoder configuration chosen per shape
     cudaGraphExec_t exec = nullptr;
     int workers = 0;
     uint64_t kernels = 0;  // kernel launches one replay performs
@@ -39,6 +49,7 @@ struct CommitWork {
     uint32_t lgk = 0, lgr = 0, block = 0;
     uint64_t n = 0;
     size_t npolys = 0, group = 0;
+    int lgk1 = 0;  // the encoder's split (0: default)
     const Tables* t = nullptr;
     double cost = 0;
     int worker = 0;
@@ -52,10 +63,24 @@ static int check_commit_job(const tg_commit_job& j, int i) {
     return TG_OK;
 }
 
-// Resolves the jobs (tables built, group sizes, costs), assigns them to `nworkers` streams and
-// returns each worker's encoder scratch in bytes (y, z).
+static size_t default_group(Device* d, uint32_t lgk, uint32_t lgr, size_t npolys) {
+    const size_t k = (size_t)1 << lgk, n = k << lgr;
+    return std::min<size_t>(std::max<size_t>(1, d->cfg.lde_group_bytes / ((k + n) * 8)), std::max<size_t>(npolys, 1));
+}
+
+static const tg_encode_tuning* find_shape(const std::vector<tg_encode_tuning>& shapes, uint32_t lgk, uint32_t lgr,
+                                          size_t npolys) {
+    for (const auto& t : shapes)
+        if (t.log_k == lgk && t.log_inv_rate == lgr && t.npolys == npolys) return &t;
+    return nullptr;
+}
+
+// Resolves the jobs (tables built, group sizes and splits — tuned where `shapes` has the job's
+// shape —, costs), assigns them to `nworkers` streams and returns each worker's encoder scratch
+// in bytes (y, z).
 static int plan_work(Device* d, const tg_commit_job* jobs, int njobs, int nworkers, std::vector<CommitWork>& work,
-                     std::vector<size_t>& ybytes, std::vector<size_t>& zbytes) {
+                     std::vector<size_t>& ybytes, std::vector<size_t>& zbytes,
+                     const std::vector<tg_encode_tuning>* shapes = nullptr) {
     work.clear();
     for (int i = 0; i < njobs; i++) {
         const tg_commit_job& j = jobs[i];
@@ -66,8 +91,12 @@ static int plan_work(Device* d, const tg_commit_job* jobs, int njobs, int nworke
         w.block = j.row_block;
         w.n = 1ull << (j.log_k + j.log_inv_rate);
         w.npolys = j.npolys;
-        const size_t k = (size_t)1 << w.lgk;
-        w.group = std::min<size_t>(std::max<size_t>(1, d->cfg.lde_group_bytes / ((k + w.n) * 8)), std::max<size_t>(j.npolys, 1));
+        w.group = default_group(d, w.lgk, w.lgr, j.npolys);
+        if (shapes)
+            if (const tg_encode_tuning* t = find_shape(*shapes, w.lgk, w.lgr, j.npolys)) {
+                w.group = (size_t)t->group;
+                w.lgk1 = t->split_log;
+            }
         int rc = d->get_tables(w.lgk + w.lgr, w.lgk, &w.t);
         if (rc) return rc;
         // the encoder's butterflies per symbol grow with log n; one chain step per block per column
@@ -119,7 +148,7 @@ static int enqueue(Device* d, const tg_commit_job* jobs, const std::vector<Commi
             if (w.worker != wi) continue;
             const tg_commit_job& j = jobs[w.index];
             int rc = lde_encode_into(d, w.lgk, w.lgr, 0, j.rows, w.npolys, nullptr, j.codewords, wk->s, w.t->pw,
-                                     w.t->pow7k, false, ys[wi], zs[wi], w.group);
+                                     w.t->pow7k, false, ys[wi], zs[wi], w.group, w.lgk1);
             if (!rc) rc = column_init(d, j.commitment_id, w.n, j.nodes, wk->s);
             if (!rc) rc = column_absorb(d, j.nodes, w.n, j.codewords, w.n, w.npolys, w.block, wk->s);
             if (!rc) rc = merkle_tree(d, j.nodes, w.n, j.nodes, wk->s);
@@ -134,6 +163,158 @@ static int enqueue(Device* d, const tg_commit_job* jobs, const std::vector<Commi
 }
 
 static int default_workers(int njobs) { return std::max(1, std::min(4, njobs)); }
+
+// ---- the encoder autotuner -----------------------------------------------------------------------
+
+static const char* cache_path() {
+    const char* p = getenv("TESSERA_GB300_TUNE_CACHE");
+    return p && *p ? p : nullptr;
+}
+
+// The cache file holds one line per shape (the last line of a shape wins):
+//   encode <SM count> <log2 k> <log2 inverse rate> <rows> <log2 K1> <rows per group> <ms default> <ms tuned>
+static void cache_read(Device* d, std::vector<tg_encode_tuning>& out) {
+    const char* path = cache_path();
+    if (!path) return;
+    FILE* f = fopen(path, "r");
+    if (!f) return;
+    char line[256];
+    while (fgets(line, sizeof line, f)) {
+        int sm = 0, split = 0;
+        unsigned lgk = 0, lgr = 0;
+        unsigned long long np = 0, group = 0;
+        double md = 0, mb = 0;
+        if (sscanf(line, "encode %d %u %u %llu %d %llu %lf %lf", &sm, &lgk, &lgr, &np, &split, &group, &md, &mb) != 8)
+            continue;
+        if (sm != d->sm_count || lgr < 1 || lgr > 4 || np == 0 || group == 0 || group > np || group > 65535 ||
+            !encode_split_valid(lgk, split))
+            continue;
+        tg_encode_tuning t;
+        memset(&t, 0, sizeof t);
+        t.log_k = lgk;
+        t.log_inv_rate = lgr;
+        t.npolys = np;
+        t.split_log = split;
+        t.group = group;
+        t.ms_default = md;
+        t.ms_tuned = mb;
+        t.from_cache = 1;
+        bool replaced = false;
+        for (auto& o : out)
+            if (o.log_k == lgk && o.log_inv_rate == lgr && o.npolys == np) {
+                o = t;
+                replaced = true;
+            }
+        if (!replaced) out.push_back(t);
+    }
+    fclose(f);
+}
+
+static void cache_append(Device* d, const std::vector<tg_encode_tuning>& fresh) {
+    const char* path = cache_path();
+    if (!path || fresh.empty()) return;
+    FILE* f = fopen(path, "a");
+    if (!f) return;
+    for (const auto& t : fresh)
+        fprintf(f, "encode %d %u %u %llu %d %llu %.4f %.4f\n", d->sm_count, t.log_k, t.log_inv_rate,
+                (unsigned long long)t.npolys, t.split_log, (unsigned long long)t.group, t.ms_default, t.ms_tuned);
+    fclose(f);
+}
+
+// One encode of job j with (split, group) on the device stream: a warm-up, then the faster of two
+// timed runs.
+static int time_encode(Device* d, const tg_commit_job& j, const Tables* t, int split, size_t group, uint64_t* y,
+                       uint64_t* z, cudaEvent_t e0, cudaEvent_t e1, double* ms) {
+    cudaStream_t s = d->stream;
+    double best = -1;
+    for (int rep = 0; rep < 3; rep++) {
+        if (rep) TG_CUDA(cudaEventRecord(e0, s));
+        int rc = lde_encode_into(d, j.log_k, j.log_inv_rate, 0, j.rows, j.npolys, nullptr, j.codewords, s, t->pw,
+                                 t->pow7k, false, y, z, group, split);
+        if (rc) return rc;
+        if (!rep) continue;
+        TG_CUDA(cudaEventRecord(e1, s));
+        TG_CUDA(cudaEventSynchronize(e1));
+        float m = 0;
+        TG_CUDA(cudaEventElapsedTime(&m, e0, e1));
+        if (best < 0 || m < best) best = m;
+    }
+    *ms = best;
+    return TG_OK;
+}
+
+// Step 1 of plan creation: the encoder configuration of every shape of the register-resident
+// encoder among the jobs, from the cache or by timing the candidates on the first job of the shape.
+static int tune_shapes(Device* d, tg_commit_plan* p) {
+    std::vector<tg_encode_tuning> cached, fresh;
+    cache_read(d, cached);
+    int l2 = 0;
+    TG_CUDA(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, d->ordinal));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    TG_CUDA(cudaEventCreate(&e0));
+    cudaError_t ce = cudaEventCreate(&e1);
+    if (ce != cudaSuccess) {
+        cudaEventDestroy(e0);
+        return cuda_fail(ce, "cudaEventCreate");
+    }
+    DevBuf y, z;
+    int rc = TG_OK;
+    for (const tg_commit_job& j : p->jobs) {
+        const int c0 = (int)(j.log_k + 1) / 2;
+        if (j.npolys == 0 || !encode_split_valid(j.log_k, c0)) continue;
+        if (find_shape(p->shapes, j.log_k, j.log_inv_rate, j.npolys)) continue;
+        if (const tg_encode_tuning* c = find_shape(cached, j.log_k, j.log_inv_rate, j.npolys)) {
+            p->shapes.push_back(*c);
+            continue;
+        }
+        const size_t k = (size_t)1 << j.log_k, n = k << j.log_inv_rate;
+        const size_t gd = default_group(d, j.log_k, j.log_inv_rate, j.npolys);
+        // rows whose scratch (k + n words each) fits in three quarters of L2
+        const size_t gl = std::max<size_t>(1, (size_t)l2 * 3 / 4 / ((k + n) * 8));
+        std::vector<int> splits = {c0};
+        for (int c : {c0 - 1, c0 + 1})
+            if (encode_split_valid(j.log_k, c)) splits.push_back(c);
+        std::vector<size_t> groups = {gd};
+        if (gl < gd) groups.push_back(gl);
+        rc = y.ensure(gd * k * 8);
+        if (!rc) rc = z.ensure(gd * n * 8);
+        if (rc) break;
+        const Tables* t = nullptr;
+        rc = d->get_tables(j.log_k + j.log_inv_rate, j.log_k, &t);
+        if (rc) break;
+        tg_encode_tuning best;
+        memset(&best, 0, sizeof best);
+        best.log_k = j.log_k;
+        best.log_inv_rate = j.log_inv_rate;
+        best.npolys = j.npolys;
+        best.ms_tuned = -1;
+        for (int c : splits) {
+            for (size_t g : groups) {
+                double ms = 0;
+                rc = time_encode(d, j, t, c, g, (uint64_t*)y.ptr, (uint64_t*)z.ptr, e0, e1, &ms);
+                if (rc) break;
+                best.candidates++;
+                if (c == c0 && g == gd) best.ms_default = ms;
+                if (best.ms_tuned < 0 || ms < best.ms_tuned) {
+                    best.ms_tuned = ms;
+                    best.split_log = c;
+                    best.group = g;
+                }
+            }
+            if (rc) break;
+        }
+        if (rc) break;
+        fresh.push_back(best);
+        p->shapes.push_back(best);
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (!rc) {
+        TG_CUDA(cudaStreamSynchronize(d->stream));  // the scratch is freed on return
+        cache_append(d, fresh);
+    }
+    return rc;
+}
 
 }  // namespace tg
 
@@ -178,7 +359,7 @@ static int capture(Device* d, tg_commit_plan* p, int nw, cudaGraphExec_t* exec, 
                    std::vector<std::unique_ptr<DevBuf>>& scratch) {
     std::vector<CommitWork> work;
     std::vector<size_t> yb, zb;
-    int rc = plan_work(d, p->jobs.data(), (int)p->jobs.size(), nw, work, yb, zb);
+    int rc = plan_work(d, p->jobs.data(), (int)p->jobs.size(), nw, work, yb, zb, &p->shapes);
     if (rc) return rc;
     scratch.clear();
     std::vector<uint64_t*> ys(nw), zs(nw);
@@ -226,6 +407,11 @@ extern "C" int tg_commit_plan_create(tg_device* dev, const tg_commit_job* jobs, 
     p->d = d;
     p->jobs.assign(jobs, jobs + njobs);
     int rc = p->roots.ensure((size_t)njobs * 32);
+    if (rc) {
+        delete p;
+        return rc;
+    }
+    rc = tune_shapes(d, p);
     if (rc) {
         delete p;
         return rc;
@@ -301,6 +487,13 @@ extern "C" int tg_commit_plan_info(const tg_commit_plan* p, int* workers, uint64
     if (workers) *workers = p->workers;
     if (kernels) *kernels = p->kernels;
     if (tuned_ms) memcpy(tuned_ms, p->tuned_ms, sizeof p->tuned_ms);
+    return TG_OK;
+}
+
+extern "C" int tg_commit_plan_tuning(const tg_commit_plan* p, tg_encode_tuning* out, int cap, int* count) {
+    if (!p || !count || (cap > 0 && !out)) return fail(TG_ERR_INVALID, "tg_commit_plan_tuning: null argument");
+    *count = (int)p->shapes.size();
+    for (int i = 0; i < cap && i < (int)p->shapes.size(); i++) out[i] = p->shapes[i];
     return TG_OK;
 }
 

@@ -134,10 +134,13 @@ int lde_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P, const uint64_t
                const uint64_t* masks, uint64_t* codewords, cudaStream_t s);
 
 // The same encoder over caller-owned tables (pw: n words, pow7k: k words; rebuilt when
-// build_tables) and scratch (y: group x k words, z: group x n words); allocates nothing.
+// build_tables) and scratch (y: group x k words, z: group x n words); allocates nothing. For
+// 2^13 <= k <= 2^22, lgk1 picks the split of the row transform into 2^lgk1 by 2^(lgk − lgk1)
+// (0: the default; encode_split_valid says which are built).
 int lde_encode_into(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P, const uint64_t* rows, size_t npolys,
                     const uint64_t* masks, uint64_t* codewords, cudaStream_t s, uint64_t* pw, uint64_t* pow7k,
-                    bool build_tables, uint64_t* y, uint64_t* z, size_t group);
+                    bool build_tables, uint64_t* y, uint64_t* z, size_t group, int lgk1 = 0);
+bool encode_split_valid(uint32_t lgk, int lgk1);
 
 // Standalone transforms over nrows rows of n = 2^lgn values in place, natural order on both
 // sides (NttPlan::{ntt, intt, coset_ntt, coset_intt}, crates/tessera-pcs/src/ntt.rs:461-516);

@@ -359,18 +359,28 @@ static int fast_rb(int lg) { return lg <= 7 ? 8 : lg <= 9 ? 16 : 32; }
 // Words of one CTA's tile: 8,192 for every column length (32 elements per thread).
 static uint64_t fast_tile(int) { return 8192; }
 
-// Encodes rows in groups through the three register-resident passes; y/z hold `group` rows.
+bool encode_split_valid(uint32_t lgk, int lgk1) {
+    const int lgk2 = (int)lgk - lgk1;
+    return fast_shape(lgk) && lgk1 >= 6 && lgk1 <= 11 && lgk2 >= 6 && lgk2 <= 11;
+}
+
+// Encodes rows in groups through the four register-resident passes; y/z hold `group` rows. The
+// row's transform of length k = K1·K2 splits as K1 = 2^lgk1 (passes M1, M2) by K2 (passes A, C);
+// lgk1 = 0 takes the default, K1 = 2^ceil(lgk/2).
 static int fast_encode(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_t* rows, size_t npolys,
                        const uint64_t* masks, uint64_t* codewords, cudaStream_t s, const uint64_t* pw,
-                       const uint64_t* pow7k, uint64_t* y, uint64_t* z, size_t group) {
+                       const uint64_t* pow7k, uint64_t* y, uint64_t* z, size_t group, int lgk1) {
+    if (lgk1 == 0) lgk1 = (int)(lgk + 1) / 2;
+    if (!encode_split_valid(lgk, lgk1))
+        return fail(TG_ERR_INVALID, "no split of 2^%u into 2^%d columns of 2^%d", lgk, lgk1, (int)lgk - lgk1);
     fast::Args a = {};
     a.pw = pw;
     a.pow7k = pow7k;
     a.lgk = (int)lgk;
     a.lgr = (int)lgr;
     a.P = (int)P_;
-    a.lgk1 = (int)(lgk + 1) / 2;
-    a.lgk2 = (int)lgk / 2;
+    a.lgk1 = lgk1;
+    a.lgk2 = (int)lgk - lgk1;
     a.y = y;
     a.z = z;
     const uint32_t lgn = lgk + lgr;
@@ -465,7 +475,7 @@ namespace tg {
 // of scratch (k and n words per row; unused for k <= 2^11).
 int lde_encode_into(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const uint64_t* rows, size_t npolys,
                     const uint64_t* masks, uint64_t* codewords, cudaStream_t s, uint64_t* pw, uint64_t* pow7k,
-                    bool build_tables, uint64_t* y, uint64_t* z, size_t group) {
+                    bool build_tables, uint64_t* y, uint64_t* z, size_t group, int lgk1) {
     const uint32_t lgn = lgk + lgr;
     const uint64_t k = 1ull << lgk, n = 1ull << lgn;
     if (build_tables) {
@@ -509,7 +519,7 @@ int lde_encode_into(Device* d, uint32_t lgk, uint32_t lgr, uint32_t P_, const ui
     }
     if (fast_shape(lgk)) {
         if (group < 1) return fail(TG_ERR_INVALID, "no scratch for one row");
-        return fast_encode(d, lgk, lgr, P_, rows, npolys, masks, codewords, s, pw, pow7k, y, z, group);
+        return fast_encode(d, lgk, lgr, P_, rows, npolys, masks, codewords, s, pw, pow7k, y, z, group, lgk1);
     }
     a.lgk1 = (int)(lgk + 1) / 2;
     a.lgk2 = (int)lgk / 2;

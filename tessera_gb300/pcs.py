@@ -361,8 +361,16 @@ class CommitPlan:
         w, kern = ctypes.c_int(), ctypes.c_uint64()
         ms = (ctypes.c_double * 4)()
         N.call("tg_commit_plan_info", self._plan, ctypes.byref(w), ctypes.byref(kern), ms)
+        count = ctypes.c_int()
+        N.call("tg_commit_plan_tuning", self._plan, None, 0, ctypes.byref(count))
+        shapes = (N.EncodeTuningC * max(count.value, 1))()
+        N.call("tg_commit_plan_tuning", self._plan, shapes, count.value, ctypes.byref(count))
         return {"workers": w.value, "kernels_per_launch": kern.value,
-                "tuned_ms": {c: ms[i] for i, c in enumerate((1, 2, 4, 8)) if ms[i] > 0}}
+                "tuned_ms": {c: ms[i] for i, c in enumerate((1, 2, 4, 8)) if ms[i] > 0},
+                "encoder_shapes": [{"log_k": t.log_k, "log_inv_rate": t.log_inv_rate, "rows": t.npolys,
+                                    "split_log": t.split_log, "group": t.group, "candidates": t.candidates,
+                                    "ms_default": t.ms_default, "ms_tuned": t.ms_tuned,
+                                    "from_cache": bool(t.from_cache)} for t in shapes[:count.value]]}
 
     def close(self):
         if self._plan:

@@ -15,7 +15,8 @@ HEADER = Path(__file__).resolve().parent.parent / "include" / "tessera_gb300.h"
 MIRRORS = {"tg_config": N.Config, "tg_transcript": N.TranscriptState, "tg_table": N.TableC,
            "tg_instance": N.InstanceC, "tg_commit_job": N.CommitJobC, "tg_proof_request": N.ProofRequestC,
            "tg_proof_result": N.ProofResultC, "tg_server_stats": N.ServerStatsC, "tg_leaf_gen": N.LeafGenC,
-           "tg_tree": N.TreeC, "tg_tree_level_proof": N.TreeLevelProofC, "tg_sumcheck_job": N.SumcheckJobC}
+           "tg_tree": N.TreeC, "tg_tree_level_proof": N.TreeLevelProofC, "tg_sumcheck_job": N.SumcheckJobC,
+           "tg_encode_tuning": N.EncodeTuningC}
 
 
 def c_fields(name: str) -> list[str]:

@@ -257,6 +257,51 @@ def test_commit_plan_replays(dev):
         plan.close()
 
 
+def test_commit_plan_tuning_cache(dev, tmp_path, monkeypatch):
+    """Encoder configurations read from the tuning cache — splits of the row transform other than
+    the default (columns of 2,048 in passes A/C or M1/M2 among them) and groups of one to three
+    rows — commit exactly what the plain path commits; a plan over shapes missing from the cache
+    times their candidates and appends one line per shape."""
+    import torch
+
+    from tessera_gb300.pcs import CommitmentParams, CommitPlan
+    from tessera_gb300.workloads import splitmix_words
+
+    sm = torch.cuda.get_device_properties(dev.ordinal).multi_processor_count
+    # (log k, log inverse rate, rows, log K1, rows per group)
+    forced = [(13, 1, 4, 7, 2), (16, 1, 8, 7, 3), (19, 2, 4, 11, 1), (20, 1, 2, 9, 1), (21, 1, 2, 10, 1)]
+    cache = tmp_path / "tune.txt"
+    cache.write_text("".join(f"encode {sm} {lk} {lr} {np_} {c} {g} 1.0 1.0\n" for lk, lr, np_, c, g in forced)
+                     + "encode 1 13 1 4 6 1 1.0 1.0\nnot a line\n")
+    monkeypatch.setenv("TESSERA_GB300_TUNE_CACHE", str(cache))
+    params = [CommitmentParams(lk, lr, 0, 32, bytes([lk]) * 32) for lk, lr, _, _, _ in forced]
+    rows = [torch.from_numpy(splitmix_words(0x7700 + i, np_ << lk).view(np.int64)).to(f"cuda:{dev.ordinal}")
+            for i, (lk, _, np_, _, _) in enumerate(forced)]
+    plan = CommitPlan(params, rows, device=dev, workers=2)
+    try:
+        shapes = {(s["log_k"], s["log_inv_rate"], s["rows"]): s for s in plan.info()["encoder_shapes"]}
+        for lk, lr, np_, c, g in forced:
+            s = shapes[(lk, lr, np_)]
+            assert s["from_cache"] and s["split_log"] == c and s["group"] == g
+        for p, r, c, root in zip(params, rows, plan.commitments, plan.launch()):
+            proot, nodes, cw = _plain(dev, p, r)
+            assert root == proot and torch.equal(c.nodes, nodes) and torch.equal(c.codewords, cw)
+    finally:
+        plan.close()
+    before = cache.read_text().count("\n")
+    extra = [CommitmentParams(15, 2, 0, 32, bytes(32))]
+    xrows = [torch.from_numpy(splitmix_words(0x7800, 16 << 15).view(np.int64)).to(f"cuda:{dev.ordinal}")]
+    plan = CommitPlan(extra, xrows, device=dev, workers=1)
+    try:
+        (s,) = plan.info()["encoder_shapes"]
+        assert not s["from_cache"] and s["candidates"] >= 2 and s["ms_tuned"] <= s["ms_default"]
+        assert plan.launch()[0] == _plain(dev, extra[0], xrows[0])[0]
+    finally:
+        plan.close()
+    lines = cache.read_text().splitlines()
+    assert len(lines) == before + 1 and lines[-1].startswith(f"encode {sm} 15 2 16 ")
+
+
 def test_commit_many_large_shapes(dev):
     """The batched workload with k up to 2^18 and up to 128 rows per commitment: batched equals
     plain on every root."""
