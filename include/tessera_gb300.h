@@ -73,6 +73,13 @@ int tg_device_launches(tg_device *dev, uint64_t *launches);
  * driver, zeroed first. tg_device_close does the same. */
 int tg_device_trim(tg_device *dev);
 
+/* Reads one byte of every page of a host buffer on the calling thread. On the GB300's Arm host a
+ * copy to the device from host memory that the CPU has not read or written for some seconds can
+ * run at a small fraction of the link's speed (measured: 64 MiB requests at 7-13 GB/s instead of
+ * about 190 GB/s); reading its pages first restores the full speed, for well under a millisecond
+ * per 64 MiB. The proof server does this for each request's rows and tables on submission. */
+int tg_host_prefault(const void *p, size_t bytes);
+
 /* Integer-pipe peaks of the device, measured with register-only microbenchmarks (no reference
  * counterpart: these are the denominators of the integer-bound kernels' rooflines). Rates per
  * second over the whole GPU: mad.wide.u32 operations, Goldilocks products, radix-2 butterflies

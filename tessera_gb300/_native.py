@@ -172,6 +172,7 @@ SIGNATURES = {
     "tg_commit_plan_launch": [V, V],
     "tg_commit_plan_info": [V, V, V, V],
     "tg_commit_plan_tuning": [V, V, INT, V],
+    "tg_host_prefault": [V, SZ],
     "tg_commit_plan_destroy": [V],
     "tg_column_sink_open": [V, U32, U32, U32, U32, V, SZ, V],
     "tg_column_sink_select": [V, V, SZ, V, V],

@@ -7,6 +7,7 @@
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
+#include <unistd.h>
 
 #include <algorithm>
 #include <string>
@@ -229,6 +230,21 @@ struct tg_matrix {
     bool closed = false, finished = false;
 };
 
+namespace tg {
+void host_prefault(const void* p, size_t bytes) {
+    if (!p || !bytes) return;
+    static const size_t page = [] {
+        const long v = sysconf(_SC_PAGESIZE);
+        return v > 0 ? (size_t)v : (size_t)4096;
+    }();
+    const volatile uint8_t* b = static_cast<const volatile uint8_t*>(p);
+    uint8_t acc = 0;
+    for (size_t i = 0; i < bytes; i += page) acc ^= b[i];
+    acc ^= b[bytes - 1];
+    (void)acc;
+}
+}  // namespace tg
+
 extern "C" {
 
 int tg_version(void) { return 1; }
@@ -396,6 +412,12 @@ int tg_device_trim(tg_device* dev) {
     Device* d = reinterpret_cast<Device*>(dev);
     if (!d) return fail(TG_ERR_INVALID, "null device");
     spare_trim(d);
+    return TG_OK;
+}
+
+int tg_host_prefault(const void* p, size_t bytes) {
+    if (!p && bytes) return fail(TG_ERR_INVALID, "tg_host_prefault: null buffer");
+    host_prefault(p, bytes);
     return TG_OK;
 }
 

@@ -110,6 +110,9 @@ int readback_ensure(Device* d, size_t bytes);
 
 cudaStream_t pick_stream(Device* d, void* stream);
 
+// Reads one byte of every page of a host buffer (tg_host_prefault).
+void host_prefault(const void* p, size_t bytes);
+
 // The workspace cache: b (empty) gets a spare buffer of at least `want` bytes (at most twice that)
 // or a new one; spare_give returns b's memory to the cache (a borrowed buffer is only dropped);
 // spare_trim zeroes and frees every spare buffer.

@@ -445,6 +445,9 @@ extern "C" int tg_server_submit(tg_server* sv, const tg_proof_request* req, tg_p
     if (rc) return rc;
     if (req->queries && (!out->query_indices || !out->columns || !out->siblings))
         return fail(TG_ERR_INVALID, "an opening round needs the result's index, column and sibling buffers");
+    // the request's host buffers are read by copies soon: their pages, touched now, copy at full speed
+    host_prefault(req->rows, req->npolys * ((size_t)8 << req->log_k));
+    for (int k = 0; k < req->ntables; k++) host_prefault(req->tables[k], (size_t)8 << req->vars);
     ServeReq* r = new ServeReq();
     r->req = *req;
     r->table_ptrs.assign(req->tables, req->tables + req->ntables);

@@ -177,6 +177,10 @@ def prove_plain(req: ProofRequest, device: Device | None = None) -> ProofResult:
     p = req.params
     rows = _words(req.rows)
     npolys = rows.size >> p.log2_k
+    # as the server does on submission: the host pages are touched before they are copied
+    for x in [rows] + [_words(t) for t in req.tables]:
+        if x.size:
+            N.call("tg_host_prefault", ctypes.c_void_p(x.ctypes.data), x.nbytes)
     root = ctypes.create_string_buffer(32)
     cid = (ctypes.c_uint8 * 32)(*bytes(p.commitment_id))
     resident = None

@@ -79,3 +79,17 @@ def test_device_calls_fail_loudly_without_a_gpu():
     h = ctypes.c_void_p()
     with pytest.raises(N.TesseraError):
         N.call("tg_device_open", 0, None, ctypes.byref(h))
+
+
+def test_host_prefault():
+    """tg_host_prefault reads every page of a host buffer and touches nothing on a device."""
+    import numpy as np
+
+    buf = np.arange(3 << 17, dtype=np.uint64)
+    before = buf.copy()
+    N.call("tg_host_prefault", ctypes.c_void_p(buf.ctypes.data), buf.nbytes)
+    N.call("tg_host_prefault", ctypes.c_void_p(buf.ctypes.data), 1)
+    N.call("tg_host_prefault", None, 0)
+    assert np.array_equal(buf, before)
+    with pytest.raises(N.TesseraError):
+        N.call("tg_host_prefault", None, 8)
