@@ -394,10 +394,14 @@ def run_gpu(args) -> None:
         e2e_ms = float(tt.item())
     h2d = COMMITTED * 8 + 3 * (1 << SC_VARS) * 8
     d2h = 32 + SC_VARS * SC_DEGREE * 16 + 3 * 16
-    # Release torch's buffers while the library's stream (which their copies used) still exists.
+    # Release torch's buffers while the library's stream (which their copies used) still exists,
+    # and return torch's cached pinned blocks while the context is certainly alive.
     stream.synchronize()
-    del rows_hw, tabs_hw, rows_h, tabs_h, rows_d, tabs_d, cw_d, nodes_d
+    del rows_hw, tabs_hw, rows_h, tabs_h, rows_d, tabs_d, cw_d, nodes_d, link
     torch.cuda.synchronize()
+    torch.cuda.empty_cache()
+    if hasattr(torch._C, "_host_emptyCache"):
+        torch._C._host_emptyCache()
     dev.close()
 
     if rank != 0:

@@ -449,7 +449,9 @@ int tg_encode_rows(tg_device* dev, uint32_t log_k, uint32_t log_inv_rate, uint32
     if (!rc) rc = c.ensure(nrows * n * 8);
     if (rc) return rc;
     cudaStream_t s = d->stream;
+    host_prefault(rows, nrows * k * 8);
     TG_CUDA(cudaMemcpyAsync(r.ptr, rows, nrows * k * 8, cudaMemcpyHostToDevice, s));
+    if (mask_coeffs) host_prefault(masks, nrows * mask_coeffs * 8);
     if (mask_coeffs) TG_CUDA(cudaMemcpyAsync(m.ptr, masks, nrows * mask_coeffs * 8, cudaMemcpyHostToDevice, s));
     {
         std::lock_guard<std::mutex> lock(d->mu);
@@ -482,6 +484,7 @@ static int ntt_host(tg_device* dev, int kind, uint32_t log_n, uint64_t shift, ui
     int rc = v.ensure(bytes);
     if (rc) return rc;
     cudaStream_t s = d->stream;
+    host_prefault(values, bytes);
     TG_CUDA(cudaMemcpyAsync(v.ptr, values, bytes, cudaMemcpyHostToDevice, s));
     {
         std::lock_guard<std::mutex> lock(d->mu);
@@ -655,6 +658,7 @@ int tg_commit_unmasked(tg_device* dev, uint32_t log_k, uint32_t log_inv_rate, ui
             }
             at = 0;
             for (size_t q = 0; q < np; q++) {
+                host_prefault(rows + at * k, piece[q] * k * 8);
                 TG_CUDA(cudaMemcpyAsync(half + at * k, rows + at * k, piece[q] * k * 8, cudaMemcpyHostToDevice, cs));
                 TG_CUDA(cudaEventRecord(d->ramp[q], cs));
                 at += piece[q];
@@ -667,6 +671,7 @@ int tg_commit_unmasked(tg_device* dev, uint32_t log_k, uint32_t log_inv_rate, ui
                 at += piece[q];
             }
         } else {
+            host_prefault(rows + r0 * k, g * k * 8);
             TG_CUDA(cudaMemcpyAsync(half, rows + r0 * k, g * k * 8, cudaMemcpyHostToDevice, cs));
             TG_CUDA(cudaEventRecord(d->staged[b], cs));
             TG_CUDA(cudaStreamWaitEvent(s, d->staged[b], 0));
@@ -747,7 +752,9 @@ int tg_sink_absorb(tg_sink* sk, const uint64_t* rows, size_t nrows, const uint64
     Device* d = sk->d;
     cudaStream_t s = d->stream;
     const size_t k = (size_t)1 << sk->lgk;
+    host_prefault(rows, nrows * k * 8);
     TG_CUDA(cudaMemcpyAsync(sk->rows.ptr, rows, nrows * k * 8, cudaMemcpyHostToDevice, s));
+    if (sk->P) host_prefault(masks, nrows * sk->P * 8);
     if (sk->P) TG_CUDA(cudaMemcpyAsync(sk->masks.ptr, masks, nrows * sk->P * 8, cudaMemcpyHostToDevice, s));
     std::lock_guard<std::mutex> lock(d->mu);
     int rc = lde_encode(d, sk->lgk, sk->lgr, sk->P, (const uint64_t*)sk->rows.ptr, nrows,
@@ -829,6 +836,7 @@ int tg_matrix_absorb(tg_matrix* m, const uint64_t* rows, size_t nrows, uint64_t*
     Device* d = m->d;
     cudaStream_t s = d->stream;
     const size_t k = (size_t)1 << m->lgk;
+    host_prefault(rows, nrows * k * 8);
     TG_CUDA(cudaMemcpyAsync(m->rows.ptr, rows, nrows * k * 8, cudaMemcpyHostToDevice, s));
     std::lock_guard<std::mutex> lock(d->mu);
     int rc = lde_encode(d, m->lgk, m->lgr, 0, (const uint64_t*)m->rows.ptr, nrows, nullptr, (uint64_t*)m->cw.ptr, s);

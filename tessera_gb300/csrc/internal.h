@@ -64,6 +64,7 @@ struct Device {
     cudaStream_t stream = nullptr;
     int sm_count = 0;
     size_t smem_optin = 0;
+    int coop = -1;  // cooperative launches supported (1) or not (0); −1 until asked
     std::mutex mu;  // guards the caches and the shared scratch below
     std::map<uint64_t, Tables> tables;
     DevBuf scratch_y, scratch_z, scratch_misc;

@@ -194,6 +194,7 @@ int tg_level_load(tg_device* dev, int shape, const uint64_t lambda[2], const uin
     for (int k = 0; k < columns && !rc; k++) {
         rc = l->buf[0][k].ensure(len * 16);
         if (!rc) rc = l->buf[1][k].ensure(std::max<size_t>(len / 2, 1) * 16);
+        if (!rc) host_prefault(tables[k], len * 16);
         if (!rc && cudaMemcpyAsync(l->buf[0][k].ptr, tables[k], len * 16, cudaMemcpyHostToDevice, d->stream) != cudaSuccess)
             rc = fail(TG_ERR_CUDA, "level table upload failed");
     }

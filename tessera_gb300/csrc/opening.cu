@@ -173,7 +173,9 @@ static int sink_run(tg_column_sink* sk, const uint64_t* rows, size_t nrows, cons
         if (rc) return rc;
         TG_CUDA(cudaMemcpyAsync(sk->coeff.ptr, coefficients, groups * nrows * 16, cudaMemcpyHostToDevice, s));
     }
+    host_prefault(rows, nrows * k * 8);
     TG_CUDA(cudaMemcpyAsync(sk->rows.ptr, rows, nrows * k * 8, cudaMemcpyHostToDevice, s));
+    if (sk->P) host_prefault(masks, nrows * sk->P * 8);
     if (sk->P) TG_CUDA(cudaMemcpyAsync(sk->masks.ptr, masks, nrows * sk->P * 8, cudaMemcpyHostToDevice, s));
     std::lock_guard<std::mutex> lock(d->mu);
     if (coefficients) {

@@ -38,9 +38,14 @@ constexpr int SC_MAX_DEGREE = 7;
 constexpr int SC_THREADS = 256;
 constexpr int SC_MAX_SEG_BLOCKS = 1024;
 constexpr int SC_MSG_WORDS = 2 * SC_MAX_DEGREE;  // one instance's round sums, as Fp2 words
-// The last rounds run in one block (sc_tail) from the first whose segments hold this many pairs in
-// all, when every job has a warp of that block for its transcript.
-constexpr uint64_t SC_TAIL_PAIRS = 4096;
+// The last rounds run in one block from the first whose segments hold this many pairs in all,
+// when every job has a warp of that block for its transcript (fewer when the rounds before them
+// run in the same launch as well).
+constexpr uint64_t SC_TAIL_PAIRS = 4096, SC_TAIL_PAIRS_PERSIST = 512;
+// With cooperative launches, the rounds from the first whose segments hold at most this many pairs
+// in all run in one launch of sc_persist, on at most SC_PERSIST_BLOCKS blocks.
+constexpr uint64_t SC_PERSIST_PAIRS = 1ull << 16;
+constexpr int SC_PERSIST_BLOCKS = 128;
 
 // One instance's share of one launch.
 struct Seg {
@@ -52,7 +57,7 @@ struct Seg {
     uint32_t base_mask;                  // bit k: table k's source holds prime-field words
     int nt, degree, bind, kind;          // kind 0: round sums, 1: Σ_x Π_k T_k[x]
     int block0, nblocks, part0;          // the segment's blocks in the launch, its first partials row
-    int pad_;
+    int inst;                            // the instance
 };
 static_assert(sizeof(Seg) % 8 == 0, "Seg copies as words");
 
@@ -68,10 +73,19 @@ struct EvalRef {
     int base, pad_;
 };
 
+// CG: through L2 only, for tables that other blocks of the same launch wrote (the persistent rounds).
+template <bool CG = false>
 __device__ __forceinline__ fp2 load_entry(const uint64_t* t, bool base, uint64_t i) {
-    if (base) return e_lift(t[i]);
-    const ulonglong2 v = reinterpret_cast<const ulonglong2*>(t)[i];  // (c0, c1) words
+    if (base) return e_lift(CG ? __ldcg(t + i) : t[i]);
+    const ulonglong2 v = CG ? __ldcg(reinterpret_cast<const ulonglong2*>(t) + i)
+                            : reinterpret_cast<const ulonglong2*>(t)[i];  // (c0, c1) words
     return {v.x, v.y};
+}
+
+// The challenge to bind, written by the previous round's transcript.
+template <bool CG>
+__device__ __forceinline__ fp2 load_r(const uint64_t* r) {
+    return CG ? fp2{__ldcg(r), __ldcg(r + 1)} : fp2{r[0], r[1]};
 }
 
 // a + r·(b − a) on lazy words (bound tables hold lazy words; the last bind canonicalises); r7 =
@@ -105,9 +119,143 @@ __device__ __forceinline__ void block_sum(uint64_t (&v)[NW]) {
     __syncthreads();
 }
 
+// A table's 16 bytes at p, streamed (every entry is read once per round); CG: through L2 only.
+template <bool CG>
+__device__ __forceinline__ ulonglong2 ld_once(const uint64_t* t, uint64_t p) {
+    ulonglong2 v;
+    if constexpr (CG)
+        asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(t + 2 * p));
+    else
+        asm volatile("ld.global.cs.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(t + 2 * p));
+    return v;
+}
+
+// Block lb's share of a segment of the commonest shapes — NT tables multiplied at degree DEG (three
+// at degree 3: Σ f·g·h; two at degree 2: Σ f·g) — with the tables' field fixed at compile time:
+// the first round (prime-field tables, nothing to bind) sums in the prime field; the later rounds
+// bind r into their source (prime-field or Fp2 entries), store the bound pair and sum in Fp2. All
+// of a thread's loads for U pairs are issued before any is used, so that each thread keeps
+// U·NT·(1, 2 or 4) 16-byte loads in flight.
+template <int D, int NT, int DEG, bool BIND, bool SRC_BASE, int U, bool CG>
+__device__ __forceinline__ void seg_sums_fixed(const Seg& g, int lb, uint64_t (&words)[2 * D]) {
+    static_assert(DEG <= D && NT <= DEG && (BIND || SRC_BASE), "shape");
+    const uint64_t stride = (uint64_t)g.nblocks * blockDim.x, n = g.n;
+    const uint64_t start = (uint64_t)lb * blockDim.x + threadIdx.x;
+    if constexpr (!BIND) {
+        uint64_t acc[DEG];
+#pragma unroll
+        for (int d = 0; d < DEG; d++) acc[d] = 0;
+        for (uint64_t p0 = start; p0 < n; p0 += U * stride) {
+            ulonglong2 x[U][NT];
+#pragma unroll
+            for (int q = 0; q < U; q++) {
+                const uint64_t p = p0 + q * stride;
+#pragma unroll
+                for (int k = 0; k < NT; k++) x[q][k] = p < n ? ld_once<CG>(g.src[k], p) : make_ulonglong2(0, 0);
+            }
+#pragma unroll
+            for (int q = 0; q < U; q++) {
+                uint64_t prod[DEG];
+#pragma unroll
+                for (int k = 0; k < NT; k++) {
+                    const uint64_t u = x[q][k].x, v = x[q][k].y, diff = lz::sub(v, u);
+                    uint64_t t = v;  // node 1, then 2, 3, …
+                    prod[0] = k ? lz::mul(prod[0], u) : u;
+#pragma unroll
+                    for (int d = 1; d < DEG; d++) {
+                        t = lz::add(t, diff);
+                        prod[d] = k ? lz::mul(prod[d], t) : t;
+                    }
+                }
+#pragma unroll
+                for (int d = 0; d < DEG; d++) acc[d] = lz::add(acc[d], prod[d]);
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < DEG; d++) words[2 * d] = lz::canon(acc[d]);
+    } else {
+        const fp2 r = load_r<CG>(g.r);
+        const uint64_t r7 = lz::mul7(r.c1);
+        constexpr int L = SRC_BASE ? 2 : 4;  // 16-byte loads per table and pair: 4 source entries
+        fp2 acc[DEG];
+#pragma unroll
+        for (int d = 0; d < DEG; d++) acc[d] = {0, 0};
+        for (uint64_t p0 = start; p0 < n; p0 += U * stride) {
+            ulonglong2 x[U][NT][L];
+#pragma unroll
+            for (int q = 0; q < U; q++) {
+                const uint64_t p = p0 + q * stride;
+#pragma unroll
+                for (int k = 0; k < NT; k++)
+#pragma unroll
+                    for (int l = 0; l < L; l++) x[q][k][l] = p < n ? ld_once<CG>(g.src[k], L * p + l) : make_ulonglong2(0, 0);
+            }
+#pragma unroll
+            for (int q = 0; q < U; q++) {
+                const uint64_t p = p0 + q * stride;
+                fp2 prod[DEG];
+#pragma unroll
+                for (int k = 0; k < NT; k++) {
+                    fp2 u, v;
+                    if constexpr (SRC_BASE) {  // entries 4p, 4p + 1 | 4p + 2, 4p + 3 as words
+                        u = bind_pair(e_lift(x[q][k][0].x), e_lift(x[q][k][0].y), r, r7, true);
+                        v = bind_pair(e_lift(x[q][k][1].x), e_lift(x[q][k][1].y), r, r7, true);
+                    } else {
+                        u = bind_pair({x[q][k][0].x, x[q][k][0].y}, {x[q][k][1].x, x[q][k][1].y}, r, r7, false);
+                        v = bind_pair({x[q][k][2].x, x[q][k][2].y}, {x[q][k][3].x, x[q][k][3].y}, r, r7, false);
+                    }
+                    if (p < n) {
+                        ulonglong2* out = reinterpret_cast<ulonglong2*>(g.dst[k]);
+                        out[2 * p] = make_ulonglong2(u.c0, u.c1);
+                        out[2 * p + 1] = make_ulonglong2(v.c0, v.c1);
+                    }
+                    const fp2 diff = l2_sub(v, u);
+                    fp2 t = v;
+                    prod[0] = k ? l2_muls(prod[0], u) : u;
+#pragma unroll
+                    for (int d = 1; d < DEG; d++) {
+                        t = l2_add(t, diff);
+                        prod[d] = k ? l2_muls(prod[d], t) : t;
+                    }
+                }
+#pragma unroll
+                for (int d = 0; d < DEG; d++) acc[d] = l2_add(acc[d], prod[d]);
+            }
+        }
+#pragma unroll
+        for (int d = 0; d < DEG; d++) {
+            const fp2 c = l2_canon(acc[d]);
+            words[2 * d] = c.c0;
+            words[2 * d + 1] = c.c1;
+        }
+    }
+}
+
+// The shapes seg_sums_fixed covers; false leaves the segment to the general loops.
+template <int D, bool CG = false>
+__device__ __forceinline__ bool seg_sums_fast(const Seg& g, int lb, uint64_t (&words)[2 * D]) {
+    if (g.kind != 0) return false;
+    const bool all_base = g.base_mask == (1u << g.nt) - 1, all_ext = g.base_mask == 0;
+    if constexpr (D >= 3) {
+        if (g.nt == 3 && g.degree == 3) {
+            if (!g.bind && all_base) return seg_sums_fixed<D, 3, 3, false, true, 4, CG>(g, lb, words), true;
+            if (g.bind && all_base) return seg_sums_fixed<D, 3, 3, true, true, 2, CG>(g, lb, words), true;
+            if (g.bind && all_ext) return seg_sums_fixed<D, 3, 3, true, false, 1, CG>(g, lb, words), true;
+        }
+    }
+    if constexpr (D >= 2) {
+        if (g.nt == 2 && g.degree == 2) {
+            if (!g.bind && all_base) return seg_sums_fixed<D, 2, 2, false, true, 4, CG>(g, lb, words), true;
+            if (g.bind && all_base) return seg_sums_fixed<D, 2, 2, true, true, 2, CG>(g, lb, words), true;
+            if (g.bind && all_ext) return seg_sums_fixed<D, 2, 2, true, false, 2, CG>(g, lb, words), true;
+        }
+    }
+    return false;
+}
+
 // Block lb's share of a segment's sums (a grid-stride loop over the segment's nblocks blocks),
 // canonical, in this thread's words: the d node sums as Fp2 words (kind 0), or the product sum.
-template <int D>
+template <int D, bool CG = false>
 __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&words)[2 * D]) {
     const uint64_t stride = (uint64_t)g.nblocks * blockDim.x;
     const int deg = g.degree, nt = g.nt;
@@ -120,7 +268,7 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
         for (uint64_t x = (uint64_t)lb * blockDim.x + threadIdx.x; x < g.n; x += stride) {
             fp2 prod = {1, 0};
             for (int k = 0; k < nt; k++) {
-                const fp2 e = load_entry(g.src[k], (g.base_mask >> k) & 1, x);
+                const fp2 e = load_entry<CG>(g.src[k], (g.base_mask >> k) & 1, x);
                 prod = k ? l2_muls(prod, e) : e;
             }
             acc = l2_add(acc, prod);
@@ -138,7 +286,8 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
 #pragma unroll
             for (int d = 0; d < D; d++) prod[d] = 1;
             for (int k = 0; k < nt; k++) {  // the first table's values start the products
-                const ulonglong2 v = reinterpret_cast<const ulonglong2*>(g.src[k])[p];
+                const ulonglong2 v = CG ? __ldcg(reinterpret_cast<const ulonglong2*>(g.src[k]) + p)
+                                        : reinterpret_cast<const ulonglong2*>(g.src[k])[p];
                 const uint64_t diff = lz::sub(v.y, v.x);
                 uint64_t x = v.y;  // value at node 1
                 prod[0] = k ? lz::mul(prod[0], v.x) : v.x;
@@ -159,7 +308,7 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
         fp2 acc[D];
 #pragma unroll
         for (int d = 0; d < D; d++) acc[d] = {0, 0};
-        const fp2 r = g.bind ? fp2{g.r[0], g.r[1]} : fp2{0, 0};
+        const fp2 r = g.bind ? load_r<CG>(g.r) : fp2{0, 0};
         const uint64_t r7 = lz::mul7(r.c1);
         for (uint64_t p = (uint64_t)lb * blockDim.x + threadIdx.x; p < g.n; p += stride) {
             fp2 prod[D];
@@ -169,14 +318,16 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
                 const bool base = (g.base_mask >> k) & 1;
                 fp2 u, v;
                 if (g.bind) {
-                    u = bind_pair(load_entry(g.src[k], base, 4 * p), load_entry(g.src[k], base, 4 * p + 1), r, r7, base);
-                    v = bind_pair(load_entry(g.src[k], base, 4 * p + 2), load_entry(g.src[k], base, 4 * p + 3), r, r7, base);
+                    u = bind_pair(load_entry<CG>(g.src[k], base, 4 * p), load_entry<CG>(g.src[k], base, 4 * p + 1), r, r7,
+                                  base);
+                    v = bind_pair(load_entry<CG>(g.src[k], base, 4 * p + 2), load_entry<CG>(g.src[k], base, 4 * p + 3), r,
+                                  r7, base);
                     ulonglong2* out = reinterpret_cast<ulonglong2*>(g.dst[k]);
                     out[2 * p] = make_ulonglong2(u.c0, u.c1);
                     out[2 * p + 1] = make_ulonglong2(v.c0, v.c1);
                 } else {
-                    u = load_entry(g.src[k], base, 2 * p);
-                    v = load_entry(g.src[k], base, 2 * p + 1);
+                    u = load_entry<CG>(g.src[k], base, 2 * p);
+                    v = load_entry<CG>(g.src[k], base, 2 * p + 1);
                 }
                 const fp2 diff = l2_sub(v, u);
                 fp2 x = v;
@@ -295,17 +446,18 @@ __device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, cons
     for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {  // every lane forms the message
         const fp2 wi = {w[2 * i], w[2 * i + 1]};
         if (j < pad[i]) {
-            const fp2 v = e_mul(wi, e_scale(fp2{S[2 * i], S[2 * i + 1]}, (1ull << (pad[i] - j - 1)) % P));
+            const fp2 v = e_mul(wi, e_scale(fp2{__ldcg(S + 2 * i), __ldcg(S + 2 * i + 1)}, (1ull << (pad[i] - j - 1)) % P));
             for (int x = 0; x < degree; x++) msg[x] = e_add(msg[x], v);
         } else {
             const uint64_t* m = msgbuf + (size_t)i * SC_MSG_WORDS;
-            for (int x = 0; x < degree; x++) msg[x] = e_add(msg[x], e_mul(wi, fp2{m[2 * x], m[2 * x + 1]}));
+            for (int x = 0; x < degree; x++) msg[x] = e_add(msg[x], e_mul(wi, fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)}));
         }
     }
+    // the state through L2: the persistent rounds move a job's transcript between blocks
     uint32_t state[8];
 #pragma unroll
-    for (int i = 0; i < 8; i++) state[i] = reinterpret_cast<const uint32_t*>(st->state)[i];
-    uint64_t counter = st->counter;
+    for (int i = 0; i < 8; i++) state[i] = __ldcg(reinterpret_cast<const uint32_t*>(st->state) + i);
+    uint64_t counter = __ldcg(&st->counter);
     if (lane == 0) {
         uint64_t* rj = rounds_out + jb.rounds_off + (size_t)j * 2 * degree;
         for (int x = 0; x < degree; x++) rj[2 * x] = msg[x].c0, rj[2 * x + 1] = msg[x].c1;
@@ -343,10 +495,17 @@ __global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const 
     sc_fs_job(states, jobs, t, j, keys, w, pad, S, msgbuf, rounds_out, chal_out, sbuf[threadIdx.x / 32]);
 }
 
-// The small last rounds of a batch, j0 to J − 1, in one block with no launch between them: each
-// round sums its segments (every segment one block's work: nblocks = 1) with the whole block, then
-// the block's warps run the jobs' transcripts, whose challenges the next round binds.
-struct ScTail {
+// The rounds jp … J − 1 of a batch in one launch, with no launch between rounds. The first `multi`
+// of them are spread over the launch's G co-resident blocks (a cooperative launch): a round's
+// virtual blocks — its segments' blocks as a launch of sc_rounds would lay them out — are dealt
+// round-robin to the G blocks, which write their partial sums; the blocks meet; the warp that owns
+// a job (job b: warp (b / G) mod 8 of block b mod G) reduces the partial rows of its instances into
+// their messages and runs the job's transcript step; the blocks meet again, and the next round
+// binds the new challenges. The rounds after those, whose segments are one block's work, run in
+// block 0 alone (the others have returned): each sums its segments with the whole block, then the
+// block's warps run the transcripts. Whatever another block may have written — tables, partial
+// sums, messages, transcript states — is read through L2.
+struct ScPersist {
     FsKeys keys;
     FsState* states;
     const FsJob* jobs;
@@ -356,23 +515,129 @@ struct ScTail {
     uint64_t* msgbuf;
     uint64_t* rounds_out;
     uint64_t* chal_out;
-    const Seg* segs;   // the tail rounds' segments in round order
-    const int* first;  // round j0 + t's segments are segs[first[t] .. first[t + 1])
-    int njobs, j0, rounds, pad_;
+    const Seg* segs;     // the rounds' segments in round order
+    const int* first;    // round jp + t's segments are segs[first[t] .. first[t + 1])
+    const int* vblocks;  // the virtual blocks of round jp + t, t < multi
+    uint64_t* partials;
+    unsigned* bar;       // the blocks' meeting point: arrivals, generation, gave up
+    int njobs, jp, rounds, multi;
 };
 
+constexpr unsigned SC_BAR_POLLS = 1u << 24;  // about a second of polling before a meeting gives up
+
+// All G blocks of the launch meet. A block waits at most SC_BAR_POLLS polls, and stops waiting
+// once another block has given up; then every thread of the block gets false (and the caller
+// returns, so that no block waits on one that has left). The transcripts record the failure.
+__device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen) {
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        const unsigned target = gen + 1;
+        int good = 1;
+        __threadfence();
+        if (atomicAdd(bar, 1u) == G - 1) {
+            atomicExch(bar, 0u);
+            __threadfence();
+            atomicExch(bar + 1, target);
+        } else {
+            for (unsigned it = 0;; it++) {
+                if (*(volatile unsigned*)(bar + 1) == target) break;
+                if (*(volatile unsigned*)(bar + 2) || it >= SC_BAR_POLLS) {
+                    atomicExch(bar + 2, 1u);
+                    good = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        ok = good && !*(volatile unsigned*)(bar + 2);
+    }
+    __syncthreads();
+    gen++;
+    return ok;
+}
+
 template <int D>
-__global__ void __launch_bounds__(SC_THREADS, 1) sc_tail(const ScTail* A) {
+__global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) {
     __shared__ Seg g;
+    __shared__ int si_s;
     __shared__ uint32_t sbuf[SC_THREADS / 32][FS_BUF_WORDS];
-    const int warp = threadIdx.x >> 5;
-    for (int t = 0; t < A->rounds; t++) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const unsigned G = gridDim.x;
+    unsigned gen = 0;
+    for (int t = 0; t < A->multi; t++) {
+        const int s0 = A->first[t], s1 = A->first[t + 1];
+        for (int vb = blockIdx.x; vb < A->vblocks[t]; vb += G) {
+            if (threadIdx.x == 0) {  // the segment that holds virtual block vb
+                int lo = s0, hi = s1 - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) / 2;
+                    if (A->segs[mid].block0 <= vb)
+                        lo = mid;
+                    else
+                        hi = mid - 1;
+                }
+                si_s = lo;
+            }
+            __syncthreads();
+            if (threadIdx.x < (int)(sizeof(Seg) / 8))
+                reinterpret_cast<uint64_t*>(&g)[threadIdx.x] = reinterpret_cast<const uint64_t*>(A->segs + si_s)[threadIdx.x];
+            __syncthreads();
+            const int lb = vb - g.block0;
+            uint64_t words[2 * D];
+#pragma unroll
+            for (int w = 0; w < 2 * D; w++) words[w] = 0;
+            if (!seg_sums_fast<D, true>(g, lb, words)) sc_seg_sums<D, true>(g, lb, words);
+            block_sum<2 * D>(words);  // ends with a barrier
+            if (threadIdx.x == 0)
+#pragma unroll
+                for (int w = 0; w < 2 * D; w++) A->partials[(size_t)(g.part0 + lb) * 2 * D + w] = words[w];
+            __syncthreads();  // g and si_s are rewritten for the next virtual block
+        }
+        if (!grid_meet(A->bar, G, gen)) {
+            if (threadIdx.x == 0)
+                for (int b = blockIdx.x; b < A->njobs; b += G) atomicExch(&A->states[b].err, 2u);
+            return;
+        }
+        for (int b = blockIdx.x + G * warp; b < A->njobs; b += G * (SC_THREADS / 32)) {
+            const FsJob& jb = A->jobs[b];
+            for (int si = s0; si < s1; si++) {
+                const Seg& q = A->segs[si];
+                if (q.inst < jb.inst0 || q.inst >= jb.inst0 + jb.ninst) continue;
+                uint64_t acc[2 * D];
+#pragma unroll
+                for (int w = 0; w < 2 * D; w++) acc[w] = 0;
+                for (int lb = lane; lb < q.nblocks; lb += 32)
+#pragma unroll
+                    for (int w = 0; w < 2 * D; w++)
+                        acc[w] = add(acc[w], __ldcg(&A->partials[(size_t)(q.part0 + lb) * 2 * D + w]));
+#pragma unroll
+                for (int w = 0; w < 2 * D; w++)
+                    for (int o = 16; o > 0; o >>= 1) acc[w] = add(acc[w], __shfl_xor_sync(0xFFFFFFFFu, acc[w], o));
+                if (lane == 0)
+                    for (int w = 0; w < 2 * q.degree; w++) q.out[w] = acc[w];
+            }
+            __syncwarp();
+            sc_fs_job(A->states, A->jobs, b, A->jp + t, A->keys, A->w, A->pad, A->S, A->msgbuf, A->rounds_out,
+                      A->chal_out, sbuf[warp]);
+        }
+        if (!grid_meet(A->bar, G, gen)) {
+            if (threadIdx.x == 0)
+                for (int b = blockIdx.x; b < A->njobs; b += G) atomicExch(&A->states[b].err, 2u);
+            return;
+        }
+    }
+    if (blockIdx.x != 0) return;
+    for (int t = A->multi; t < A->rounds; t++) {
         for (int si = A->first[t]; si < A->first[t + 1]; si++) {
             if (threadIdx.x < (int)(sizeof(Seg) / 8))
                 reinterpret_cast<uint64_t*>(&g)[threadIdx.x] = reinterpret_cast<const uint64_t*>(A->segs + si)[threadIdx.x];
             __syncthreads();
             uint64_t words[2 * D];
-            sc_seg_sums<D>(g, 0, words);
+#pragma unroll
+            for (int w = 0; w < 2 * D; w++) words[w] = 0;
+            if (!seg_sums_fast<D, true>(g, 0, words)) sc_seg_sums<D, true>(g, 0, words);
             block_sum<2 * D>(words);  // ends with a barrier
             if (threadIdx.x == 0) {
                 const int nout = g.kind == 1 ? 2 : 2 * g.degree;
@@ -381,13 +646,14 @@ __global__ void __launch_bounds__(SC_THREADS, 1) sc_tail(const ScTail* A) {
             __syncthreads();
         }
         for (int job = warp; job < A->njobs; job += SC_THREADS / 32)
-            sc_fs_job(A->states, A->jobs, job, A->j0 + t, A->keys, A->w, A->pad, A->S, A->msgbuf, A->rounds_out,
-                            A->chal_out, sbuf[warp]);
+            sc_fs_job(A->states, A->jobs, job, A->jp + t, A->keys, A->w, A->pad, A->S, A->msgbuf, A->rounds_out,
+                      A->chal_out, sbuf[warp]);
         __syncthreads();
     }
 }
 
 // ---- host driver -----------------------------------------------------------------------------
+
 
 template <typename F>
 static void with_degree(int degree, F&& f) {
@@ -437,6 +703,26 @@ struct Plan {
     int blocks = 0;
 };
 
+// Whether the device takes cooperative launches (the persistent rounds' blocks must be co-resident).
+static bool cooperative(Device* d) {
+    if (d->coop < 0) {
+        int v = 0;
+        d->coop = cudaDeviceGetAttribute(&v, cudaDevAttrCooperativeLaunch, d->ordinal) == cudaSuccess && v ? 1 : 0;
+    }
+    return d->coop == 1;
+}
+
+// Blocks of sc_persist<D> that fit on one SM at once.
+template <int D>
+static int persist_blocks_per_sm() {
+    static int nb = -1;
+    if (nb < 0) {
+        int v = 0;
+        nb = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&v, sc_persist<D>, SC_THREADS, 0) == cudaSuccess ? v : 0;
+    }
+    return nb;
+}
+
 // One prove_many call in flight: planned on the host (γ drawn), then enqueued on a stream over
 // a device arena, then finished on the host once the stream has run.
 struct ScRun {
@@ -453,13 +739,14 @@ struct ScRun {
     std::vector<Plan> plans;
     size_t max_segs = 1, max_blocks = 1, total_segs = 0, nbind = 0;
     int seg_cap = 1;
-    int j0 = 0;  // rounds j0 … J − 1 run in sc_tail
-    ScTail tail_h;
-    std::vector<int> tail_first;
+    int j0 = 0;  // rounds j0 … J − 1 are one block's work
+    int jp = 0;  // rounds jp … J − 1 run in sc_persist (jp <= j0)
+    ScPersist persist_h;
+    std::vector<int> persist_first, persist_vblocks;
     // arena layout (offsets from the arena's base)
     size_t off_fs = 0, off_jobs = 0, off_w = 0, off_pad = 0, off_S = 0, off_msg = 0, off_rounds = 0, off_chal = 0,
-           off_partials = 0, off_counters = 0, off_segs = 0, off_bind = 0, off_erefs = 0, off_evals = 0, off_tail = 0,
-           off_first = 0;
+           off_partials = 0, off_counters = 0, off_segs = 0, off_bind = 0, off_erefs = 0, off_evals = 0, off_persist = 0,
+           off_first = 0, off_vblocks = 0, off_bar = 0;
     size_t arena_bytes = 0;
     // host-side staging that the enqueued copies read (kept until finish)
     std::vector<FsState> fs0;
@@ -585,14 +872,18 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
         r->max_blocks = std::max(r->max_blocks, (size_t)p.blocks);
         r->total_segs += p.who.size();
     }
+    auto plan_pairs = [&](int j) {
+        uint64_t pairs = 0;
+        for (auto& w : r->plans[1 + j].who) pairs += 1ull << (r->inst[w.first].vars - w.second - 1);
+        return pairs;
+    };
+    const bool coop = cooperative(d);
     r->j0 = r->J;
     if (njobs <= SC_THREADS / 32)
-        for (int j = r->J - 1; j >= 0; j--) {
-            uint64_t pairs = 0;
-            for (auto& w : r->plans[1 + j].who) pairs += 1ull << (r->inst[w.first].vars - w.second - 1);
-            if (pairs > SC_TAIL_PAIRS) break;
-            r->j0 = j;
-        }
+        for (int j = r->J - 1; j >= 0 && plan_pairs(j) <= (coop ? SC_TAIL_PAIRS_PERSIST : SC_TAIL_PAIRS); j--) r->j0 = j;
+    r->jp = r->j0;
+    if (coop)
+        for (int j = r->j0 - 1; j >= 0 && plan_pairs(j) <= SC_PERSIST_PAIRS; j--) r->jp = j;
 
     // the arena: tables, transcripts, plans and outputs
     Arena ar;
@@ -615,8 +906,10 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
     r->off_partials = ar.take(r->max_blocks * 2 * SC_MAX_DEGREE * 8);
     r->off_counters = ar.take(4 * r->max_segs);
     r->off_segs = ar.take(sizeof(Seg) * std::max<size_t>(r->total_segs, 1));
-    r->off_tail = ar.take(sizeof(ScTail));
-    r->off_first = ar.take(4 * ((size_t)(r->J - r->j0) + 1));
+    r->off_persist = ar.take(sizeof(ScPersist));
+    r->off_first = ar.take(4 * ((size_t)(r->J - r->jp) + 1));
+    r->off_vblocks = ar.take(4 * ((size_t)(r->j0 - r->jp) + 1));
+    r->off_bar = ar.take(16);
     for (auto& is : r->inst)
         if (is.vars >= 1) r->nbind += is.tables.size();
     r->off_bind = ar.take(sizeof(BindLast) * std::max<size_t>(r->nbind, 1));
@@ -645,6 +938,7 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
             if (ts.host) {
                 uint64_t* dst = ar.at<uint64_t>(ts.up_off);
                 const size_t bytes = ((size_t)1 << is.vars) * (ts.base ? 8 : 16);
+                host_prefault(ts.host, bytes);
                 TG_CUDA(cudaMemcpyAsync(dst, ts.host, bytes, cudaMemcpyHostToDevice, s));
                 ts.src = dst;
             }
@@ -690,10 +984,11 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
                     for (int k = 0; k < g.nt; k++) g.dst[k] = ar.at<uint64_t>(is.tables[k].buf_off[(own - 1) & 1]);
                 }
             }
-            const bool tail = &p - r->plans.data() >= 1 + r->j0;  // one block's work in sc_tail
+            const bool tail = &p - r->plans.data() >= 1 + r->j0;  // one block's work in sc_persist
             g.block0 = tail ? 0 : block0;
             g.nblocks = tail ? 1 : blocks_for(g.n);
             g.part0 = g.block0;
+            g.inst = w.first;
             block0 += g.nblocks;
             r->all_segs.push_back(g);
         }
@@ -769,8 +1064,9 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         TG_CUDA(cudaMemcpyAsync(ar.at<EvalRef>(r->off_erefs), r->erefs.data(), sizeof(EvalRef) * r->erefs.size(),
                                 cudaMemcpyHostToDevice, s));
     TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(r->off_counters), 0, 4 * r->max_segs, s));
-    if (r->j0 < r->J) {
-        ScTail& t = r->tail_h;
+    int persist_grid = 1;
+    if (r->jp < r->J) {
+        ScPersist& t = r->persist_h;
         memset(&t, 0, sizeof t);
         t.keys = keys;
         t.states = dfs;
@@ -781,16 +1077,35 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         t.msgbuf = dmsg;
         t.rounds_out = ar.at<uint64_t>(r->off_rounds);
         t.chal_out = ar.at<uint64_t>(r->off_chal);
-        t.segs = ar.at<Seg>(r->off_segs) + r->plan_seg0[1 + r->j0];
+        t.segs = ar.at<Seg>(r->off_segs) + r->plan_seg0[1 + r->jp];
         t.first = ar.at<int>(r->off_first);
+        t.vblocks = ar.at<int>(r->off_vblocks);
+        t.partials = ar.at<uint64_t>(r->off_partials);
+        t.bar = ar.at<unsigned>(r->off_bar);
         t.njobs = njobs;
-        t.j0 = r->j0;
-        t.rounds = r->J - r->j0;
-        r->tail_first.assign(1, 0);
-        for (int j = r->j0; j < r->J; j++) r->tail_first.push_back(r->tail_first.back() + (int)r->plans[1 + j].who.size());
-        TG_CUDA(cudaMemcpyAsync(ar.at<ScTail>(r->off_tail), &t, sizeof t, cudaMemcpyHostToDevice, s));
-        TG_CUDA(cudaMemcpyAsync(ar.at<int>(r->off_first), r->tail_first.data(), 4 * r->tail_first.size(),
+        t.jp = r->jp;
+        t.rounds = r->J - r->jp;
+        t.multi = r->j0 - r->jp;
+        r->persist_first.assign(1, 0);
+        for (int j = r->jp; j < r->J; j++) r->persist_first.push_back(r->persist_first.back() + (int)r->plans[1 + j].who.size());
+        r->persist_vblocks.clear();
+        int most = 1;
+        for (int j = r->jp; j < r->j0; j++) {
+            r->persist_vblocks.push_back(r->plans[1 + j].blocks);
+            most = std::max(most, r->plans[1 + j].blocks);
+        }
+        if (r->jp < r->j0) {
+            int per_sm = 0;
+            with_degree(r->D, [&](auto D_) { per_sm = persist_blocks_per_sm<decltype(D_)::value>(); });
+            persist_grid = std::max(1, std::min({SC_PERSIST_BLOCKS, most, per_sm * d->sm_count}));
+        }
+        TG_CUDA(cudaMemcpyAsync(ar.at<ScPersist>(r->off_persist), &t, sizeof t, cudaMemcpyHostToDevice, s));
+        TG_CUDA(cudaMemcpyAsync(ar.at<int>(r->off_first), r->persist_first.data(), 4 * r->persist_first.size(),
                                 cudaMemcpyHostToDevice, s));
+        if (!r->persist_vblocks.empty())
+            TG_CUDA(cudaMemcpyAsync(ar.at<int>(r->off_vblocks), r->persist_vblocks.data(), 4 * r->persist_vblocks.size(),
+                                    cudaMemcpyHostToDevice, s));
+        TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(r->off_bar), 0, 16, s));
     }
 
     // the launches
@@ -814,7 +1129,7 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
     };
     int rc = run_plan(0, "sumcheck_product_sum");
     if (rc) return rc;
-    for (int j = 0; j < r->j0; j++) {
+    for (int j = 0; j < r->jp; j++) {
         rc = run_plan(1 + j, "sumcheck_round");
         if (rc) return rc;
         {
@@ -825,15 +1140,24 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         }
         TG_CUDA(cudaGetLastError());
     }
-    if (r->j0 < r->J) {
+    if (r->jp < r->J) {
         uint64_t units = 0;
-        for (int j = r->j0; j < r->J; j++)
+        for (int j = r->jp; j < r->J; j++)
             for (size_t q = 0; q < r->plans[1 + j].who.size(); q++) units += r->all_segs[r->plan_seg0[1 + j] + q].n;
-        Launch L(d, s, "sumcheck_tail", 1, units);
+        Launch L(d, s, "sumcheck_persist", 1, units);
+        const ScPersist* arg = ar.at<ScPersist>(r->off_persist);
+        cudaError_t e = cudaSuccess;
         with_degree(r->D, [&](auto D_) {
             constexpr int DD = decltype(D_)::value;
-            sc_tail<DD><<<1, SC_THREADS, 0, s>>>(ar.at<ScTail>(r->off_tail));
+            if (persist_grid > 1) {  // the blocks meet between rounds: all of them must be resident at once
+                void* args[] = {(void*)&arg};
+                e = cudaLaunchCooperativeKernel((const void*)sc_persist<DD>, dim3(persist_grid), dim3(SC_THREADS), args, 0,
+                                                s);
+            } else {
+                sc_persist<DD><<<1, SC_THREADS, 0, s>>>(arg);
+            }
         });
+        if (e != cudaSuccess) return cuda_fail(e, "cudaLaunchCooperativeKernel(sc_persist)");
         TG_CUDA(cudaGetLastError());
     }
     if (!r->binds.empty()) {
@@ -869,10 +1193,13 @@ int sc_finish(ScRun* r) {
     const uint64_t* hr = reinterpret_cast<const uint64_t*>(h);
     const uint64_t* hc = hr + r->rounds_words;
     const uint64_t* he = hc + r->chal_words;
-    for (int b = 0; b < njobs; b++)
+    for (int b = 0; b < njobs; b++) {
+        if (fs1[b].err == 2)
+            return sc_restore(r, fail(TG_ERR_STATE, "job %d: the persistent rounds' blocks gave up waiting for each other", b));
         if (fs1[b].err)
             return sc_restore(r, fail(TG_ERR_STATE, "job %d: a transcript challenge found no canonical Fp2 in %d squeezes",
                                       b, FS_MAX_TRIES));
+    }
     for (int b = 0; b < njobs; b++) {
         tg_sumcheck_job& jb = r->jobs[b];
         memcpy(jb.transcript->state, fs1[b].state, 32);

@@ -925,6 +925,7 @@ extern "C" int tg_leaf_stage_open(tg_device* dev, const tg_tree* specs, int ntre
             }
             const int rc = spare_take(d, b, leaves * es);
             if (rc) return rc;
+            if (!on_device) host_prefault(src, leaves * es);
             TG_CUDA(cudaMemcpyAsync(b.ptr, src, leaves * es, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
             return TG_OK;
         };
