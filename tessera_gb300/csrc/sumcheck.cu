@@ -43,9 +43,10 @@ constexpr int SC_MSG_WORDS = 2 * SC_MAX_DEGREE;  // one instance's round sums, a
 // run in the same launch as well).
 constexpr uint64_t SC_TAIL_PAIRS = 4096, SC_TAIL_PAIRS_PERSIST = 512;
 // With cooperative launches, the rounds from the first whose segments hold at most this many pairs
-// in all run in one launch of sc_persist, on at most SC_PERSIST_BLOCKS blocks.
-constexpr uint64_t SC_PERSIST_PAIRS = 1ull << 16;
-constexpr int SC_PERSIST_BLOCKS = 128;
+// in all run in one launch of sc_persist, on one block per SC_PERSIST_BLOCK_PAIRS pairs of its largest
+// round: blocks wait for each other at every round's transcript, and the fewer they are, the more of
+// the GPU stays free for other streams' work (the proof server's requests).
+constexpr uint64_t SC_PERSIST_PAIRS = 1ull << 16, SC_PERSIST_BLOCK_PAIRS = 2048;
 
 // One instance's share of one launch.
 struct Seg {
@@ -354,8 +355,10 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
 
 // One launch of round sums (and product sums) over all segments: a block finds its segment, runs
 // a grid-stride loop over the segment's pairs, and the segment's last block to finish reduces the
-// segment's partial rows into seg.out.
-template <int D>
+// segment's partial rows into seg.out. SHAPE 0 takes any segment; SHAPE 1–6 (sc_shape) only
+// segments of that one shape, through its fixed-shape sums, so that the launch carries the
+// registers of that form alone.
+template <int D, int SHAPE>
 __global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nseg, uint64_t* partials,
                                                         unsigned* counters) {
     __shared__ Seg g;
@@ -381,7 +384,15 @@ __global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nse
     const int lb = blockIdx.x - g.block0;
     const int deg = g.degree;
     uint64_t words[2 * D];
-    sc_seg_sums<D>(g, lb, words);
+#pragma unroll
+    for (int w = 0; w < 2 * D; w++) words[w] = 0;
+    if constexpr (SHAPE == 0) sc_seg_sums<D>(g, lb, words);
+    else if constexpr (SHAPE == 1) seg_sums_fixed<D, 3, 3, false, true, 4, false>(g, lb, words);
+    else if constexpr (SHAPE == 2) seg_sums_fixed<D, 3, 3, true, true, 1, false>(g, lb, words);
+    else if constexpr (SHAPE == 3) seg_sums_fixed<D, 3, 3, true, false, 1, false>(g, lb, words);
+    else if constexpr (SHAPE == 4) seg_sums_fixed<D, 2, 2, false, true, 4, false>(g, lb, words);
+    else if constexpr (SHAPE == 5) seg_sums_fixed<D, 2, 2, true, true, 2, false>(g, lb, words);
+    else seg_sums_fixed<D, 2, 2, true, false, 1, false>(g, lb, words);
     block_sum<2 * D>(words);
 
     // the segment's last block reduces its partial rows
@@ -654,6 +665,18 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) 
 
 // ---- host driver -----------------------------------------------------------------------------
 
+
+// The fixed shape of a segment for sc_rounds' SHAPE (0: none): 1–3 three tables at degree 3 (the
+// first round over prime-field tables; a bind of prime-field entries; a bind of Fp2 entries), 4–6
+// two tables at degree 2, likewise.
+static int sc_shape(const Seg& g) {
+    if (g.kind != 0) return 0;
+    const bool all_base = g.base_mask == (1u << g.nt) - 1, all_ext = g.base_mask == 0;
+    const int first = (g.nt == 3 && g.degree == 3) ? 1 : (g.nt == 2 && g.degree == 2) ? 4 : 0;
+    if (!first) return 0;
+    if (!g.bind) return all_base ? first : 0;
+    return all_base ? first + 1 : all_ext ? first + 2 : 0;
+}
 
 template <typename F>
 static void with_degree(int degree, F&& f) {
@@ -1089,15 +1112,18 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         r->persist_first.assign(1, 0);
         for (int j = r->jp; j < r->J; j++) r->persist_first.push_back(r->persist_first.back() + (int)r->plans[1 + j].who.size());
         r->persist_vblocks.clear();
-        int most = 1;
+        uint64_t most = 0;
         for (int j = r->jp; j < r->j0; j++) {
             r->persist_vblocks.push_back(r->plans[1 + j].blocks);
-            most = std::max(most, r->plans[1 + j].blocks);
+            uint64_t pairs = 0;
+            for (auto& w : r->plans[1 + j].who) pairs += 1ull << (r->inst[w.first].vars - w.second - 1);
+            most = std::max(most, pairs);
         }
         if (r->jp < r->j0) {
             int per_sm = 0;
             with_degree(r->D, [&](auto D_) { per_sm = persist_blocks_per_sm<decltype(D_)::value>(); });
-            persist_grid = std::max(1, std::min({SC_PERSIST_BLOCKS, most, per_sm * d->sm_count}));
+            persist_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(most / SC_PERSIST_BLOCK_PAIRS,
+                                                                         (uint64_t)per_sm * d->sm_count));
         }
         TG_CUDA(cudaMemcpyAsync(ar.at<ScPersist>(r->off_persist), &t, sizeof t, cudaMemcpyHostToDevice, s));
         TG_CUDA(cudaMemcpyAsync(ar.at<int>(r->off_first), r->persist_first.data(), 4 * r->persist_first.size(),
@@ -1119,11 +1145,26 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         const Seg* segs = ar.at<Seg>(r->off_segs) + r->plan_seg0[pi];
         uint64_t units = 0;
         for (size_t q = 0; q < p.who.size(); q++) units += r->all_segs[r->plan_seg0[pi] + q].n;
+        int shape = sc_shape(r->all_segs[r->plan_seg0[pi]]);
+        for (size_t q = 1; q < p.who.size() && shape; q++)
+            if (sc_shape(r->all_segs[r->plan_seg0[pi] + q]) != shape) shape = 0;
         Launch L(d, s, name, 1, units);
-        with_degree(r->D, [&](auto D_) {
-            constexpr int DD = decltype(D_)::value;
-            sc_rounds<DD><<<p.blocks, SC_THREADS, 0, s>>>(segs, (int)p.who.size(), partials, counters);
-        });
+        const dim3 grid(p.blocks), block(SC_THREADS);
+        const int nseg = (int)p.who.size();
+        if (r->D == 3 && shape >= 1 && shape <= 3) {
+            if (shape == 1) sc_rounds<3, 1><<<grid, block, 0, s>>>(segs, nseg, partials, counters);
+            else if (shape == 2) sc_rounds<3, 2><<<grid, block, 0, s>>>(segs, nseg, partials, counters);
+            else sc_rounds<3, 3><<<grid, block, 0, s>>>(segs, nseg, partials, counters);
+        } else if (r->D == 2 && shape >= 4) {
+            if (shape == 4) sc_rounds<2, 4><<<grid, block, 0, s>>>(segs, nseg, partials, counters);
+            else if (shape == 5) sc_rounds<2, 5><<<grid, block, 0, s>>>(segs, nseg, partials, counters);
+            else sc_rounds<2, 6><<<grid, block, 0, s>>>(segs, nseg, partials, counters);
+        } else {
+            with_degree(r->D, [&](auto D_) {
+                constexpr int DD = decltype(D_)::value;
+                sc_rounds<DD, 0><<<grid, block, 0, s>>>(segs, nseg, partials, counters);
+            });
+        }
         TG_CUDA(cudaGetLastError());
         return TG_OK;
     };
