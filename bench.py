@@ -426,6 +426,8 @@ def run_gpu(args) -> None:
         "algorithmic_bytes_per_row": bytes_per_row, "rows_per_launch": rows_per_group,
         "traffic": (traffic * rows_per_group) if traffic else None,
         "traffic_unit": "DRAM bytes per launch (all passes, ncu, scaled by rows)",
+        "traffic_source": ("profiles/traffic.json, captured at commit " + traffic_table().get("captured_at_commit", "?"))
+                          if traffic else None,
         "note": "the encoder is bound by the integer pipes, not by HBM; int_rate gives its fraction of the measured integer peak",
     }
     butterflies_per_row = ((1 << LOG_K) // 2) * LOG_K + ((1 << (LOG_K + LOG_R)) // 2) * (LOG_K + LOG_R)
