@@ -46,7 +46,7 @@ constexpr uint64_t SC_TAIL_PAIRS = 4096, SC_TAIL_PAIRS_PERSIST = 512;
 // in all run in one launch of sc_persist, on one block per SC_PERSIST_BLOCK_PAIRS pairs of its largest
 // round: blocks wait for each other at every round's transcript, and the fewer they are, the more of
 // the GPU stays free for other streams' work (the proof server's requests).
-constexpr uint64_t SC_PERSIST_PAIRS = 1ull << 16, SC_PERSIST_BLOCK_PAIRS = 2048;
+constexpr uint64_t SC_PERSIST_PAIRS = 1ull << 16, SC_PERSIST_BLOCK_PAIRS = 1024;
 
 // One instance's share of one launch.
 struct Seg {
@@ -507,12 +507,12 @@ __global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const 
 }
 
 // The rounds jp … J − 1 of a batch in one launch, with no launch between rounds. The first `multi`
-// of them are spread over the launch's G co-resident blocks (a cooperative launch): a round's
-// virtual blocks — its segments' blocks as a launch of sc_rounds would lay them out — are dealt
-// round-robin to the G blocks, which write their partial sums; the blocks meet; the warp that owns
-// a job (job b: warp (b / G) mod 8 of block b mod G) reduces the partial rows of its instances into
-// their messages and runs the job's transcript step; the blocks meet again, and the next round
-// binds the new challenges. The rounds after those, whose segments are one block's work, run in
+// of them are spread over the launch's G co-resident blocks (a cooperative launch): every block
+// takes its share of every segment of the round (a grid-stride loop over the segment's pairs, one
+// partial row per block and segment); the blocks meet; the warp that owns a job (job b: warp
+// (b / G) mod 8 of block b mod G) reduces the partial rows of its instances into their messages and
+// runs the job's transcript step; the blocks meet again, and the next round binds the new
+// challenges. The rounds after those, whose segments are one block's work, run in
 // block 0 alone (the others have returned): each sums its segments with the whole block, then the
 // block's warps run the transcripts. Whatever another block may have written — tables, partial
 // sums, messages, transcript states — is read through L2.
@@ -528,12 +528,14 @@ struct ScPersist {
     uint64_t* chal_out;
     const Seg* segs;     // the rounds' segments in round order
     const int* first;    // round jp + t's segments are segs[first[t] .. first[t + 1])
-    const int* vblocks;  // the virtual blocks of round jp + t, t < multi
-    uint64_t* partials;
-    unsigned* bar;       // the blocks' meeting point: arrivals, generation, gave up
+    uint64_t* partials;  // G rows per segment of a multi-block round
+    unsigned* bar;       // the blocks' meeting point: arrivals, generation, gave up (each on its own 128-byte line)
     int njobs, jp, rounds, multi;
 };
 
+// The meeting point's words, each on its own 128-byte line so that the arrivals' atomics and the
+// waiting blocks' polls do not contend for one line.
+constexpr int SC_BAR_COUNT = 0, SC_BAR_GEN = 32, SC_BAR_FAIL = 64, SC_BAR_WORDS = 96;
 constexpr unsigned SC_BAR_POLLS = 1u << 24;  // about a second of polling before a meeting gives up
 
 // All G blocks of the launch meet. A block waits at most SC_BAR_POLLS polls, and stops waiting
@@ -546,23 +548,23 @@ __device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen) {
         const unsigned target = gen + 1;
         int good = 1;
         __threadfence();
-        if (atomicAdd(bar, 1u) == G - 1) {
-            atomicExch(bar, 0u);
+        if (atomicAdd(bar + SC_BAR_COUNT, 1u) == G - 1) {
+            atomicExch(bar + SC_BAR_COUNT, 0u);
             __threadfence();
-            atomicExch(bar + 1, target);
+            atomicExch(bar + SC_BAR_GEN, target);
         } else {
-            for (unsigned it = 0;; it++) {
-                if (*(volatile unsigned*)(bar + 1) == target) break;
-                if (*(volatile unsigned*)(bar + 2) || it >= SC_BAR_POLLS) {
-                    atomicExch(bar + 2, 1u);
+            for (unsigned it = 1;; it++) {
+                if (*(volatile unsigned*)(bar + SC_BAR_GEN) == target) break;
+                if ((it & 255) == 0 && (*(volatile unsigned*)(bar + SC_BAR_FAIL) || it >= SC_BAR_POLLS)) {
+                    atomicExch(bar + SC_BAR_FAIL, 1u);
                     good = 0;
                     break;
                 }
-                __nanosleep(64);
+                __nanosleep(32);
             }
         }
         __threadfence();
-        ok = good && !*(volatile unsigned*)(bar + 2);
+        ok = good && !*(volatile unsigned*)(bar + SC_BAR_FAIL);
     }
     __syncthreads();
     gen++;
@@ -572,39 +574,27 @@ __device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen) {
 template <int D>
 __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) {
     __shared__ Seg g;
-    __shared__ int si_s;
     __shared__ uint32_t sbuf[SC_THREADS / 32][FS_BUF_WORDS];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned G = gridDim.x;
     unsigned gen = 0;
     for (int t = 0; t < A->multi; t++) {
         const int s0 = A->first[t], s1 = A->first[t + 1];
-        for (int vb = blockIdx.x; vb < A->vblocks[t]; vb += G) {
-            if (threadIdx.x == 0) {  // the segment that holds virtual block vb
-                int lo = s0, hi = s1 - 1;
-                while (lo < hi) {
-                    const int mid = (lo + hi + 1) / 2;
-                    if (A->segs[mid].block0 <= vb)
-                        lo = mid;
-                    else
-                        hi = mid - 1;
-                }
-                si_s = lo;
-            }
-            __syncthreads();
+        for (int si = s0; si < s1; si++) {
             if (threadIdx.x < (int)(sizeof(Seg) / 8))
-                reinterpret_cast<uint64_t*>(&g)[threadIdx.x] = reinterpret_cast<const uint64_t*>(A->segs + si_s)[threadIdx.x];
+                reinterpret_cast<uint64_t*>(&g)[threadIdx.x] = reinterpret_cast<const uint64_t*>(A->segs + si)[threadIdx.x];
             __syncthreads();
-            const int lb = vb - g.block0;
+            if (threadIdx.x == 0) g.nblocks = (int)G;  // the segment over all blocks of the launch
+            __syncthreads();
             uint64_t words[2 * D];
 #pragma unroll
             for (int w = 0; w < 2 * D; w++) words[w] = 0;
-            if (!seg_sums_fast<D, true>(g, lb, words)) sc_seg_sums<D, true>(g, lb, words);
+            if (!seg_sums_fast<D, true>(g, blockIdx.x, words)) sc_seg_sums<D, true>(g, blockIdx.x, words);
             block_sum<2 * D>(words);  // ends with a barrier
             if (threadIdx.x == 0)
 #pragma unroll
-                for (int w = 0; w < 2 * D; w++) A->partials[(size_t)(g.part0 + lb) * 2 * D + w] = words[w];
-            __syncthreads();  // g and si_s are rewritten for the next virtual block
+                for (int w = 0; w < 2 * D; w++) A->partials[((size_t)(si - s0) * G + blockIdx.x) * 2 * D + w] = words[w];
+            __syncthreads();  // g is rewritten for the next segment
         }
         if (!grid_meet(A->bar, G, gen)) {
             if (threadIdx.x == 0)
@@ -619,10 +609,10 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) 
                 uint64_t acc[2 * D];
 #pragma unroll
                 for (int w = 0; w < 2 * D; w++) acc[w] = 0;
-                for (int lb = lane; lb < q.nblocks; lb += 32)
+                for (int lb = lane; lb < (int)G; lb += 32)
 #pragma unroll
                     for (int w = 0; w < 2 * D; w++)
-                        acc[w] = add(acc[w], __ldcg(&A->partials[(size_t)(q.part0 + lb) * 2 * D + w]));
+                        acc[w] = add(acc[w], __ldcg(&A->partials[((size_t)(si - s0) * G + lb) * 2 * D + w]));
 #pragma unroll
                 for (int w = 0; w < 2 * D; w++)
                     for (int o = 16; o > 0; o >>= 1) acc[w] = add(acc[w], __shfl_xor_sync(0xFFFFFFFFu, acc[w], o));
@@ -765,11 +755,12 @@ struct ScRun {
     int j0 = 0;  // rounds j0 … J − 1 are one block's work
     int jp = 0;  // rounds jp … J − 1 run in sc_persist (jp <= j0)
     ScPersist persist_h;
-    std::vector<int> persist_first, persist_vblocks;
+    std::vector<int> persist_first;
+    int persist_grid = 1;  // sc_persist's blocks
     // arena layout (offsets from the arena's base)
     size_t off_fs = 0, off_jobs = 0, off_w = 0, off_pad = 0, off_S = 0, off_msg = 0, off_rounds = 0, off_chal = 0,
            off_partials = 0, off_counters = 0, off_segs = 0, off_bind = 0, off_erefs = 0, off_evals = 0, off_persist = 0,
-           off_first = 0, off_vblocks = 0, off_bar = 0;
+           off_first = 0, off_bar = 0;
     size_t arena_bytes = 0;
     // host-side staging that the enqueued copies read (kept until finish)
     std::vector<FsState> fs0;
@@ -907,6 +898,15 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
     r->jp = r->j0;
     if (coop)
         for (int j = r->j0 - 1; j >= 0 && plan_pairs(j) <= SC_PERSIST_PAIRS; j--) r->jp = j;
+    // the persistent launch's blocks, and the partial rows its multi-block rounds write
+    size_t persist_rows = 0;
+    if (r->jp < r->j0) {
+        int per_sm = 0;
+        with_degree(r->D, [&](auto D_) { per_sm = persist_blocks_per_sm<decltype(D_)::value>(); });
+        r->persist_grid = (int)std::max<uint64_t>(
+            1, std::min<uint64_t>(plan_pairs(r->jp) / SC_PERSIST_BLOCK_PAIRS, (uint64_t)per_sm * d->sm_count));
+        for (int j = r->jp; j < r->j0; j++) persist_rows = std::max(persist_rows, r->plans[1 + j].who.size() * r->persist_grid);
+    }
 
     // the arena: tables, transcripts, plans and outputs
     Arena ar;
@@ -926,13 +926,12 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
     r->off_msg = ar.take((size_t)8 * SC_MSG_WORDS * ninst);
     r->off_rounds = ar.take(8 * std::max<size_t>(r->rounds_words, 1));
     r->off_chal = ar.take(8 * std::max<size_t>(r->chal_words, 1));
-    r->off_partials = ar.take(r->max_blocks * 2 * SC_MAX_DEGREE * 8);
+    r->off_partials = ar.take(std::max(r->max_blocks, persist_rows) * 2 * SC_MAX_DEGREE * 8);
     r->off_counters = ar.take(4 * r->max_segs);
     r->off_segs = ar.take(sizeof(Seg) * std::max<size_t>(r->total_segs, 1));
     r->off_persist = ar.take(sizeof(ScPersist));
     r->off_first = ar.take(4 * ((size_t)(r->J - r->jp) + 1));
-    r->off_vblocks = ar.take(4 * ((size_t)(r->j0 - r->jp) + 1));
-    r->off_bar = ar.take(16);
+    r->off_bar = ar.take(4 * SC_BAR_WORDS + 128);
     for (auto& is : r->inst)
         if (is.vars >= 1) r->nbind += is.tables.size();
     r->off_bind = ar.take(sizeof(BindLast) * std::max<size_t>(r->nbind, 1));
@@ -1087,7 +1086,7 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         TG_CUDA(cudaMemcpyAsync(ar.at<EvalRef>(r->off_erefs), r->erefs.data(), sizeof(EvalRef) * r->erefs.size(),
                                 cudaMemcpyHostToDevice, s));
     TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(r->off_counters), 0, 4 * r->max_segs, s));
-    int persist_grid = 1;
+    const int persist_grid = r->persist_grid;
     if (r->jp < r->J) {
         ScPersist& t = r->persist_h;
         memset(&t, 0, sizeof t);
@@ -1102,7 +1101,6 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         t.chal_out = ar.at<uint64_t>(r->off_chal);
         t.segs = ar.at<Seg>(r->off_segs) + r->plan_seg0[1 + r->jp];
         t.first = ar.at<int>(r->off_first);
-        t.vblocks = ar.at<int>(r->off_vblocks);
         t.partials = ar.at<uint64_t>(r->off_partials);
         t.bar = ar.at<unsigned>(r->off_bar);
         t.njobs = njobs;
@@ -1111,27 +1109,10 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         t.multi = r->j0 - r->jp;
         r->persist_first.assign(1, 0);
         for (int j = r->jp; j < r->J; j++) r->persist_first.push_back(r->persist_first.back() + (int)r->plans[1 + j].who.size());
-        r->persist_vblocks.clear();
-        uint64_t most = 0;
-        for (int j = r->jp; j < r->j0; j++) {
-            r->persist_vblocks.push_back(r->plans[1 + j].blocks);
-            uint64_t pairs = 0;
-            for (auto& w : r->plans[1 + j].who) pairs += 1ull << (r->inst[w.first].vars - w.second - 1);
-            most = std::max(most, pairs);
-        }
-        if (r->jp < r->j0) {
-            int per_sm = 0;
-            with_degree(r->D, [&](auto D_) { per_sm = persist_blocks_per_sm<decltype(D_)::value>(); });
-            persist_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(most / SC_PERSIST_BLOCK_PAIRS,
-                                                                         (uint64_t)per_sm * d->sm_count));
-        }
         TG_CUDA(cudaMemcpyAsync(ar.at<ScPersist>(r->off_persist), &t, sizeof t, cudaMemcpyHostToDevice, s));
         TG_CUDA(cudaMemcpyAsync(ar.at<int>(r->off_first), r->persist_first.data(), 4 * r->persist_first.size(),
                                 cudaMemcpyHostToDevice, s));
-        if (!r->persist_vblocks.empty())
-            TG_CUDA(cudaMemcpyAsync(ar.at<int>(r->off_vblocks), r->persist_vblocks.data(), 4 * r->persist_vblocks.size(),
-                                    cudaMemcpyHostToDevice, s));
-        TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(r->off_bar), 0, 16, s));
+        TG_CUDA(cudaMemsetAsync(ar.at<unsigned>(r->off_bar), 0, 4 * SC_BAR_WORDS, s));
     }
 
     // the launches
