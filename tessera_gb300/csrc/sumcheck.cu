@@ -438,37 +438,30 @@ __global__ void sc_gather_evals(const EvalRef* refs, int n, uint64_t* out) {
     out[2 * i + 1] = e.base ? 0 : e.ptr[1];
 }
 
-// ---- the transcripts on the device (one thread per job) -----------------------------------------
+// ---- the transcripts on the device (one warp per job) ------------------------------------------
 
-// Round j's message of each job: Σ over its instances of w_i·(own sums, or 2^{pad_i − j − 1}·S_i
-// while padded), absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
-// <prefix>/r/j.
-// One warp runs job t's round (buf: FS_BUF_WORDS of the warp's shared memory).
-__device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, const FsKeys& keys, const uint64_t* w,
-                          const int* pad, const uint64_t* S, const uint64_t* msgbuf, uint64_t* rounds_out,
-                          uint64_t* chal_out, uint32_t* buf) {
-    const int lane = threadIdx.x & 31;
-    const FsJob& jb = jobs[t];
-    if (j >= jb.n_max) return;
-    FsState* st = states + t;
-    const int degree = jb.degree;
-    fp2 msg[SC_MAX_DEGREE];
-    for (int x = 0; x < SC_MAX_DEGREE; x++) msg[x] = {0, 0};
-    for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {  // every lane forms the message
+// The padded instances' part of job jb's round-j message, added to msg: w_i·2^{pad_i − j − 1}·S_i
+// at every node of each instance still in its padding rounds.
+__device__ __forceinline__ void sc_fs_padded(const FsJob& jb, int j, const uint64_t* w, const int* pad,
+                                             const uint64_t* S, fp2 (&msg)[SC_MAX_DEGREE]) {
+    for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {
+        if (j >= pad[i]) continue;
         const fp2 wi = {w[2 * i], w[2 * i + 1]};
-        if (j < pad[i]) {
-            const fp2 v = e_mul(wi, e_scale(fp2{__ldcg(S + 2 * i), __ldcg(S + 2 * i + 1)}, (1ull << (pad[i] - j - 1)) % P));
-            for (int x = 0; x < degree; x++) msg[x] = e_add(msg[x], v);
-        } else {
-            const uint64_t* m = msgbuf + (size_t)i * SC_MSG_WORDS;
-            for (int x = 0; x < degree; x++) msg[x] = e_add(msg[x], e_mul(wi, fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)}));
-        }
+        const fp2 v = e_mul(wi, e_scale(fp2{__ldcg(S + 2 * i), __ldcg(S + 2 * i + 1)}, (1ull << (pad[i] - j - 1)) % P));
+        for (int x = 0; x < jb.degree; x++) msg[x] = e_add(msg[x], v);
     }
-    // the state through L2: the persistent rounds move a job's transcript between blocks
-    uint32_t state[8];
-#pragma unroll
-    for (int i = 0; i < 8; i++) state[i] = __ldcg(reinterpret_cast<const uint32_t*>(st->state) + i);
-    uint64_t counter = __ldcg(&st->counter);
+}
+
+// Round j's transcript step of job t, its message formed (the same in every lane): the message into
+// rounds_out, absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
+// <prefix>/r/j. state and counter (the same in every lane) are read and updated here; lane 0 writes
+// them, r_j and the challenge back to the job's FsState and to chal_out.
+__device__ void sc_fs_step(FsState* states, const FsJob& jb, int t, int j, const FsKeys& keys,
+                           const fp2 (&msg)[SC_MAX_DEGREE], uint32_t (&state)[8], uint64_t& counter,
+                           uint64_t* rounds_out, uint64_t* chal_out, uint32_t* buf) {
+    const int lane = threadIdx.x & 31;
+    const int degree = jb.degree;
+    FsState* st = states + t;
     if (lane == 0) {
         uint64_t* rj = rounds_out + jb.rounds_off + (size_t)j * 2 * degree;
         for (int x = 0; x < degree; x++) rj[2 * x] = msg[x].c0, rj[2 * x + 1] = msg[x].c1;
@@ -494,6 +487,31 @@ __device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, cons
     st->r[1] = c1;
     chal_out[jb.chal_off + 2 * j] = c0;
     chal_out[jb.chal_off + 2 * j + 1] = c1;
+}
+
+// Round j's message of each job: Σ over its instances of w_i·(own sums, or 2^{pad_i − j − 1}·S_i
+// while padded), absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
+// <prefix>/r/j. One warp runs job t's round (buf: FS_BUF_WORDS of the warp's shared memory), the
+// state read from the job's FsState (through L2: the persistent rounds move a job between blocks).
+__device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, const FsKeys& keys, const uint64_t* w,
+                          const int* pad, const uint64_t* S, const uint64_t* msgbuf, uint64_t* rounds_out,
+                          uint64_t* chal_out, uint32_t* buf) {
+    const FsJob& jb = jobs[t];
+    if (j >= jb.n_max) return;
+    fp2 msg[SC_MAX_DEGREE];
+    for (int x = 0; x < SC_MAX_DEGREE; x++) msg[x] = {0, 0};
+    for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {  // every lane forms the message
+        if (j < pad[i]) continue;
+        const fp2 wi = {w[2 * i], w[2 * i + 1]};
+        const uint64_t* m = msgbuf + (size_t)i * SC_MSG_WORDS;
+        for (int x = 0; x < jb.degree; x++) msg[x] = e_add(msg[x], e_mul(wi, fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)}));
+    }
+    sc_fs_padded(jb, j, w, pad, S, msg);
+    uint32_t state[8];
+#pragma unroll
+    for (int i = 0; i < 8; i++) state[i] = __ldcg(reinterpret_cast<const uint32_t*>(states[t].state) + i);
+    uint64_t counter = __ldcg(&states[t].counter);
+    sc_fs_step(states, jb, t, j, keys, msg, state, counter, rounds_out, chal_out, buf);
 }
 
 __global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const FsJob* jobs, int njobs, int j,
@@ -571,10 +589,38 @@ __device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen) {
     return ok;
 }
 
+// Segments of a one-block round whose sums the block keeps in shared memory for the transcripts
+// (the rest go through their instances' message words in device memory).
+constexpr int SC_SMSG_SEGS = 32;
+
+// The transcript state of the job a warp owns, kept in shared memory between its rounds: the 8
+// state words, then the counter as two words.
+__device__ __forceinline__ void fst_load(const uint32_t* f, uint32_t (&state)[8], uint64_t& counter) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) state[i] = f[i];
+    counter = (uint64_t)f[8] | ((uint64_t)f[9] << 32);
+}
+__device__ __forceinline__ void fst_store(uint32_t* f, const uint32_t (&state)[8], uint64_t counter) {
+    if ((threadIdx.x & 31) == 0) {
+#pragma unroll
+        for (int i = 0; i < 8; i++) f[i] = state[i];
+        f[8] = (uint32_t)counter;
+        f[9] = (uint32_t)(counter >> 32);
+    }
+    __syncwarp();
+}
+__device__ __forceinline__ void fst_global(const FsState& st, uint32_t (&state)[8], uint64_t& counter) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) state[i] = __ldcg(reinterpret_cast<const uint32_t*>(st.state) + i);
+    counter = __ldcg(&st.counter);
+}
+
 template <int D>
 __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) {
     __shared__ Seg g;
     __shared__ uint32_t sbuf[SC_THREADS / 32][FS_BUF_WORDS];
+    __shared__ uint32_t fst[SC_THREADS / 32][10];
+    __shared__ uint64_t smsg[SC_SMSG_SEGS][2 * D];
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned G = gridDim.x;
     unsigned gen = 0;
@@ -601,11 +647,17 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) 
                 for (int b = blockIdx.x; b < A->njobs; b += G) atomicExch(&A->states[b].err, 2u);
             return;
         }
+        // each warp owns at most one job when there are few: its state then stays in shared memory
+        const bool keep = A->njobs <= (int)G * (SC_THREADS / 32);
         for (int b = blockIdx.x + G * warp; b < A->njobs; b += G * (SC_THREADS / 32)) {
             const FsJob& jb = A->jobs[b];
+            const int j = A->jp + t;
+            if (j >= jb.n_max) continue;
+            fp2 msg[SC_MAX_DEGREE];
+            for (int x = 0; x < SC_MAX_DEGREE; x++) msg[x] = {0, 0};
             for (int si = s0; si < s1; si++) {
-                const Seg& q = A->segs[si];
-                if (q.inst < jb.inst0 || q.inst >= jb.inst0 + jb.ninst) continue;
+                const int inst = __ldg(&A->segs[si].inst);
+                if (inst < jb.inst0 || inst >= jb.inst0 + jb.ninst) continue;
                 uint64_t acc[2 * D];
 #pragma unroll
                 for (int w = 0; w < 2 * D; w++) acc[w] = 0;
@@ -616,12 +668,20 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) 
 #pragma unroll
                 for (int w = 0; w < 2 * D; w++)
                     for (int o = 16; o > 0; o >>= 1) acc[w] = add(acc[w], __shfl_xor_sync(0xFFFFFFFFu, acc[w], o));
-                if (lane == 0)
-                    for (int w = 0; w < 2 * q.degree; w++) q.out[w] = acc[w];
+                const fp2 wi = {A->w[2 * inst], A->w[2 * inst + 1]};
+#pragma unroll
+                for (int x = 0; x < D; x++)
+                    if (x < jb.degree) msg[x] = e_add(msg[x], e_mul(wi, fp2{acc[2 * x], acc[2 * x + 1]}));
             }
-            __syncwarp();
-            sc_fs_job(A->states, A->jobs, b, A->jp + t, A->keys, A->w, A->pad, A->S, A->msgbuf, A->rounds_out,
-                      A->chal_out, sbuf[warp]);
+            sc_fs_padded(jb, j, A->w, A->pad, A->S, msg);
+            uint32_t state[8];
+            uint64_t counter;
+            if (keep && t > 0)
+                fst_load(fst[warp], state, counter);
+            else
+                fst_global(A->states[b], state, counter);
+            sc_fs_step(A->states, jb, b, j, A->keys, msg, state, counter, A->rounds_out, A->chal_out, sbuf[warp]);
+            if (keep) fst_store(fst[warp], state, counter);
         }
         if (!grid_meet(A->bar, G, gen)) {
             if (threadIdx.x == 0)
@@ -630,8 +690,11 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) 
         }
     }
     if (blockIdx.x != 0) return;
+    // every warp owns at most one job here (at most 8 jobs take this path): job `warp`, its state in
+    // shared memory from its first round on
     for (int t = A->multi; t < A->rounds; t++) {
-        for (int si = A->first[t]; si < A->first[t + 1]; si++) {
+        const int s0 = A->first[t], s1 = A->first[t + 1];
+        for (int si = s0; si < s1; si++) {
             if (threadIdx.x < (int)(sizeof(Seg) / 8))
                 reinterpret_cast<uint64_t*>(&g)[threadIdx.x] = reinterpret_cast<const uint64_t*>(A->segs + si)[threadIdx.x];
             __syncthreads();
@@ -641,14 +704,45 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) 
             if (!seg_sums_fast<D, true>(g, 0, words)) sc_seg_sums<D, true>(g, 0, words);
             block_sum<2 * D>(words);  // ends with a barrier
             if (threadIdx.x == 0) {
-                const int nout = g.kind == 1 ? 2 : 2 * g.degree;
-                for (int w = 0; w < nout; w++) g.out[w] = words[w];
+                if (si - s0 < SC_SMSG_SEGS) {
+#pragma unroll
+                    for (int w = 0; w < 2 * D; w++) smsg[si - s0][w] = words[w];
+                } else {
+                    const int nout = g.kind == 1 ? 2 : 2 * g.degree;
+                    for (int w = 0; w < nout; w++) g.out[w] = words[w];
+                }
             }
             __syncthreads();
         }
-        for (int job = warp; job < A->njobs; job += SC_THREADS / 32)
-            sc_fs_job(A->states, A->jobs, job, A->jp + t, A->keys, A->w, A->pad, A->S, A->msgbuf, A->rounds_out,
-                      A->chal_out, sbuf[warp]);
+        if (warp < A->njobs) {
+            const int b = warp;
+            const FsJob& jb = A->jobs[b];
+            const int j = A->jp + t;
+            if (j < jb.n_max) {
+                fp2 msg[SC_MAX_DEGREE];
+                for (int x = 0; x < SC_MAX_DEGREE; x++) msg[x] = {0, 0};
+                for (int si = s0; si < s1; si++) {
+                    const int inst = __ldg(&A->segs[si].inst);
+                    if (inst < jb.inst0 || inst >= jb.inst0 + jb.ninst) continue;
+                    const fp2 wi = {A->w[2 * inst], A->w[2 * inst + 1]};
+                    const uint64_t* m = si - s0 < SC_SMSG_SEGS ? smsg[si - s0] : A->msgbuf + (size_t)inst * SC_MSG_WORDS;
+                    for (int x = 0; x < jb.degree; x++) {
+                        const fp2 v = si - s0 < SC_SMSG_SEGS ? fp2{m[2 * x], m[2 * x + 1]}
+                                                              : fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)};
+                        msg[x] = e_add(msg[x], e_mul(wi, v));
+                    }
+                }
+                sc_fs_padded(jb, j, A->w, A->pad, A->S, msg);
+                uint32_t state[8];
+                uint64_t counter;
+                if (t > A->multi)
+                    fst_load(fst[warp], state, counter);
+                else
+                    fst_global(A->states[b], state, counter);
+                sc_fs_step(A->states, jb, b, j, A->keys, msg, state, counter, A->rounds_out, A->chal_out, sbuf[warp]);
+                fst_store(fst[warp], state, counter);
+            }
+        }
         __syncthreads();
     }
 }
