@@ -132,6 +132,29 @@ def test_prove_many_batched_workload_vs_plain(dev, max_vars):
             assert (alone.gamma, alone.proof.rounds, alone.point, alone.proof.final_evals) == (g, rounds, chal, evals)
 
 
+def test_prove_many_many_small_jobs_vs_oracle(dev):
+    """200 small jobs (4..9 variables, degree 2 or 3) in one prove_many: more jobs than the
+    persistent rounds' warps, so each job's transcript state goes through device memory between
+    rounds; every job equals the CPU oracle's proof on its own transcript."""
+    from tessera_gb300.hash import Transcript
+    from tessera_gb300.sumcheck import Instance, Protocol, Table, prove_many
+    from tessera_gb300.workloads import splitmix_words
+
+    rs = np.random.default_rng(11)
+    specs = []
+    for b in range(200):
+        vars_, degree = int(rs.integers(4, 10)), int(rs.integers(2, 4))
+        specs.append((vars_, degree, [splitmix_words(0x9100 + 7 * b + i, 1 << vars_) for i in range(degree)]))
+    ts = [Transcript(ctx(b.to_bytes(16, "little"))) for b in range(len(specs))]
+    res = prove_many([(ts[b], Protocol.ONE, "stage/0", deg, [Instance([Table.base(x) for x in tabs])])
+                      for b, (_, deg, tabs) in enumerate(specs)], device=dev)
+    for b, ((_, deg, tabs), pb) in enumerate(zip(specs, res)):
+        ot = O.OracleTranscript(ctx(b.to_bytes(16, "little")).tce())
+        g, rounds, chal, evals = O.prove_batch(ot, "stage/0", deg, [[(x, False, False) for x in tabs]])
+        assert (pb.gamma, pb.proof.rounds, pb.point, pb.proof.final_evals) == (g, rounds, chal, evals), b
+        assert ts[b].state == ot.state and ts[b].counter == ot.counter
+
+
 def test_prove_many_device_tables(dev):
     """Tables already in device memory (torch tensors) go through without copies."""
     import torch
