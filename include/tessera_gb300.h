@@ -102,6 +102,12 @@ int tg_measure_int_peaks(tg_device *dev, tg_int_peaks *out);
  * Σ_{k<64} words[(i+k) % n]·words[(i+2k+1) % n] as one unreduced sum. n ≥ 4; host buffers. */
 #define TG_LAZY_CHECK_OUTS 16
 int tg_check_lazy_arith(tg_device *dev, const uint64_t *words, size_t n, uint64_t *out);
+/* A self-check of the bounded meetings between the persistent sumcheck rounds' blocks: `blocks`
+ * co-resident blocks (at most one per SM) meet `meetings` times, except block `absent` (-1: none),
+ * which leaves first; the others then give up after `polls` polls each (at least 256) instead of
+ * waiting for it. *met = the blocks that met every time, *gave_up = whether the meeting point
+ * recorded a give-up. */
+int tg_check_grid_meet(tg_device *dev, int blocks, int meetings, int absent, uint32_t polls, int *met, int *gave_up);
 
 /* Synthetic inputs on the device (no reference counterpart; the reference benchmark draws the
  * same words on the host, crates/tessera-bench/benches/primitives.rs:52-69): out[i] is the

@@ -121,6 +121,7 @@ SIGNATURES = {
     "tg_device_launches": [V, V],
     "tg_measure_int_peaks": [V, V],
     "tg_check_lazy_arith": [V, V, SZ, V],
+    "tg_check_grid_meet": [V, INT, INT, INT, U32, V, V],
     "tg_fill_splitmix": [V, V, SZ, U64, V],
     "tg_fill_counter": [V, V, SZ, U64, V],
     "tg_device_trim": [V],

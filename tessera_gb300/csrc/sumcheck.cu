@@ -559,7 +559,7 @@ constexpr unsigned SC_BAR_POLLS = 1u << 24;  // about a second of polling before
 // All G blocks of the launch meet. A block waits at most SC_BAR_POLLS polls, and stops waiting
 // once another block has given up; then every thread of the block gets false (and the caller
 // returns, so that no block waits on one that has left). The transcripts record the failure.
-__device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen) {
+__device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen, unsigned polls = SC_BAR_POLLS) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -573,7 +573,7 @@ __device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen) {
         } else {
             for (unsigned it = 1;; it++) {
                 if (*(volatile unsigned*)(bar + SC_BAR_GEN) == target) break;
-                if ((it & 255) == 0 && (*(volatile unsigned*)(bar + SC_BAR_FAIL) || it >= SC_BAR_POLLS)) {
+                if ((it & 255) == 0 && (*(volatile unsigned*)(bar + SC_BAR_FAIL) || it >= polls)) {
                     atomicExch(bar + SC_BAR_FAIL, 1u);
                     good = 0;
                     break;
@@ -587,6 +587,20 @@ __device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen) {
     __syncthreads();
     gen++;
     return ok;
+}
+
+// A self-check of the meeting point (for tests): the launch's blocks meet `meetings` times, except
+// block `absent` (−1: none), which leaves before the first meeting, so the others must give up
+// after `polls` polls. out[0] counts the blocks that met every time, out[1] is the give-up flag.
+__global__ void grid_meet_check(unsigned* bar, int meetings, int absent, unsigned polls, unsigned* out) {
+    if ((int)blockIdx.x == absent) return;
+    unsigned gen = 0;
+    bool all = true;
+    for (int m = 0; m < meetings && all; m++) all = grid_meet(bar, gridDim.x, gen, polls);
+    if (threadIdx.x == 0) {
+        if (all) atomicAdd(out, 1u);
+        if (*(volatile unsigned*)(bar + SC_BAR_FAIL)) out[1] = 1;
+    }
 }
 
 // Segments of a one-block round whose sums the block keeps in shared memory for the transcripts
@@ -1395,5 +1409,31 @@ extern "C" int tg_prove_batch(tg_device* dev, tg_transcript* t, const char* pref
     gamma[0] = jb.gamma[0];
     gamma[1] = jb.gamma[1];
     *n_evals = jb.n_evals;
+    return TG_OK;
+}
+
+extern "C" int tg_check_grid_meet(tg_device* dev, int blocks, int meetings, int absent, uint32_t polls, int* met,
+                                  int* gave_up) {
+    Device* d = reinterpret_cast<Device*>(dev);
+    if (!d || !met || !gave_up) return fail(TG_ERR_INVALID, "tg_check_grid_meet: null argument");
+    if (blocks < 1 || blocks > d->sm_count || meetings < 0 || absent >= blocks || polls < 256)
+        return fail(TG_ERR_INVALID, "tg_check_grid_meet: %d blocks, %d meetings, absent %d, %u polls", blocks, meetings,
+                    absent, polls);
+    if (!cooperative(d)) return fail(TG_ERR_STATE, "the device takes no cooperative launches");
+    std::lock_guard<std::mutex> lock(d->mu);
+    DevBuf b;
+    int rc = b.ensure(4 * SC_BAR_WORDS + 8);
+    if (rc) return rc;
+    cudaStream_t s = d->stream;
+    unsigned* bar = (unsigned*)b.ptr;
+    unsigned* out = bar + SC_BAR_WORDS;
+    TG_CUDA(cudaMemsetAsync(b.ptr, 0, 4 * SC_BAR_WORDS + 8, s));
+    void* args[] = {(void*)&bar, (void*)&meetings, (void*)&absent, (void*)&polls, (void*)&out};
+    TG_CUDA(cudaLaunchCooperativeKernel((const void*)grid_meet_check, dim3(blocks), dim3(SC_THREADS), args, 0, s));
+    unsigned h[2] = {0, 0};
+    TG_CUDA(cudaMemcpyAsync(h, out, 8, cudaMemcpyDeviceToHost, s));
+    TG_CUDA(cudaStreamSynchronize(s));
+    *met = (int)h[0];
+    *gave_up = (int)h[1];
     return TG_OK;
 }

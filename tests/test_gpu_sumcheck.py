@@ -216,3 +216,23 @@ def test_grind_matches_oracle_20_bits(dev):
     ot = O.OracleTranscript(bench_context().tce())
     assert t.grind("query-pow", 16, device=dev) == ot.grind("query-pow", 16)
     assert t.state == ot.state
+
+
+def test_persistent_rounds_meetings_are_bounded(dev):
+    """The persistent rounds' blocks meet between rounds with bounded waits: 64 blocks meet 200
+    times; with one block gone before the first meeting, the others give up after their polls, the
+    meeting point records it, and the call returns (no block waits for good)."""
+    import ctypes
+    import time
+
+    from tessera_gb300 import _native as N
+
+    met, gave = ctypes.c_int(), ctypes.c_int()
+    N.call("tg_check_grid_meet", dev.handle, 64, 200, -1, 1 << 22, ctypes.byref(met), ctypes.byref(gave))
+    assert (met.value, gave.value) == (64, 0)
+    t0 = time.perf_counter()
+    N.call("tg_check_grid_meet", dev.handle, 64, 200, 5, 1 << 14, ctypes.byref(met), ctypes.byref(gave))
+    assert (met.value, gave.value) == (0, 1)
+    assert time.perf_counter() - t0 < 10
+    with pytest.raises(N.TesseraError):
+        N.call("tg_check_grid_meet", dev.handle, 64, 1, 64, 1 << 14, ctypes.byref(met), ctypes.byref(gave))
