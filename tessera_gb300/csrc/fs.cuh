@@ -31,8 +31,10 @@ struct FsJob {
     char label[168];  // the job's prefix
     int label_len;
     int degree, ninst, n_max, inst0;  // inst0: the job's first instance in the per-instance arrays
+    int pad_max;                      // the most padding rounds of any of its instances
     uint64_t rounds_off, chal_off;    // word offsets of the job's rounds and challenges
 };
+static_assert(sizeof(FsJob) % 8 == 0, "FsJob copies as words");
 
 // A message is built as bytes in a shared-memory buffer and hashed a 64-byte block at a time
 // straight from the buffer's words (little-endian, as BLAKE3 reads them).
@@ -88,22 +90,35 @@ static __device__ __forceinline__ void compress_one(uint32_t cv[8], const uint32
 #undef FS_ROUND
 #undef FS_G
 
-// BLAKE3 in derive-key-material mode under `key` of the first len bytes of buf (zero from len to
-// the next block boundary), by lane 0 of a warp; every lane gets the output.
-static __device__ __noinline__ void fs_hash_warp(const uint32_t key[8], const uint32_t* buf, uint32_t len, uint32_t out[8]) {
-    uint32_t h[8];
+// Eight words passed and returned by value, so that a call keeps them in registers (an array
+// passed by address would live in local memory around every call).
+struct Fs8 {
+    uint32_t w[8];
+};
+static __device__ __forceinline__ Fs8 fs8(const uint32_t* p) {
+    Fs8 v;
 #pragma unroll
-    for (int i = 0; i < 8; i++) h[i] = key[i];
+    for (int i = 0; i < 8; i++) v.w[i] = p[i];
+    return v;
+}
+
+// BLAKE3 in derive-key-material mode under `key` of the first len bytes of buf (zero from len to
+// the next block boundary), by lane 0 of a warp; every lane gets the output. One copy of the
+// compression serves every call site.
+static __device__ __noinline__ Fs8 fs_hash_warp(Fs8 key, const uint32_t* buf, uint32_t len) {
+    Fs8 h = key;
     if ((threadIdx.x & 31) == 0) {
         const uint32_t nb = len == 0 ? 1 : (len + 63) / 64;
         for (uint32_t b = 0; b < nb; b++) {
             const bool last = b + 1 == nb;
-            compress_one(h, buf + 16 * b, last ? len - 64 * b : 64,
+            compress_one(h.w, buf + 16 * b, last ? len - 64 * b : 64,
                          b3::DERIVE_KEY_MATERIAL | (b == 0 ? b3::CHUNK_START : 0) | (last ? (b3::CHUNK_END | b3::ROOT) : 0));
         }
     }
+    Fs8 out;
 #pragma unroll
-    for (int i = 0; i < 8; i++) out[i] = __shfl_sync(0xFFFFFFFFu, h[i], 0);
+    for (int i = 0; i < 8; i++) out.w[i] = __shfl_sync(0xFFFFFFFFu, h.w[i], 0);
+    return out;
 }
 
 // A label tail ("/round/", "/r/") as little-endian bytes of one word, and its length.
@@ -123,8 +138,9 @@ constexpr int fs_len(const char* t) {
 // lane), then zeros to the next block boundary; returns the length in every lane. Each lane writes
 // its own bytes (the caller syncs the warp before buf is read).
 template <int NP>
-static __device__ uint32_t fs_msg_warp(const uint32_t state[8], const FsJob& jb, uint64_t tail, int tail_len, int j,
-                                       const uint64_t (&pay)[NP], int np, uint32_t* buf) {
+static __device__ __forceinline__ uint32_t fs_msg_warp(const uint32_t (&state)[8], const FsJob& jb, uint64_t tail,
+                                                       int tail_len, int j, const uint64_t (&pay)[NP], int np,
+                                                       uint32_t* buf) {
     const int lane = threadIdx.x & 31;
     uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
     int nd = 1;  // decimal digits of j
@@ -168,18 +184,23 @@ static __device__ uint32_t fs_msg_warp(const uint32_t state[8], const FsJob& jb,
 // squeezes <prefix>/r/j until the first two words are a canonical Fp2 (c0, c1), every lane building
 // the squeeze and ratchet inputs. state and counter are the same in every lane. False after
 // FS_MAX_TRIES squeezes.
-static __device__ bool fs_round_warp(const FsKeys& keys, const FsJob& jb, int j, uint32_t* buf, uint32_t len,
-                                     uint32_t state[8], uint64_t* counter, uint64_t* c0, uint64_t* c1) {
+static __device__ __forceinline__ bool fs_round_warp(const FsKeys& keys, const FsJob& jb, int j, uint32_t* buf,
+                                                     uint32_t len, uint32_t (&state)[8], uint64_t* counter,
+                                                     uint64_t* c0, uint64_t* c1) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
-    fs_hash_warp(keys.absorb, buf, len, state);
+    {
+        const Fs8 h = fs_hash_warp(fs8(keys.absorb), buf, len);
+#pragma unroll
+        for (int i = 0; i < 8; i++) state[i] = h.w[i];
+    }
     __syncwarp();
     for (int tries = 0; tries < FS_MAX_TRIES; tries++) {
         const uint64_t pay[1] = {*counter};
         const uint32_t l2 = fs_msg_warp<1>(state, jb, fs_pack("/r/"), fs_len("/r/"), j, pay, 1, buf);
         __syncwarp();
-        uint32_t out[8];
-        fs_hash_warp(keys.squeeze, buf, l2, out);
+        const Fs8 sq = fs_hash_warp(fs8(keys.squeeze), buf, l2);
+        const uint32_t(&out)[8] = sq.w;
         __syncwarp();
         *counter += 1;
         if (lane < 16) {  // the ratchet's input: state ‖ squeezed block
@@ -192,7 +213,11 @@ static __device__ bool fs_round_warp(const FsKeys& keys, const FsJob& jb, int j,
             buf[lane] = v;
         }
         __syncwarp();
-        fs_hash_warp(keys.ratchet, buf, 64, state);
+        {
+            const Fs8 h = fs_hash_warp(fs8(keys.ratchet), buf, 64);
+#pragma unroll
+            for (int i = 0; i < 8; i++) state[i] = h.w[i];
+        }
         __syncwarp();
         *c0 = (uint64_t)out[0] | ((uint64_t)out[1] << 32);
         *c1 = (uint64_t)out[2] | ((uint64_t)out[3] << 32);

@@ -19,6 +19,7 @@
 // are absorbed on the host after them; each transcript travels to the device and back once.
 // tg_prove_batch is the one-job case.
 #include <cuda_runtime.h>
+#include <stddef.h>
 #include <stdint.h>
 #include <string.h>
 
@@ -58,9 +59,12 @@ struct Seg {
     uint32_t base_mask;                  // bit k: table k's source holds prime-field words
     int nt, degree, bind, kind;          // kind 0: round sums, 1: Σ_x Π_k T_k[x]
     int block0, nblocks, part0;          // the segment's blocks in the launch, its first partials row
-    int inst;                            // the instance
+    int inst, job;                       // the instance and its job
 };
 static_assert(sizeof(Seg) % 8 == 0, "Seg copies as words");
+// sc_persist patches words of a Seg as it copies them into shared memory
+static_assert(offsetof(Seg, r) % 8 == 0 && offsetof(Seg, nblocks) % 8 == 0 && offsetof(Seg, job) % 8 == 4,
+              "Seg word layout");
 
 struct BindLast {
     const uint64_t* src;
@@ -74,20 +78,22 @@ struct EvalRef {
     int base, pad_;
 };
 
-// CG: through L2 only, for tables that other blocks of the same launch wrote (the persistent rounds).
-template <bool CG = false>
+// How a round reads its tables: MEM_LAUNCH in a launch of its own (streamed past the caches), MEM_L2
+// where other blocks of the same launch may have written them (the persistent rounds: through L2
+// only). The challenge is read with plain loads in both modes: a launched round reads it from
+// device memory that an earlier launch wrote, the persistent rounds from the block's shared memory.
+enum { MEM_LAUNCH = 0, MEM_L2 = 1 };
+
+template <int MEM = MEM_LAUNCH>
 __device__ __forceinline__ fp2 load_entry(const uint64_t* t, bool base, uint64_t i) {
-    if (base) return e_lift(CG ? __ldcg(t + i) : t[i]);
-    const ulonglong2 v = CG ? __ldcg(reinterpret_cast<const ulonglong2*>(t) + i)
-                            : reinterpret_cast<const ulonglong2*>(t)[i];  // (c0, c1) words
+    if (base) return e_lift(MEM == MEM_L2 ? __ldcg(t + i) : t[i]);
+    const ulonglong2 v = MEM == MEM_L2 ? __ldcg(reinterpret_cast<const ulonglong2*>(t) + i)
+                                       : reinterpret_cast<const ulonglong2*>(t)[i];  // (c0, c1) words
     return {v.x, v.y};
 }
 
 // The challenge to bind, written by the previous round's transcript.
-template <bool CG>
-__device__ __forceinline__ fp2 load_r(const uint64_t* r) {
-    return CG ? fp2{__ldcg(r), __ldcg(r + 1)} : fp2{r[0], r[1]};
-}
+__device__ __forceinline__ fp2 load_r(const uint64_t* r) { return fp2{r[0], r[1]}; }
 
 // a + r·(b − a) on lazy words (bound tables hold lazy words; the last bind canonicalises); r7 =
 // 7·r.c1.
@@ -120,11 +126,12 @@ __device__ __forceinline__ void block_sum(uint64_t (&v)[NW]) {
     __syncthreads();
 }
 
-// A table's 16 bytes at p, streamed (every entry is read once per round); CG: through L2 only.
-template <bool CG>
+// A table's 16 bytes at p, read as MEM says (streamed in a launch of its own: every entry is read
+// once per round).
+template <int MEM>
 __device__ __forceinline__ ulonglong2 ld_once(const uint64_t* t, uint64_t p) {
     ulonglong2 v;
-    if constexpr (CG)
+    if constexpr (MEM == MEM_L2)
         asm volatile("ld.global.cg.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(t + 2 * p));
     else
         asm volatile("ld.global.cs.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "l"(t + 2 * p));
@@ -137,7 +144,7 @@ __device__ __forceinline__ ulonglong2 ld_once(const uint64_t* t, uint64_t p) {
 // bind r into their source (prime-field or Fp2 entries), store the bound pair and sum in Fp2. All
 // of a thread's loads for U pairs are issued before any is used, so that each thread keeps
 // U·NT·(1, 2 or 4) 16-byte loads in flight.
-template <int D, int NT, int DEG, bool BIND, bool SRC_BASE, int U, bool CG>
+template <int D, int NT, int DEG, bool BIND, bool SRC_BASE, int U, int MEM>
 __device__ __forceinline__ void seg_sums_fixed(const Seg& g, int lb, uint64_t (&words)[2 * D]) {
     static_assert(DEG <= D && NT <= DEG && (BIND || SRC_BASE), "shape");
     const uint64_t stride = (uint64_t)g.nblocks * blockDim.x, n = g.n;
@@ -152,7 +159,7 @@ __device__ __forceinline__ void seg_sums_fixed(const Seg& g, int lb, uint64_t (&
             for (int q = 0; q < U; q++) {
                 const uint64_t p = p0 + q * stride;
 #pragma unroll
-                for (int k = 0; k < NT; k++) x[q][k] = p < n ? ld_once<CG>(g.src[k], p) : make_ulonglong2(0, 0);
+                for (int k = 0; k < NT; k++) x[q][k] = p < n ? ld_once<MEM>(g.src[k], p) : make_ulonglong2(0, 0);
             }
 #pragma unroll
             for (int q = 0; q < U; q++) {
@@ -175,7 +182,7 @@ __device__ __forceinline__ void seg_sums_fixed(const Seg& g, int lb, uint64_t (&
 #pragma unroll
         for (int d = 0; d < DEG; d++) words[2 * d] = lz::canon(acc[d]);
     } else {
-        const fp2 r = load_r<CG>(g.r);
+        const fp2 r = load_r(g.r);
         const uint64_t r7 = lz::mul7(r.c1);
         constexpr int L = SRC_BASE ? 2 : 4;  // 16-byte loads per table and pair: 4 source entries
         fp2 acc[DEG];
@@ -189,7 +196,7 @@ __device__ __forceinline__ void seg_sums_fixed(const Seg& g, int lb, uint64_t (&
 #pragma unroll
                 for (int k = 0; k < NT; k++)
 #pragma unroll
-                    for (int l = 0; l < L; l++) x[q][k][l] = p < n ? ld_once<CG>(g.src[k], L * p + l) : make_ulonglong2(0, 0);
+                    for (int l = 0; l < L; l++) x[q][k][l] = p < n ? ld_once<MEM>(g.src[k], L * p + l) : make_ulonglong2(0, 0);
             }
 #pragma unroll
             for (int q = 0; q < U; q++) {
@@ -232,23 +239,106 @@ __device__ __forceinline__ void seg_sums_fixed(const Seg& g, int lb, uint64_t (&
     }
 }
 
-// The shapes seg_sums_fixed covers; false leaves the segment to the general loops.
-template <int D, bool CG = false>
+// The bind rounds of seg_sums_fixed's shapes when a segment has at most two pairs per group of
+// four threads: four lanes take a pair; lane q < NT binds table q's pair and forms its values at the
+// NT nodes, then lane d < NT multiplies the tables' values at node d — passed round the group by
+// shuffles, at step s from the lane of table (d + s) mod NT — and keeps node d's sum. A pair's
+// arithmetic is spread over NT lanes instead of one: the persistent launch's small rounds, whose
+// threads hold a pair or none, are bound by that arithmetic's latency.
+template <int D, int NT, bool SRC_BASE, int MEM>
+__device__ __forceinline__ void seg_sums_split(const Seg& g, int lb, uint64_t (&words)[2 * D]) {
+    static_assert(NT <= D && NT >= 2 && NT <= 3, "shape");
+    constexpr int L = SRC_BASE ? 2 : 4;  // 16-byte loads of a table's pair: its four source entries
+    const int lane = threadIdx.x & 31, q = lane & 3;
+    const bool act = q < NT;
+    const uint64_t n = g.n, groups = (uint64_t)g.nblocks * (blockDim.x / 4);
+    const fp2 r = load_r(g.r);
+    const uint64_t r7 = lz::mul7(r.c1);
+    const uint64_t* src = g.src[act ? q : 0];
+    ulonglong2* out = reinterpret_cast<ulonglong2*>(g.dst[act ? q : 0]);
+    fp2 acc = {0, 0};
+    // warp-uniform steps: every lane of the warp takes part in every shuffle
+    for (uint64_t p0 = (uint64_t)lb * (blockDim.x / 4) + (threadIdx.x >> 5) * 8; p0 < n; p0 += groups) {
+        const uint64_t p = p0 + (lane >> 2);
+        const bool live = act && p < n;
+        ulonglong2 x[L];
+#pragma unroll
+        for (int l = 0; l < L; l++) x[l] = live ? ld_once<MEM>(src, L * p + l) : make_ulonglong2(0, 0);
+        fp2 u, v;
+        if constexpr (SRC_BASE) {
+            u = bind_pair(e_lift(x[0].x), e_lift(x[0].y), r, r7, true);
+            v = bind_pair(e_lift(x[1].x), e_lift(x[1].y), r, r7, true);
+        } else {
+            u = bind_pair({x[0].x, x[0].y}, {x[1].x, x[1].y}, r, r7, false);
+            v = bind_pair({x[2].x, x[2].y}, {x[3].x, x[3].y}, r, r7, false);
+        }
+        if (live) {
+            out[2 * p] = make_ulonglong2(u.c0, u.c1);
+            out[2 * p + 1] = make_ulonglong2(v.c0, v.c1);
+        }
+        fp2 val[NT];  // this lane's table at the nodes: u, then v + (v − u), …
+        const fp2 diff = l2_sub(v, u);
+        val[0] = u;
+        fp2 t = v;
+#pragma unroll
+        for (int d = 1; d < NT; d++) {
+            t = l2_add(t, diff);
+            val[d] = t;
+        }
+        fp2 prod = val[0];
+#pragma unroll
+        for (int d = 1; d < NT; d++)
+            if (q == d) prod = val[d];
+#pragma unroll
+        for (int st = 1; st < NT; st++) {
+            // lane q serves the lane d with (d + st) mod NT = q: its value at node d
+            const int need = (q + NT - st) % NT;
+            fp2 sv = val[0];
+#pragma unroll
+            for (int d = 1; d < NT; d++)
+                if (need == d) sv = val[d];
+            const int from = (lane & ~3) | (act ? (q + st) % NT : q);
+            const fp2 rv = {__shfl_sync(0xFFFFFFFFu, sv.c0, from), __shfl_sync(0xFFFFFFFFu, sv.c1, from)};
+            prod = l2_muls(prod, rv);
+        }
+        if (live) acc = l2_add(acc, prod);
+    }
+    const fp2 c = l2_canon(acc);
+#pragma unroll
+    for (int d = 0; d < NT; d++)
+        if (q == d) words[2 * d] = c.c0, words[2 * d + 1] = c.c1;
+}
+
+// The shapes seg_sums_fixed covers; false leaves the segment to the general loops. SPLIT: the small
+// bind rounds of those shapes through seg_sums_split.
+template <int D, int MEM = MEM_LAUNCH, bool SPLIT = false>
 __device__ __forceinline__ bool seg_sums_fast(const Seg& g, int lb, uint64_t (&words)[2 * D]) {
     if (g.kind != 0) return false;
     const bool all_base = g.base_mask == (1u << g.nt) - 1, all_ext = g.base_mask == 0;
+    if constexpr (SPLIT) {
+        if (g.bind && g.nt == g.degree && g.n <= (uint64_t)g.nblocks * (blockDim.x / 2)) {
+            if constexpr (D >= 3) {
+                if (g.nt == 3 && all_base) return seg_sums_split<D, 3, true, MEM>(g, lb, words), true;
+                if (g.nt == 3 && all_ext) return seg_sums_split<D, 3, false, MEM>(g, lb, words), true;
+            }
+            if constexpr (D >= 2) {
+                if (g.nt == 2 && all_base) return seg_sums_split<D, 2, true, MEM>(g, lb, words), true;
+                if (g.nt == 2 && all_ext) return seg_sums_split<D, 2, false, MEM>(g, lb, words), true;
+            }
+        }
+    }
     if constexpr (D >= 3) {
         if (g.nt == 3 && g.degree == 3) {
-            if (!g.bind && all_base) return seg_sums_fixed<D, 3, 3, false, true, 4, CG>(g, lb, words), true;
-            if (g.bind && all_base) return seg_sums_fixed<D, 3, 3, true, true, 2, CG>(g, lb, words), true;
-            if (g.bind && all_ext) return seg_sums_fixed<D, 3, 3, true, false, 1, CG>(g, lb, words), true;
+            if (!g.bind && all_base) return seg_sums_fixed<D, 3, 3, false, true, 4, MEM>(g, lb, words), true;
+            if (g.bind && all_base) return seg_sums_fixed<D, 3, 3, true, true, 2, MEM>(g, lb, words), true;
+            if (g.bind && all_ext) return seg_sums_fixed<D, 3, 3, true, false, 1, MEM>(g, lb, words), true;
         }
     }
     if constexpr (D >= 2) {
         if (g.nt == 2 && g.degree == 2) {
-            if (!g.bind && all_base) return seg_sums_fixed<D, 2, 2, false, true, 4, CG>(g, lb, words), true;
-            if (g.bind && all_base) return seg_sums_fixed<D, 2, 2, true, true, 2, CG>(g, lb, words), true;
-            if (g.bind && all_ext) return seg_sums_fixed<D, 2, 2, true, false, 2, CG>(g, lb, words), true;
+            if (!g.bind && all_base) return seg_sums_fixed<D, 2, 2, false, true, 4, MEM>(g, lb, words), true;
+            if (g.bind && all_base) return seg_sums_fixed<D, 2, 2, true, true, 2, MEM>(g, lb, words), true;
+            if (g.bind && all_ext) return seg_sums_fixed<D, 2, 2, true, false, 2, MEM>(g, lb, words), true;
         }
     }
     return false;
@@ -256,7 +346,7 @@ __device__ __forceinline__ bool seg_sums_fast(const Seg& g, int lb, uint64_t (&w
 
 // Block lb's share of a segment's sums (a grid-stride loop over the segment's nblocks blocks),
 // canonical, in this thread's words: the d node sums as Fp2 words (kind 0), or the product sum.
-template <int D, bool CG = false>
+template <int D, int MEM = MEM_LAUNCH>
 __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&words)[2 * D]) {
     const uint64_t stride = (uint64_t)g.nblocks * blockDim.x;
     const int deg = g.degree, nt = g.nt;
@@ -269,7 +359,7 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
         for (uint64_t x = (uint64_t)lb * blockDim.x + threadIdx.x; x < g.n; x += stride) {
             fp2 prod = {1, 0};
             for (int k = 0; k < nt; k++) {
-                const fp2 e = load_entry<CG>(g.src[k], (g.base_mask >> k) & 1, x);
+                const fp2 e = load_entry<MEM>(g.src[k], (g.base_mask >> k) & 1, x);
                 prod = k ? l2_muls(prod, e) : e;
             }
             acc = l2_add(acc, prod);
@@ -287,8 +377,8 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
 #pragma unroll
             for (int d = 0; d < D; d++) prod[d] = 1;
             for (int k = 0; k < nt; k++) {  // the first table's values start the products
-                const ulonglong2 v = CG ? __ldcg(reinterpret_cast<const ulonglong2*>(g.src[k]) + p)
-                                        : reinterpret_cast<const ulonglong2*>(g.src[k])[p];
+                const ulonglong2 v = MEM == MEM_L2 ? __ldcg(reinterpret_cast<const ulonglong2*>(g.src[k]) + p)
+                                                   : reinterpret_cast<const ulonglong2*>(g.src[k])[p];
                 const uint64_t diff = lz::sub(v.y, v.x);
                 uint64_t x = v.y;  // value at node 1
                 prod[0] = k ? lz::mul(prod[0], v.x) : v.x;
@@ -309,7 +399,7 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
         fp2 acc[D];
 #pragma unroll
         for (int d = 0; d < D; d++) acc[d] = {0, 0};
-        const fp2 r = g.bind ? load_r<CG>(g.r) : fp2{0, 0};
+        const fp2 r = g.bind ? load_r(g.r) : fp2{0, 0};
         const uint64_t r7 = lz::mul7(r.c1);
         for (uint64_t p = (uint64_t)lb * blockDim.x + threadIdx.x; p < g.n; p += stride) {
             fp2 prod[D];
@@ -319,16 +409,16 @@ __device__ __forceinline__ void sc_seg_sums(const Seg& g, int lb, uint64_t (&wor
                 const bool base = (g.base_mask >> k) & 1;
                 fp2 u, v;
                 if (g.bind) {
-                    u = bind_pair(load_entry<CG>(g.src[k], base, 4 * p), load_entry<CG>(g.src[k], base, 4 * p + 1), r, r7,
+                    u = bind_pair(load_entry<MEM>(g.src[k], base, 4 * p), load_entry<MEM>(g.src[k], base, 4 * p + 1), r, r7,
                                   base);
-                    v = bind_pair(load_entry<CG>(g.src[k], base, 4 * p + 2), load_entry<CG>(g.src[k], base, 4 * p + 3), r,
+                    v = bind_pair(load_entry<MEM>(g.src[k], base, 4 * p + 2), load_entry<MEM>(g.src[k], base, 4 * p + 3), r,
                                   r7, base);
                     ulonglong2* out = reinterpret_cast<ulonglong2*>(g.dst[k]);
                     out[2 * p] = make_ulonglong2(u.c0, u.c1);
                     out[2 * p + 1] = make_ulonglong2(v.c0, v.c1);
                 } else {
-                    u = load_entry<CG>(g.src[k], base, 2 * p);
-                    v = load_entry<CG>(g.src[k], base, 2 * p + 1);
+                    u = load_entry<MEM>(g.src[k], base, 2 * p);
+                    v = load_entry<MEM>(g.src[k], base, 2 * p + 1);
                 }
                 const fp2 diff = l2_sub(v, u);
                 fp2 x = v;
@@ -387,12 +477,12 @@ __global__ void __launch_bounds__(SC_THREADS) sc_rounds(const Seg* segs, int nse
 #pragma unroll
     for (int w = 0; w < 2 * D; w++) words[w] = 0;
     if constexpr (SHAPE == 0) sc_seg_sums<D>(g, lb, words);
-    else if constexpr (SHAPE == 1) seg_sums_fixed<D, 3, 3, false, true, 4, false>(g, lb, words);
-    else if constexpr (SHAPE == 2) seg_sums_fixed<D, 3, 3, true, true, 1, false>(g, lb, words);
-    else if constexpr (SHAPE == 3) seg_sums_fixed<D, 3, 3, true, false, 1, false>(g, lb, words);
-    else if constexpr (SHAPE == 4) seg_sums_fixed<D, 2, 2, false, true, 4, false>(g, lb, words);
-    else if constexpr (SHAPE == 5) seg_sums_fixed<D, 2, 2, true, true, 2, false>(g, lb, words);
-    else seg_sums_fixed<D, 2, 2, true, false, 1, false>(g, lb, words);
+    else if constexpr (SHAPE == 1) seg_sums_fixed<D, 3, 3, false, true, 4, MEM_LAUNCH>(g, lb, words);
+    else if constexpr (SHAPE == 2) seg_sums_fixed<D, 3, 3, true, true, 1, MEM_LAUNCH>(g, lb, words);
+    else if constexpr (SHAPE == 3) seg_sums_fixed<D, 3, 3, true, false, 1, MEM_LAUNCH>(g, lb, words);
+    else if constexpr (SHAPE == 4) seg_sums_fixed<D, 2, 2, false, true, 4, MEM_LAUNCH>(g, lb, words);
+    else if constexpr (SHAPE == 5) seg_sums_fixed<D, 2, 2, true, true, 2, MEM_LAUNCH>(g, lb, words);
+    else seg_sums_fixed<D, 2, 2, true, false, 1, MEM_LAUNCH>(g, lb, words);
     block_sum<2 * D>(words);
 
     // the segment's last block reduces its partial rows
@@ -440,42 +530,55 @@ __global__ void sc_gather_evals(const EvalRef* refs, int n, uint64_t* out) {
 
 // ---- the transcripts on the device (one warp per job) ------------------------------------------
 
+// A job's round message lives in registers: D (the batch's largest degree) values, of which the
+// job's first `degree` are its own; the loops over them unroll to fixed indices.
+
 // The padded instances' part of job jb's round-j message, added to msg: w_i·2^{pad_i − j − 1}·S_i
 // at every node of each instance still in its padding rounds.
+template <int D>
 __device__ __forceinline__ void sc_fs_padded(const FsJob& jb, int j, const uint64_t* w, const int* pad,
-                                             const uint64_t* S, fp2 (&msg)[SC_MAX_DEGREE]) {
+                                             const uint64_t* S, fp2 (&msg)[D]) {
+    if (j >= jb.pad_max) return;  // every instance of the job is past its padding rounds
     for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {
         if (j >= pad[i]) continue;
         const fp2 wi = {w[2 * i], w[2 * i + 1]};
         const fp2 v = e_mul(wi, e_scale(fp2{__ldcg(S + 2 * i), __ldcg(S + 2 * i + 1)}, (1ull << (pad[i] - j - 1)) % P));
-        for (int x = 0; x < jb.degree; x++) msg[x] = e_add(msg[x], v);
+#pragma unroll
+        for (int x = 0; x < D; x++)
+            if (x < jb.degree) msg[x] = e_add(msg[x], v);
     }
 }
 
 // Round j's transcript step of job t, its message formed (the same in every lane): the message into
 // rounds_out, absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
 // <prefix>/r/j. state and counter (the same in every lane) are read and updated here; lane 0 writes
-// them, r_j and the challenge back to the job's FsState and to chal_out.
-__device__ void sc_fs_step(FsState* states, const FsJob& jb, int t, int j, const FsKeys& keys,
-                           const fp2 (&msg)[SC_MAX_DEGREE], uint32_t (&state)[8], uint64_t& counter,
-                           uint64_t* rounds_out, uint64_t* chal_out, uint32_t* buf) {
+// them, r_j and the challenge back to the job's FsState and to chal_out (unless !write: a copy of
+// the step that another block writes), and r_j to r_local when given.
+template <int D>
+__device__ __forceinline__ void sc_fs_step(FsState* states, const FsJob& jb, int t, int j, const FsKeys& keys, const fp2 (&msg)[D],
+                           uint32_t (&state)[8], uint64_t& counter, uint64_t* rounds_out, uint64_t* chal_out,
+                           uint32_t* buf, bool write = true, uint64_t* r_local = nullptr) {
     const int lane = threadIdx.x & 31;
     const int degree = jb.degree;
     FsState* st = states + t;
-    if (lane == 0) {
+    if (lane == 0 && write) {
         uint64_t* rj = rounds_out + jb.rounds_off + (size_t)j * 2 * degree;
-        for (int x = 0; x < degree; x++) rj[2 * x] = msg[x].c0, rj[2 * x + 1] = msg[x].c1;
+#pragma unroll
+        for (int x = 0; x < D; x++)
+            if (x < degree) rj[2 * x] = msg[x].c0, rj[2 * x + 1] = msg[x].c1;
     }
     // the message as TCE Vec<Fp2>: its length, then the values
-    uint64_t pay[1 + 2 * SC_MAX_DEGREE];
+    uint64_t pay[1 + 2 * D];
     pay[0] = (uint64_t)degree;
 #pragma unroll
-    for (int x = 0; x < SC_MAX_DEGREE; x++) pay[1 + 2 * x] = msg[x].c0, pay[2 + 2 * x] = msg[x].c1;
-    const uint32_t len = fs_msg_warp<1 + 2 * SC_MAX_DEGREE>(state, jb, fs_pack("/round/"), fs_len("/round/"), j, pay,
-                                                            1 + 2 * degree, buf);
+    for (int x = 0; x < D; x++) pay[1 + 2 * x] = msg[x].c0, pay[2 + 2 * x] = msg[x].c1;
+    const uint32_t len = fs_msg_warp<1 + 2 * D>(state, jb, fs_pack("/round/"), fs_len("/round/"), j, pay,
+                                                1 + 2 * degree, buf);
     uint64_t c0, c1;
     const bool ok = fs_round_warp(keys, jb, j, buf, len, state, &counter, &c0, &c1);
     if (lane != 0) return;
+    if (r_local) r_local[0] = c0, r_local[1] = c1;
+    if (!write) return;
     if (!ok) {
         st->err = 1;
         return;
@@ -493,18 +596,22 @@ __device__ void sc_fs_step(FsState* states, const FsJob& jb, int t, int j, const
 // while padded), absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
 // <prefix>/r/j. One warp runs job t's round (buf: FS_BUF_WORDS of the warp's shared memory), the
 // state read from the job's FsState (through L2: the persistent rounds move a job between blocks).
+template <int D>
 __device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, const FsKeys& keys, const uint64_t* w,
                           const int* pad, const uint64_t* S, const uint64_t* msgbuf, uint64_t* rounds_out,
                           uint64_t* chal_out, uint32_t* buf) {
     const FsJob& jb = jobs[t];
     if (j >= jb.n_max) return;
-    fp2 msg[SC_MAX_DEGREE];
-    for (int x = 0; x < SC_MAX_DEGREE; x++) msg[x] = {0, 0};
+    fp2 msg[D];
+#pragma unroll
+    for (int x = 0; x < D; x++) msg[x] = {0, 0};
     for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {  // every lane forms the message
         if (j < pad[i]) continue;
         const fp2 wi = {w[2 * i], w[2 * i + 1]};
         const uint64_t* m = msgbuf + (size_t)i * SC_MSG_WORDS;
-        for (int x = 0; x < jb.degree; x++) msg[x] = e_add(msg[x], e_mul(wi, fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)}));
+#pragma unroll
+        for (int x = 0; x < D; x++)
+            if (x < jb.degree) msg[x] = e_add(msg[x], e_mul(wi, fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)}));
     }
     sc_fs_padded(jb, j, w, pad, S, msg);
     uint32_t state[8];
@@ -514,6 +621,7 @@ __device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, cons
     sc_fs_step(states, jb, t, j, keys, msg, state, counter, rounds_out, chal_out, buf);
 }
 
+template <int D>
 __global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const FsJob* jobs, int njobs, int j,
                                                          FsKeys keys, const uint64_t* w, const int* pad,
                                                          const uint64_t* S, const uint64_t* msgbuf,
@@ -521,19 +629,23 @@ __global__ void __launch_bounds__(FS_THREADS) sc_fs_many(FsState* states, const 
     __shared__ uint32_t sbuf[FS_THREADS / 32][FS_BUF_WORDS];
     const int t = (blockIdx.x * blockDim.x + threadIdx.x) / 32;
     if (t >= njobs) return;  // whole warps leave together
-    sc_fs_job(states, jobs, t, j, keys, w, pad, S, msgbuf, rounds_out, chal_out, sbuf[threadIdx.x / 32]);
+    sc_fs_job<D>(states, jobs, t, j, keys, w, pad, S, msgbuf, rounds_out, chal_out, sbuf[threadIdx.x / 32]);
 }
 
 // The rounds jp … J − 1 of a batch in one launch, with no launch between rounds. The first `multi`
 // of them are spread over the launch's G co-resident blocks (a cooperative launch): every block
 // takes its share of every segment of the round (a grid-stride loop over the segment's pairs, one
-// partial row per block and segment); the blocks meet; the warp that owns a job (job b: warp
-// (b / G) mod 8 of block b mod G) reduces the partial rows of its instances into their messages and
-// runs the job's transcript step; the blocks meet again, and the next round binds the new
-// challenges. The rounds after those, whose segments are one block's work, run in
-// block 0 alone (the others have returned): each sums its segments with the whole block, then the
-// block's warps run the transcripts. Whatever another block may have written — tables, partial
-// sums, messages, transcript states — is read through L2.
+// partial row per block and segment), and the blocks meet. With at most eight jobs ("local"), every
+// block then runs every job's transcript step itself — warp b reduces the partial rows of job b's
+// instances into its message and draws its challenge, the same in every block, which only block 0
+// writes out — and goes on to the next round with the challenges in its shared memory: one meeting
+// a round, the partial rows alternating between two halves of the buffer so that a block already
+// in the next round does not overwrite rows that another still reads. With more jobs, the warp that
+// owns a job (job b: warp (b / G) mod 8 of block b mod G) runs its step and the blocks meet again
+// before the next round reads the challenges. The rounds after those, whose segments are one
+// block's work, run in block 0 alone (the others have returned): each sums its segments with the
+// whole block, then the block's warps run the transcripts. Whatever another block may have written
+// — tables, partial sums, messages, transcript states — is read through L2.
 struct ScPersist {
     FsKeys keys;
     FsState* states;
@@ -548,8 +660,11 @@ struct ScPersist {
     const int* first;    // round jp + t's segments are segs[first[t] .. first[t + 1])
     uint64_t* partials;  // G rows per segment of a multi-block round
     unsigned* bar;       // the blocks' meeting point: arrivals, generation, gave up (each on its own 128-byte line)
+    size_t part_words;   // the second half of partials (local): rounds alternate between the halves
     int njobs, jp, rounds, multi;
 };
+static_assert(sizeof(ScPersist) % 8 == 0, "ScPersist copies as words");
+constexpr int SC_MAX_VARS = 40;  // an instance's variables at most (so at most 40 rounds)
 
 // The meeting point's words, each on its own 128-byte line so that the arrivals' atomics and the
 // waiting blocks' polls do not contend for one line.
@@ -582,7 +697,9 @@ __device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen, unsigned pol
             }
         }
         __threadfence();
-        ok = good && !*(volatile unsigned*)(bar + SC_BAR_FAIL);
+        // a block that gave up before the last arrival is seen at the next meeting (its flag is
+        // polled there, and it does not arrive); the rounds up to here had every block's share
+        ok = good;
     }
     __syncthreads();
     gen++;
@@ -629,64 +746,233 @@ __device__ __forceinline__ void fst_global(const FsState& st, uint32_t (&state)[
     counter = __ldcg(&st.counter);
 }
 
+// Segment si's Seg into shared memory, word i by the calling thread (threads with i in 0 … 21 of
+// one warp or of the block; no barrier), patched on the way: nblocks replaces the segment's block
+// count (the multi-block rounds take every segment over all blocks of the launch); the challenge
+// pointer is redirected to shared memory — to the job's latest challenge in sr[job] when local,
+// else to sr_seg, into which the thread copies the challenge from device memory (through L2:
+// another block wrote it).
+__device__ __forceinline__ void persist_seg_load(const Seg* segs, int si, Seg& g, int nblocks, bool local,
+                                                 uint64_t (*sr)[2], uint64_t* sr_seg, int i) {
+    constexpr int W = sizeof(Seg) / 8, WR = offsetof(Seg, r) / 8, WNB = offsetof(Seg, nblocks) / 8,
+                  WJOB = offsetof(Seg, job) / 8;
+    static_assert(W <= 32, "a warp copies a Seg");
+    const uint64_t* src = reinterpret_cast<const uint64_t*>(segs + si);
+    if (i < W) {
+        uint64_t v = src[i];
+        if (i == WR) {
+            if (local) {
+                v = reinterpret_cast<uint64_t>(&sr[(int)(src[WJOB] >> 32)][0]);
+            } else {
+                const uint64_t* rp = reinterpret_cast<const uint64_t*>(v);
+                sr_seg[0] = __ldcg(rp);
+                sr_seg[1] = __ldcg(rp + 1);
+                v = reinterpret_cast<uint64_t>(sr_seg);
+            }
+        }
+        if (i == WNB) v = (v & 0xFFFFFFFF00000000ull) | (uint32_t)nblocks;
+        reinterpret_cast<uint64_t*>(&g)[i] = v;
+    }
+}
+
+// The instance of segment si of a round whose first segment is s0 (recorded in sinst while the
+// block summed the round's segments).
+__device__ __forceinline__ int persist_inst(const ScPersist* A, const int* sinst, int si, int s0) {
+    return si - s0 < SC_SMSG_SEGS ? sinst[si - s0] : __ldg(&A->segs[si].inst);
+}
+
+// Warp-wide: round j's message of job jb from the G partial rows of each of its segments of the
+// round (part: the round's rows, through L2), the same in every lane.
+// Instance inst's weight: from the job's first SC_SW weights in shared memory (sw, when given), else
+// from device memory.
+constexpr int SC_SW = 8;
+__device__ __forceinline__ fp2 persist_weight(const ScPersist* A, const FsJob& jb, const uint64_t (*sw)[2], int inst) {
+    const int k = inst - jb.inst0;
+    if (sw && k < SC_SW) return fp2{sw[k][0], sw[k][1]};
+    return fp2{A->w[2 * inst], A->w[2 * inst + 1]};
+}
+
 template <int D>
-__global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) {
+__device__ __forceinline__ void persist_msg_rows(const ScPersist* A, const FsJob& jb, const uint64_t (*sw)[2],
+                                                 const uint64_t* part, const int* sinst, int s0, int s1, unsigned G,
+                                                 fp2 (&msg)[D]) {
+    const int lane = threadIdx.x & 31;
+#pragma unroll
+    for (int x = 0; x < D; x++) msg[x] = {0, 0};
+    for (int si = s0; si < s1; si++) {
+        const int inst = persist_inst(A, sinst, si, s0);
+        if (inst < jb.inst0 || inst >= jb.inst0 + jb.ninst) continue;
+        uint64_t acc[2 * D];
+#pragma unroll
+        for (int w = 0; w < 2 * D; w++) acc[w] = 0;
+        const uint64_t* rows = part + (size_t)(si - s0) * G * 2 * D;
+        for (int lb0 = lane; lb0 < (int)G; lb0 += 4 * 32) {  // four rows' loads in flight per lane
+            uint64_t v[4][2 * D];
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+#pragma unroll
+                for (int w = 0; w < 2 * D; w++) v[q][w] = lb0 + 32 * q < (int)G ? __ldcg(&rows[(size_t)(lb0 + 32 * q) * 2 * D + w]) : 0;
+#pragma unroll
+            for (int q = 0; q < 4; q++)
+#pragma unroll
+                for (int w = 0; w < 2 * D; w++) acc[w] = add(acc[w], v[q][w]);
+        }
+#pragma unroll
+        for (int w = 0; w < 2 * D; w++)
+            for (int o = 16; o > 0; o >>= 1) acc[w] = add(acc[w], __shfl_xor_sync(0xFFFFFFFFu, acc[w], o));
+        const fp2 wi = persist_weight(A, jb, sw, inst);
+#pragma unroll
+        for (int x = 0; x < D; x++)
+            if (x < jb.degree) msg[x] = e_add(msg[x], e_mul(wi, fp2{acc[2 * x], acc[2 * x + 1]}));
+    }
+}
+
+// Warp-wide: round j's message of job jb from the sums of its segments that this block kept (smsg,
+// or the instance's message words in device memory past SC_SMSG_SEGS segments), the same in every
+// lane.
+template <int D>
+__device__ __forceinline__ void persist_msg_block(const ScPersist* A, const FsJob& jb, const uint64_t (*sw)[2],
+                                                  const uint64_t (*smsg)[2 * D], const int* sinst, int s0, int s1,
+                                                  fp2 (&msg)[D]) {
+#pragma unroll
+    for (int x = 0; x < D; x++) msg[x] = {0, 0};
+    for (int si = s0; si < s1; si++) {
+        const int inst = persist_inst(A, sinst, si, s0);
+        if (inst < jb.inst0 || inst >= jb.inst0 + jb.ninst) continue;
+        const fp2 wi = persist_weight(A, jb, sw, inst);
+        const bool kept = si - s0 < SC_SMSG_SEGS;
+        const uint64_t* m = kept ? smsg[si - s0] : A->msgbuf + (size_t)inst * SC_MSG_WORDS;
+#pragma unroll
+        for (int x = 0; x < D; x++) {
+            if (x >= jb.degree) continue;
+            const fp2 v = kept ? fp2{m[2 * x], m[2 * x + 1]} : fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)};
+            msg[x] = e_add(msg[x], e_mul(wi, v));
+        }
+    }
+}
+
+// Warp-wide: the rest of job b's round-j step with its state in shared memory (fstb) and its
+// message formed: the padded instances' part, then the transcript step; r_j into srb.
+template <int D>
+__device__ __forceinline__ void persist_step(const ScPersist* A, const FsJob& jb, const FsKeys& keys, int b, int j,
+                                             fp2 (&msg)[D], uint32_t* fstb, uint64_t* srb, uint32_t* buf, bool write) {
+    sc_fs_padded(jb, j, A->w, A->pad, A->S, msg);
+    uint32_t state[8];
+    uint64_t counter;
+    fst_load(fstb, state, counter);
+    sc_fs_step(A->states, jb, b, j, keys, msg, state, counter, A->rounds_out, A->chal_out, buf, write, srb);
+    fst_store(fstb, state, counter);
+}
+
+// Every block sets the given jobs' error flag (each job by one block) before the launch returns.
+__device__ __forceinline__ void persist_gave_up(const ScPersist* A) {
+    if (threadIdx.x == 0)
+        for (int b = blockIdx.x; b < A->njobs; b += gridDim.x) atomicExch(&A->states[b].err, 2u);
+}
+
+template <int D>
+__global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* __restrict__ Ag) {
+    constexpr int NW = SC_THREADS / 32;
+    // the launch's descriptor and round table in shared memory: they are read at every step, and
+    // after each meeting's fence a load from device memory would miss the L1
+    __shared__ ScPersist sA;
+    __shared__ int sfirst[SC_MAX_VARS + 1];
+    for (int i = threadIdx.x; i < (int)(sizeof(ScPersist) / 8); i += SC_THREADS)
+        reinterpret_cast<uint64_t*>(&sA)[i] = reinterpret_cast<const uint64_t*>(Ag)[i];
+    for (int i = threadIdx.x; i <= Ag->rounds; i += SC_THREADS) sfirst[i] = Ag->first[i];
+    const ScPersist* A = &sA;
     __shared__ Seg g;
-    __shared__ uint32_t sbuf[SC_THREADS / 32][FS_BUF_WORDS];
-    __shared__ uint32_t fst[SC_THREADS / 32][10];
+    __shared__ uint32_t sbuf[NW][FS_BUF_WORDS];
+    __shared__ uint32_t fst[NW][10];
     __shared__ uint64_t smsg[SC_SMSG_SEGS][2 * D];
+    __shared__ int sinst[SC_SMSG_SEGS];
+    __shared__ FsJob sjob[NW];
+    __shared__ uint64_t sw[NW][SC_SW][2];  // each job's first instances' weights (local)
+    __shared__ uint64_t sr[NW][2];  // each job's latest challenge (local)
+    __shared__ uint64_t sr_seg[2];  // the current segment's challenge (not local)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned G = gridDim.x;
+    const int njobs = Ag->njobs;
+    const bool local = njobs <= NW;
+    if (local) {  // the jobs, their transcripts, weights and latest challenges, in every block
+        for (int i = threadIdx.x; i < njobs * (int)(sizeof(FsJob) / 8); i += SC_THREADS)
+            reinterpret_cast<uint64_t*>(sjob)[i] = reinterpret_cast<const uint64_t*>(Ag->jobs)[i];
+        if (warp < njobs) {
+            const FsState& st = Ag->states[warp];
+            if (lane < 10)
+                fst[warp][lane] = lane < 8 ? reinterpret_cast<const uint32_t*>(st.state)[lane]
+                                           : (uint32_t)(st.counter >> (32 * (lane - 8)));
+            if (lane < 2) sr[warp][lane] = st.r[lane];
+            const FsJob& jb = Ag->jobs[warp];
+            if (lane < SC_SW && lane < jb.ninst) {
+                sw[warp][lane][0] = Ag->w[2 * (jb.inst0 + lane)];
+                sw[warp][lane][1] = Ag->w[2 * (jb.inst0 + lane) + 1];
+            }
+        }
+    }
+    __syncthreads();
     unsigned gen = 0;
-    for (int t = 0; t < A->multi; t++) {
-        const int s0 = A->first[t], s1 = A->first[t + 1];
+    // the block's last warp has no job (local, fewer than eight jobs): while the others run the
+    // transcripts it copies the next round's first Seg into g, which the round's sums no longer read
+    const bool prefetch = local && njobs < NW;
+    bool have_seg = false;  // g already holds the round's first Seg
+    // One loop over all rounds, so that the sums and the transcript step are each one copy of code
+    // (a copy first run in a later round would start there with its instructions out of cache).
+    for (int t = 0; t < A->rounds; t++) {
+        const bool multi = t < A->multi;
+        if (!multi && blockIdx.x != 0) return;  // one block's work from here: at most eight jobs (local)
+        const int s0 = sfirst[t], s1 = sfirst[t + 1];
+        uint64_t* part = A->partials + (local && (t & 1) ? A->part_words : 0);
         for (int si = s0; si < s1; si++) {
-            if (threadIdx.x < (int)(sizeof(Seg) / 8))
-                reinterpret_cast<uint64_t*>(&g)[threadIdx.x] = reinterpret_cast<const uint64_t*>(A->segs + si)[threadIdx.x];
-            __syncthreads();
-            if (threadIdx.x == 0) g.nblocks = (int)G;  // the segment over all blocks of the launch
+            // a multi-block round takes every segment over all blocks of the launch
+            if (si > s0 || !have_seg) persist_seg_load(A->segs, si, g, multi ? (int)G : 1, local, sr, sr_seg, threadIdx.x);
             __syncthreads();
             uint64_t words[2 * D];
 #pragma unroll
             for (int w = 0; w < 2 * D; w++) words[w] = 0;
-            if (!seg_sums_fast<D, true>(g, blockIdx.x, words)) sc_seg_sums<D, true>(g, blockIdx.x, words);
+            const int lb = multi ? (int)blockIdx.x : 0;
+            if (!seg_sums_fast<D, MEM_L2, true>(g, lb, words)) sc_seg_sums<D, MEM_L2>(g, lb, words);
             block_sum<2 * D>(words);  // ends with a barrier
-            if (threadIdx.x == 0)
+            if (threadIdx.x == 0) {
+                if (si - s0 < SC_SMSG_SEGS) sinst[si - s0] = g.inst;
+                if (multi) {
 #pragma unroll
-                for (int w = 0; w < 2 * D; w++) A->partials[((size_t)(si - s0) * G + blockIdx.x) * 2 * D + w] = words[w];
+                    for (int w = 0; w < 2 * D; w++) part[((size_t)(si - s0) * G + blockIdx.x) * 2 * D + w] = words[w];
+                } else if (si - s0 < SC_SMSG_SEGS) {
+#pragma unroll
+                    for (int w = 0; w < 2 * D; w++) smsg[si - s0][w] = words[w];
+                } else {
+                    for (int w = 0; w < 2 * g.degree; w++) g.out[w] = words[w];
+                }
+            }
             __syncthreads();  // g is rewritten for the next segment
         }
-        if (!grid_meet(A->bar, G, gen)) {
-            if (threadIdx.x == 0)
-                for (int b = blockIdx.x; b < A->njobs; b += G) atomicExch(&A->states[b].err, 2u);
-            return;
+        if (multi && !grid_meet(A->bar, G, gen)) return persist_gave_up(A);
+        const int j = A->jp + t;
+        if (local) {
+            if (warp < njobs && j < sjob[warp].n_max) {
+                const FsJob& jb = sjob[warp];
+                fp2 msg[D];
+                if (multi)
+                    persist_msg_rows<D>(A, jb, sw[warp], part, sinst, s0, s1, G, msg);
+                else
+                    persist_msg_block<D>(A, jb, sw[warp], smsg, sinst, s0, s1, msg);
+                persist_step(A, jb, A->keys, warp, j, msg, fst[warp], sr[warp], sbuf[warp], blockIdx.x == 0);
+            } else if (prefetch && warp == NW - 1 && t + 1 < A->rounds) {
+                const bool multi_next = t + 1 < A->multi;
+                persist_seg_load(A->segs, sfirst[t + 1], g, multi_next ? (int)G : 1, true, sr, sr_seg, lane);
+            }
+            __syncthreads();  // the challenges in sr (and the next Seg in g) for the next round
+            have_seg = prefetch && t + 1 < A->rounds;
+            continue;
         }
         // each warp owns at most one job when there are few: its state then stays in shared memory
-        const bool keep = A->njobs <= (int)G * (SC_THREADS / 32);
-        for (int b = blockIdx.x + G * warp; b < A->njobs; b += G * (SC_THREADS / 32)) {
+        const bool keep = njobs <= (int)G * NW;
+        for (int b = blockIdx.x + G * warp; b < njobs; b += G * NW) {
             const FsJob& jb = A->jobs[b];
-            const int j = A->jp + t;
             if (j >= jb.n_max) continue;
-            fp2 msg[SC_MAX_DEGREE];
-            for (int x = 0; x < SC_MAX_DEGREE; x++) msg[x] = {0, 0};
-            for (int si = s0; si < s1; si++) {
-                const int inst = __ldg(&A->segs[si].inst);
-                if (inst < jb.inst0 || inst >= jb.inst0 + jb.ninst) continue;
-                uint64_t acc[2 * D];
-#pragma unroll
-                for (int w = 0; w < 2 * D; w++) acc[w] = 0;
-                for (int lb = lane; lb < (int)G; lb += 32)
-#pragma unroll
-                    for (int w = 0; w < 2 * D; w++)
-                        acc[w] = add(acc[w], __ldcg(&A->partials[((size_t)(si - s0) * G + lb) * 2 * D + w]));
-#pragma unroll
-                for (int w = 0; w < 2 * D; w++)
-                    for (int o = 16; o > 0; o >>= 1) acc[w] = add(acc[w], __shfl_xor_sync(0xFFFFFFFFu, acc[w], o));
-                const fp2 wi = {A->w[2 * inst], A->w[2 * inst + 1]};
-#pragma unroll
-                for (int x = 0; x < D; x++)
-                    if (x < jb.degree) msg[x] = e_add(msg[x], e_mul(wi, fp2{acc[2 * x], acc[2 * x + 1]}));
-            }
+            fp2 msg[D];
+            persist_msg_rows<D>(A, jb, nullptr, part, sinst, s0, s1, G, msg);
             sc_fs_padded(jb, j, A->w, A->pad, A->S, msg);
             uint32_t state[8];
             uint64_t counter;
@@ -697,67 +983,7 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* A) 
             sc_fs_step(A->states, jb, b, j, A->keys, msg, state, counter, A->rounds_out, A->chal_out, sbuf[warp]);
             if (keep) fst_store(fst[warp], state, counter);
         }
-        if (!grid_meet(A->bar, G, gen)) {
-            if (threadIdx.x == 0)
-                for (int b = blockIdx.x; b < A->njobs; b += G) atomicExch(&A->states[b].err, 2u);
-            return;
-        }
-    }
-    if (blockIdx.x != 0) return;
-    // every warp owns at most one job here (at most 8 jobs take this path): job `warp`, its state in
-    // shared memory from its first round on
-    for (int t = A->multi; t < A->rounds; t++) {
-        const int s0 = A->first[t], s1 = A->first[t + 1];
-        for (int si = s0; si < s1; si++) {
-            if (threadIdx.x < (int)(sizeof(Seg) / 8))
-                reinterpret_cast<uint64_t*>(&g)[threadIdx.x] = reinterpret_cast<const uint64_t*>(A->segs + si)[threadIdx.x];
-            __syncthreads();
-            uint64_t words[2 * D];
-#pragma unroll
-            for (int w = 0; w < 2 * D; w++) words[w] = 0;
-            if (!seg_sums_fast<D, true>(g, 0, words)) sc_seg_sums<D, true>(g, 0, words);
-            block_sum<2 * D>(words);  // ends with a barrier
-            if (threadIdx.x == 0) {
-                if (si - s0 < SC_SMSG_SEGS) {
-#pragma unroll
-                    for (int w = 0; w < 2 * D; w++) smsg[si - s0][w] = words[w];
-                } else {
-                    const int nout = g.kind == 1 ? 2 : 2 * g.degree;
-                    for (int w = 0; w < nout; w++) g.out[w] = words[w];
-                }
-            }
-            __syncthreads();
-        }
-        if (warp < A->njobs) {
-            const int b = warp;
-            const FsJob& jb = A->jobs[b];
-            const int j = A->jp + t;
-            if (j < jb.n_max) {
-                fp2 msg[SC_MAX_DEGREE];
-                for (int x = 0; x < SC_MAX_DEGREE; x++) msg[x] = {0, 0};
-                for (int si = s0; si < s1; si++) {
-                    const int inst = __ldg(&A->segs[si].inst);
-                    if (inst < jb.inst0 || inst >= jb.inst0 + jb.ninst) continue;
-                    const fp2 wi = {A->w[2 * inst], A->w[2 * inst + 1]};
-                    const uint64_t* m = si - s0 < SC_SMSG_SEGS ? smsg[si - s0] : A->msgbuf + (size_t)inst * SC_MSG_WORDS;
-                    for (int x = 0; x < jb.degree; x++) {
-                        const fp2 v = si - s0 < SC_SMSG_SEGS ? fp2{m[2 * x], m[2 * x + 1]}
-                                                              : fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)};
-                        msg[x] = e_add(msg[x], e_mul(wi, v));
-                    }
-                }
-                sc_fs_padded(jb, j, A->w, A->pad, A->S, msg);
-                uint32_t state[8];
-                uint64_t counter;
-                if (t > A->multi)
-                    fst_load(fst[warp], state, counter);
-                else
-                    fst_global(A->states[b], state, counter);
-                sc_fs_step(A->states, jb, b, j, A->keys, msg, state, counter, A->rounds_out, A->chal_out, sbuf[warp]);
-                fst_store(fst[warp], state, counter);
-            }
-        }
-        __syncthreads();
+        if (!grid_meet(A->bar, G, gen)) return persist_gave_up(A);
     }
 }
 
@@ -811,7 +1037,7 @@ static int check_job(const tg_sumcheck_job& jb, int index) {
         if (in.ntables < 1 || !in.tables) return fail(TG_ERR_INVALID, "instance %d has no table", i);
         if (in.ntables > jb.degree)
             return fail(TG_ERR_INVALID, "instance %d: a product of %d tables exceeds degree %d", i, in.ntables, jb.degree);
-        if (in.vars < 0 || in.vars > 40) return fail(TG_ERR_INVALID, "instance %d: %d variables", i, in.vars);
+        if (in.vars < 0 || in.vars > SC_MAX_VARS) return fail(TG_ERR_INVALID, "instance %d: %d variables", i, in.vars);
         for (int k = 0; k < in.ntables; k++)
             if (!in.tables[k].values) return fail(TG_ERR_INVALID, "instance %d table %d: null values", i, k);
     }
@@ -865,6 +1091,7 @@ struct ScRun {
     ScPersist persist_h;
     std::vector<int> persist_first;
     int persist_grid = 1;  // sc_persist's blocks
+    size_t persist_rows = 0;  // partial rows of sc_persist's largest multi-block round (two sets of them)
     // arena layout (offsets from the arena's base)
     size_t off_fs = 0, off_jobs = 0, off_w = 0, off_pad = 0, off_S = 0, off_msg = 0, off_rounds = 0, off_chal = 0,
            off_partials = 0, off_counters = 0, off_segs = 0, off_bind = 0, off_erefs = 0, off_evals = 0, off_persist = 0,
@@ -1007,7 +1234,7 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
     if (coop)
         for (int j = r->j0 - 1; j >= 0 && plan_pairs(j) <= SC_PERSIST_PAIRS; j--) r->jp = j;
     // the persistent launch's blocks, and the partial rows its multi-block rounds write
-    size_t persist_rows = 0;
+    size_t& persist_rows = r->persist_rows;
     if (r->jp < r->j0) {
         int per_sm = 0;
         with_degree(r->D, [&](auto D_) { per_sm = persist_blocks_per_sm<decltype(D_)::value>(); });
@@ -1034,7 +1261,7 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
     r->off_msg = ar.take((size_t)8 * SC_MSG_WORDS * ninst);
     r->off_rounds = ar.take(8 * std::max<size_t>(r->rounds_words, 1));
     r->off_chal = ar.take(8 * std::max<size_t>(r->chal_words, 1));
-    r->off_partials = ar.take(std::max(r->max_blocks, persist_rows) * 2 * SC_MAX_DEGREE * 8);
+    r->off_partials = ar.take(std::max(r->max_blocks, 2 * persist_rows) * 2 * SC_MAX_DEGREE * 8);
     r->off_counters = ar.take(4 * r->max_segs);
     r->off_segs = ar.take(sizeof(Seg) * std::max<size_t>(r->total_segs, 1));
     r->off_persist = ar.take(sizeof(ScPersist));
@@ -1119,6 +1346,7 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
             g.nblocks = tail ? 1 : blocks_for(g.n);
             g.part0 = g.block0;
             g.inst = w.first;
+            g.job = is.job;
             block0 += g.nblocks;
             r->all_segs.push_back(g);
         }
@@ -1171,6 +1399,8 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         r->hj[b].inst0 = r->inst0[b];
         r->hj[b].rounds_off = r->rounds_off[b];
         r->hj[b].chal_off = r->chal_off[b];
+        for (int i = 0; i < jobs[b].ninstances; i++)
+            r->hj[b].pad_max = std::max(r->hj[b].pad_max, r->inst[r->inst0[b] + i].pad);
     }
     r->wv.assign(2 * ninst, 0);
     r->pads.assign(ninst, 0);
@@ -1211,6 +1441,7 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         t.first = ar.at<int>(r->off_first);
         t.partials = ar.at<uint64_t>(r->off_partials);
         t.bar = ar.at<unsigned>(r->off_bar);
+        t.part_words = r->persist_rows * 2 * r->D;
         t.njobs = njobs;
         t.jp = r->jp;
         t.rounds = r->J - r->jp;
@@ -1264,9 +1495,12 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         if (rc) return rc;
         {
             Launch L(d, s, "sumcheck_transcript", 1, njobs);
-            sc_fs_many<<<(njobs * 32 + FS_THREADS - 1) / FS_THREADS, FS_THREADS, 0, s>>>(dfs, ar.at<FsJob>(r->off_jobs), njobs, j, keys,
-                                                        ar.at<uint64_t>(r->off_w), ar.at<int>(r->off_pad), dS, dmsg,
-                                                        drounds, dchal);
+            with_degree(r->D, [&](auto D_) {
+                constexpr int DD = decltype(D_)::value;
+                sc_fs_many<DD><<<(njobs * 32 + FS_THREADS - 1) / FS_THREADS, FS_THREADS, 0, s>>>(
+                    dfs, ar.at<FsJob>(r->off_jobs), njobs, j, keys, ar.at<uint64_t>(r->off_w), ar.at<int>(r->off_pad), dS,
+                    dmsg, drounds, dchal);
+            });
         }
         TG_CUDA(cudaGetLastError());
     }
