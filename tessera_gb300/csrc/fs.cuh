@@ -71,10 +71,7 @@ static __device__ __forceinline__ void b3_g_alu(uint32_t& a, uint32_t& b, uint32
     FS_G(s1, s6, s11, s12, m10, m11)                                                    \
     FS_G(s2, s7, s8, s13, m12, m13)                                                     \
     FS_G(s3, s4, s9, s14, m14, m15)
-static __device__ __forceinline__ void compress_one(uint32_t cv[8], const uint32_t* mp, uint32_t len, uint32_t flags) {
-    uint32_t m[16];
-#pragma unroll
-    for (int i = 0; i < 16; i++) m[i] = mp[i];
+static __device__ __forceinline__ void compress_m(uint32_t cv[8], const uint32_t (&m)[16], uint32_t len, uint32_t flags) {
     uint32_t s0 = cv[0], s1 = cv[1], s2 = cv[2], s3 = cv[3], s4 = cv[4], s5 = cv[5], s6 = cv[6], s7 = cv[7];
     uint32_t s8 = TG_B3_IV0, s9 = TG_B3_IV1, s10 = TG_B3_IV2, s11 = TG_B3_IV3, s12 = 0, s13 = 0, s14 = len, s15 = flags;
     FS_ROUND(m[0], m[1], m[2], m[3], m[4], m[5], m[6], m[7], m[8], m[9], m[10], m[11], m[12], m[13], m[14], m[15])
@@ -89,6 +86,12 @@ static __device__ __forceinline__ void compress_one(uint32_t cv[8], const uint32
 }
 #undef FS_ROUND
 #undef FS_G
+static __device__ __forceinline__ void compress_one(uint32_t cv[8], const uint32_t* mp, uint32_t len, uint32_t flags) {
+    uint32_t m[16];
+#pragma unroll
+    for (int i = 0; i < 16; i++) m[i] = mp[i];
+    compress_m(cv, m, len, flags);
+}
 
 // Eight words passed and returned by value, so that a call keeps them in registers (an array
 // passed by address would live in local memory around every call).
@@ -133,20 +136,22 @@ constexpr int fs_len(const char* t) {
     return n;
 }
 
-// state ‖ u64 len(label) ‖ label ‖ payload into buf by a whole warp, label = prefix ‖ tail ‖
-// decimal j and payload np little-endian u64 words (np ≤ NP; the same state, j and payload in every
-// lane), then zeros to the next block boundary; returns the length in every lane. Each lane writes
-// its own bytes (the caller syncs the warp before buf is read).
-template <int NP>
-static __device__ __forceinline__ uint32_t fs_msg_warp(const uint32_t (&state)[8], const FsJob& jb, uint64_t tail,
-                                                       int tail_len, int j, const uint64_t (&pay)[NP], int np,
-                                                       uint32_t* buf) {
+// Decimal digits of j.
+static __device__ __forceinline__ int fs_digits(int j) {
+    int nd = 1;
+    for (uint32_t q = (uint32_t)j; q >= 10; q /= 10) nd++;
+    return nd;
+}
+
+// The head of a message by a whole warp: state ‖ u64 len(label) ‖ label into buf's first bytes,
+// label = prefix ‖ tail ‖ decimal j (the same state and j in every lane); returns the head's length
+// in every lane. Each lane writes its own bytes (the caller syncs the warp before buf is read).
+static __device__ __forceinline__ uint32_t fs_head_warp(const uint32_t (&state)[8], const FsJob& jb, uint64_t tail,
+                                                        int tail_len, int j, uint32_t* buf) {
     const int lane = threadIdx.x & 31;
     uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
-    int nd = 1;  // decimal digits of j
-    for (uint32_t q = (uint32_t)j; q >= 10; q /= 10) nd++;
+    const int nd = fs_digits(j);
     const int pre = jb.label_len, L = pre + tail_len + nd;
-    const uint32_t len = 40 + (uint32_t)L + 8 * (uint32_t)np;
     if (lane < 10) {  // words 0–9: the state and the label's length
         uint32_t v = lane == 8 ? (uint32_t)L : 0u;
 #pragma unroll
@@ -167,26 +172,49 @@ static __device__ __forceinline__ uint32_t fs_msg_warp(const uint32_t (&state)[8
         }
         bytes[40 + k] = (uint8_t)c;
     }
+    return 40 + (uint32_t)L;
+}
+
+// The payload of a message by a whole warp: np little-endian u64 words (np ≤ NP; the same in every
+// lane) from byte off of buf, then zeros to the next block boundary; returns the message's length.
+template <int NP>
+static __device__ __forceinline__ uint32_t fs_pay_warp(const uint64_t (&pay)[NP], int np, uint32_t off, uint32_t* buf) {
+    const int lane = threadIdx.x & 31;
+    uint8_t* bytes = reinterpret_cast<uint8_t*>(buf);
+    const uint32_t len = off + 8 * (uint32_t)np;
     for (int k = lane; k < 8 * np; k += 32) {
         uint64_t v = 0;
 #pragma unroll
         for (int i = 0; i < NP; i++)
             if ((k >> 3) == i) v = pay[i];
-        bytes[40 + L + k] = (uint8_t)(v >> (8 * (k & 7)));
+        bytes[off + k] = (uint8_t)(v >> (8 * (k & 7)));
     }
     const uint32_t end = (len + 63) / 64 * 64;
     for (uint32_t i = len + lane; i < end; i += 32) bytes[i] = 0;
     return len;
 }
 
+// A whole message: state ‖ u64 len(label) ‖ label ‖ payload into buf by a whole warp, label =
+// prefix ‖ tail ‖ decimal j and payload np little-endian u64 words, then zeros to the next block
+// boundary; returns the length in every lane.
+template <int NP>
+static __device__ __forceinline__ uint32_t fs_msg_warp(const uint32_t (&state)[8], const FsJob& jb, uint64_t tail,
+                                                       int tail_len, int j, const uint64_t (&pay)[NP], int np,
+                                                       uint32_t* buf) {
+    const uint32_t off = fs_head_warp(state, jb, tail, tail_len, j, buf);
+    return fs_pay_warp<NP>(pay, np, off, buf);
+}
+
 // Round j's transcript step by a whole warp, its absorb input (state ‖ label length ‖
 // <prefix>/round/j ‖ message) already in buf and zero padded (fs_msg_warp): absorbs it, then
 // squeezes <prefix>/r/j until the first two words are a canonical Fp2 (c0, c1), every lane building
 // the squeeze and ratchet inputs. state and counter are the same in every lane. False after
-// FS_MAX_TRIES squeezes.
+// FS_MAX_TRIES squeezes. sq (when given) holds the first squeeze's input, sq_len bytes, built by
+// another warp all but its first eight words, the state after the absorb, which are written here.
 static __device__ __forceinline__ bool fs_round_warp(const FsKeys& keys, const FsJob& jb, int j, uint32_t* buf,
                                                      uint32_t len, uint32_t (&state)[8], uint64_t* counter,
-                                                     uint64_t* c0, uint64_t* c1) {
+                                                     uint64_t* c0, uint64_t* c1, uint32_t* sq = nullptr,
+                                                     uint32_t sq_len = 0) {
     const int lane = threadIdx.x & 31;
     __syncwarp();
     {
@@ -196,11 +224,19 @@ static __device__ __forceinline__ bool fs_round_warp(const FsKeys& keys, const F
     }
     __syncwarp();
     for (int tries = 0; tries < FS_MAX_TRIES; tries++) {
-        const uint64_t pay[1] = {*counter};
-        const uint32_t l2 = fs_msg_warp<1>(state, jb, fs_pack("/r/"), fs_len("/r/"), j, pay, 1, buf);
+        const uint32_t* in = buf;
+        uint32_t l2;
+        if (tries == 0 && sq) {
+            if (lane < 8) sq[lane] = state[lane];
+            in = sq;
+            l2 = sq_len;
+        } else {
+            const uint64_t pay[1] = {*counter};
+            l2 = fs_msg_warp<1>(state, jb, fs_pack("/r/"), fs_len("/r/"), j, pay, 1, buf);
+        }
         __syncwarp();
-        const Fs8 sq = fs_hash_warp(fs8(keys.squeeze), buf, l2);
-        const uint32_t(&out)[8] = sq.w;
+        const Fs8 sqh = fs_hash_warp(fs8(keys.squeeze), in, l2);
+        const uint32_t(&out)[8] = sqh.w;
         __syncwarp();
         *counter += 1;
         if (lane < 16) {  // the ratchet's input: state ‖ squeezed block

@@ -530,6 +530,10 @@ __global__ void sc_gather_evals(const EvalRef* refs, int n, uint64_t* out) {
 
 // ---- the transcripts on the device (one warp per job) ------------------------------------------
 
+// Warp 0 and warp SC_THREADS / 32 − 1 of a block meet (named barrier 1): the second builds the
+// first's transcript inputs.
+__device__ __forceinline__ void pair_sync() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+
 // A job's round message lives in registers: D (the batch's largest degree) values, of which the
 // job's first `degree` are its own; the loops over them unroll to fixed indices.
 
@@ -553,11 +557,14 @@ __device__ __forceinline__ void sc_fs_padded(const FsJob& jb, int j, const uint6
 // rounds_out, absorbed as TCE Vec<Fp2> under <prefix>/round/j; then r_j = challenge_fp2 under
 // <prefix>/r/j. state and counter (the same in every lane) are read and updated here; lane 0 writes
 // them, r_j and the challenge back to the job's FsState and to chal_out (unless !write: a copy of
-// the step that another block writes), and r_j to r_local when given.
+// the step that another block writes), and r_j to r_local when given. With sq, another warp has
+// built the absorb input's head in buf and the first squeeze's input in sq (fs_round_warp); the
+// two warps meet at named barrier 1 before this one adds the message.
 template <int D>
-__device__ __forceinline__ void sc_fs_step(FsState* states, const FsJob& jb, int t, int j, const FsKeys& keys, const fp2 (&msg)[D],
-                           uint32_t (&state)[8], uint64_t& counter, uint64_t* rounds_out, uint64_t* chal_out,
-                           uint32_t* buf, bool write = true, uint64_t* r_local = nullptr) {
+__device__ __forceinline__ void sc_fs_step(FsState* states, const FsJob& jb, int t, int j, const FsKeys& keys,
+                                           const fp2 (&msg)[D], uint32_t (&state)[8], uint64_t& counter,
+                                           uint64_t* rounds_out, uint64_t* chal_out, uint32_t* buf, bool write = true,
+                                           uint64_t* r_local = nullptr, uint32_t* sq = nullptr) {
     const int lane = threadIdx.x & 31;
     const int degree = jb.degree;
     FsState* st = states + t;
@@ -572,10 +579,17 @@ __device__ __forceinline__ void sc_fs_step(FsState* states, const FsJob& jb, int
     pay[0] = (uint64_t)degree;
 #pragma unroll
     for (int x = 0; x < D; x++) pay[1 + 2 * x] = msg[x].c0, pay[2 + 2 * x] = msg[x].c1;
-    const uint32_t len = fs_msg_warp<1 + 2 * D>(state, jb, fs_pack("/round/"), fs_len("/round/"), j, pay,
-                                                1 + 2 * degree, buf);
+    uint32_t len, sq_len = 0;
+    if (sq) {
+        const int nd = fs_digits(j);
+        sq_len = 40 + jb.label_len + fs_len("/r/") + nd + 8;
+        pair_sync();
+        len = fs_pay_warp<1 + 2 * D>(pay, 1 + 2 * degree, 40 + jb.label_len + fs_len("/round/") + nd, buf);
+    } else {
+        len = fs_msg_warp<1 + 2 * D>(state, jb, fs_pack("/round/"), fs_len("/round/"), j, pay, 1 + 2 * degree, buf);
+    }
     uint64_t c0, c1;
-    const bool ok = fs_round_warp(keys, jb, j, buf, len, state, &counter, &c0, &c1);
+    const bool ok = fs_round_warp(keys, jb, j, buf, len, state, &counter, &c0, &c1, sq, sq_len);
     if (lane != 0) return;
     if (r_local) r_local[0] = c0, r_local[1] = c1;
     if (!write) return;
@@ -792,13 +806,21 @@ __device__ __forceinline__ fp2 persist_weight(const ScPersist* A, const FsJob& j
     return fp2{A->w[2 * inst], A->w[2 * inst + 1]};
 }
 
+// The message from each lane's node (lane x holds node x, lazy; the rest zero) into every lane.
+template <int D>
+__device__ __forceinline__ void persist_msg_gather(fp2 mine, fp2 (&msg)[D]) {
+    mine = l2_canon(mine);
+#pragma unroll
+    for (int x = 0; x < D; x++)
+        msg[x] = {__shfl_sync(0xFFFFFFFFu, mine.c0, x), __shfl_sync(0xFFFFFFFFu, mine.c1, x)};
+}
+
 template <int D>
 __device__ __forceinline__ void persist_msg_rows(const ScPersist* A, const FsJob& jb, const uint64_t (*sw)[2],
                                                  const uint64_t* part, const int* sinst, int s0, int s1, unsigned G,
                                                  fp2 (&msg)[D]) {
     const int lane = threadIdx.x & 31;
-#pragma unroll
-    for (int x = 0; x < D; x++) msg[x] = {0, 0};
+    fp2 mine = {0, 0};
     for (int si = s0; si < s1; si++) {
         const int inst = persist_inst(A, sinst, si, s0);
         if (inst < jb.inst0 || inst >= jb.inst0 + jb.ninst) continue;
@@ -820,11 +842,15 @@ __device__ __forceinline__ void persist_msg_rows(const ScPersist* A, const FsJob
 #pragma unroll
         for (int w = 0; w < 2 * D; w++)
             for (int o = 16; o > 0; o >>= 1) acc[w] = add(acc[w], __shfl_xor_sync(0xFFFFFFFFu, acc[w], o));
-        const fp2 wi = persist_weight(A, jb, sw, inst);
+        if (lane < jb.degree) {  // lane x: node x
+            fp2 v = {acc[0], acc[1]};
 #pragma unroll
-        for (int x = 0; x < D; x++)
-            if (x < jb.degree) msg[x] = e_add(msg[x], e_mul(wi, fp2{acc[2 * x], acc[2 * x + 1]}));
+            for (int x = 1; x < D; x++)
+                if (lane == x) v = {acc[2 * x], acc[2 * x + 1]};
+            mine = l2_add(mine, l2_mul(persist_weight(A, jb, sw, inst), v));
+        }
     }
+    persist_msg_gather<D>(mine, msg);
 }
 
 // Warp-wide: round j's message of job jb from the sums of its segments that this block kept (smsg,
@@ -834,33 +860,30 @@ template <int D>
 __device__ __forceinline__ void persist_msg_block(const ScPersist* A, const FsJob& jb, const uint64_t (*sw)[2],
                                                   const uint64_t (*smsg)[2 * D], const int* sinst, int s0, int s1,
                                                   fp2 (&msg)[D]) {
-#pragma unroll
-    for (int x = 0; x < D; x++) msg[x] = {0, 0};
+    const int lane = threadIdx.x & 31;
+    fp2 mine = {0, 0};  // lane x: node x
     for (int si = s0; si < s1; si++) {
         const int inst = persist_inst(A, sinst, si, s0);
-        if (inst < jb.inst0 || inst >= jb.inst0 + jb.ninst) continue;
-        const fp2 wi = persist_weight(A, jb, sw, inst);
+        if (inst < jb.inst0 || inst >= jb.inst0 + jb.ninst || lane >= jb.degree) continue;
         const bool kept = si - s0 < SC_SMSG_SEGS;
         const uint64_t* m = kept ? smsg[si - s0] : A->msgbuf + (size_t)inst * SC_MSG_WORDS;
-#pragma unroll
-        for (int x = 0; x < D; x++) {
-            if (x >= jb.degree) continue;
-            const fp2 v = kept ? fp2{m[2 * x], m[2 * x + 1]} : fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)};
-            msg[x] = e_add(msg[x], e_mul(wi, v));
-        }
+        const fp2 v = kept ? fp2{m[2 * lane], m[2 * lane + 1]} : fp2{__ldcg(m + 2 * lane), __ldcg(m + 2 * lane + 1)};
+        mine = l2_add(mine, l2_mul(persist_weight(A, jb, sw, inst), v));
     }
+    persist_msg_gather<D>(mine, msg);
 }
 
 // Warp-wide: the rest of job b's round-j step with its state in shared memory (fstb) and its
 // message formed: the padded instances' part, then the transcript step; r_j into srb.
 template <int D>
 __device__ __forceinline__ void persist_step(const ScPersist* A, const FsJob& jb, const FsKeys& keys, int b, int j,
-                                             fp2 (&msg)[D], uint32_t* fstb, uint64_t* srb, uint32_t* buf, bool write) {
+                                             fp2 (&msg)[D], uint32_t* fstb, uint64_t* srb, uint32_t* buf, bool write,
+                                             uint32_t* sq) {
     sc_fs_padded(jb, j, A->w, A->pad, A->S, msg);
     uint32_t state[8];
     uint64_t counter;
     fst_load(fstb, state, counter);
-    sc_fs_step(A->states, jb, b, j, keys, msg, state, counter, A->rounds_out, A->chal_out, buf, write, srb);
+    sc_fs_step(A->states, jb, b, j, keys, msg, state, counter, A->rounds_out, A->chal_out, buf, write, srb, sq);
     fst_store(fstb, state, counter);
 }
 
@@ -913,8 +936,9 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* __r
     __syncthreads();
     unsigned gen = 0;
     // the block's last warp has no job (local, fewer than eight jobs): while the others run the
-    // transcripts it copies the next round's first Seg into g, which the round's sums no longer read
-    const bool prefetch = local && njobs < NW;
+    // transcripts it copies the next round's first Seg into g, which the round's sums no longer read;
+    // with one job it first builds that job's transcript inputs but the message (build)
+    const bool prefetch = local && njobs < NW, build = local && njobs == 1;
     bool have_seg = false;  // g already holds the round's first Seg
     // One loop over all rounds, so that the sums and the transcript step are each one copy of code
     // (a copy first run in a later round would start there with its instructions out of cache).
@@ -957,10 +981,22 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* __r
                     persist_msg_rows<D>(A, jb, sw[warp], part, sinst, s0, s1, G, msg);
                 else
                     persist_msg_block<D>(A, jb, sw[warp], smsg, sinst, s0, s1, msg);
-                persist_step(A, jb, A->keys, warp, j, msg, fst[warp], sr[warp], sbuf[warp], blockIdx.x == 0);
-            } else if (prefetch && warp == NW - 1 && t + 1 < A->rounds) {
-                const bool multi_next = t + 1 < A->multi;
-                persist_seg_load(A->segs, sfirst[t + 1], g, multi_next ? (int)G : 1, true, sr, sr_seg, lane);
+                persist_step(A, jb, A->keys, warp, j, msg, fst[warp], sr[warp], sbuf[warp], blockIdx.x == 0,
+                             build ? sbuf[NW - 1] : nullptr);
+            } else if (prefetch && warp == NW - 1) {
+                if (build && j < sjob[0].n_max) {  // job 0's absorb head and first squeeze input
+                    uint32_t state[8];
+                    uint64_t counter;
+                    fst_load(fst[0], state, counter);
+                    fs_head_warp(state, sjob[0], fs_pack("/round/"), fs_len("/round/"), j, sbuf[0]);
+                    const uint64_t pay[1] = {counter};
+                    fs_msg_warp<1>(state, sjob[0], fs_pack("/r/"), fs_len("/r/"), j, pay, 1, sbuf[NW - 1]);
+                    pair_sync();
+                }
+                if (t + 1 < A->rounds) {
+                    const bool multi_next = t + 1 < A->multi;
+                    persist_seg_load(A->segs, sfirst[t + 1], g, multi_next ? (int)G : 1, true, sr, sr_seg, lane);
+                }
             }
             __syncthreads();  // the challenges in sr (and the next Seg in g) for the next round
             have_seg = prefetch && t + 1 < A->rounds;
