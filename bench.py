@@ -602,13 +602,18 @@ def run_serve(args) -> None:
     reqs, arrivals, units, sizes = [], [], 0, []
     t = 0.0
     keep = []
+    shapes = []
     for i in range(args.requests):
-        log_k, polys, log_r = rs.randint(10, 16), rs.choice([8, 32, 128]), rs.choice([1, 2])
-        vars_, degree = rs.randint(10, 18), rs.choice([2, 3])
-        rows = torch.from_numpy(splitmix_words(SEED_SERVE + 2 * i, polys << log_k).view(np.int64)).pin_memory()
-        tabs = [torch.from_numpy(splitmix_words(SEED_SERVE + 7919 * i + k, 1 << vars_).view(np.int64)).pin_memory()
-                for k in range(degree)]
-        keep.append((rows, tabs))
+        if i < args.distinct:  # a new input set; later requests take input set i mod distinct again
+            log_k, polys, log_r = rs.randint(10, 16), rs.choice([8, 32, 128]), rs.choice([1, 2])
+            vars_, degree = rs.randint(10, 18), rs.choice([2, 3])
+            rows = torch.from_numpy(splitmix_words(SEED_SERVE + 2 * i, polys << log_k).view(np.int64)).pin_memory()
+            tabs = [torch.from_numpy(splitmix_words(SEED_SERVE + 7919 * i + k, 1 << vars_).view(np.int64)).pin_memory()
+                    for k in range(degree)]
+            keep.append((rows, tabs))
+            shapes.append((log_k, polys, log_r, vars_, degree))
+        log_k, polys, log_r, vars_, degree = shapes[i % args.distinct]
+        rows, tabs = keep[i % args.distinct]
         ctx = SessionContext("tessera-protocol/1", Mode.NON_INTERACTIVE, "test-small/1", bytes([0x65]) * 32,
                              i.to_bytes(16, "little"))
         cid = bytes(rs.randrange(256) for _ in range(32))
@@ -685,7 +690,8 @@ def run_serve(args) -> None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic",
         "config": {"workload": f"serve: {len(reqs)} proof requests (commit 8/32/128 x 2^10..2^16 at rate 1/2 or 1/4, "
                                f"B = 32, then a degree-2/3 sumcheck over 2^10..2^18 bound to the root, then "
-                               f"{args.queries} column queries answered from the resident commitment), Poisson "
+                               f"{args.queries} column queries answered from the resident commitment; request i proves input set "
+                               f"i mod {min(args.distinct, len(reqs))} on its own transcript), Poisson "
                                f"{args.rate} req/s, then all at once", "seed": SEED_SERVE, "slots": args.slots,
                    "queries": args.queries,
                    "hbm_budget_gib": args.serve_budget_gib, "elems": units,
@@ -1067,7 +1073,9 @@ def main():
     ap.add_argument("--workload", choices=["large", "batched", "serve", "logup", "cc", "forest"], default="large",
                     help="large: the 256 x 2^20 commitment + 2^22 sumcheck headline; batched: batched vs plain; "
                          "serve: the proof server against one-at-a-time proofs")
-    ap.add_argument("--requests", type=int, default=400, help="serve: requests in the stream")
+    ap.add_argument("--requests", type=int, default=2000, help="serve: requests in the stream")
+    ap.add_argument("--distinct", type=int, default=400,
+                    help="serve: distinct input sets (request i proves input set i mod distinct, on its own transcript)")
     ap.add_argument("--lookups-log", type=int, default=30, help="logup: log2 of the lookups")
     ap.add_argument("--cc-log-k", type=int, default=22, help="cc: log2 of the row length")
     ap.add_argument("--forest-trees-log", type=int, default=16, help="forest: log2 of the trees")
