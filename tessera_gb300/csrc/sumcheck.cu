@@ -676,6 +676,9 @@ struct ScPersist {
     unsigned* bar;       // the blocks' meeting point: arrivals, generation, gave up (each on its own 128-byte line)
     size_t part_words;   // the second half of partials (local): rounds alternate between the halves
     int njobs, jp, rounds, multi;
+    int la_from;         // rounds la_from … rounds − 1 take their sums from the look-ahead (−1: none)
+    int pad_;
+    uint64_t* const* la_scratch;  // 2·D pointers to tables of 8 Fp2 entries, for the look-ahead's warm-up
 };
 static_assert(sizeof(ScPersist) % 8 == 0, "ScPersist copies as words");
 constexpr int SC_MAX_VARS = 40;  // an instance's variables at most (so at most 40 rounds)
@@ -887,6 +890,151 @@ __device__ __forceinline__ void persist_step(const ScPersist* A, const FsJob& jb
     fst_store(fstb, state, counter);
 }
 
+// ---- the look-ahead of the small one-block rounds ----------------------------------------------
+//
+// With one job of one instance of NT tables at degree NT (Σ f·g·h, Σ f·g), a one-block round of at
+// most SC_LA_PAIRS pairs takes its sums from the round before it: while warp 0 draws r_t, warps
+// 1 … 7 write round t+1's sums as polynomials in r_t. Pair p of round t+1 is T_{t+1}[2p] =
+// a + r_t·(b − a), T_{t+1}[2p+1] = c + r_t·(d − c) with (a, b, c, d) = T_t[4p … 4p+3], so each node
+// value is α + r_t·β and the product over the tables a polynomial of degree NT in r_t, whose
+// coefficients the warps sum over the pairs. Once r_t is drawn, round t+1's message is those sums
+// evaluated at r_t, and its transcript step starts at once; in its shadow the warps bind r_t into T_t
+// (forming T_{t+1}, which the later rounds and the final evaluations read) and write round t+2's
+// polynomials. The round's own sums, about a third of a one-block round, leave the critical path.
+constexpr uint64_t SC_LA_PAIRS = 32;
+__device__ int g_la_sink;  // written only to keep the look-ahead's warm-up call
+constexpr int SC_LA_GROUPS = (SC_THREADS / 32 - 1) * 8;  // lane groups of four in warps 1 … 7
+
+// Warps 1 … 7 of the block (named barrier 2): with bind, T_t = T_{t−1} bound by rprev (src → dst,
+// n_t pairs of round t); with cubic, round t+1's polynomials from T_t (dst) summed into cub[x] (node
+// x, NT + 1 Fp2 coefficients in lazy words, lowest first). red: the warps' rows.
+template <int NT>
+__device__ __noinline__ void persist_lookahead(const uint64_t* const* src, uint64_t* const* dst, uint64_t n_t, fp2 rprev,
+                                               bool bind, bool cubic, uint64_t (*red)[NT][2 * (NT + 1)],
+                                               uint64_t (*cub)[2 * (NT + 1)]) {
+    constexpr int C = NT + 1;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, q = lane & 3;
+    const uint64_t r7 = lz::mul7(rprev.c1);
+    if (!cubic) {  // the last round: only T_t, 2·n_t entries a table
+        for (uint64_t e = threadIdx.x - 32; e < (uint64_t)NT * 2 * n_t; e += SC_THREADS - 32) {
+            const int k = (int)(e / (2 * n_t));
+            const uint64_t i = e % (2 * n_t);
+            const ulonglong2* s2 = reinterpret_cast<const ulonglong2*>(src[k]);
+            const ulonglong2 x0 = __ldcg(s2 + 2 * i), x1 = __ldcg(s2 + 2 * i + 1);
+            const fp2 v = bind_pair({x0.x, x0.y}, {x1.x, x1.y}, rprev, r7, false);
+            reinterpret_cast<ulonglong2*>(dst[k])[i] = make_ulonglong2(v.c0, v.c1);
+        }
+        asm volatile("bar.sync 2, %0;" ::"r"(SC_THREADS - 32) : "memory");
+        return;
+    }
+    const bool act = q < NT;
+    const uint64_t n_next = n_t / 2;
+    fp2 acc[C];
+#pragma unroll
+    for (int i = 0; i < C; i++) acc[i] = {0, 0};
+    const int group = (warp - 1) * 8 + (lane >> 2);
+    for (uint64_t p0 = 0; p0 < n_next; p0 += SC_LA_GROUPS) {  // the same steps in every lane
+        const uint64_t p = p0 + group;
+        const bool live = act && p < n_next;
+        fp2 e[4];
+        if (live) {
+            if (bind) {  // T_t[4p + i] from T_{t−1}[8p + 2i], [8p + 2i + 1]
+                const ulonglong2* s2 = reinterpret_cast<const ulonglong2*>(src[q]) + 8 * p;
+                ulonglong2 x[8];
+#pragma unroll
+                for (int i = 0; i < 8; i++) x[i] = __ldcg(s2 + i);
+                ulonglong2* d2 = reinterpret_cast<ulonglong2*>(dst[q]) + 4 * p;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    e[i] = bind_pair({x[2 * i].x, x[2 * i].y}, {x[2 * i + 1].x, x[2 * i + 1].y}, rprev, r7, false);
+                    d2[i] = make_ulonglong2(e[i].c0, e[i].c1);
+                }
+            } else {
+                const ulonglong2* d2 = reinterpret_cast<const ulonglong2*>(dst[q]) + 4 * p;
+#pragma unroll
+                for (int i = 0; i < 4; i++) {
+                    const ulonglong2 v = __ldcg(d2 + i);
+                    e[i] = {v.x, v.y};
+                }
+            }
+        } else {
+#pragma unroll
+            for (int i = 0; i < 4; i++) e[i] = {0, 0};
+        }
+        // this table's nodes 0, 2, 3 as α + r·β: u = e0 + r(e1 − e0), v = e2 + r(e3 − e2)
+        const fp2 au = e[0], bu = l2_sub(e[1], e[0]), av = e[2], bv = l2_sub(e[3], e[2]);
+        fp2 al[NT], be[NT];
+        al[0] = au, be[0] = bu;
+        const fp2 da = l2_sub(av, au), db = l2_sub(bv, bu);  // v − u
+        fp2 ta = av, tb = bv;
+#pragma unroll
+        for (int x = 1; x < NT; x++) {
+            ta = l2_add(ta, da), tb = l2_add(tb, db);
+            al[x] = ta, be[x] = tb;
+        }
+        // lane x gathers node x of every table (at step st from the lane of table (x + st) mod NT)
+        fp2 ga[NT], gb[NT];
+        ga[0] = al[0], gb[0] = be[0];
+#pragma unroll
+        for (int x = 1; x < NT; x++)
+            if (q == x) ga[0] = al[x], gb[0] = be[x];
+#pragma unroll
+        for (int st = 1; st < NT; st++) {
+            const int need = (q + NT - st) % NT;
+            fp2 sa = al[0], sb = be[0];
+#pragma unroll
+            for (int x = 1; x < NT; x++)
+                if (need == x) sa = al[x], sb = be[x];
+            const int from = (lane & ~3) | (act ? (q + st) % NT : q);
+            ga[st] = {__shfl_sync(0xFFFFFFFFu, sa.c0, from), __shfl_sync(0xFFFFFFFFu, sa.c1, from)};
+            gb[st] = {__shfl_sync(0xFFFFFFFFu, sb.c0, from), __shfl_sync(0xFFFFFFFFu, sb.c1, from)};
+        }
+        if (live) {  // Π_k (ga_k + r·gb_k): coefficients of r^0 … r^NT
+            const fp2 pa = l2_mul(ga[0], ga[1]), pb = l2_mul(gb[0], gb[1]);
+            const fp2 pm = l2_sub(l2_sub(l2_mul(l2_add(ga[0], gb[0]), l2_add(ga[1], gb[1])), pa), pb);
+            if constexpr (NT == 2) {
+                acc[0] = l2_add(acc[0], pa), acc[1] = l2_add(acc[1], pm), acc[2] = l2_add(acc[2], pb);
+            } else {
+                acc[0] = l2_add(acc[0], l2_mul(pa, ga[2]));
+                acc[1] = l2_add(acc[1], l2_add(l2_mul(pa, gb[2]), l2_mul(pm, ga[2])));
+                acc[2] = l2_add(acc[2], l2_add(l2_mul(pm, gb[2]), l2_mul(pb, ga[2])));
+                acc[3] = l2_add(acc[3], l2_mul(pb, gb[2]));
+            }
+        }
+    }
+    // the lanes of one node across the warp's eight groups, then across the warps
+#pragma unroll
+    for (int i = 0; i < C; i++)
+        for (int o = 4; o < 32; o <<= 1) {
+            acc[i].c0 = lz::add(acc[i].c0, __shfl_xor_sync(0xFFFFFFFFu, acc[i].c0, o));
+            acc[i].c1 = lz::add(acc[i].c1, __shfl_xor_sync(0xFFFFFFFFu, acc[i].c1, o));
+        }
+    if (lane < NT)
+#pragma unroll
+        for (int i = 0; i < C; i++) red[warp - 1][lane][2 * i] = acc[i].c0, red[warp - 1][lane][2 * i + 1] = acc[i].c1;
+    asm volatile("bar.sync 2, %0;" ::"r"(SC_THREADS - 32) : "memory");
+    if (warp == 1 && lane < NT)
+#pragma unroll
+        for (int i = 0; i < 2 * C; i++) {
+            uint64_t v = red[0][lane][i];
+            for (int w = 1; w < SC_THREADS / 32 - 1; w++) v = lz::add(v, red[w][lane][i]);
+            cub[lane][i] = v;
+        }
+}
+
+// Lane x (< D) of a warp: node x of the message from the look-ahead's polynomials (cub) at r, the
+// round before's challenge, times the instance's weight w (lazy words); zero in the other lanes.
+// One copy of the code for every call, so that a call in an earlier round has fetched it.
+template <int D>
+__device__ __noinline__ fp2 persist_eval_lookahead(const uint64_t (*cub)[2 * (D + 1)], fp2 r, fp2 w) {
+    const int lane = threadIdx.x & 31;
+    if (lane >= D) return fp2{0, 0};
+    fp2 v = {cub[lane][2 * D], cub[lane][2 * D + 1]};  // by Horner from the top coefficient
+#pragma unroll
+    for (int i = D - 1; i >= 0; i--) v = l2_add(l2_mul(v, r), fp2{cub[lane][2 * i], cub[lane][2 * i + 1]});
+    return w.c0 == 1 && w.c1 == 0 ? v : l2_mul(w, v);
+}
+
 // Every block sets the given jobs' error flag (each job by one block) before the launch returns.
 __device__ __forceinline__ void persist_gave_up(const ScPersist* A) {
     if (threadIdx.x == 0)
@@ -912,6 +1060,12 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* __r
     __shared__ FsJob sjob[NW];
     __shared__ uint64_t sw[NW][SC_SW][2];  // each job's first instances' weights (local)
     __shared__ uint64_t sr[NW][2];  // each job's latest challenge (local)
+    // the look-ahead (one job): round t's challenge by round parity, the polynomials of the round
+    // they are for by its parity, and the warps' rows
+    __shared__ uint64_t srl[2][2];
+    constexpr int LNT = D == 2 || D == 3 ? D : 2;
+    __shared__ uint64_t cub[2][LNT][2 * (LNT + 1)];
+    __shared__ uint64_t red[NW - 1][LNT][2 * (LNT + 1)];
     __shared__ uint64_t sr_seg[2];  // the current segment's challenge (not local)
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const unsigned G = gridDim.x;
@@ -947,7 +1101,9 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* __r
         if (!multi && blockIdx.x != 0) return;  // one block's work from here: at most eight jobs (local)
         const int s0 = sfirst[t], s1 = sfirst[t + 1];
         uint64_t* part = A->partials + (local && (t & 1) ? A->part_words : 0);
-        for (int si = s0; si < s1; si++) {
+        // this round's sums came from the look-ahead (g holds its Seg, fetched in the round before)
+        const bool ahead = A->la_from >= 0 && t >= A->la_from;
+        for (int si = s0; si < s1 && !ahead; si++) {
             // a multi-block round takes every segment over all blocks of the launch
             if (si > s0 || !have_seg) persist_seg_load(A->segs, si, g, multi ? (int)G : 1, local, sr, sr_seg, threadIdx.x);
             __syncthreads();
@@ -974,15 +1130,29 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* __r
         if (multi && !grid_meet(A->bar, G, gen)) return persist_gave_up(A);
         const int j = A->jp + t;
         if (local) {
+            // warps 1 … 7 work in this round's transcript step's shadow: round t+1's polynomials
+            // (binding r_{t−1} into this round's tables first when its sums came from the look-ahead),
+            // or after the last round its bound tables alone
+            const bool work_ahead =
+                A->la_from >= 0 && !multi && (t + 1 < A->rounds ? t + 1 >= A->la_from : ahead);
             if (warp < njobs && j < sjob[warp].n_max) {
                 const FsJob& jb = sjob[warp];
                 fp2 msg[D];
-                if (multi)
-                    persist_msg_rows<D>(A, jb, sw[warp], part, sinst, s0, s1, G, msg);
-                else
-                    persist_msg_block<D>(A, jb, sw[warp], smsg, sinst, s0, s1, msg);
+                if constexpr (D == 2 || D == 3) {
+                    if (ahead)
+                        persist_msg_gather<D>(persist_eval_lookahead<D>(cub[t & 1], fp2{sr[0][0], sr[0][1]},
+                                                                        persist_weight(A, jb, sw[warp], jb.inst0)),
+                                              msg);
+                }
+                if (!ahead) {
+                    if (multi)
+                        persist_msg_rows<D>(A, jb, sw[warp], part, sinst, s0, s1, G, msg);
+                    else
+                        persist_msg_block<D>(A, jb, sw[warp], smsg, sinst, s0, s1, msg);
+                }
                 persist_step(A, jb, A->keys, warp, j, msg, fst[warp], sr[warp], sbuf[warp], blockIdx.x == 0,
                              build ? sbuf[NW - 1] : nullptr);
+                if (lane == 0) srl[t & 1][0] = sr[warp][0], srl[t & 1][1] = sr[warp][1];
             } else if (prefetch && warp == NW - 1) {
                 if (build && j < sjob[0].n_max) {  // job 0's absorb head and first squeeze input
                     uint32_t state[8];
@@ -993,9 +1163,30 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* __r
                     fs_msg_warp<1>(state, sjob[0], fs_pack("/r/"), fs_len("/r/"), j, pay, 1, sbuf[NW - 1]);
                     pair_sync();
                 }
+                if constexpr (D == 2 || D == 3) {
+                    if (work_ahead)
+                        persist_lookahead<D>(g.src, g.dst, g.n, fp2{srl[(t + 1) & 1][0], srl[(t + 1) & 1][1]}, ahead,
+                                             t + 1 < A->rounds, red, cub[(t + 1) & 1]);
+                }
                 if (t + 1 < A->rounds) {
                     const bool multi_next = t + 1 < A->multi;
                     persist_seg_load(A->segs, sfirst[t + 1], g, multi_next ? (int)G : 1, true, sr, sr_seg, lane);
+                }
+            } else if (work_ahead && warp >= 1) {
+                if constexpr (D == 2 || D == 3)
+                    persist_lookahead<D>(g.src, g.dst, g.n, fp2{srl[(t + 1) & 1][0], srl[(t + 1) & 1][1]}, ahead,
+                                         t + 1 < A->rounds, red, cub[(t + 1) & 1]);
+            }
+            if constexpr (D == 2 || D == 3) {
+                // round 0 (or the first round, when it is one block's): warps 1 … 7 of block 0 run the
+                // look-ahead's code once on a scratch table, in the transcript step's shadow, so that
+                // its first real use does not fetch its instructions from device memory
+                if (A->la_from >= 2 && t == 0 && blockIdx.x == 0 && warp >= 1) {
+                    const uint64_t* const* src = A->la_scratch;
+                    persist_lookahead<D>(src, A->la_scratch + D, 2, fp2{1, 0}, true, true, red, cub[1]);
+                    persist_lookahead<D>(src, A->la_scratch + D, 2, fp2{1, 0}, false, true, red, cub[1]);
+                    const fp2 v = persist_eval_lookahead<D>(cub[1], fp2{1, 0}, fp2{2, 0});
+                    if (lane == 0 && v.c0 == 1 && v.c1 == 1) g_la_sink = 1;  // keeps the call
                 }
             }
             __syncthreads();  // the challenges in sr (and the next Seg in g) for the next round
@@ -1131,7 +1322,8 @@ struct ScRun {
     // arena layout (offsets from the arena's base)
     size_t off_fs = 0, off_jobs = 0, off_w = 0, off_pad = 0, off_S = 0, off_msg = 0, off_rounds = 0, off_chal = 0,
            off_partials = 0, off_counters = 0, off_segs = 0, off_bind = 0, off_erefs = 0, off_evals = 0, off_persist = 0,
-           off_first = 0, off_bar = 0;
+           off_first = 0, off_bar = 0, off_la = 0;
+    std::vector<uint64_t*> la_ptrs;
     size_t arena_bytes = 0;
     // host-side staging that the enqueued copies read (kept until finish)
     std::vector<FsState> fs0;
@@ -1303,6 +1495,7 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
     r->off_persist = ar.take(sizeof(ScPersist));
     r->off_first = ar.take(4 * ((size_t)(r->J - r->jp) + 1));
     r->off_bar = ar.take(4 * SC_BAR_WORDS + 128);
+    r->off_la = ar.take(2 * SC_MAX_TABLES * 8 + (size_t)SC_MAX_TABLES * 12 * 16);  // the look-ahead's warm-up tables
     for (auto& is : r->inst)
         if (is.vars >= 1) r->nbind += is.tables.size();
     r->off_bind = ar.take(sizeof(BindLast) * std::max<size_t>(r->nbind, 1));
@@ -1482,6 +1675,29 @@ int sc_enqueue(Device* d, ScRun* r, cudaStream_t s, void* arena, void* host_out)
         t.jp = r->jp;
         t.rounds = r->J - r->jp;
         t.multi = r->j0 - r->jp;
+        // the look-ahead: one job of one instance (one segment a round) of D tables at degree D, from
+        // the first one-block round of at most SC_LA_PAIRS pairs whose round before is one-block too
+        // and whose tables were bound from Fp2 entries (round 2 on)
+        t.la_from = -1;
+        {  // the warm-up's tables (zeros): D sources of 8 Fp2 entries, then D destinations of 4
+            uint8_t* base = ar.at<uint8_t>(r->off_la);
+            uint64_t* data = reinterpret_cast<uint64_t*>(base + 2 * SC_MAX_TABLES * 8);
+            r->la_ptrs.assign(2 * SC_MAX_TABLES, nullptr);
+            for (int k = 0; k < r->D; k++) {
+                r->la_ptrs[k] = data + 16 * k;
+                r->la_ptrs[r->D + k] = data + 16 * SC_MAX_TABLES + 8 * k;
+            }
+            t.la_scratch = reinterpret_cast<uint64_t* const*>(base);
+            TG_CUDA(cudaMemcpyAsync(base, r->la_ptrs.data(), 2 * SC_MAX_TABLES * 8, cudaMemcpyHostToDevice, s));
+            TG_CUDA(cudaMemsetAsync(data, 0, (size_t)SC_MAX_TABLES * 12 * 16, s));
+        }
+        if (njobs == 1 && ninst == 1 && (r->D == 2 || r->D == 3) && jobs[0].degree == r->D &&
+            (int)r->inst[0].tables.size() == r->D)
+            for (int tt = t.rounds - 1; tt >= 1; tt--) {
+                const int j = r->jp + tt;
+                if (j < 2 || tt - 1 < t.multi || r->all_segs[r->plan_seg0[1 + j]].n > SC_LA_PAIRS) break;
+                t.la_from = tt;
+            }
         r->persist_first.assign(1, 0);
         for (int j = r->jp; j < r->J; j++) r->persist_first.push_back(r->persist_first.back() + (int)r->plans[1 + j].who.size());
         TG_CUDA(cudaMemcpyAsync(ar.at<ScPersist>(r->off_persist), &t, sizeof t, cudaMemcpyHostToDevice, s));
