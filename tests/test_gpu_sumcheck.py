@@ -79,6 +79,18 @@ def test_sumcheck_fgh_2p22(dev):
     run_both(dev, "stage/0", 3, [[(f, False, False), (g, False, False), (h, False, False)]])
 
 
+@pytest.mark.parametrize("degree", [2, 3])
+@pytest.mark.parametrize("log_len", [3, 4, 6, 9, 12, 17])
+def test_sumcheck_one_instance_small_rounds(dev, degree, log_len):
+    """One instance of `degree` tables at that degree: every round of at most 2^16 pairs runs in the
+    persistent launch, and from round 2 the one-block rounds of at most 32 pairs take their sums from
+    the look-ahead (round t+1's sums as a polynomial in r_t, written while r_t is drawn). Prime-field
+    and Fp2 tables, one of them public."""
+    n = 1 << log_len
+    specs = [[(O.splitmix(40 + k, (2 if k == 1 else 1) * n), k == 1, k == degree - 1) for k in range(degree)]]
+    run_both(dev, "stage/2", degree, specs)
+
+
 def test_sumcheck_mixed_public_padded(dev):
     """Prime-field and Fp2 tables in one product, a public factor, front padding, a constant."""
     specs = [
