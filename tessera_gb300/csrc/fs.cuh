@@ -205,6 +205,10 @@ static __device__ __forceinline__ uint32_t fs_msg_warp(const uint32_t (&state)[8
     return fs_pay_warp<NP>(pay, np, off, buf);
 }
 
+// Two warps of a block meet (named barrier 1, 64 threads): one has built the other's transcript
+// inputs (the absorb's head, the first squeeze's input) while the other formed the message.
+static __device__ __forceinline__ void fs_pair_sync() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
+
 // Round j's transcript step by a whole warp, its absorb input (state ‖ label length ‖
 // <prefix>/round/j ‖ message) already in buf and zero padded (fs_msg_warp): absorbs it, then
 // squeezes <prefix>/r/j until the first two words are a canonical Fp2 (c0, c1), every lane building

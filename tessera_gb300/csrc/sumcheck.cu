@@ -530,9 +530,6 @@ __global__ void sc_gather_evals(const EvalRef* refs, int n, uint64_t* out) {
 
 // ---- the transcripts on the device (one warp per job) ------------------------------------------
 
-// Warp 0 and warp SC_THREADS / 32 − 1 of a block meet (named barrier 1): the second builds the
-// first's transcript inputs.
-__device__ __forceinline__ void pair_sync() { asm volatile("bar.sync 1, 64;" ::: "memory"); }
 
 // A job's round message lives in registers: D (the batch's largest degree) values, of which the
 // job's first `degree` are its own; the loops over them unroll to fixed indices.
@@ -583,7 +580,7 @@ __device__ __forceinline__ void sc_fs_step(FsState* states, const FsJob& jb, int
     if (sq) {
         const int nd = fs_digits(j);
         sq_len = 40 + jb.label_len + fs_len("/r/") + nd + 8;
-        pair_sync();
+        fs_pair_sync();
         len = fs_pay_warp<1 + 2 * D>(pay, 1 + 2 * degree, 40 + jb.label_len + fs_len("/round/") + nd, buf);
     } else {
         len = fs_msg_warp<1 + 2 * D>(state, jb, fs_pack("/round/"), fs_len("/round/"), j, pay, 1 + 2 * degree, buf);
@@ -1161,7 +1158,7 @@ __global__ void __launch_bounds__(SC_THREADS, 2) sc_persist(const ScPersist* __r
                     fs_head_warp(state, sjob[0], fs_pack("/round/"), fs_len("/round/"), j, sbuf[0]);
                     const uint64_t pay[1] = {counter};
                     fs_msg_warp<1>(state, sjob[0], fs_pack("/r/"), fs_len("/r/"), j, pay, 1, sbuf[NW - 1]);
-                    pair_sync();
+                    fs_pair_sync();
                 }
                 if constexpr (D == 2 || D == 3) {
                     if (work_ahead)
