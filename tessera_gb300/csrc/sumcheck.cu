@@ -8,11 +8,12 @@
 // batch is front-padded and contributes 2^{n_max − n_i − j − 1}·S_i to each of its padding rounds.
 //
 // Many independent proofs ("jobs", each a prove_batch with its own transcript) advance in
-// lockstep: round j of every job is ONE launch of sc_rounds, whose blocks are split among the
-// (job, instance) segments of that round in proportion to their pairs, and ONE launch of
-// sc_fs_many, one thread per job, which forms the job's message, absorbs it into the job's
+// lockstep: a large round j of every job is ONE launch of sc_rounds, whose blocks are split among
+// the (job, instance) segments of that round in proportion to their pairs, and ONE launch of
+// sc_fs_many, one warp per job, which forms the job's message, absorbs it into the job's
 // Fiat–Shamir transcript and squeezes its challenge with BLAKE3 on the device
-// (crates/tessera-hash/src/transcript.rs:168-219). A segment binds the previous challenge into its
+// (crates/tessera-hash/src/transcript.rs:168-219); the rounds of at most SC_PERSIST_PAIRS pairs
+// run in one persistent launch of sc_persist. A segment binds the previous challenge into its
 // tables (t'[i] = t[2i] + r·(t[2i+1] − t[2i])) in the same pass that accumulates the d node sums
 // of the new table, and the last of its blocks to finish reduces the blocks' partial sums. The
 // rounds never return to the host: γ is drawn on the host before them, and the final evaluations
