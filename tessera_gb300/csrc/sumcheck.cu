@@ -681,37 +681,37 @@ struct ScPersist {
 static_assert(sizeof(ScPersist) % 8 == 0, "ScPersist copies as words");
 constexpr int SC_MAX_VARS = 40;  // an instance's variables at most (so at most 40 rounds)
 
-// The meeting point's words, each on its own 128-byte line so that the arrivals' atomics and the
-// waiting blocks' polls do not contend for one line.
-constexpr int SC_BAR_COUNT = 0, SC_BAR_GEN = 32, SC_BAR_FAIL = 64, SC_BAR_WORDS = 96;
+// The meeting point's words: the arrivals (which the waiting blocks poll) and, on its own 128-byte
+// line, the give-up flag.
+constexpr int SC_BAR_COUNT = 0, SC_BAR_FAIL = 32, SC_BAR_WORDS = 64;
 constexpr unsigned SC_BAR_POLLS = 1u << 24;  // about a second of polling before a meeting gives up
 
-// All G blocks of the launch meet. A block waits at most SC_BAR_POLLS polls, and stops waiting
-// once another block has given up; then every thread of the block gets false (and the caller
-// returns, so that no block waits on one that has left). The transcripts record the failure.
+// All G blocks of the launch meet. The arrivals count up one word that is never reset within a
+// launch (the host zeroes it before): meeting m is complete once it reaches G·m. Thread 0 of each
+// block adds its arrival with an acquire-release atomic (its block's writes, ordered before it by
+// the barrier, go out with it) and polls the count with acquire loads (the other blocks' writes come
+// in with it); the barrier after hands both to the block's other threads. A block waits at most
+// SC_BAR_POLLS polls, and stops waiting once another block has given up; then every thread of the
+// block gets false (and the caller returns, so that no block waits on one that has left). The
+// transcripts record the failure.
 __device__ bool grid_meet(unsigned* bar, unsigned G, unsigned& gen, unsigned polls = SC_BAR_POLLS) {
     __shared__ int ok;
     __syncthreads();
     if (threadIdx.x == 0) {
-        const unsigned target = gen + 1;
+        const unsigned target = G * (gen + 1);
         int good = 1;
-        __threadfence();
-        if (atomicAdd(bar + SC_BAR_COUNT, 1u) == G - 1) {
-            atomicExch(bar + SC_BAR_COUNT, 0u);
-            __threadfence();
-            atomicExch(bar + SC_BAR_GEN, target);
-        } else {
-            for (unsigned it = 1;; it++) {
-                if (*(volatile unsigned*)(bar + SC_BAR_GEN) == target) break;
-                if ((it & 255) == 0 && (*(volatile unsigned*)(bar + SC_BAR_FAIL) || it >= polls)) {
-                    atomicExch(bar + SC_BAR_FAIL, 1u);
-                    good = 0;
-                    break;
-                }
-                __nanosleep(32);
+        unsigned seen;
+        asm volatile("atom.acq_rel.gpu.global.add.u32 %0, [%1], 1;" : "=r"(seen) : "l"(bar + SC_BAR_COUNT) : "memory");
+        seen += 1;
+        for (unsigned it = 1; seen < target; it++) {
+            if ((it & 255) == 0 && (*(volatile unsigned*)(bar + SC_BAR_FAIL) || it >= polls)) {
+                atomicExch(bar + SC_BAR_FAIL, 1u);
+                good = 0;
+                break;
             }
+            __nanosleep(32);
+            asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(seen) : "l"(bar + SC_BAR_COUNT) : "memory");
         }
-        __threadfence();
         // a block that gave up before the last arrival is seen at the next meeting (its flag is
         // polled there, and it does not arrive); the rounds up to here had every block's share
         ok = good;
