@@ -102,6 +102,35 @@ def test_prove_many_uneven_vs_oracle(dev):
         assert ts[b].state == ot.state and ts[b].counter == ot.counter
 
 
+@pytest.mark.parametrize("njobs,lo,hi", [(2, 12, 15), (7, 0, 12), (8, 11, 14), (9, 0, 12)])
+def test_prove_many_job_counts_vs_oracle(dev, njobs, lo, hi):
+    """Up to eight jobs keep their transcripts in every block of the persistent rounds (one meeting
+    a round; with fewer than eight a spare warp fetches the next segment); nine or more take the
+    owner-warp path with two meetings. Jobs of 2^lo..2^hi entries, several instances each, so that
+    the larger ones have multi-block persistent rounds."""
+    from tessera_gb300.hash import Transcript
+    from tessera_gb300.sumcheck import Protocol, prove_many
+
+    rs = np.random.default_rng(100 + njobs)
+    jobs = []
+    for b in range(njobs):
+        degree = int(rs.integers(1, 5))
+        specs = []
+        for i in range(int(rs.integers(1, 3))):
+            vars_ = int(rs.integers(lo, hi + 1))
+            specs.append([(O.splitmix(5000 * b + 10 * i + k, (2 if k == 1 else 1) << vars_), k == 1, False)
+                          for k in range(degree)])
+        jobs.append((f"stage/{b}", degree, specs))
+    ts = [Transcript(ctx(b.to_bytes(16, "little"))) for b in range(njobs)]
+    res = prove_many([(ts[b], Protocol.ONE, pre, deg, _insts(specs)) for b, (pre, deg, specs) in enumerate(jobs)],
+                     device=dev)
+    for b, ((pre, deg, specs), pb) in enumerate(zip(jobs, res)):
+        ot = O.OracleTranscript(ctx(b.to_bytes(16, "little")).tce())
+        g, rounds, chal, evals = O.prove_batch(ot, pre, deg, specs)
+        assert pb.gamma == g and pb.proof.rounds == rounds and pb.point == chal and pb.proof.final_evals == evals, b
+        assert ts[b].state == ot.state and ts[b].counter == ot.counter
+
+
 def _batched_jobs(max_vars, count=64):
     from tessera_gb300.workloads import batched, splitmix_words
 
