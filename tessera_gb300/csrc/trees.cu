@@ -650,33 +650,36 @@ __device__ void tl_quad(const TlTree& T, int jj, const ulonglong2* q, fp2& a, fp
 __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& keys, TlTree* trees, int ntrees,
                             ulonglong2* q, uint64_t* rounds_out, uint64_t* chal_out, uint32_t* sbuf) {
     const int lane = threadIdx.x & 31;
-    fp2 msg[3] = {{0, 0}, {0, 0}, {0, 0}};
-    for (int i = 0; i < ntrees; i++) {  // every lane forms the message (the same reads)
+    // lane x (< 3) forms node x of the message (X = 0, 2, 3), lazy words; the others follow along
+    const int x = lane < 3 ? lane : 0;
+    fp2 mine = {0, 0};
+    for (int i = 0; i < ntrees; i++) {
         const TlTree& T = trees[i];
         const fp2 w = {T.w[0], T.w[1]};
         const int jj = j - T.pad;
-        // lazy words throughout; the message is canonicalised once
         if (jj < 0) {
             const fp2 ws = l2_mul(w, fp2{T.S[0], T.S[1]});
-            const fp2 v = {mul_pow2_lt64(ws.c0, T.pad - j - 1), mul_pow2_lt64(ws.c1, T.pad - j - 1)};
-            for (int x = 0; x < 3; x++) msg[x] = l2_add(msg[x], v);
+            mine = l2_add(mine, fp2{mul_pow2_lt64(ws.c0, T.pad - j - 1), mul_pow2_lt64(ws.c1, T.pad - j - 1)});
         } else {
+            // γ^i·C·eq1(t, X) at this lane's node (1 − t, 3t − 1, 5t − 2), independent of the sums
+            const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
+            const fp2 t2 = l2_add(t, t), t3 = l2_add(t2, t);
+            const fp2 e = x == 0 ? l2_sub(fp2{1, 0}, t) : x == 1 ? l2_sub(t3, fp2{1, 0}) : l2_sub(l2_add(t3, t2), fp2{2, 0});
+            const fp2 wce = l2_mul(l2_mul(w, fp2{T.C[0], T.C[1]}), e);
             fp2 a, b, c;
             tl_quad(T, jj, q + 4 * i, a, b, c);
             if (lane == 0) q[4 * i + 3] = make_ulonglong2(b.c0, b.c1);  // for the update after the challenge
-            const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
-            const fp2 wc = l2_mul(w, fp2{T.C[0], T.C[1]});
-            // q(2) = a + 2b + 4c, q(3) = a + 3b + 9c; eq1(t, X) at 0, 2, 3: 1 − t, 3t − 1, 5t − 2
-            const fp2 b2 = l2_add(b, b), c2 = l2_add(c, c), c4 = l2_add(c2, c2), c8 = l2_add(c4, c4);
-            const fp2 q2 = l2_add(a, l2_add(b2, c4)), q3 = l2_add(l2_add(a, l2_add(b2, b)), l2_add(c8, c));
-            const fp2 t2 = l2_add(t, t), t3 = l2_add(t2, t), t5 = l2_add(t3, t2);
-            const fp2 e0 = l2_sub(fp2{1, 0}, t), e2 = l2_sub(t3, fp2{1, 0}), e3 = l2_sub(t5, fp2{2, 0});
-            msg[0] = l2_add(msg[0], l2_mul(wc, l2_mul(e0, a)));
-            msg[1] = l2_add(msg[1], l2_mul(wc, l2_mul(e2, q2)));
-            msg[2] = l2_add(msg[2], l2_mul(wc, l2_mul(e3, q3)));
+            // q(0) = a, q(2) = a + 2b + 4c, q(3) = a + 3b + 9c
+            const fp2 b2 = l2_add(b, b), c2 = l2_add(c, c), c4 = l2_add(c2, c2);
+            const fp2 qx = x == 0 ? a
+                         : x == 1 ? l2_add(a, l2_add(b2, c4))
+                                  : l2_add(l2_add(a, l2_add(b2, b)), l2_add(l2_add(c4, c4), c));
+            mine = l2_add(mine, l2_mul(wce, qx));
         }
     }
-    for (int x = 0; x < 3; x++) msg[x] = l2_canon(msg[x]);
+    mine = l2_canon(mine);
+    fp2 msg[3];
+    for (int k = 0; k < 3; k++) msg[k] = {__shfl_sync(0xFFFFFFFFu, mine.c0, k), __shfl_sync(0xFFFFFFFFu, mine.c1, k)};
     uint32_t state[8];
     for (int i = 0; i < 8; i++) state[i] = reinterpret_cast<const uint32_t*>(st->state)[i];
     uint64_t counter = st->counter;
@@ -686,28 +689,34 @@ __device__ void tl_fs_round(FsState* st, const FsJob& jb, int j, const FsKeys& k
     const uint64_t pay[7] = {3, msg[0].c0, msg[0].c1, msg[1].c0, msg[1].c1, msg[2].c0, msg[2].c1};
     const uint32_t len = fs_msg_warp<7>(state, jb, fs_pack("/round/"), fs_len("/round/"), j, pay, 7, sbuf);
     uint64_t c0, c1;
-    const bool ok = fs_round_warp(keys, jb, j, sbuf, len, state, &counter, &c0, &c1);
-    if (lane != 0) return;
-    if (!ok) {
-        st->err = 1;
-        return;
+    const bool ok = fs_round_warp(keys, jb, j, sbuf, len, state, &counter, &c0, &c1);  // ends with a warp barrier
+    if (lane == 0) {
+        if (!ok) {
+            st->err = 1;
+        } else {
+            for (int i = 0; i < 8; i++) reinterpret_cast<uint32_t*>(st->state)[i] = state[i];
+            st->counter = counter;
+            st->r[0] = c0, st->r[1] = c1;
+            chal_out[2 * j] = c0, chal_out[2 * j + 1] = c1;
+        }
     }
-    for (int i = 0; i < 8; i++) reinterpret_cast<uint32_t*>(st->state)[i] = state[i];
-    st->counter = counter;
-    st->r[0] = c0, st->r[1] = c1;
-    chal_out[2 * j] = c0, chal_out[2 * j + 1] = c1;
+    if (!ok || lane < 1 || lane > 2) return;
+    // each tree in its own rounds: lane 1 takes Q ← q(r), lane 2 C ← C·eq1(t, r)
     const fp2 r = {c0, c1};
     for (int i = 0; i < ntrees; i++) {
         TlTree& T = trees[i];
         const int jj = j - T.pad;
         if (jj < 0) continue;
-        const fp2 a = ld2(q + 4 * i), b = ld2(q + 4 * i + 3), c = ld2(q + 4 * i + 2);  // b as the message pass left it
-        const fp2 Q = l2_add(a, l2_mul(r, l2_add(b, l2_mul(r, c))));
-        const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
-        const fp2 tr = l2_mul(t, r);  // eq1(t, r) = 1 − t − r + 2·t·r
-        const fp2 C = l2_mul(fp2{T.C[0], T.C[1]}, l2_add(l2_sub(l2_sub(fp2{1, 0}, t), r), l2_add(tr, tr)));
-        T.Q[0] = Q.c0, T.Q[1] = Q.c1;
-        T.C[0] = C.c0, T.C[1] = C.c1;
+        if (lane == 1) {
+            const fp2 a = ld2(q + 4 * i), b = ld2(q + 4 * i + 3), c = ld2(q + 4 * i + 2);  // b as the message pass left it
+            const fp2 Q = l2_add(a, l2_mul(r, l2_add(b, l2_mul(r, c))));
+            T.Q[0] = Q.c0, T.Q[1] = Q.c1;
+        } else {
+            const fp2 t = {T.point[2 * jj], T.point[2 * jj + 1]};
+            const fp2 tr = l2_mul(t, r);  // eq1(t, r) = 1 − t − r + 2·t·r
+            const fp2 C = l2_mul(fp2{T.C[0], T.C[1]}, l2_add(l2_sub(l2_sub(fp2{1, 0}, t), r), l2_add(tr, tr)));
+            T.C[0] = C.c0, T.C[1] = C.c1;
+        }
     }
 }
 
