@@ -535,6 +535,16 @@ __global__ void sc_gather_evals(const EvalRef* refs, int n, uint64_t* out) {
 // A job's round message lives in registers: D (the batch's largest degree) values, of which the
 // job's first `degree` are its own; the loops over them unroll to fixed indices.
 
+// The message from each lane's node (lane x holds node x, lazy; the rest zero) into every lane.
+template <int D>
+__device__ __forceinline__ void persist_msg_gather(fp2 mine, fp2 (&msg)[D]) {
+    mine = l2_canon(mine);
+#pragma unroll
+    for (int x = 0; x < D; x++)
+        msg[x] = {__shfl_sync(0xFFFFFFFFu, mine.c0, x), __shfl_sync(0xFFFFFFFFu, mine.c1, x)};
+}
+
+
 // The padded instances' part of job jb's round-j message, added to msg: w_i·2^{pad_i − j − 1}·S_i
 // at every node of each instance still in its padding rounds.
 template <int D>
@@ -614,17 +624,15 @@ __device__ void sc_fs_job(FsState* states, const FsJob* jobs, int t, int j, cons
                           uint64_t* chal_out, uint32_t* buf) {
     const FsJob& jb = jobs[t];
     if (j >= jb.n_max) return;
-    fp2 msg[D];
-#pragma unroll
-    for (int x = 0; x < D; x++) msg[x] = {0, 0};
-    for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {  // every lane forms the message
-        if (j < pad[i]) continue;
-        const fp2 wi = {w[2 * i], w[2 * i + 1]};
-        const uint64_t* m = msgbuf + (size_t)i * SC_MSG_WORDS;
-#pragma unroll
-        for (int x = 0; x < D; x++)
-            if (x < jb.degree) msg[x] = e_add(msg[x], e_mul(wi, fp2{__ldcg(m + 2 * x), __ldcg(m + 2 * x + 1)}));
+    const int lane = threadIdx.x & 31;
+    fp2 mine = {0, 0};  // lane x: node x of the message, lazy words
+    for (int i = jb.inst0; i < jb.inst0 + jb.ninst; i++) {
+        if (j < pad[i] || lane >= jb.degree) continue;
+        const uint64_t* m = msgbuf + (size_t)i * SC_MSG_WORDS + 2 * lane;
+        mine = l2_add(mine, l2_mul(fp2{w[2 * i], w[2 * i + 1]}, fp2{__ldcg(m), __ldcg(m + 1)}));
     }
+    fp2 msg[D];
+    persist_msg_gather<D>(mine, msg);
     sc_fs_padded(jb, j, w, pad, S, msg);
     uint32_t state[8];
 #pragma unroll
@@ -805,15 +813,6 @@ __device__ __forceinline__ fp2 persist_weight(const ScPersist* A, const FsJob& j
     const int k = inst - jb.inst0;
     if (sw && k < SC_SW) return fp2{sw[k][0], sw[k][1]};
     return fp2{A->w[2 * inst], A->w[2 * inst + 1]};
-}
-
-// The message from each lane's node (lane x holds node x, lazy; the rest zero) into every lane.
-template <int D>
-__device__ __forceinline__ void persist_msg_gather(fp2 mine, fp2 (&msg)[D]) {
-    mine = l2_canon(mine);
-#pragma unroll
-    for (int x = 0; x < D; x++)
-        msg[x] = {__shfl_sync(0xFFFFFFFFu, mine.c0, x), __shfl_sync(0xFFFFFFFFu, mine.c1, x)};
 }
 
 template <int D>
