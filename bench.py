@@ -677,6 +677,11 @@ def run_serve(args) -> None:
             "served": {"proofs_per_s": len(reqs) / sw, "elems_per_s": units / sw,
                        "latency_ms": {"p50": q(sl, 0.5), "p99": q(sl, 0.99)}, "slowest": tail(sl),
                        "slowest_stages_ms": [st["stages"][i] for _, i, _ in tail(sl)],
+                       # each stage's own time (admission wait, commit, sumcheck, opening), p50 and p99
+                       "stage_ms": {name: {"p50": q([x / 1e3 for x in ds], 0.5), "p99": q([x / 1e3 for x in ds], 0.99)}
+                                    for name, ds in zip(("queued", "commit", "sumcheck", "opening"),
+                                                        zip(*[(g[0], g[1] - g[0], g[2] - g[1], g[3] - g[2])
+                                                              for g in st["stages"] if len(g) == 4]))},
                        "peak_inflight": st["peak_inflight"], "peak_gib": st["peak_bytes"] / 2**30},
         }
     del keep

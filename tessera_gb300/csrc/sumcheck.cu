@@ -49,6 +49,7 @@ constexpr uint64_t SC_TAIL_PAIRS = 4096, SC_TAIL_PAIRS_PERSIST = 512;
 // round: blocks wait for each other at every round's transcript, and the fewer they are, the more of
 // the GPU stays free for other streams' work (the proof server's requests).
 constexpr uint64_t SC_PERSIST_PAIRS = 1ull << 16, SC_PERSIST_BLOCK_PAIRS = 1024;
+constexpr uint64_t SC_PERSIST_MIN_BLOCKS = 16, SC_PERSIST_MIN_BLOCK_PAIRS = 256;
 
 // One instance's share of one launch.
 struct Seg {
@@ -1463,8 +1464,13 @@ ScRun* sc_prepare(Device* d, tg_sumcheck_job* jobs, int njobs, int tables_on_dev
     if (r->jp < r->j0) {
         int per_sm = 0;
         with_degree(r->D, [&](auto D_) { per_sm = persist_blocks_per_sm<decltype(D_)::value>(); });
-        r->persist_grid = (int)std::max<uint64_t>(
-            1, std::min<uint64_t>(plan_pairs(r->jp) / SC_PERSIST_BLOCK_PAIRS, (uint64_t)per_sm * d->sm_count));
+        // one block per SC_PERSIST_BLOCK_PAIRS pairs of the first round, but at least SC_PERSIST_MIN_BLOCKS
+        // while each keeps SC_PERSIST_MIN_BLOCK_PAIRS (a small proof's first rounds are otherwise
+        // a few blocks' long sums)
+        const uint64_t p0 = plan_pairs(r->jp);
+        const uint64_t want = std::max<uint64_t>(p0 / SC_PERSIST_BLOCK_PAIRS,
+                                                 std::min<uint64_t>(SC_PERSIST_MIN_BLOCKS, p0 / SC_PERSIST_MIN_BLOCK_PAIRS));
+        r->persist_grid = (int)std::max<uint64_t>(1, std::min<uint64_t>(want, (uint64_t)per_sm * d->sm_count));
         for (int j = r->jp; j < r->j0; j++) persist_rows = std::max(persist_rows, r->plans[1 + j].who.size() * r->persist_grid);
     }
 
