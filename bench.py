@@ -113,6 +113,24 @@ def dist_env():
     return world, rank, local
 
 
+def max_over_ranks(value: float, world: int, device) -> float:
+    """The largest of every rank's value through the process group (the whole job's time is the
+    slowest rank's); the value itself with one rank."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank: float, world: int, ms: float) -> float:
+    """Whole-job throughput: every rank's units over the slowest rank's time (ms)."""
+    return units_per_rank * world / (ms / 1e3)
+
+
 # ---- CPU port (the reference arm and the cpu_baseline leg) ---------------------------------------
 
 class CpuStep:
@@ -350,15 +368,9 @@ def run_gpu(args) -> None:
     launches = dev.launches() - launches0
     barrier()
     step_ms = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[-1])
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([total_ms], device=cuda)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        total_ms = float(tt.item())
+    total_ms = max_over_ranks(ev[0].elapsed_time(ev[-1]), world, cuda)
     ms_per_step = total_ms / args.steps
-    value = UNITS * world / (total_ms / 1e3 / args.steps)
+    value = job_rate(UNITS, world, ms_per_step)
 
     # the host link's rate from pinned memory (the best of three 512 MiB copies), which bounds the
     # end-to-end step from below: it moves h2d bytes per step
@@ -385,13 +397,7 @@ def run_gpu(args) -> None:
         step_e2e()
     e1.record(stream)
     stream.synchronize()
-    e2e_ms = e0.elapsed_time(e1) / args.steps
-    if world > 1:
-        import torch.distributed as dist
-
-        tt = torch.tensor([e2e_ms], device=cuda)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_ms = float(tt.item())
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / args.steps, world, cuda)
     h2d = COMMITTED * 8 + 3 * (1 << SC_VARS) * 8
     d2h = 32 + SC_VARS * SC_DEGREE * 16 + 3 * 16
     # Release torch's buffers while the library's stream (which their copies used) still exists,
@@ -455,7 +461,7 @@ def run_gpu(args) -> None:
         "metric": "committed+sumchecked field elems/s", "value": value, "unit": "elems/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64 (Goldilocks)", "data": "synthetic", "config": CONFIG,
-        "e2e": {"value": UNITS * world / (e2e_ms / 1e3), "unit": "elems/s", "ms_per_step": e2e_ms,
+        "e2e": {"value": job_rate(UNITS, world, e2e_ms), "unit": "elems/s", "ms_per_step": e2e_ms,
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "host_link_gbs": link_gbs, "host_link_floor_ms": h2d / (link_gbs * 1e9) * 1e3 if link_gbs else None,
                 "note": "the step's copies cross the host link at host_link_gbs (measured here, pinned memory); "
