@@ -57,3 +57,15 @@ def test_two_ranks_slowest_time_and_job_rate(tmp_path):
     # every rank's units over the slowest rank's time: 2 x 1e9 units in 15 ms
     assert bench.job_rate(1e9, 2, 15.0) == pytest.approx(2e9 / 0.015)
     assert bench.max_over_ranks(3.5, 1, "cpu") == 3.5
+
+
+def test_reference_arm_other_ranks_exit_without_work():
+    """Under torchrun the reference arm runs on rank 0 alone; another rank exits 0 at once and
+    prints nothing."""
+    import subprocess
+
+    env = dict(os.environ, RANK="1", LOCAL_RANK="1", WORLD_SIZE="2", MASTER_ADDR="127.0.0.1")
+    out = subprocess.run([sys.executable, str(ROOT / "bench.py"), "--impl", "reference", "--gpus", "2"],
+                         cwd=ROOT, env=env, capture_output=True, text=True, timeout=120)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.strip() == ""
